@@ -1,0 +1,430 @@
+#!/usr/bin/env python3
+"""Benchmark: sampled Brandes betweenness on an undirected R-MAT scale-20 graph.
+
+Workload (one "step"): betweenness_centrality(g, 4096) on R-MAT scale 20
+(n = 2^20, 16 n edge draws, a/b/c/d = .57/.19/.19/.05, self-loops and
+duplicates removed, ids permuted; Int32 CSR), sources drawn without
+replacement by `sample` (seed 2 + rank).  Sources of degree 0 are skipped, as
+in the reference.  Metric: GTEPS = (active sources x undirected edges) / time.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  `value` times K steps with the graph resident
+in HBM (CUDA events on the library's stream); `e2e` times the C-ABI call with
+host buffers: graph upload from pinned memory, the betweenness call, the
+result read back, and the handle freed, every step.  The inputs (CSR 134 MB,
+per-batch lane state 1 GB) are larger than the 129 MB L2, so no L2 flush is
+inserted.  `--impl reference` times the CPU restatement of the reference
+algorithm (heap Dijkstra + predecessor lists, one source per host thread).
+"""
+from __future__ import annotations
+
+import argparse
+import csv
+import ctypes
+import io
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "lightgraphs.jl_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "Brandes BC GTEPS on 1 GB300"
+UNIT = "GTEPS"
+LANES = 64
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# ----------------------------------------------------------------------------- ranks
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo", rank=self.rank, world_size=self.world)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ----------------------------------------------------------------------------- clocks
+class Clocks:
+    """nvidia-smi samples taken every 200 ms while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join("/tmp", f"lgbc_clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for row in csv.reader(f):
+                if len(row) < 9:
+                    continue
+                try:
+                    sm.append(float(row[1]))
+                    smax.append(float(row[2]))
+                except ValueError:
+                    continue
+                for nm, val in zip(names, row[5:9]):
+                    if val.strip().lower() == "active":
+                        reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------- helpers
+def peak_hbm() -> tuple[float, str]:
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def bc_algorithmic_bytes(n: int, nnz: int, k_act: int) -> int:
+    """Brandes bytes for k_act sources in batches of 64 lanes: per batch the
+    CSR is streamed forward and backward and bc read-modified once
+    (8 nnz + 32 n + 16 bytes); per source the lane state (write d 4 B + sigma
+    8 B, read d 4 B + sigma 8 B, write delta 8 B) is 32 n bytes."""
+    return math.ceil(k_act / LANES) * (8 * nnz + 32 * n + 16) + 32 * n * k_act
+
+
+def gd_algorithmic_bytes(n: int, nnz: int, q: int) -> int:
+    return math.ceil(q / LANES) * (4 * nnz + 8 * (n + 1)) + 4 * n * q
+
+
+def traffic_per_step() -> float | None:
+    """DRAM bytes per step from the committed ncu summary, if one exists."""
+    p = os.path.join(ROOT, "profiles", "bc_rmat20_k4096_traffic.txt")
+    try:
+        with open(p) as f:
+            for line in f:
+                if line.startswith("dram_bytes_per_step:"):
+                    return float(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+def workload(rank: int, k: int, scale: int):
+    from lgbc import generators as G
+    import lgbc
+    t = time.perf_counter()
+    g = G.rmat(scale, 16, seed=1)
+    gen_s = time.perf_counter() - t
+    src1 = lgbc.sample(g.vertices(), k, rng=np.random.default_rng(2 + rank))
+    src = (np.asarray(src1, np.int64) - 1).astype(np.int32)
+    rp, ci = g.csr()
+    deg = np.diff(rp)
+    k_act = int(np.count_nonzero(deg[src] > 0))
+    return g, src, k_act, gen_s
+
+
+# ----------------------------------------------------------------------------- CPU arms
+def cpu_betweenness_sample(g, src: np.ndarray, nthreads: int, target_s: float, seed: int):
+    """Time the oracle's faithful mode (the reference's algorithm) on a bounded
+    sample of the workload's sources; returns (GTEPS, sample description)."""
+    from oracle import oracle
+    rp, ci = g.csr()
+    deg = np.diff(rp)
+    act = src[deg[src] > 0]
+    rng = np.random.default_rng(seed)
+    # calibrate with one source per thread
+    cal = rng.choice(act, size=min(len(act), nthreads), replace=False)
+    t = time.perf_counter()
+    oracle.betweenness_raw(rp, ci, cal, mode="faithful", nthreads=nthreads)
+    dt = max(time.perf_counter() - t, 1e-3)
+    per_round = dt
+    rounds = max(1, int(target_s / per_round))
+    count = min(len(act), rounds * nthreads)
+    samp = rng.choice(act, size=count, replace=False)
+    t = time.perf_counter()
+    oracle.betweenness_raw(rp, ci, samp, mode="faithful", nthreads=nthreads)
+    dt = time.perf_counter() - t
+    m = g.ne()
+    return count * m / dt / 1e9, dt, count
+
+
+def run_reference(args, dist: Dist):
+    """--impl reference: the reference's algorithm on the host cores."""
+    if dist.rank != 0:
+        return
+    nthreads = os.cpu_count() or 1
+    g, src, k_act, _ = workload(0, args.k, args.scale)
+    rp, ci = g.csr()
+    deg = np.diff(rp)
+    act = src[deg[src] > 0]
+    from oracle import oracle
+    oracle.build()
+    m = g.ne()
+    per_step = []
+    count = None
+    for it in range(args.warmup + args.steps):
+        if count is None:
+            # size one step to about 10 s of CPU work
+            cal = act[:nthreads]
+            t = time.perf_counter()
+            oracle.betweenness_raw(rp, ci, cal, mode="faithful", nthreads=nthreads)
+            dt = max(time.perf_counter() - t, 1e-3)
+            count = min(len(act), max(nthreads, int(10.0 / dt) * nthreads))
+        samp = act[(it * count) % len(act):][:count]
+        if len(samp) < count:
+            samp = np.concatenate([samp, act[:count - len(samp)]])
+        t = time.perf_counter()
+        oracle.betweenness_raw(rp, ci, samp, mode="faithful", nthreads=nthreads)
+        dt = time.perf_counter() - t
+        if it >= args.warmup:
+            per_step.append(dt)
+    t_step = statistics.mean(per_step)
+    value = count * m / t_step / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"rmat{args.scale}_sampled_bc_k{args.k}", "scale": args.scale,
+                   "edgefactor": 16, "k": args.k, "n": g.nv(), "m": m,
+                   "active_sources": k_act},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
+                         "sample": f"{count} of the {k_act} active sources per step "
+                                   "(heap Dijkstra + predecessor lists, as "
+                                   "src/shortestpaths/dijkstra.jl:59-141; Julia is not "
+                                   "installed, so the C++ restatement stands in)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------------------- GPU arm
+def run_ours(args, dist: Dist):
+    visible = [d for d in os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",") if d.strip()]
+    if dist.world > 1:
+        # one GPU per rank: rank-local device 0 (set before the library loads)
+        mine = visible[dist.local] if len(visible) > dist.local else str(dist.local)
+        os.environ["CUDA_VISIBLE_DEVICES"] = mine
+        visible = [mine]
+    smi_index = int(visible[0]) if visible and visible[0].strip().isdigit() else 0
+    import lgbc
+    from lgbc import _lib
+    lib = _lib.lib()
+    g, src, k_act, gen_s = workload(dist.rank, args.k, args.scale)
+    n, m = g.nv(), g.ne()
+    rp, ci = g.csr()
+    nnz = len(ci)
+    log(f"[rank {dist.rank}] R-MAT scale {args.scale}: n={n} m={m} nnz={nnz} "
+        f"k={args.k} active={k_act} (generated in {gen_s:.1f}s)")
+
+    dg = g.device_handle()
+    h = dg.handle
+    bc_dev = ctypes.c_void_p()
+    _lib.check(lib.lgbc_device_alloc(ctypes.byref(bc_dev), 8 * n))
+    srcp = _lib.ptr(src)
+
+    def step_dev():
+        _lib.check(lib.lgbc_betweenness_dev(h, srcp, len(src), 0, bc_dev))
+
+    for _ in range(args.warmup):
+        step_dev()
+    _lib.check(lib.lgbc_graph_sync(h))
+    stats = dg.stats()
+
+    clocks = Clocks(smi_index)
+    dist.barrier()
+    _lib.check(lib.lgbc_graph_sync(h))
+    clocks.start()
+    _lib.check(lib.lgbc_timer_start(h))
+    for _ in range(args.steps):
+        step_dev()
+    ms = ctypes.c_double()
+    launches = ctypes.c_int64()
+    _lib.check(lib.lgbc_timer_stop(h, ctypes.byref(ms), ctypes.byref(launches)))
+    clk = clocks.stop()
+    dist.barrier()
+    t_dev = dist.max(ms.value / 1e3)
+    te_step = k_act * m
+    value = dist.sum(te_step * args.steps) / t_dev / 1e9
+
+    # bc result sanity: finite and non-negative
+    host_bc = np.empty(n, np.float64)
+    _lib.check(lib.lgbc_memcpy(_lib.ptr(host_bc), bc_dev, 8 * n, 2))
+    assert np.all(np.isfinite(host_bc)) and host_bc.min() >= 0
+
+    # ---- end to end through the C ABI with host buffers ----------------------------
+    prp = ctypes.c_void_p()
+    pci = ctypes.c_void_p()
+    _lib.check(lib.lgbc_host_alloc(ctypes.byref(prp), 8 * (n + 1)))
+    _lib.check(lib.lgbc_host_alloc(ctypes.byref(pci), 4 * nnz))
+    ctypes.memmove(prp, rp.ctypes.data, 8 * (n + 1))
+    ctypes.memmove(pci, ci.ctypes.data, 4 * nnz)
+    out = np.empty(n, np.float64)
+
+    def step_e2e():
+        hh = ctypes.c_void_p()
+        _lib.check(lib.lgbc_graph_create(ctypes.byref(hh), n, nnz, prp, pci, None, None, 0))
+        try:
+            _lib.check(lib.lgbc_betweenness(hh, srcp, len(src), 0, _lib.ptr(out)))
+        finally:
+            lib.lgbc_graph_destroy(hh)
+
+    e2e_steps = max(1, min(args.steps, 5))
+    step_e2e()
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        step_e2e()
+    t_e2e = dist.max((time.perf_counter() - t0) / e2e_steps)
+    e2e_value = dist.sum(te_step) / t_e2e / 1e9
+    lib.lgbc_host_free(prp)
+    lib.lgbc_host_free(pci)
+
+    # ---- gdistances from 64 sources (the workload's BFS part) ----------------------
+    rng = np.random.default_rng(3 + dist.rank)
+    gsrc = rng.choice(n, 64, replace=False).astype(np.int32)
+    dist_out = np.empty((64, n), np.int32)
+    _lib.check(lib.lgbc_gdistances_batch(h, _lib.ptr(gsrc), 64, _lib.ptr(dist_out)))
+    _lib.check(lib.lgbc_timer_start(h))
+    gd_reps = 3
+    for _ in range(gd_reps):
+        _lib.check(lib.lgbc_gdistances_batch(h, _lib.ptr(gsrc), 64, _lib.ptr(dist_out)))
+    _lib.check(lib.lgbc_timer_stop(h, ctypes.byref(ms), None))
+    gd_t = ms.value / 1e3 / gd_reps
+    gd_active = int(np.count_nonzero(np.diff(rp)[gsrc] > 0))
+
+    # ---- roofline --------------------------------------------------------------------
+    peak, peak_kind = peak_hbm()
+    t_step = t_dev / args.steps
+    abytes = bc_algorithmic_bytes(n, nnz, k_act)
+    achieved = abytes / t_step / 1e9
+    traffic = traffic_per_step()
+
+    # ---- CPU baseline (rank 0, N = 1 only) -------------------------------------------
+    cpu = None
+    if dist.world == 1 and not args.no_cpu:
+        nthreads = os.cpu_count() or 1
+        cpu_v, cpu_t, cpu_n = cpu_betweenness_sample(g, src, nthreads, args.cpu_seconds, 7)
+        cpu = {"value": cpu_v, "unit": UNIT, "cores": nthreads, "kind": "port",
+               "sample": f"{cpu_n} of the {k_act} active sources ({cpu_t:.1f} s), faithful "
+                         "heap-Dijkstra restatement of src/shortestpaths/dijkstra.jl:59-141 + "
+                         "_accumulate_basic!, one source per thread"}
+
+    if dist.rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "u64 path counts, df32/f64 dependencies", "data": "synthetic",
+            "config": {"workload": f"rmat{args.scale}_sampled_bc_k{args.k}", "scale": args.scale,
+                       "edgefactor": 16, "abcd": [0.57, 0.19, 0.19, 0.05], "k": args.k,
+                       "n": n, "m": m, "nnz": nnz, "active_sources": k_act,
+                       "lanes": LANES, "parallelism": f"replicas x{dist.world}",
+                       "l2": "inputs larger than L2 (CSR 134 MB, lane state 1 GB); no flush"},
+            "e2e": {"value": e2e_value, "unit": UNIT,
+                    "h2d_bytes_per_step": 8 * (n + 1) + 4 * nnz + 4 * len(src),
+                    "d2h_bytes_per_step": 8 * n,
+                    "ms_per_step": t_e2e * 1e3},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "peak_source": f"{peak_kind} hbm_gbs",
+                         "algorithmic_bytes_per_step": abytes,
+                         "scope": "whole Brandes pass (all kernels of one step)"},
+            "cpu_baseline": cpu,
+            "clocks": clk,
+            "gpu_launches": int(launches.value),
+            "kernel_stats_per_step": stats,
+            "gdistances": {"sources": 64, "active": gd_active, "ms": gd_t * 1e3,
+                           "gteps": gd_active * m / gd_t / 1e9,
+                           "algorithmic_gbs": gd_algorithmic_bytes(n, nnz, 64) / gd_t / 1e9},
+        }
+        print(json.dumps(line), flush=True)
+    lib.lgbc_device_free(bc_dev)
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawTextHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--scale", type=int, default=20)
+    ap.add_argument("--k", type=int, default=4096)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0,
+                    help="approximate CPU-baseline sample length")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    args = ap.parse_args()
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            run_reference(args, dist)
+        else:
+            run_ours(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

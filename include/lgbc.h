@@ -1,0 +1,161 @@
+/* lgbc.h -- C ABI of the GB300-native betweenness-centrality / BFS library.
+ *
+ * This is the drop-in boundary for LightGraphs.jl's unit-weight betweenness
+ * centrality and gdistances (LightGraphs v1.3.5; paths below are relative to
+ * that project).  Host code (the Julia module in
+ * lightgraphs.jl_gb300/julia/, or the Python mirror in
+ * lightgraphs.jl_gb300/lgbc/) flattens SimpleGraph / SimpleDiGraph
+ * `fadjlist` (and `badjlist`) to a 0-based CSR and calls these entry points;
+ * every computation runs as hand-written sm_103a CUDA kernels.  There is no
+ * CPU fallback: a missing or failing GPU is reported as an error.
+ *
+ * Conventions
+ *  - Vertex ids are 0-based int32; rowptr is int64 (n+1 entries), colidx is
+ *    int32 (nnz entries), each row sorted ascending without duplicates, as
+ *    SimpleGraph's add_edge! keeps it (src/SimpleGraphs/simplegraph.jl:445-461,
+ *    simpledigraph.jl:414-429).
+ *  - The caller owns every host array.  The library copies what it needs to
+ *    device memory before it returns and never keeps a host pointer.
+ *  - Every entry point returns LGBC_OK (0) or a negative LGBC_E* code;
+ *    lgbc_last_error() then returns a thread-local message.
+ *  - A graph handle owns one CUDA stream.  Calls on one handle are serialised
+ *    by a mutex; host-buffer calls are blocking (the stream is synchronised
+ *    before they return).  "_dev" entry points are asynchronous on the
+ *    handle's stream; lgbc_graph_sync() waits for them.
+ */
+#ifndef LGBC_H
+#define LGBC_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LGBC_OK 0
+#define LGBC_EINVAL (-1)     /* bad vertex id, size or argument (ArgumentError/BoundsError) */
+#define LGBC_ENOMEM (-2)     /* device or host allocation failed */
+#define LGBC_ECUDA (-3)      /* a CUDA call failed (no GPU, launch failure, ...) */
+#define LGBC_ETIMEOUT (-4)   /* a bounded device wait ran out; the context stays usable */
+
+#define LGBC_UNREACHED INT32_MAX /* distance of a vertex no source reaches */
+
+typedef struct lgbc_graph lgbc_graph; /* opaque; owns the device CSR */
+
+/* Library version string, e.g. "lgbc 0.1.0 sm_103a". */
+const char *lgbc_version(void);
+
+/* Thread-local message describing the last error on this host thread. */
+const char *lgbc_last_error(void);
+
+/* Number of visible CUDA devices (0 if none); never fails. */
+int lgbc_device_count(void);
+
+/* Create a device-resident graph.
+ * Replaces the per-call `g.fadjlist[u]` pointer chasing of
+ * src/SimpleGraphs/SimpleGraphs.jl:78-79,93 (outneighbors) and
+ * :85-86 (inneighbors) with one upload per graph.
+ *   rowptr/colidx        out-CSR (fadjlist), nnz entries
+ *   in_rowptr/in_colidx  in-CSR (badjlist) for directed graphs; NULL when
+ *                        directed == 0 (an undirected graph is its own in-CSR)
+ * A self-loop of an undirected graph is stored once, as add_edge! does
+ * (src/SimpleGraphs/simplegraph.jl:455). */
+int lgbc_graph_create(lgbc_graph **out, int64_t n, int64_t nnz,
+                      const int64_t *rowptr, const int32_t *colidx,
+                      const int64_t *in_rowptr, const int32_t *in_colidx,
+                      int directed);
+
+/* Free the handle and all its device memory. NULL is accepted. */
+int lgbc_graph_destroy(lgbc_graph *g);
+
+/* Number of vertices / stored CSR entries / directedness of a handle. */
+int lgbc_graph_info(const lgbc_graph *g, int64_t *n, int64_t *nnz, int *directed);
+
+/* gdistances!(g, sources, dists) -- src/traversals/bfs.jl:95-124,141 and the
+ * Parallel variant src/Parallel/traversals/gdistances.jl:36-139.
+ * Multi-source BFS: every source has distance 0, every other vertex the hop
+ * count to the nearest source; LGBC_UNREACHED where no source reaches.
+ * nsrc == 0 gives all LGBC_UNREACHED (test/traversals/bfs.jl:33). */
+int lgbc_gdistances(lgbc_graph *g, const int32_t *src, int64_t nsrc,
+                    int32_t *dist_out /* n */);
+
+/* nsrc independent single-source gdistances, one per source, written as
+ * dist_out[i * n + v] (row i = source i).  Runs sources as bit lanes of a
+ * multi-source BFS that shares every edge read. */
+int lgbc_gdistances_batch(lgbc_graph *g, const int32_t *src, int64_t nsrc,
+                          int32_t *dist_out /* nsrc x n */);
+
+/* Unscaled Brandes betweenness over the given sources:
+ * the source loop of src/centrality/betweenness.jl:46-68 (and of
+ * Parallel.betweenness_centrality, src/Parallel/centrality/betweenness.jl:9-72)
+ * with unit weights (DefaultDistance, src/distance.jl:8-21), i.e.
+ * dijkstra_shortest_paths(allpaths=true) (src/shortestpaths/dijkstra.jl:59-141)
+ * followed by _accumulate_basic! (:81-107) or, with endpoints != 0,
+ * _accumulate_endpoints! (:109-134).  Sources with degree(g, s) == 0 are
+ * skipped (:58; degree is in+out for digraphs, src/core.jl:66-67).
+ * src == NULL means all vertices 0..n-1 (nsrc is then ignored).  Duplicate
+ * sources are processed once per occurrence.  The caller applies _rescale!
+ * (:136-160) with k = the number of sources passed (not the active count).
+ * bc_raw_out: n doubles, overwritten. */
+int lgbc_betweenness(lgbc_graph *g, const int32_t *src, int64_t nsrc,
+                     int endpoints, double *bc_raw_out);
+
+/* As lgbc_betweenness, but the result stays in device memory: bc_raw_dev is
+ * a device pointer to n doubles (overwritten).  The source list is read from
+ * host memory before the call returns; the computation is queued on the
+ * handle's stream and may still run when the call returns. */
+int lgbc_betweenness_dev(lgbc_graph *g, const int32_t *src, int64_t nsrc,
+                         int endpoints, double *bc_raw_dev);
+
+/* Wait for all work queued on the handle's stream. */
+int lgbc_graph_sync(lgbc_graph *g);
+
+/* Device-side timing on the handle's stream: lgbc_timer_start records a CUDA
+ * event, lgbc_timer_stop records a second one, synchronises, and returns the
+ * elapsed milliseconds and the number of library kernels launched between
+ * the two. */
+int lgbc_timer_start(lgbc_graph *g);
+int lgbc_timer_stop(lgbc_graph *g, double *elapsed_ms, int64_t *kernel_launches);
+
+/* Statistics of the last betweenness / gdistances call on this handle. */
+typedef struct lgbc_stats {
+  int64_t kernel_launches;   /* kernels the call launched */
+  int64_t batches;           /* source batches (<= 64 sources each) */
+  int64_t levels;            /* BFS levels summed over batches */
+  int64_t active_sources;    /* sources with degree > 0 */
+  int64_t wide_batches;      /* batches replayed in FP64 because a path count exceeded 2^64 */
+  int64_t topdown_levels;    /* levels expanded top-down */
+  int64_t bottomup_levels;   /* levels expanded bottom-up */
+} lgbc_stats;
+int lgbc_graph_stats(const lgbc_graph *g, lgbc_stats *out);
+
+/* Tunables (the autotuner writes these; defaults are used otherwise).
+ *   alpha, beta   direction switch: go bottom-up when the frontier's edges
+ *                 exceed (unvisited edges)/alpha; return top-down when the
+ *                 frontier has fewer than n/beta vertices.
+ *   hub_degree    vertices with at least this many neighbours are expanded by
+ *                 a whole thread block instead of one warp.
+ *   lanes         sources per multi-source batch (1..64). */
+typedef struct lgbc_tuning {
+  double alpha;
+  double beta;
+  int32_t hub_degree;
+  int32_t lanes;
+} lgbc_tuning;
+int lgbc_get_tuning(const lgbc_graph *g, lgbc_tuning *out);
+int lgbc_set_tuning(lgbc_graph *g, const lgbc_tuning *t);
+
+/* Device / pinned-host memory helpers for callers without their own CUDA
+ * allocator (bench and test harnesses).  lgbc_memcpy kinds: 1 = host to
+ * device, 2 = device to host, 3 = device to device. */
+int lgbc_device_alloc(void **ptr, int64_t bytes);
+int lgbc_device_free(void *ptr);
+int lgbc_host_alloc(void **ptr, int64_t bytes);
+int lgbc_host_free(void *ptr);
+int lgbc_memcpy(void *dst, const void *src, int64_t bytes, int kind);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LGBC_H */

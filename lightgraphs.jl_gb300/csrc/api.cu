@@ -1,0 +1,753 @@
+// api.cu -- the C ABI of include/lgbc.h: graph handles, workspaces and the
+// host side of the level loops.  All arithmetic runs in the kernels of
+// msbfs.cu / bfs.cu / util.cu; there is no CPU fallback.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "lgbc.h"
+#include "lgbc_kernels.h"
+
+using namespace lgbc;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  return fail(LGBC_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define LGBC_CUDA(call)                                   \
+  do {                                                    \
+    cudaError_t _e = (call);                              \
+    if (_e != cudaSuccess) return cuda_fail(_e, #call);   \
+  } while (0)
+
+#define LGBC_TRY(expr)          \
+  do {                          \
+    int _rc = (expr);           \
+    if (_rc != LGBC_OK) return _rc; \
+  } while (0)
+
+template <class T>
+int dev_alloc(T** p, size_t count) {
+  *p = nullptr;
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T));
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    *p = nullptr;
+    return fail(LGBC_ENOMEM, std::string("cudaMalloc of ") + std::to_string(count * sizeof(T)) +
+                                 " bytes failed: " + cudaGetErrorString(e));
+  }
+  return LGBC_OK;
+}
+
+template <class T>
+void dev_free(T*& p) {
+  if (p) cudaFree(p);
+  p = nullptr;
+}
+
+// Multi-source workspace (msbfs.cu), sized for one batch of 64 lanes.
+struct MsWorkspace {
+  uint64_t* visit = nullptr;
+  uint64_t* mb0 = nullptr;
+  uint64_t* mb1 = nullptr;
+  void* sigma = nullptr;
+  void* psi = nullptr;
+  int32_t* qv = nullptr;
+  uint64_t* qm = nullptr;
+  unsigned long long* lvl_off = nullptr;
+  BatchCtl* ctl = nullptr;
+  unsigned long long cap = 0;
+  bool have_sigma = false;
+
+  void release() {
+    dev_free(visit);
+    dev_free(mb0);
+    dev_free(mb1);
+    if (sigma) cudaFree(sigma);
+    if (psi) cudaFree(psi);
+    sigma = psi = nullptr;
+    dev_free(qv);
+    dev_free(qm);
+    dev_free(lvl_off);
+    dev_free(ctl);
+    cap = 0;
+    have_sigma = false;
+  }
+};
+
+struct BfsWorkspace {
+  int32_t* queue = nullptr;
+  uint32_t* bm0 = nullptr;
+  uint32_t* bm1 = nullptr;
+  BatchCtl* ctl = nullptr;
+  void release() {
+    dev_free(queue);
+    dev_free(bm0);
+    dev_free(bm1);
+    dev_free(ctl);
+  }
+};
+
+}  // namespace
+
+struct lgbc_graph {
+  int device = 0;
+  int64_t n = 0;
+  int64_t nnz = 0;
+  int directed = 0;
+  cudaStream_t stream = nullptr;
+  int64_t* d_rowptr = nullptr;
+  int32_t* d_colidx = nullptr;
+  int64_t* d_in_rowptr = nullptr;   // == d_rowptr for undirected graphs
+  int32_t* d_in_colidx = nullptr;
+  std::vector<uint8_t> has_degree;  // degree(g, v) > 0, host copy for filtering
+  std::mutex mu;
+  MsWorkspace ms;
+  BfsWorkspace bfs;
+  int32_t* d_src = nullptr;         // device copy of a call's source list
+  int64_t d_src_cap = 0;
+  double* d_bc = nullptr;           // device result buffer for host-buffer calls
+  int32_t* d_dist = nullptr;        // device distance buffer (gdistances)
+  int64_t d_dist_cap = 0;
+  BatchCtl* h_ctl = nullptr;        // pinned mirror of a control block
+  cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
+  int64_t launches = 0;             // running count of kernels launched
+  int64_t launches_at_start = 0;
+  LaunchCfg cfg{};
+  size_t max_smem = 0;
+  lgbc_stats stats{};
+  lgbc_tuning tune{14.0, 24.0, 4096, 64};
+
+  DevGraph dev() const {
+    return DevGraph{n, nnz, d_rowptr, d_colidx, d_in_rowptr, d_in_colidx};
+  }
+};
+
+namespace {
+
+int check_graph(const lgbc_graph* g) {
+  if (!g) return fail(LGBC_EINVAL, "null graph handle");
+  return LGBC_OK;
+}
+
+int use_device(lgbc_graph* g) {
+  LGBC_CUDA(cudaSetDevice(g->device));
+  return LGBC_OK;
+}
+
+int check_sources(const lgbc_graph* g, const int32_t* src, int64_t nsrc) {
+  if (nsrc < 0) return fail(LGBC_EINVAL, "negative source count");
+  if (nsrc > 0 && !src) return fail(LGBC_EINVAL, "null source list");
+  for (int64_t i = 0; i < nsrc; ++i) {
+    if (src[i] < 0 || src[i] >= g->n) {
+      char buf[160];
+      std::snprintf(buf, sizeof buf, "source %lld at position %lld is not a vertex of a graph with %lld vertices",
+                    static_cast<long long>(src[i]), static_cast<long long>(i),
+                    static_cast<long long>(g->n));
+      return fail(LGBC_EINVAL, buf);
+    }
+  }
+  return LGBC_OK;
+}
+
+int ensure_src(lgbc_graph* g, int64_t count) {
+  if (count <= g->d_src_cap) return LGBC_OK;
+  dev_free(g->d_src);
+  g->d_src_cap = 0;
+  LGBC_TRY(dev_alloc(&g->d_src, static_cast<size_t>(std::max<int64_t>(count, 64))));
+  g->d_src_cap = std::max<int64_t>(count, 64);
+  return LGBC_OK;
+}
+
+int ensure_ms(lgbc_graph* g, bool need_sigma) {
+  MsWorkspace& w = g->ms;
+  const size_t n = static_cast<size_t>(g->n);
+  if (!w.visit) {
+    LGBC_TRY(dev_alloc(&w.visit, n));
+    LGBC_TRY(dev_alloc(&w.mb0, n));
+    LGBC_TRY(dev_alloc(&w.mb1, n));
+    LGBC_TRY(dev_alloc(&w.lvl_off, n + 3));
+    LGBC_TRY(dev_alloc(&w.ctl, 1));
+    LGBC_CUDA(cudaMemsetAsync(w.visit, 0, n * 8, g->stream));
+    LGBC_CUDA(cudaMemsetAsync(w.mb0, 0, n * 8, g->stream));
+    LGBC_CUDA(cudaMemsetAsync(w.mb1, 0, n * 8, g->stream));
+  }
+  if (!w.qv) {
+    const unsigned long long cap = 4ull * n + 1024;
+    LGBC_TRY(dev_alloc(&w.qv, cap));
+    LGBC_TRY(dev_alloc(&w.qm, cap));
+    w.cap = cap;
+  }
+  if (need_sigma && !w.have_sigma) {
+    unsigned long long* s = nullptr;
+    unsigned long long* p = nullptr;
+    LGBC_TRY(dev_alloc(&s, n * kMaxLanes));
+    int rc = dev_alloc(&p, n * kMaxLanes);
+    if (rc != LGBC_OK) {
+      cudaFree(s);
+      return rc;
+    }
+    w.sigma = s;
+    w.psi = p;
+    w.have_sigma = true;
+  }
+  return LGBC_OK;
+}
+
+int grow_ms_lists(lgbc_graph* g) {
+  MsWorkspace& w = g->ms;
+  const unsigned long long n = static_cast<unsigned long long>(g->n);
+  const unsigned long long max_cap = 65ull * n + 1024;  // 64 lanes x n levels + level 0
+  unsigned long long cap = std::min(max_cap, w.cap * 2);
+  if (cap <= w.cap) return fail(LGBC_ENOMEM, "level lists cannot grow further");
+  LGBC_CUDA(cudaStreamSynchronize(g->stream));
+  dev_free(w.qv);
+  dev_free(w.qm);
+  LGBC_TRY(dev_alloc(&w.qv, cap));
+  LGBC_TRY(dev_alloc(&w.qm, cap));
+  w.cap = cap;
+  return LGBC_OK;
+}
+
+int ensure_bfs(lgbc_graph* g) {
+  BfsWorkspace& w = g->bfs;
+  if (w.queue) return LGBC_OK;
+  const size_t n = static_cast<size_t>(g->n);
+  const size_t words = (n + 31) / 32 + 4;
+  LGBC_TRY(dev_alloc(&w.queue, n + 1));
+  LGBC_TRY(dev_alloc(&w.bm0, words));
+  LGBC_TRY(dev_alloc(&w.bm1, words));
+  LGBC_TRY(dev_alloc(&w.ctl, 1));
+  return LGBC_OK;
+}
+
+int ensure_dist(lgbc_graph* g, int64_t count) {
+  if (count <= g->d_dist_cap) return LGBC_OK;
+  dev_free(g->d_dist);
+  g->d_dist_cap = 0;
+  LGBC_TRY(dev_alloc(&g->d_dist, static_cast<size_t>(count)));
+  g->d_dist_cap = count;
+  return LGBC_OK;
+}
+
+int read_ctl(lgbc_graph* g, const BatchCtl* dctl) {
+  LGBC_CUDA(cudaMemcpyAsync(g->h_ctl, dctl, sizeof(BatchCtl), cudaMemcpyDeviceToHost, g->stream));
+  LGBC_CUDA(cudaStreamSynchronize(g->stream));
+  return LGBC_OK;
+}
+
+int check_launch(lgbc_graph* g) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+  (void)g;
+  return LGBC_OK;
+}
+
+MsBuffers ms_buffers(lgbc_graph* g, const int32_t* lane_src) {
+  MsWorkspace& w = g->ms;
+  MsBuffers b;
+  b.visit = w.visit;
+  b.mb[0] = w.mb0;
+  b.mb[1] = w.mb1;
+  b.sigma = w.sigma;
+  b.psi = w.psi;
+  b.qv = w.qv;
+  b.qm = w.qm;
+  b.lvl_off = w.lvl_off;
+  b.ctl = w.ctl;
+  b.lane_src = lane_src;
+  b.cap = w.cap;
+  return b;
+}
+
+// Direction choice for the next level of a multi-source batch: bottom-up when
+// the frontier's out-edges exceed the unfinished vertices' in-edges / alpha,
+// back to top-down when the frontier is smaller than n / beta (Beamer,
+// Asanovic & Patterson, SC 2012, applied to the union of the lanes).
+bool choose_bottom_up(const lgbc_graph* g, const BatchCtl& c, bool was_bu) {
+  const double mf = static_cast<double>(c.mf_cur);
+  const double mu = static_cast<double>(g->nnz) - static_cast<double>(c.mu_done);
+  const double nf = static_cast<double>(c.hi - c.lo);
+  if (was_bu) return nf >= static_cast<double>(g->n) / g->tune.beta;
+  return mf > mu / g->tune.alpha;
+}
+
+// One multi-source batch: forward level loop, then (with sigma) the backward
+// dependency sweep into bc.  Returns LGBC_OK, or 1 when the batch must be
+// replayed with FP64 path counts.
+int run_ms_batch(lgbc_graph* g, const int32_t* lane_src, int nl, int sigma_kind, double* bc,
+                 int32_t* dist, int64_t dist_ld) {
+  const DevGraph dg = g->dev();
+  const uint64_t act = nl >= 64 ? ~0ull : ((1ull << nl) - 1ull);
+  for (;;) {
+    MsBuffers b = ms_buffers(g, lane_src);
+    g->launches += ms_init(g->stream, dg, b, nl, sigma_kind, dist, dist_ld);
+    LGBC_TRY(check_launch(g));
+    bool bu = false;
+    bool regrow = false;
+    int64_t levels = 0;
+    for (;;) {
+      if (bu) {
+        g->launches += ms_bottomup(g->cfg, g->stream, dg, b, act, sigma_kind, dist, dist_ld);
+        g->stats.bottomup_levels++;
+      } else {
+        g->launches += ms_topdown(g->cfg, g->stream, dg, b, act, sigma_kind, dist, dist_ld);
+        g->stats.topdown_levels++;
+      }
+      g->launches += ms_advance(g->stream, dg, b);
+      LGBC_TRY(check_launch(g));
+      LGBC_TRY(read_ctl(g, b.ctl));
+      ++levels;
+      // every level settles at least one new (vertex, lane) pair, so a sweep
+      // longer than n + 1 levels can only mean a fault
+      if (levels > g->n + 1) return fail(LGBC_ETIMEOUT, "forward sweep exceeded n + 1 levels");
+      const BatchCtl& c = *g->h_ctl;
+      if (c.overflow_sigma && sigma_kind == kSigmaU64) break;
+      if (c.done) break;
+      if (c.overflow_list) {
+        regrow = true;
+        break;
+      }
+      bu = choose_bottom_up(g, c, bu);
+    }
+    g->stats.levels += levels;
+    if (regrow) {
+      LGBC_TRY(grow_ms_lists(g));
+      g->launches += ms_reset_all(g->stream, dg, ms_buffers(g, lane_src));
+      continue;
+    }
+    if (g->h_ctl->overflow_sigma && sigma_kind == kSigmaU64) {
+      g->launches += ms_reset_all(g->stream, dg, b);
+      return 1;
+    }
+    if (sigma_kind == kSigmaNone) {
+      g->launches += ms_cleanup_all(g->cfg, g->stream, b);
+      return check_launch(g);
+    }
+    const int maxl = g->h_ctl->maxlevel;
+    g->launches += ms_begin_backward(g->stream, b);
+    for (int L = maxl; L >= 0; --L)
+      g->launches += ms_backward_level(g->cfg, g->stream, dg, b, sigma_kind, bc);
+    g->launches += ms_cleanup(g->cfg, g->stream, b);
+    return check_launch(g);
+  }
+}
+
+// Brandes over the active sources already on the device (g->d_src[0, k)),
+// accumulating into bc_dev (zeroed here).
+int run_betweenness(lgbc_graph* g, int64_t k_act, int endpoints, double* bc_dev) {
+  g->launches += fill_f64(g->cfg, g->stream, bc_dev, g->n, 0.0);
+  if (k_act > 0) LGBC_TRY(ensure_ms(g, true));
+  const int lanes = std::max(1, std::min<int>(kMaxLanes, g->tune.lanes));
+  for (int64_t s0 = 0; s0 < k_act; s0 += lanes) {
+    const int nl = static_cast<int>(std::min<int64_t>(lanes, k_act - s0));
+    int rc = run_ms_batch(g, g->d_src + s0, nl, kSigmaU64, bc_dev, nullptr, 0);
+    if (rc == 1) {
+      g->stats.wide_batches++;
+      rc = run_ms_batch(g, g->d_src + s0, nl, kSigmaF64, bc_dev, nullptr, 0);
+    }
+    if (rc != LGBC_OK) return rc;
+    g->stats.batches++;
+  }
+  if (endpoints) g->launches += add_endpoints(g->cfg, g->stream, bc_dev, g->n, g->d_src, k_act);
+  return check_launch(g);
+}
+
+// Host-side part shared by the betweenness entry points: validate, filter
+// degree-0 sources (betweenness.jl:58) and upload the active list.
+int prepare_sources(lgbc_graph* g, const int32_t* src, int64_t nsrc, int64_t* k_act) {
+  std::vector<int32_t> active;
+  if (!src) {
+    active.reserve(static_cast<size_t>(g->n));
+    for (int64_t v = 0; v < g->n; ++v)
+      if (g->has_degree[static_cast<size_t>(v)]) active.push_back(static_cast<int32_t>(v));
+  } else {
+    LGBC_TRY(check_sources(g, src, nsrc));
+    active.reserve(static_cast<size_t>(nsrc));
+    for (int64_t i = 0; i < nsrc; ++i)
+      if (g->has_degree[static_cast<size_t>(src[i])]) active.push_back(src[i]);
+  }
+  *k_act = static_cast<int64_t>(active.size());
+  LGBC_TRY(ensure_src(g, *k_act));
+  if (*k_act > 0)
+    LGBC_CUDA(cudaMemcpyAsync(g->d_src, active.data(), active.size() * sizeof(int32_t),
+                              cudaMemcpyHostToDevice, g->stream));
+  // the pageable source vector must outlive the copy
+  LGBC_CUDA(cudaStreamSynchronize(g->stream));
+  return LGBC_OK;
+}
+
+void reset_stats(lgbc_graph* g) {
+  g->stats = lgbc_stats{};
+  g->stats.kernel_launches = g->launches;
+}
+
+void finish_stats(lgbc_graph* g) { g->stats.kernel_launches = g->launches - g->stats.kernel_launches; }
+
+// Fills a freshly constructed handle; on failure the caller destroys it.
+int create_impl(lgbc_graph* g, int64_t n, int64_t nnz, const int64_t* rowptr, const int32_t* colidx,
+                const int64_t* in_rowptr, const int32_t* in_colidx, int directed) {
+  LGBC_CUDA(cudaGetDevice(&g->device));
+  g->n = n;
+  g->nnz = nnz;
+  g->directed = directed ? 1 : 0;
+  cudaDeviceProp prop;
+  LGBC_CUDA(cudaGetDeviceProperties(&prop, g->device));
+  g->cfg.sms = prop.multiProcessorCount;
+  g->cfg.block = 256;
+  g->cfg.grid = prop.multiProcessorCount * 8;
+  g->max_smem = prop.sharedMemPerBlockOptin;
+  bfs_configure(g->max_smem);
+  LGBC_CUDA(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
+  LGBC_CUDA(cudaEventCreate(&g->ev_start));
+  LGBC_CUDA(cudaEventCreate(&g->ev_stop));
+  LGBC_CUDA(cudaMallocHost(reinterpret_cast<void**>(&g->h_ctl), sizeof(BatchCtl)));
+
+  LGBC_TRY(dev_alloc(&g->d_rowptr, static_cast<size_t>(n + 1)));
+  LGBC_TRY(dev_alloc(&g->d_colidx, static_cast<size_t>(nnz)));
+  LGBC_CUDA(cudaMemcpyAsync(g->d_rowptr, rowptr, static_cast<size_t>(n + 1) * 8,
+                            cudaMemcpyHostToDevice, g->stream));
+  if (nnz > 0)
+    LGBC_CUDA(cudaMemcpyAsync(g->d_colidx, colidx, static_cast<size_t>(nnz) * 4,
+                              cudaMemcpyHostToDevice, g->stream));
+  if (directed) {
+    LGBC_TRY(dev_alloc(&g->d_in_rowptr, static_cast<size_t>(n + 1)));
+    LGBC_TRY(dev_alloc(&g->d_in_colidx, static_cast<size_t>(nnz)));
+    LGBC_CUDA(cudaMemcpyAsync(g->d_in_rowptr, in_rowptr, static_cast<size_t>(n + 1) * 8,
+                              cudaMemcpyHostToDevice, g->stream));
+    if (nnz > 0)
+      LGBC_CUDA(cudaMemcpyAsync(g->d_in_colidx, in_colidx, static_cast<size_t>(nnz) * 4,
+                                cudaMemcpyHostToDevice, g->stream));
+  } else {
+    g->d_in_rowptr = g->d_rowptr;
+    g->d_in_colidx = g->d_colidx;
+  }
+  // the CSR is validated on the device: one pass over rowptr / colidx
+  int* d_bad = nullptr;
+  LGBC_TRY(dev_alloc(&d_bad, 1));
+  cudaMemsetAsync(d_bad, 0, sizeof(int), g->stream);
+  g->launches += validate_csr(g->cfg, g->stream, g->d_rowptr, g->d_colidx, n, nnz, d_bad);
+  if (directed)
+    g->launches += validate_csr(g->cfg, g->stream, g->d_in_rowptr, g->d_in_colidx, n, nnz, d_bad);
+  int bad = 0;
+  cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, g->stream);
+  // degree(g, v) > 0: in+out for digraphs (src/core.jl:66-67), kept on the host
+  g->has_degree.assign(static_cast<size_t>(n), 0);
+  for (int64_t v = 0; v < n; ++v) {
+    int64_t d = rowptr[v + 1] - rowptr[v];
+    if (directed) d += in_rowptr[v + 1] - in_rowptr[v];
+    g->has_degree[static_cast<size_t>(v)] = d > 0 ? 1 : 0;
+  }
+  cudaError_t e = cudaStreamSynchronize(g->stream);
+  cudaFree(d_bad);
+  if (e != cudaSuccess) return cuda_fail(e, "graph upload");
+  LGBC_TRY(check_launch(g));
+  if (bad & 1) return fail(LGBC_EINVAL, "rowptr must be non-decreasing");
+  if (bad & 2) return fail(LGBC_EINVAL, "column index out of range");
+  return LGBC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* lgbc_version(void) { return "lgbc 0.1.0 sm_103a"; }
+
+const char* lgbc_last_error(void) { return g_last_error.c_str(); }
+
+int lgbc_device_count(void) {
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return count;
+}
+
+int lgbc_graph_create(lgbc_graph** out, int64_t n, int64_t nnz, const int64_t* rowptr,
+                      const int32_t* colidx, const int64_t* in_rowptr, const int32_t* in_colidx,
+                      int directed) {
+  if (!out) return fail(LGBC_EINVAL, "null output handle pointer");
+  *out = nullptr;
+  if (n < 0 || nnz < 0) return fail(LGBC_EINVAL, "negative vertex or edge count");
+  if (n >= INT32_MAX) return fail(LGBC_EINVAL, "vertex ids must fit in int32");
+  if (!rowptr || (nnz > 0 && !colidx)) return fail(LGBC_EINVAL, "null CSR array");
+  if (directed && (!in_rowptr || (nnz > 0 && !in_colidx)))
+    return fail(LGBC_EINVAL, "a directed graph needs its in-CSR (badjlist)");
+  if (rowptr[0] != 0 || rowptr[n] != nnz) return fail(LGBC_EINVAL, "rowptr must run from 0 to nnz");
+  if (directed && (in_rowptr[0] != 0 || in_rowptr[n] != nnz))
+    return fail(LGBC_EINVAL, "in_rowptr must run from 0 to nnz");
+
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return fail(LGBC_ECUDA, std::string("no CUDA device available: ") +
+                                (e != cudaSuccess ? cudaGetErrorString(e) : "0 devices"));
+  }
+  lgbc_graph* g = new (std::nothrow) lgbc_graph();
+  if (!g) return fail(LGBC_ENOMEM, "host allocation failed");
+  const int rc = create_impl(g, n, nnz, rowptr, colidx, in_rowptr, in_colidx, directed);
+  if (rc != LGBC_OK) {
+    const std::string msg = g_last_error;
+    lgbc_graph_destroy(g);
+    g_last_error = msg;
+    return rc;
+  }
+  *out = g;
+  return LGBC_OK;
+}
+
+int lgbc_graph_destroy(lgbc_graph* g) {
+  if (!g) return LGBC_OK;
+  cudaSetDevice(g->device);
+  if (g->stream) cudaStreamSynchronize(g->stream);
+  g->ms.release();
+  g->bfs.release();
+  if (g->d_in_rowptr != g->d_rowptr) dev_free(g->d_in_rowptr);
+  if (g->d_in_colidx != g->d_colidx) dev_free(g->d_in_colidx);
+  dev_free(g->d_rowptr);
+  dev_free(g->d_colidx);
+  dev_free(g->d_src);
+  dev_free(g->d_bc);
+  dev_free(g->d_dist);
+  if (g->h_ctl) cudaFreeHost(g->h_ctl);
+  if (g->ev_start) cudaEventDestroy(g->ev_start);
+  if (g->ev_stop) cudaEventDestroy(g->ev_stop);
+  if (g->stream) cudaStreamDestroy(g->stream);
+  delete g;
+  return LGBC_OK;
+}
+
+int lgbc_graph_info(const lgbc_graph* g, int64_t* n, int64_t* nnz, int* directed) {
+  LGBC_TRY(check_graph(g));
+  if (n) *n = g->n;
+  if (nnz) *nnz = g->nnz;
+  if (directed) *directed = g->directed;
+  return LGBC_OK;
+}
+
+int lgbc_gdistances(lgbc_graph* g, const int32_t* src, int64_t nsrc, int32_t* dist_out) {
+  LGBC_TRY(check_graph(g));
+  std::lock_guard<std::mutex> lock(g->mu);
+  LGBC_TRY(use_device(g));
+  if (!dist_out && g->n > 0) return fail(LGBC_EINVAL, "null output");
+  LGBC_TRY(check_sources(g, src, nsrc));
+  reset_stats(g);
+  if (g->n == 0) return LGBC_OK;
+  LGBC_TRY(ensure_bfs(g));
+  LGBC_TRY(ensure_dist(g, g->n));
+  LGBC_TRY(ensure_src(g, nsrc));
+  if (nsrc > 0)
+    LGBC_CUDA(cudaMemcpyAsync(g->d_src, src, static_cast<size_t>(nsrc) * 4, cudaMemcpyHostToDevice,
+                              g->stream));
+  const DevGraph dg = g->dev();
+  BfsBuffers b{g->bfs.queue, {g->bfs.bm0, g->bfs.bm1}, g->bfs.ctl};
+  g->launches += fill_i32(g->cfg, g->stream, g->d_dist, g->n, kUnreached);
+  g->launches += bfs_init(g->cfg, g->stream, dg, b, g->d_src, nsrc, g->d_dist);
+  LGBC_TRY(check_launch(g));
+  LGBC_TRY(read_ctl(g, b.ctl));
+  const size_t bm_bytes = static_cast<size_t>(((g->n + 31) / 32 + 3) & ~int64_t(3)) * 4;
+  const int stage = bm_bytes <= g->max_smem ? 1 : 0;
+  bool bu = false;
+  while (!g->h_ctl->done) {
+    const BatchCtl& c = *g->h_ctl;
+    const double mf = static_cast<double>(c.mf_cur);
+    const double mu = static_cast<double>(g->nnz) - static_cast<double>(c.mu_done);
+    const double nf = static_cast<double>(c.hi - c.lo);
+    bu = bu ? (nf >= static_cast<double>(g->n) / g->tune.beta) : (mf > mu / g->tune.alpha);
+    if (bu) {
+      g->launches += bfs_bottomup(g->cfg, g->stream, dg, b, g->d_dist, stage);
+      g->stats.bottomup_levels++;
+    } else {
+      g->launches += bfs_topdown(g->cfg, g->stream, dg, b, g->d_dist);
+      g->stats.topdown_levels++;
+    }
+    g->launches += bfs_advance(g->stream, b);
+    LGBC_TRY(check_launch(g));
+    LGBC_TRY(read_ctl(g, b.ctl));
+    g->stats.levels++;
+    if (g->stats.levels > g->n + 1) return fail(LGBC_ETIMEOUT, "BFS exceeded n + 1 levels");
+  }
+  LGBC_CUDA(cudaMemcpyAsync(dist_out, g->d_dist, static_cast<size_t>(g->n) * 4,
+                            cudaMemcpyDeviceToHost, g->stream));
+  LGBC_CUDA(cudaStreamSynchronize(g->stream));
+  finish_stats(g);
+  return LGBC_OK;
+}
+
+int lgbc_gdistances_batch(lgbc_graph* g, const int32_t* src, int64_t nsrc, int32_t* dist_out) {
+  LGBC_TRY(check_graph(g));
+  std::lock_guard<std::mutex> lock(g->mu);
+  LGBC_TRY(use_device(g));
+  LGBC_TRY(check_sources(g, src, nsrc));
+  if (nsrc > 0 && g->n > 0 && !dist_out) return fail(LGBC_EINVAL, "null output");
+  reset_stats(g);
+  if (nsrc == 0 || g->n == 0) return LGBC_OK;
+  LGBC_TRY(ensure_ms(g, false));
+  LGBC_TRY(ensure_src(g, nsrc));
+  LGBC_CUDA(cudaMemcpyAsync(g->d_src, src, static_cast<size_t>(nsrc) * 4, cudaMemcpyHostToDevice,
+                            g->stream));
+  const int lanes = kMaxLanes;
+  LGBC_TRY(ensure_dist(g, static_cast<int64_t>(lanes) * g->n));
+  for (int64_t s0 = 0; s0 < nsrc; s0 += lanes) {
+    const int nl = static_cast<int>(std::min<int64_t>(lanes, nsrc - s0));
+    g->launches += fill_i32(g->cfg, g->stream, g->d_dist, static_cast<int64_t>(nl) * g->n, kUnreached);
+    LGBC_TRY(run_ms_batch(g, g->d_src + s0, nl, kSigmaNone, nullptr, g->d_dist, g->n));
+    LGBC_CUDA(cudaMemcpyAsync(dist_out + s0 * g->n, g->d_dist,
+                              static_cast<size_t>(nl) * static_cast<size_t>(g->n) * 4,
+                              cudaMemcpyDeviceToHost, g->stream));
+    g->stats.batches++;
+  }
+  LGBC_CUDA(cudaStreamSynchronize(g->stream));
+  finish_stats(g);
+  return LGBC_OK;
+}
+
+int lgbc_betweenness_dev(lgbc_graph* g, const int32_t* src, int64_t nsrc, int endpoints,
+                         double* bc_raw_dev) {
+  LGBC_TRY(check_graph(g));
+  std::lock_guard<std::mutex> lock(g->mu);
+  LGBC_TRY(use_device(g));
+  if (!bc_raw_dev && g->n > 0) return fail(LGBC_EINVAL, "null output");
+  reset_stats(g);
+  int64_t k_act = 0;
+  LGBC_TRY(prepare_sources(g, src, nsrc, &k_act));
+  g->stats.active_sources = k_act;
+  LGBC_TRY(run_betweenness(g, k_act, endpoints, bc_raw_dev));
+  finish_stats(g);
+  return LGBC_OK;
+}
+
+int lgbc_betweenness(lgbc_graph* g, const int32_t* src, int64_t nsrc, int endpoints,
+                     double* bc_raw_out) {
+  LGBC_TRY(check_graph(g));
+  std::lock_guard<std::mutex> lock(g->mu);
+  LGBC_TRY(use_device(g));
+  if (!bc_raw_out && g->n > 0) return fail(LGBC_EINVAL, "null output");
+  reset_stats(g);
+  int64_t k_act = 0;
+  LGBC_TRY(prepare_sources(g, src, nsrc, &k_act));
+  g->stats.active_sources = k_act;
+  if (g->n == 0) return LGBC_OK;
+  if (!g->d_bc) LGBC_TRY(dev_alloc(&g->d_bc, static_cast<size_t>(g->n)));
+  LGBC_TRY(run_betweenness(g, k_act, endpoints, g->d_bc));
+  LGBC_CUDA(cudaMemcpyAsync(bc_raw_out, g->d_bc, static_cast<size_t>(g->n) * 8,
+                            cudaMemcpyDeviceToHost, g->stream));
+  LGBC_CUDA(cudaStreamSynchronize(g->stream));
+  finish_stats(g);
+  return LGBC_OK;
+}
+
+int lgbc_graph_sync(lgbc_graph* g) {
+  LGBC_TRY(check_graph(g));
+  LGBC_TRY(use_device(g));
+  LGBC_CUDA(cudaStreamSynchronize(g->stream));
+  return LGBC_OK;
+}
+
+int lgbc_timer_start(lgbc_graph* g) {
+  LGBC_TRY(check_graph(g));
+  LGBC_TRY(use_device(g));
+  g->launches_at_start = g->launches;
+  LGBC_CUDA(cudaEventRecord(g->ev_start, g->stream));
+  return LGBC_OK;
+}
+
+int lgbc_timer_stop(lgbc_graph* g, double* elapsed_ms, int64_t* kernel_launches) {
+  LGBC_TRY(check_graph(g));
+  LGBC_TRY(use_device(g));
+  LGBC_CUDA(cudaEventRecord(g->ev_stop, g->stream));
+  LGBC_CUDA(cudaEventSynchronize(g->ev_stop));
+  float ms = 0.f;
+  LGBC_CUDA(cudaEventElapsedTime(&ms, g->ev_start, g->ev_stop));
+  if (elapsed_ms) *elapsed_ms = ms;
+  if (kernel_launches) *kernel_launches = g->launches - g->launches_at_start;
+  return LGBC_OK;
+}
+
+int lgbc_graph_stats(const lgbc_graph* g, lgbc_stats* out) {
+  LGBC_TRY(check_graph(g));
+  if (!out) return fail(LGBC_EINVAL, "null output");
+  *out = g->stats;
+  return LGBC_OK;
+}
+
+int lgbc_get_tuning(const lgbc_graph* g, lgbc_tuning* out) {
+  LGBC_TRY(check_graph(g));
+  if (!out) return fail(LGBC_EINVAL, "null output");
+  *out = g->tune;
+  return LGBC_OK;
+}
+
+int lgbc_set_tuning(lgbc_graph* g, const lgbc_tuning* t) {
+  LGBC_TRY(check_graph(g));
+  if (!t) return fail(LGBC_EINVAL, "null tuning");
+  if (!(t->alpha > 0) || !(t->beta > 0) || t->lanes < 1 || t->lanes > kMaxLanes || t->hub_degree < 1)
+    return fail(LGBC_EINVAL, "tuning out of range (alpha, beta > 0; 1 <= lanes <= 64; hub_degree >= 1)");
+  std::lock_guard<std::mutex> lock(g->mu);
+  g->tune = *t;
+  return LGBC_OK;
+}
+
+int lgbc_device_alloc(void** ptr, int64_t bytes) {
+  if (!ptr || bytes < 0) return fail(LGBC_EINVAL, "bad allocation request");
+  cudaError_t e = cudaMalloc(ptr, static_cast<size_t>(std::max<int64_t>(bytes, 1)));
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    *ptr = nullptr;
+    return fail(LGBC_ENOMEM, std::string("cudaMalloc failed: ") + cudaGetErrorString(e));
+  }
+  return LGBC_OK;
+}
+
+int lgbc_device_free(void* ptr) {
+  if (ptr) LGBC_CUDA(cudaFree(ptr));
+  return LGBC_OK;
+}
+
+int lgbc_host_alloc(void** ptr, int64_t bytes) {
+  if (!ptr || bytes < 0) return fail(LGBC_EINVAL, "bad allocation request");
+  cudaError_t e = cudaMallocHost(ptr, static_cast<size_t>(std::max<int64_t>(bytes, 1)));
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    *ptr = nullptr;
+    return fail(LGBC_ENOMEM, std::string("cudaMallocHost failed: ") + cudaGetErrorString(e));
+  }
+  return LGBC_OK;
+}
+
+int lgbc_host_free(void* ptr) {
+  if (ptr) LGBC_CUDA(cudaFreeHost(ptr));
+  return LGBC_OK;
+}
+
+int lgbc_memcpy(void* dst, const void* src, int64_t bytes, int kind) {
+  if (bytes < 0 || (bytes > 0 && (!dst || !src))) return fail(LGBC_EINVAL, "bad copy request");
+  cudaMemcpyKind k;
+  switch (kind) {
+    case 1: k = cudaMemcpyHostToDevice; break;
+    case 2: k = cudaMemcpyDeviceToHost; break;
+    case 3: k = cudaMemcpyDeviceToDevice; break;
+    default: return fail(LGBC_EINVAL, "copy kind must be 1, 2 or 3");
+  }
+  if (bytes > 0) LGBC_CUDA(cudaMemcpy(dst, src, static_cast<size_t>(bytes), k));
+  return LGBC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,87 @@
+// lgbc_kernels.h -- host-side launch wrappers shared by the CUDA translation
+// units of the lgbc library.  Every wrapper returns the number of kernels it
+// queued, which the API layer counts for lgbc_stats / lgbc_timer_stop.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "lgbc_internal.cuh"
+
+namespace lgbc {
+
+// Path-count representation of a multi-source batch.
+enum SigmaKind : int {
+  kSigmaNone = 0,  // distances only (gdistances_batch)
+  kSigmaU64 = 1,   // exact uint64 path counts, df dependency sums
+  kSigmaF64 = 2,   // FP64 path counts and dependencies (replay after overflow)
+};
+
+struct LaunchCfg {
+  int grid;     // blocks for grid-stride kernels
+  int block;    // threads per block
+  int sms;      // streaming multiprocessors on the device
+};
+
+// ---- multi-source (bit-lane) BFS and Brandes sweeps: msbfs.cu ----------
+// Per-batch device buffers.  Lane l of vertex v lives at [v * 64 + l].
+struct MsBuffers {
+  uint64_t* visit;     // n: lanes that have reached v
+  uint64_t* mb[2];     // n each: dense level masks, F_L lives in mb[L & 1]
+  void* sigma;         // n * 64: uint64 or double path counts
+  void* psi;           // n * 64: df32 or double, (1 + delta) / sigma
+  int32_t* qv;         // cap: concatenated level lists (vertex)
+  uint64_t* qm;        // cap: lanes of that vertex at that level
+  unsigned long long* lvl_off;  // n + 3: start of each level's list
+  BatchCtl* ctl;       // control block
+  const int32_t* lane_src;      // sources of the batch (device)
+  unsigned long long cap;       // entries in qv / qm
+};
+
+int ms_init(cudaStream_t s, const DevGraph& g, const MsBuffers& b, int nlanes, int sigma_kind,
+            int32_t* dist, int64_t dist_ld);
+int ms_topdown(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
+               uint64_t act, int sigma_kind, int32_t* dist, int64_t dist_ld);
+int ms_bottomup(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
+                uint64_t act, int sigma_kind, int32_t* dist, int64_t dist_ld);
+int ms_advance(cudaStream_t s, const DevGraph& g, const MsBuffers& b);
+// Set ctl->level = maxlevel for the backward sweep (on the device).
+int ms_begin_backward(cudaStream_t s, const MsBuffers& b);
+// Backward (dependency) step for the level in ctl->level, then level--.
+int ms_backward_level(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
+                      int sigma_kind, double* bc);
+// After the backward sweep: clear the masks of levels 0 and 1.
+int ms_cleanup(const LaunchCfg& c, cudaStream_t s, const MsBuffers& b);
+// After a distance-only batch: clear visit / masks of every listed vertex.
+int ms_cleanup_all(const LaunchCfg& c, cudaStream_t s, const MsBuffers& b);
+// Zero visit and both mask buffers outright (after an aborted batch).
+int ms_reset_all(cudaStream_t s, const DevGraph& g, const MsBuffers& b);
+
+// ---- single multi-source BFS (gdistances): bfs.cu ------------------------
+struct BfsBuffers {
+  int32_t* queue;               // n: every level, concatenated
+  uint32_t* bm[2];              // (n + 31) / 32 words each: frontier bitmaps
+  BatchCtl* ctl;
+};
+int bfs_init(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const BfsBuffers& b,
+             const int32_t* src, int64_t nsrc, int32_t* dist);
+int bfs_topdown(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const BfsBuffers& b,
+                int32_t* dist);
+int bfs_bottomup(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const BfsBuffers& b,
+                 int32_t* dist, int stage_smem);
+int bfs_advance(cudaStream_t s, const BfsBuffers& b);
+// Largest dynamic shared memory the bottom-up kernel may stage (bytes).
+int bfs_configure(size_t max_dyn_smem);
+
+// ---- small utilities: util.cu ----------------------------------------------
+// ORs into *bad: 1 = rowptr decreases somewhere, 2 = a column index is not in [0, n).
+int validate_csr(const LaunchCfg& c, cudaStream_t s, const int64_t* rowptr, const int32_t* colidx,
+                 int64_t n, int64_t nnz, int* bad);
+int fill_i32(const LaunchCfg& c, cudaStream_t s, int32_t* p, int64_t count, int32_t value);
+int fill_f64(const LaunchCfg& c, cudaStream_t s, double* p, int64_t count, double value);
+// bc[v] += k_act for every v, then bc[s] += n - 2 for each active source s:
+// the endpoint terms of _accumulate_endpoints! summed over the sources.
+int add_endpoints(const LaunchCfg& c, cudaStream_t s, double* bc, int64_t n,
+                  const int32_t* active_src, int64_t k_act);
+
+}  // namespace lgbc

@@ -1,0 +1,606 @@
+// msbfs.cu -- multi-source (bit-lane) BFS with path counting and the
+// reverse-level dependency sweep of Brandes' algorithm.
+//
+// Replaces, for up to 64 sources at once, the per-source loop body of
+// betweenness_centrality (src/centrality/betweenness.jl:57-67):
+//   forward  = dijkstra_shortest_paths(g, s; allpaths=true, trackvertices=true)
+//              with unit weights (src/shortestpaths/dijkstra.jl:59-141): the
+//              distance levels and the path counts sigma (:102,118)
+//   backward = _accumulate_basic! (:81-107): delta[v] = sum over DAG
+//              successors w of sigma[v] / sigma[w] * (1 + delta[w]), added to
+//              betweenness[v] for v != s.
+// Unit-weight Dijkstra visits vertices in BFS level order, and its
+// predecessor lists are exactly the in-neighbours one level closer to the
+// source, so a level-synchronous BFS reproduces sigma exactly (integers
+// below 2^64 here; the reference's Float64 sums are exact below 2^53) and the
+// dependencies up to summation order.
+//
+// Layout in HBM (per batch of <= 64 sources, "lanes"):
+//   visit[v]          uint64  lanes that reached v
+//   mb[L & 1][v]      uint64  lanes for which v is at level L (dense)
+//   sigma[v*64 + l]   uint64 path count (or FP64 in the overflow replay)
+//   psi[v*64 + l]     df32 (1 + delta) / sigma (or FP64)
+//   qv/qm             concatenated per-level lists of (vertex, lane mask)
+// A warp owns one vertex; thread t owns lanes 2t and 2t+1, so a vertex's
+// 64 lanes are one 512-byte row read by 32 coalesced 16-byte accesses.
+#include "lgbc_kernels.h"
+
+namespace lgbc {
+namespace {
+
+__device__ __forceinline__ long long gwarp() {
+  return (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+}
+__device__ __forceinline__ long long nwarps() {
+  return (static_cast<long long>(gridDim.x) * blockDim.x) >> 5;
+}
+
+// Level-parity buffer select (a runtime index into the by-value array would
+// force the parameter struct into local memory).
+__device__ __forceinline__ uint64_t* mb_at(const MsBuffers& b, int level) {
+  return (level & 1) ? b.mb[1] : b.mb[0];
+}
+
+template <int SK> struct Sig;
+template <> struct Sig<kSigmaNone> {
+  using T = unsigned long long;
+  using Pair = ulonglong2;
+};
+template <> struct Sig<kSigmaU64> {
+  using T = unsigned long long;
+  using Pair = ulonglong2;
+};
+template <> struct Sig<kSigmaF64> {
+  using T = double;
+  using Pair = double2;
+};
+
+__device__ __forceinline__ void sig_add(unsigned long long& a, unsigned long long x, bool& ovf) {
+  unsigned long long t = a + x;
+  ovf |= (t < a);
+  a = t;
+}
+__device__ __forceinline__ void sig_add(double& a, double x, bool&) { a += x; }
+
+template <class P, class T> __device__ __forceinline__ P make_pair2(T a, T b);
+template <> __device__ __forceinline__ ulonglong2 make_pair2(unsigned long long a, unsigned long long b) {
+  return make_ulonglong2(a, b);
+}
+template <> __device__ __forceinline__ double2 make_pair2(double a, double b) {
+  return make_double2(a, b);
+}
+
+// Store the path counts of lanes (2t, 2t+1) of w that are set in `mask`.
+template <int SK>
+__device__ __forceinline__ void store_sigma(void* sigma, int32_t w, uint64_t mask,
+                                            typename Sig<SK>::T a0, typename Sig<SK>::T a1) {
+  using T = typename Sig<SK>::T;
+  using P = typename Sig<SK>::Pair;
+  const int ln = lane_id();
+  unsigned my = static_cast<unsigned>(mask >> (2 * ln)) & 3u;
+  if (my == 3u) {
+    reinterpret_cast<P*>(sigma)[static_cast<int64_t>(w) * 32 + ln] = make_pair2<P, T>(a0, a1);
+  } else if (my == 1u) {
+    reinterpret_cast<T*>(sigma)[static_cast<int64_t>(w) * 64 + 2 * ln] = a0;
+  } else if (my == 2u) {
+    reinterpret_cast<T*>(sigma)[static_cast<int64_t>(w) * 64 + 2 * ln + 1] = a1;
+  }
+}
+
+__device__ __forceinline__ void store_dist(int32_t* dist, int64_t ld, int32_t w, uint64_t mask,
+                                           int32_t level) {
+  const int ln = lane_id();
+  unsigned my = static_cast<unsigned>(mask >> (2 * ln)) & 3u;
+  if (my & 1u) dist[static_cast<int64_t>(2 * ln) * ld + w] = level;
+  if (my & 2u) dist[static_cast<int64_t>(2 * ln + 1) * ld + w] = level;
+}
+
+// Pull over the in-neighbours v of w: f = front[v] & want marks the lanes for
+// which v is a predecessor of w one level up.  Accumulates the predecessors'
+// path counts into (a0, a1) for this thread's lanes and returns the OR of all
+// f (the lanes that discover w).  With SK == kSigmaNone it stops as soon as
+// every wanted lane is found.
+template <int SK>
+__device__ __forceinline__ uint64_t pull_lanes(const int64_t* __restrict__ rp,
+                                               const int32_t* __restrict__ ci, int32_t w,
+                                               uint64_t want, const uint64_t* __restrict__ front,
+                                               const void* __restrict__ sigma,
+                                               typename Sig<SK>::T& a0, typename Sig<SK>::T& a1,
+                                               bool& ovf) {
+  using P = typename Sig<SK>::Pair;
+  const int ln = lane_id();
+  const int64_t e0 = rp[w], e1 = rp[w + 1];
+  uint64_t found = 0;
+  for (int64_t e = e0; e < e1; e += kWarp) {
+    const int64_t idx = e + ln;
+    int32_t v = 0;
+    uint64_t f = 0;
+    if (idx < e1) {
+      v = ci[idx];
+      f = front[v] & want;
+    }
+    if (SK == kSigmaNone) {
+      found |= f;
+      if (warp_or_u64(found) == want) break;
+      continue;
+    }
+    found |= f;
+    unsigned bal = __ballot_sync(kFull, f != 0);
+    while (bal) {
+      const int j = __ffs(bal) - 1;
+      bal &= bal - 1;
+      const int32_t vj = __shfl_sync(kFull, v, j);
+      const uint64_t fj = shfl_u64(f, j);
+      const unsigned my = static_cast<unsigned>(fj >> (2 * ln)) & 3u;
+      if (my) {
+        const P p = reinterpret_cast<const P*>(sigma)[static_cast<int64_t>(vj) * 32 + ln];
+        if (my & 1u) sig_add(a0, p.x, ovf);
+        if (my & 2u) sig_add(a1, p.y, ovf);
+      }
+    }
+  }
+  return warp_or_u64(found);
+}
+
+// ---------------------------------------------------------------------------
+// Batch initialisation: level 0 = the sources (one lane each; a repeated
+// source gets several lanes in one list entry).
+// ---------------------------------------------------------------------------
+template <int SK>
+__global__ void k_ms_init(DevGraph g, MsBuffers b, int nl, unsigned long long cap, int32_t* dist,
+                          int64_t ld) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  using T = typename Sig<SK>::T;
+  const uint64_t act = nl >= 64 ? ~0ull : ((1ull << nl) - 1ull);
+  uint64_t* front = b.mb[0];
+  unsigned long long tail = 0, mf = 0, mu = 0;
+  for (int l = 0; l < nl; ++l) {
+    const int32_t s = b.lane_src[l];
+    const uint64_t old = front[s];
+    front[s] = old | (1ull << l);
+    if (old == 0) {
+      b.qv[tail++] = s;
+      mf += static_cast<unsigned long long>(g.rowptr[s + 1] - g.rowptr[s]);
+    }
+    if (SK != kSigmaNone) reinterpret_cast<T*>(b.sigma)[static_cast<int64_t>(s) * 64 + l] = T(1);
+    if (dist) dist[static_cast<int64_t>(l) * ld + s] = 0;
+  }
+  for (unsigned long long i = 0; i < tail; ++i) {
+    const int32_t s = b.qv[i];
+    const uint64_t m = front[s];
+    b.qm[i] = m;
+    b.visit[s] = m;
+    if (m == act) mu += static_cast<unsigned long long>(g.in_rowptr[s + 1] - g.in_rowptr[s]);
+  }
+  BatchCtl* c = b.ctl;
+  c->lo = 0;
+  c->hi = tail;
+  c->tail = tail;
+  c->mf = 0;
+  c->mf_cur = mf;
+  c->mu_done = mu;
+  c->cap = cap;
+  c->level = 0;
+  c->maxlevel = 0;
+  c->done = 0;
+  c->overflow_list = 0;
+  c->overflow_sigma = 0;
+  c->mode = 0;
+  b.lvl_off[0] = 0;
+  b.lvl_off[1] = tail;
+}
+
+// ---------------------------------------------------------------------------
+// Top-down, phase 1: expand Q_L over out-edges; the first lane set on a new
+// vertex appends it to Q_{L+1}.  next[w] collects the discovering lanes.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_ms_td_discover(DevGraph g, MsBuffers b) {
+  BatchCtl* c = b.ctl;
+  const unsigned long long lo = c->lo, hi = c->hi;
+  const int L = c->level;
+  const uint64_t* __restrict__ visit = b.visit;
+  uint64_t* next = mb_at(b, L + 1);
+  const int ln = lane_id();
+  for (unsigned long long i = lo + gwarp(); i < hi; i += nwarps()) {
+    const int32_t v = b.qv[i];
+    const uint64_t F = b.qm[i];
+    const int64_t e0 = g.rowptr[v], e1 = g.rowptr[v + 1];
+    for (int64_t e = e0; e < e1; e += kWarp) {
+      const int64_t idx = e + ln;
+      bool app = false;
+      int32_t w = 0;
+      if (idx < e1) {
+        w = g.colidx[idx];
+        const uint64_t m = F & ~visit[w];
+        if (m) {
+          const unsigned long long old =
+              atomicOr(reinterpret_cast<unsigned long long*>(next + w), m);
+          app = (old == 0);
+        }
+      }
+      const unsigned long long slot = warp_append(app, &c->tail);
+      if (app) b.qv[slot] = w;
+    }
+  }
+}
+
+// Top-down, phase 2: for every vertex appended in phase 1, record its lane
+// mask, mark it visited and pull its path counts from its predecessors.
+template <int SK, bool DIST>
+__global__ void __launch_bounds__(256) k_ms_td_settle(DevGraph g, MsBuffers b, uint64_t act,
+                                                      int32_t* dist, int64_t ld) {
+  using T = typename Sig<SK>::T;
+  BatchCtl* c = b.ctl;
+  const unsigned long long lo = c->hi, hi = c->tail;
+  const int L = c->level;
+  const uint64_t* __restrict__ front = mb_at(b, L);
+  const uint64_t* __restrict__ next = mb_at(b, L + 1);
+  const int ln = lane_id();
+  unsigned long long mf = 0, mu = 0;
+  bool ovf = false;
+  for (unsigned long long i = lo + gwarp(); i < hi; i += nwarps()) {
+    const int32_t w = b.qv[i];
+    const uint64_t mask = next[w];
+    if (ln == 0) {
+      const uint64_t nv = b.visit[w] | mask;
+      b.qm[i] = mask;
+      b.visit[w] = nv;
+      mf += static_cast<unsigned long long>(g.rowptr[w + 1] - g.rowptr[w]);
+      if (nv == act) mu += static_cast<unsigned long long>(g.in_rowptr[w + 1] - g.in_rowptr[w]);
+    }
+    if (SK != kSigmaNone) {
+      T a0 = T(0), a1 = T(0);
+      pull_lanes<SK>(g.in_rowptr, g.in_colidx, w, mask, front, b.sigma, a0, a1, ovf);
+      store_sigma<SK>(b.sigma, w, mask, a0, a1);
+    }
+    if (DIST) store_dist(dist, ld, w, mask, L + 1);
+  }
+  if (SK == kSigmaU64 && __any_sync(kFull, ovf) && ln == 0) c->overflow_sigma = 1;
+  if (ln == 0) {
+    if (mf) atomicAdd(&c->mf, mf);
+    if (mu) atomicAdd(&c->mu_done, mu);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Bottom-up: every vertex some lane has not reached scans its in-neighbours
+// for predecessors in the current frontier.  A warp takes 32 consecutive
+// vertices, so its discoveries are appended with one atomic.
+// ---------------------------------------------------------------------------
+template <int SK, bool DIST>
+__global__ void __launch_bounds__(256) k_ms_bu(DevGraph g, MsBuffers b, uint64_t act,
+                                               int32_t* dist, int64_t ld) {
+  using T = typename Sig<SK>::T;
+  BatchCtl* c = b.ctl;
+  const int L = c->level;
+  const uint64_t* __restrict__ front = mb_at(b, L);
+  uint64_t* next = mb_at(b, L + 1);
+  const int64_t n = g.n;
+  const int ln = lane_id();
+  unsigned long long mf = 0, mu = 0;
+  bool ovf = false;
+  for (int64_t base = gwarp() * kWarp; base < n; base += nwarps() * kWarp) {
+    const int64_t wme = base + ln;
+    uint64_t vis = 0;
+    bool cand = false;
+    if (wme < n) {
+      vis = b.visit[wme];
+      cand = (vis != act) && (g.in_rowptr[wme + 1] > g.in_rowptr[wme]);
+    }
+    unsigned cb = __ballot_sync(kFull, cand);
+    uint64_t my_nm = 0;
+    while (cb) {
+      const int j = __ffs(cb) - 1;
+      cb &= cb - 1;
+      const int32_t w = static_cast<int32_t>(base + j);
+      const uint64_t want = act & ~shfl_u64(vis, j);
+      T a0 = T(0), a1 = T(0);
+      const uint64_t nm =
+          pull_lanes<SK>(g.in_rowptr, g.in_colidx, w, want, front, b.sigma, a0, a1, ovf);
+      if (nm) {
+        if (SK != kSigmaNone) store_sigma<SK>(b.sigma, w, nm, a0, a1);
+        if (DIST) store_dist(dist, ld, w, nm, L + 1);
+      }
+      if (ln == j) my_nm = nm;
+    }
+    const bool app = my_nm != 0;
+    const unsigned long long slot = warp_append(app, &c->tail);
+    if (app) {
+      b.qv[slot] = static_cast<int32_t>(wme);
+      b.qm[slot] = my_nm;
+      next[wme] = my_nm;
+      const uint64_t nv = vis | my_nm;
+      b.visit[wme] = nv;
+      mf += static_cast<unsigned long long>(g.rowptr[wme + 1] - g.rowptr[wme]);
+      if (nv == act) mu += static_cast<unsigned long long>(g.in_rowptr[wme + 1] - g.in_rowptr[wme]);
+    }
+  }
+  if (SK == kSigmaU64 && __any_sync(kFull, ovf) && ln == 0) c->overflow_sigma = 1;
+  mf = warp_sum_u64(mf);
+  mu = warp_sum_u64(mu);
+  if (ln == 0) {
+    if (mf) atomicAdd(&c->mf, mf);
+    if (mu) atomicAdd(&c->mu_done, mu);
+  }
+}
+
+// After a level: clear the old frontier's dense masks (kept when the forward
+// sweep just ended, because the backward sweep starts from them).
+__global__ void k_ms_clear_front(MsBuffers b) {
+  BatchCtl* c = b.ctl;
+  if (c->tail == c->hi) return;
+  const unsigned long long lo = c->lo, hi = c->hi;
+  uint64_t* front = mb_at(b, c->level);
+  for (unsigned long long i = lo + blockIdx.x * blockDim.x + threadIdx.x; i < hi;
+       i += static_cast<unsigned long long>(gridDim.x) * blockDim.x)
+    front[b.qv[i]] = 0;
+}
+
+__global__ void k_ms_advance(MsBuffers b, int64_t n) {
+  BatchCtl* c = b.ctl;
+  const int L = c->level;
+  b.lvl_off[L + 2] = c->tail;
+  if (c->tail == c->hi) {
+    c->done = 1;
+    c->maxlevel = L;
+    c->mf_cur = 0;
+    return;
+  }
+  c->lo = c->hi;
+  c->hi = c->tail;
+  c->level = L + 1;
+  c->mf_cur = c->mf;
+  c->mf = 0;
+  if (c->cap - c->tail < static_cast<unsigned long long>(n)) c->overflow_list = 1;
+}
+
+__global__ void k_ms_begin_backward(MsBuffers b) { b.ctl->level = b.ctl->maxlevel; }
+
+// Backward step at level L, part 1: mb[L & 1] still holds F_{L+2}; clear it.
+__global__ void k_ms_back_clear(MsBuffers b) {
+  BatchCtl* c = b.ctl;
+  const int L = c->level;
+  if (L + 2 > c->maxlevel) return;
+  const unsigned long long lo = b.lvl_off[L + 2], hi = b.lvl_off[L + 3];
+  uint64_t* other = mb_at(b, L);
+  for (unsigned long long i = lo + blockIdx.x * blockDim.x + threadIdx.x; i < hi;
+       i += static_cast<unsigned long long>(gridDim.x) * blockDim.x)
+    other[b.qv[i]] = 0;
+}
+
+// Backward step at level L, part 2 (pull): for every (v, lane) at level L,
+//   delta = sigma[v] * sum_{w in out(v), lane at level L+1 of w} psi[w]
+//   psi[v] = (1 + delta) / sigma[v]
+// and betweenness[v] += sum over lanes of delta (level 0 = sources: skipped,
+// as _accumulate_basic! skips w == s, betweenness.jl:102).
+// psi is the reference's `coeff` (betweenness.jl:96) stored once per vertex.
+template <int SK>
+__global__ void __launch_bounds__(256) k_ms_delta(DevGraph g, MsBuffers b, double* bc) {
+  BatchCtl* c = b.ctl;
+  const int L = c->level;
+  const unsigned long long lo = b.lvl_off[L], hi = b.lvl_off[L + 1];
+  const uint64_t* __restrict__ succ = mb_at(b, L + 1);
+  uint64_t* other = mb_at(b, L);
+  const int ln = lane_id();
+  for (unsigned long long i = lo + gwarp(); i < hi; i += nwarps()) {
+    const int32_t v = b.qv[i];
+    const uint64_t F = b.qm[i];
+    if (ln == 0) {
+      other[v] = F;
+      b.visit[v] = 0;
+    }
+    if (L == 0) continue;
+    const int64_t e0 = g.rowptr[v], e1 = g.rowptr[v + 1];
+    const unsigned mine = static_cast<unsigned>(F >> (2 * ln)) & 3u;
+    if (SK == kSigmaU64) {
+      df32 acc0{0.f, 0.f}, acc1{0.f, 0.f};
+      for (int64_t e = e0; e < e1; e += kWarp) {
+        const int64_t idx = e + ln;
+        int32_t w = 0;
+        uint64_t gm = 0;
+        if (idx < e1) {
+          w = g.colidx[idx];
+          gm = succ[w] & F;
+        }
+        unsigned bal = __ballot_sync(kFull, gm != 0);
+        while (bal) {
+          const int j = __ffs(bal) - 1;
+          bal &= bal - 1;
+          const int32_t wj = __shfl_sync(kFull, w, j);
+          const uint64_t gj = shfl_u64(gm, j);
+          const unsigned my = static_cast<unsigned>(gj >> (2 * ln)) & 3u;
+          if (my) {
+            const float4 p = reinterpret_cast<const float4*>(b.psi)[static_cast<int64_t>(wj) * 32 + ln];
+            if (my & 1u) acc0 = df_add(acc0, df32{p.x, p.y});
+            if (my & 2u) acc1 = df_add(acc1, df32{p.z, p.w});
+          }
+        }
+      }
+      df32 contrib{0.f, 0.f};
+      if (mine) {
+        const ulonglong2 s = reinterpret_cast<const ulonglong2*>(b.sigma)[static_cast<int64_t>(v) * 32 + ln];
+        df32 p0{0.f, 0.f}, p1{0.f, 0.f};
+        if (mine & 1u) {
+          const df32 sv = df_from_u64(s.x);
+          const df32 d = df_mul(sv, acc0);
+          p0 = df_div(df_add_f(d, 1.0f), sv);
+          contrib = d;
+        }
+        if (mine & 2u) {
+          const df32 sv = df_from_u64(s.y);
+          const df32 d = df_mul(sv, acc1);
+          p1 = df_div(df_add_f(d, 1.0f), sv);
+          contrib = df_add(contrib, d);
+        }
+        float* psi = reinterpret_cast<float*>(b.psi);
+        const int64_t base = (static_cast<int64_t>(v) * 64 + 2 * ln) * 2;
+        if (mine == 3u) {
+          reinterpret_cast<float4*>(b.psi)[static_cast<int64_t>(v) * 32 + ln] =
+              make_float4(p0.hi, p0.lo, p1.hi, p1.lo);
+        } else if (mine == 1u) {
+          *reinterpret_cast<float2*>(psi + base) = make_float2(p0.hi, p0.lo);
+        } else {
+          *reinterpret_cast<float2*>(psi + base + 2) = make_float2(p1.hi, p1.lo);
+        }
+      }
+      contrib = warp_sum_df(contrib);
+      if (ln == 0) bc[v] += df_to_double(contrib);
+    } else if (SK == kSigmaF64) {
+      double acc0 = 0.0, acc1 = 0.0;
+      for (int64_t e = e0; e < e1; e += kWarp) {
+        const int64_t idx = e + ln;
+        int32_t w = 0;
+        uint64_t gm = 0;
+        if (idx < e1) {
+          w = g.colidx[idx];
+          gm = succ[w] & F;
+        }
+        unsigned bal = __ballot_sync(kFull, gm != 0);
+        while (bal) {
+          const int j = __ffs(bal) - 1;
+          bal &= bal - 1;
+          const int32_t wj = __shfl_sync(kFull, w, j);
+          const uint64_t gj = shfl_u64(gm, j);
+          const unsigned my = static_cast<unsigned>(gj >> (2 * ln)) & 3u;
+          if (my) {
+            const double2 p = reinterpret_cast<const double2*>(b.psi)[static_cast<int64_t>(wj) * 32 + ln];
+            if (my & 1u) acc0 += p.x;
+            if (my & 2u) acc1 += p.y;
+          }
+        }
+      }
+      double contrib = 0.0;
+      if (mine) {
+        const double2 s = reinterpret_cast<const double2*>(b.sigma)[static_cast<int64_t>(v) * 32 + ln];
+        double p0 = 0.0, p1 = 0.0;
+        if (mine & 1u) {
+          const double d = s.x * acc0;
+          p0 = (1.0 + d) / s.x;
+          contrib += d;
+        }
+        if (mine & 2u) {
+          const double d = s.y * acc1;
+          p1 = (1.0 + d) / s.y;
+          contrib += d;
+        }
+        double* psi = reinterpret_cast<double*>(b.psi);
+        if (mine == 3u) {
+          reinterpret_cast<double2*>(b.psi)[static_cast<int64_t>(v) * 32 + ln] = make_double2(p0, p1);
+        } else if (mine == 1u) {
+          psi[static_cast<int64_t>(v) * 64 + 2 * ln] = p0;
+        } else {
+          psi[static_cast<int64_t>(v) * 64 + 2 * ln + 1] = p1;
+        }
+      }
+      contrib = warp_sum_f64(contrib);
+      if (ln == 0) bc[v] += contrib;
+    }
+  }
+}
+
+__global__ void k_ms_back_advance(MsBuffers b) { b.ctl->level -= 1; }
+
+// End of a Brandes batch: the backward sweep cleared visit for every listed
+// vertex; clear the dense masks of levels 0 and 1 that remain.
+__global__ void k_ms_cleanup(MsBuffers b) {
+  const unsigned long long lo = b.lvl_off[0], hi = b.lvl_off[2];
+  for (unsigned long long i = lo + blockIdx.x * blockDim.x + threadIdx.x; i < hi;
+       i += static_cast<unsigned long long>(gridDim.x) * blockDim.x) {
+    const int32_t v = b.qv[i];
+    b.mb[0][v] = 0;
+    b.mb[1][v] = 0;
+    b.visit[v] = 0;
+  }
+}
+
+// End of a distance-only batch: clear every listed vertex.
+__global__ void k_ms_cleanup_all(MsBuffers b) {
+  const unsigned long long hi = b.ctl->tail;
+  for (unsigned long long i = blockIdx.x * blockDim.x + threadIdx.x; i < hi;
+       i += static_cast<unsigned long long>(gridDim.x) * blockDim.x) {
+    const int32_t v = b.qv[i];
+    b.mb[0][v] = 0;
+    b.mb[1][v] = 0;
+    b.visit[v] = 0;
+  }
+}
+
+}  // namespace
+
+int ms_init(cudaStream_t s, const DevGraph& g, const MsBuffers& b, int nlanes, int sigma_kind,
+            int32_t* dist, int64_t dist_ld) {
+  switch (sigma_kind) {
+    case kSigmaU64: k_ms_init<kSigmaU64><<<1, 32, 0, s>>>(g, b, nlanes, b.cap, dist, dist_ld); break;
+    case kSigmaF64: k_ms_init<kSigmaF64><<<1, 32, 0, s>>>(g, b, nlanes, b.cap, dist, dist_ld); break;
+    default: k_ms_init<kSigmaNone><<<1, 32, 0, s>>>(g, b, nlanes, b.cap, dist, dist_ld); break;
+  }
+  return 1;
+}
+
+int ms_topdown(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
+               uint64_t act, int sigma_kind, int32_t* dist, int64_t dist_ld) {
+  k_ms_td_discover<<<c.grid, c.block, 0, s>>>(g, b);
+  if (dist) {
+    k_ms_td_settle<kSigmaNone, true><<<c.grid, c.block, 0, s>>>(g, b, act, dist, dist_ld);
+  } else if (sigma_kind == kSigmaU64) {
+    k_ms_td_settle<kSigmaU64, false><<<c.grid, c.block, 0, s>>>(g, b, act, dist, dist_ld);
+  } else {
+    k_ms_td_settle<kSigmaF64, false><<<c.grid, c.block, 0, s>>>(g, b, act, dist, dist_ld);
+  }
+  k_ms_clear_front<<<c.grid, c.block, 0, s>>>(b);
+  return 3;
+}
+
+int ms_bottomup(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
+                uint64_t act, int sigma_kind, int32_t* dist, int64_t dist_ld) {
+  if (dist) {
+    k_ms_bu<kSigmaNone, true><<<c.grid, c.block, 0, s>>>(g, b, act, dist, dist_ld);
+  } else if (sigma_kind == kSigmaU64) {
+    k_ms_bu<kSigmaU64, false><<<c.grid, c.block, 0, s>>>(g, b, act, dist, dist_ld);
+  } else {
+    k_ms_bu<kSigmaF64, false><<<c.grid, c.block, 0, s>>>(g, b, act, dist, dist_ld);
+  }
+  k_ms_clear_front<<<c.grid, c.block, 0, s>>>(b);
+  return 2;
+}
+
+int ms_advance(cudaStream_t s, const DevGraph& g, const MsBuffers& b) {
+  k_ms_advance<<<1, 1, 0, s>>>(b, g.n);
+  return 1;
+}
+
+int ms_begin_backward(cudaStream_t s, const MsBuffers& b) {
+  k_ms_begin_backward<<<1, 1, 0, s>>>(b);
+  return 1;
+}
+
+int ms_backward_level(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
+                      int sigma_kind, double* bc) {
+  k_ms_back_clear<<<c.grid, c.block, 0, s>>>(b);
+  if (sigma_kind == kSigmaF64)
+    k_ms_delta<kSigmaF64><<<c.grid, c.block, 0, s>>>(g, b, bc);
+  else
+    k_ms_delta<kSigmaU64><<<c.grid, c.block, 0, s>>>(g, b, bc);
+  k_ms_back_advance<<<1, 1, 0, s>>>(b);
+  return 3;
+}
+
+int ms_cleanup(const LaunchCfg& c, cudaStream_t s, const MsBuffers& b) {
+  k_ms_cleanup<<<c.grid, c.block, 0, s>>>(b);
+  return 1;
+}
+
+int ms_cleanup_all(const LaunchCfg& c, cudaStream_t s, const MsBuffers& b) {
+  k_ms_cleanup_all<<<c.grid, c.block, 0, s>>>(b);
+  return 1;
+}
+
+int ms_reset_all(cudaStream_t s, const DevGraph& g, const MsBuffers& b) {
+  const size_t bytes = static_cast<size_t>(g.n) * sizeof(uint64_t);
+  cudaMemsetAsync(b.visit, 0, bytes, s);
+  cudaMemsetAsync(b.mb[0], 0, bytes, s);
+  cudaMemsetAsync(b.mb[1], 0, bytes, s);
+  return 0;
+}
+
+}  // namespace lgbc

@@ -1,0 +1,74 @@
+// util.cu -- fills and the endpoint terms of the betweenness accumulation.
+#include "lgbc_kernels.h"
+
+namespace lgbc {
+namespace {
+
+template <class T>
+__global__ void k_fill(T* p, int64_t count, T value) {
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < count;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    p[i] = value;
+}
+
+// _accumulate_endpoints! (src/centrality/betweenness.jl:109-134) adds, per
+// source s, length(S) - 1 = n - 1 to betweenness[s] (:122; S always holds all
+// n vertices, dijkstra.jl:126-132) and 1 to every other vertex (:130).  Summed
+// over the active sources: k_act to every vertex, then n - 2 more to each
+// source occurrence.
+__global__ void k_add_all(double* bc, int64_t n, double k) {
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    bc[i] += k;
+}
+
+__global__ void k_add_sources(double* bc, const int32_t* src, int64_t k, double extra) {
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < k;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    atomicAdd(bc + src[i], extra);
+}
+
+// Flags (bit 0) a decreasing rowptr step and (bit 1) a column index outside
+// [0, n); the host rejects the graph when any bit is set.
+__global__ void k_validate_csr(const int64_t* rowptr, const int32_t* colidx, int64_t n, int64_t nnz,
+                               int* bad) {
+  int local = 0;
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t v = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; v < n; v += stride)
+    if (rowptr[v + 1] < rowptr[v]) local |= 1;
+  for (int64_t e = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; e < nnz; e += stride) {
+    const int32_t c = colidx[e];
+    if (c < 0 || c >= n) local |= 2;
+  }
+  if (__any_sync(kFull, local != 0) && local) atomicOr(bad, local);
+}
+
+}  // namespace
+
+int validate_csr(const LaunchCfg& c, cudaStream_t s, const int64_t* rowptr, const int32_t* colidx,
+                 int64_t n, int64_t nnz, int* bad) {
+  k_validate_csr<<<c.grid, c.block, 0, s>>>(rowptr, colidx, n, nnz, bad);
+  return 1;
+}
+
+int fill_i32(const LaunchCfg& c, cudaStream_t s, int32_t* p, int64_t count, int32_t value) {
+  if (count <= 0) return 0;
+  k_fill<int32_t><<<c.grid, c.block, 0, s>>>(p, count, value);
+  return 1;
+}
+
+int fill_f64(const LaunchCfg& c, cudaStream_t s, double* p, int64_t count, double value) {
+  if (count <= 0) return 0;
+  k_fill<double><<<c.grid, c.block, 0, s>>>(p, count, value);
+  return 1;
+}
+
+int add_endpoints(const LaunchCfg& c, cudaStream_t s, double* bc, int64_t n,
+                  const int32_t* active_src, int64_t k_act) {
+  if (k_act <= 0 || n <= 0) return 0;
+  k_add_all<<<c.grid, c.block, 0, s>>>(bc, n, static_cast<double>(k_act));
+  k_add_sources<<<c.grid, c.block, 0, s>>>(bc, active_src, k_act, static_cast<double>(n) - 2.0);
+  return 2;
+}
+
+}  // namespace lgbc

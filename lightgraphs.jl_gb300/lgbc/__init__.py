@@ -1,0 +1,34 @@
+"""lgbc -- GB300-native betweenness centrality and BFS for LightGraphs graphs.
+
+A host-side mirror of the LightGraphs.jl v1.3.5 interface for this path
+(1-based vertex ids, the same names, keywords and exceptions), calling the
+CUDA library ``liblgbc.so`` through its C ABI (include/lgbc.h):
+
+    betweenness_centrality(g[, vs | k][, distmx]; normalize, endpoints)
+        src/centrality/betweenness.jl:46-78
+    Parallel.betweenness_centrality(...; parallel)
+        src/Parallel/centrality/betweenness.jl:1-75
+    gdistances(g, s | sources), gdistances_(g, s, dists)  (Julia's gdistances!)
+        src/traversals/bfs.jl:95-141
+    Parallel.gdistances / Parallel.gdistances_
+        src/Parallel/traversals/gdistances.jl:36-139
+
+Graphs are ``SimpleGraph`` / ``SimpleDiGraph`` (CSR-backed mirrors of
+LightGraphs' fadjlist storage).  Every computation runs on the GPU; without
+a GPU or without the built library the calls raise ``LGBCError``.
+"""
+from . import Parallel
+from ._lib import ArgumentError, BoundsError, LGBCError, MethodError
+from .centrality import betweenness_centrality, betweenness_raw, sample, sample_, _rescale_
+from .graphs import (DefaultDistance, DeviceGraph, SimpleDiGraph, SimpleGraph, degree,
+                     is_directed, ne, nv, vertices, weights)
+from .persistence import loadgraph
+from .traversals import gdistances, gdistances_, multi_gdistances
+
+__all__ = [
+    "Parallel", "ArgumentError", "BoundsError", "LGBCError", "MethodError",
+    "betweenness_centrality", "betweenness_raw", "sample", "sample_", "_rescale_",
+    "DefaultDistance", "DeviceGraph", "SimpleDiGraph", "SimpleGraph", "degree", "is_directed",
+    "ne", "nv", "vertices", "weights", "loadgraph", "gdistances", "gdistances_",
+    "multi_gdistances",
+]

@@ -1,0 +1,153 @@
+"""ctypes loader for the CPU oracle (``lg_oracle.cpp``).
+
+TEST INFRASTRUCTURE ONLY: the oracle is the checker for the CUDA library and
+the timed CPU baseline.  Only ``tests/``, ``__graft_entry__.smoke()`` and
+``bench.py``'s CPU-baseline / reference arm import this module; the product
+package never does.
+
+The oracle restates LightGraphs.jl v1.3.5 (paths relative to that project):
+  * ``gdistances``        -- src/traversals/bfs.jl:95-124,141
+  * ``dijkstra``          -- src/shortestpaths/dijkstra.jl:59-144 (unit weights)
+  * ``betweenness_raw``   -- src/centrality/betweenness.jl:46-134 before
+                             ``_rescale!``; Parallel threaded variant
+                             src/Parallel/centrality/betweenness.jl:42-72
+  * ``rescale``           -- src/centrality/betweenness.jl:136-160
+Parity is pinned against the reference's golden vectors (tests/golden/).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_BUILD = os.path.join(_HERE, "_build")
+_SO = os.path.join(_BUILD, "liblgoracle.so")
+_SRC = os.path.join(_HERE, "lg_oracle.cpp")
+_lock = threading.Lock()
+_lib = None
+
+UNREACHED32 = np.iinfo(np.int32).max
+UNREACHED64 = np.iinfo(np.int64).max
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle into ``oracle/_build/liblgoracle.so`` (g++, -O3)."""
+    os.makedirs(_BUILD, exist_ok=True)
+    if (not force and os.path.exists(_SO)
+            and os.path.getmtime(_SO) >= os.path.getmtime(_SRC)):
+        return _SO
+    tmp = _SO + f".tmp{os.getpid()}"
+    cmd = ["g++", "-O3", "-std=c++17", "-shared", "-fPIC", "-pthread",
+           _SRC, "-o", tmp]
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, _SO)
+    return _SO
+
+
+def _load():
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        build()
+        lib = ctypes.CDLL(_SO)
+        i64, i32, dbl = ctypes.c_int64, ctypes.c_int32, ctypes.c_double
+        p = ctypes.c_void_p
+        lib.orc_gdistances.argtypes = [i64, p, p, p, i64, p]
+        lib.orc_gdistances.restype = ctypes.c_int
+        lib.orc_dijkstra.argtypes = [i64, p, p, i32, p, p, p, p, p, i64]
+        lib.orc_dijkstra.restype = i64
+        lib.orc_betweenness.argtypes = [i64, p, p, p, p, ctypes.c_int, p, i64,
+                                        ctypes.c_int, ctypes.c_int, ctypes.c_int, p]
+        lib.orc_betweenness.restype = ctypes.c_int
+        lib.orc_rescale.argtypes = [p, i64, ctypes.c_int, ctypes.c_int, i64]
+        lib.orc_rescale.restype = None
+        _lib = lib
+        return lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+def _csr(rowptr, colidx):
+    return (np.ascontiguousarray(rowptr, dtype=np.int64),
+            np.ascontiguousarray(colidx, dtype=np.int32))
+
+
+def gdistances(rowptr, colidx, sources) -> np.ndarray:
+    """Multi-source level-synchronous BFS; INT32_MAX marks unreached."""
+    lib = _load()
+    rowptr, colidx = _csr(rowptr, colidx)
+    n = len(rowptr) - 1
+    src = np.ascontiguousarray(np.atleast_1d(np.asarray(sources, dtype=np.int32)))
+    dist = np.empty(n, dtype=np.int32)
+    rc = lib.orc_gdistances(n, _ptr(rowptr), _ptr(colidx), _ptr(src), len(src), _ptr(dist))
+    if rc != 0:
+        raise ValueError("oracle gdistances: bad source")
+    return dist
+
+
+def dijkstra(rowptr, colidx, s):
+    """Unit-weight Dijkstra with all paths: (dists, pathcounts, preds, closest)."""
+    lib = _load()
+    rowptr, colidx = _csr(rowptr, colidx)
+    n = len(rowptr) - 1
+    dists = np.empty(n, np.int64)
+    pc = np.empty(n, np.float64)
+    closest = np.empty(n, np.int32)
+    poff = np.empty(n + 1, np.int64)
+    cap = max(1, len(colidx))
+    pred = np.empty(cap, np.int32)
+    tot = lib.orc_dijkstra(n, _ptr(rowptr), _ptr(colidx), int(s), _ptr(dists), _ptr(pc),
+                           _ptr(closest), _ptr(poff), _ptr(pred), cap)
+    if tot < 0:
+        raise ValueError("oracle dijkstra failed")
+    preds = [pred[poff[v]:poff[v + 1]].tolist() for v in range(n)]
+    return dists, pc, preds, closest
+
+
+def betweenness_raw(rowptr, colidx, sources, *, directed=False, in_rowptr=None,
+                    in_colidx=None, endpoints=False, mode="fast", nthreads=1) -> np.ndarray:
+    """Unscaled BC over an explicit source list (degree-0 sources skipped)."""
+    lib = _load()
+    rowptr, colidx = _csr(rowptr, colidx)
+    n = len(rowptr) - 1
+    if directed:
+        in_rowptr, in_colidx = _csr(in_rowptr, in_colidx)
+    else:
+        in_rowptr = in_colidx = None
+    src = np.ascontiguousarray(np.asarray(sources, dtype=np.int32).ravel())
+    out = np.empty(n, np.float64)
+    rc = lib.orc_betweenness(n, _ptr(rowptr), _ptr(colidx), _ptr(in_rowptr), _ptr(in_colidx),
+                             int(bool(directed)), _ptr(src), len(src), int(bool(endpoints)),
+                             0 if mode == "faithful" else 1, int(nthreads), _ptr(out))
+    if rc != 0:
+        raise ValueError("oracle betweenness: bad arguments")
+    return out
+
+
+def rescale(bc, n, normalize, directed, k) -> np.ndarray:
+    """_rescale! on a copy (src/centrality/betweenness.jl:136-160)."""
+    lib = _load()
+    out = np.ascontiguousarray(bc, dtype=np.float64).copy()
+    lib.orc_rescale(_ptr(out), int(n), int(bool(normalize)), int(bool(directed)), int(k))
+    return out
+
+
+def betweenness_centrality(rowptr, colidx, sources=None, *, directed=False, in_rowptr=None,
+                           in_colidx=None, normalize=True, endpoints=False, mode="fast",
+                           nthreads=1) -> np.ndarray:
+    """The full reference result: raw accumulation followed by ``_rescale!``."""
+    n = len(rowptr) - 1
+    if sources is None:
+        sources = np.arange(n, dtype=np.int32)
+    src = np.asarray(sources, dtype=np.int32).ravel()
+    raw = betweenness_raw(rowptr, colidx, src, directed=directed, in_rowptr=in_rowptr,
+                          in_colidx=in_colidx, endpoints=endpoints, mode=mode,
+                          nthreads=nthreads)
+    return rescale(raw, n, normalize, directed, len(src))
