@@ -309,6 +309,13 @@ def run_ours(args, dist: Dist):
     te_step = k_act * m
     value = dist.sum(te_step * args.steps) / t_dev / 1e9
 
+    if args.profile_only:
+        if dist.rank == 0:
+            print(json.dumps({"profile_only": True, "ms_per_step": ms.value / args.steps,
+                              "gpu_launches": int(launches.value)}), flush=True)
+        lib.lgbc_device_free(bc_dev)
+        return
+
     # bc result sanity: finite and non-negative
     host_bc = np.empty(n, np.float64)
     _lib.check(lib.lgbc_memcpy(_lib.ptr(host_bc), bc_dev, 8 * n, 2))
@@ -415,6 +422,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0,
                     help="approximate CPU-baseline sample length")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--profile-only", action="store_true",
+                    help="run only the device-resident steps (for ncu launch lists)")
     args = ap.parse_args()
     dist = Dist()
     try:

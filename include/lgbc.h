@@ -133,8 +133,9 @@ int lgbc_graph_stats(const lgbc_graph *g, lgbc_stats *out);
  *   alpha, beta   direction switch: go bottom-up when the frontier's edges
  *                 exceed (unvisited edges)/alpha; return top-down when the
  *                 frontier has fewer than n/beta vertices.
- *   hub_degree    vertices with at least this many neighbours are expanded by
- *                 a whole thread block instead of one warp.
+ *   hub_degree    vertices with more than this many neighbours ("hubs") are
+ *                 cut into 256-edge work items spread over the whole GPU
+ *                 instead of being expanded by one warp (default 512).
  *   lanes         sources per multi-source batch (1..64). */
 typedef struct lgbc_tuning {
   double alpha;

@@ -90,6 +90,29 @@ struct MsWorkspace {
   }
 };
 
+// Hub work items (see HubItem in lgbc_kernels.h) and their accumulators.
+struct HubTable {
+  HubItem* out_items = nullptr;
+  int64_t n_out = 0;
+  HubItem* in_items = nullptr;   // == out_items for undirected graphs
+  int64_t n_in = 0;
+  unsigned long long* acc = nullptr;
+  unsigned long long* mask = nullptr;
+  unsigned int* cnt = nullptr;
+  int64_t nslots = 0;
+  int built_for = -1;            // hub_degree the table was built with
+  void release() {
+    if (in_items && in_items != out_items) cudaFree(in_items);
+    dev_free(out_items);
+    in_items = nullptr;
+    dev_free(acc);
+    dev_free(mask);
+    dev_free(cnt);
+    n_out = n_in = nslots = 0;
+    built_for = -1;
+  }
+};
+
 struct BfsWorkspace {
   int32_t* queue = nullptr;
   uint32_t* bm0 = nullptr;
@@ -119,6 +142,7 @@ struct lgbc_graph {
   std::mutex mu;
   MsWorkspace ms;
   BfsWorkspace bfs;
+  HubTable hubs;
   int32_t* d_src = nullptr;         // device copy of a call's source list
   int64_t d_src_cap = 0;
   double* d_bc = nullptr;           // device result buffer for host-buffer calls
@@ -131,7 +155,7 @@ struct lgbc_graph {
   LaunchCfg cfg{};
   size_t max_smem = 0;
   lgbc_stats stats{};
-  lgbc_tuning tune{14.0, 24.0, 4096, 64};
+  lgbc_tuning tune{14.0, 24.0, 512, 64};
 
   DevGraph dev() const {
     return DevGraph{n, nnz, d_rowptr, d_colidx, d_in_rowptr, d_in_colidx};
@@ -245,6 +269,98 @@ int ensure_dist(lgbc_graph* g, int64_t count) {
   return LGBC_OK;
 }
 
+// Cut every edge list longer than H into kHubChunk-edge items.
+void make_items(const int64_t* rowptr, int64_t n, int H, const std::vector<int32_t>& slot_of,
+                std::vector<HubItem>& items) {
+  items.clear();
+  for (int64_t v = 0; v < n; ++v) {
+    const int64_t e0 = rowptr[v], e1 = rowptr[v + 1];
+    if (e1 - e0 <= H) continue;
+    const int32_t nit = static_cast<int32_t>((e1 - e0 + kHubChunk - 1) / kHubChunk);
+    for (int64_t lo = e0; lo < e1; lo += kHubChunk) {
+      HubItem it;
+      it.lo = lo;
+      it.hi = std::min<int64_t>(lo + kHubChunk, e1);
+      it.v = static_cast<int32_t>(v);
+      it.slot = slot_of[static_cast<size_t>(v)];
+      it.nitems = nit;
+      it.pad = 0;
+      items.push_back(it);
+    }
+  }
+}
+
+int upload_items(const std::vector<HubItem>& items, HubItem** out) {
+  *out = nullptr;
+  if (items.empty()) return LGBC_OK;
+  LGBC_TRY(dev_alloc(out, items.size()));
+  LGBC_CUDA(cudaMemcpy(*out, items.data(), items.size() * sizeof(HubItem), cudaMemcpyHostToDevice));
+  return LGBC_OK;
+}
+
+// Build the hub work items from host copies of rowptr / in_rowptr.
+int build_hubs(lgbc_graph* g, const int64_t* rowptr, const int64_t* in_rowptr, int H) {
+  g->hubs.release();
+  const int64_t n = g->n;
+  std::vector<int32_t> slot_of(static_cast<size_t>(n), -1);
+  int64_t nslots = 0;
+  for (int64_t v = 0; v < n; ++v) {
+    const int64_t dout = rowptr[v + 1] - rowptr[v];
+    const int64_t din = in_rowptr[v + 1] - in_rowptr[v];
+    if (dout > H || din > H) slot_of[static_cast<size_t>(v)] = static_cast<int32_t>(nslots++);
+  }
+  g->hubs.nslots = nslots;
+  g->hubs.built_for = H;
+  if (nslots == 0) return LGBC_OK;
+  std::vector<HubItem> items;
+  make_items(rowptr, n, H, slot_of, items);
+  g->hubs.n_out = static_cast<int64_t>(items.size());
+  LGBC_TRY(upload_items(items, &g->hubs.out_items));
+  if (g->directed) {
+    make_items(in_rowptr, n, H, slot_of, items);
+    g->hubs.n_in = static_cast<int64_t>(items.size());
+    LGBC_TRY(upload_items(items, &g->hubs.in_items));
+  } else {
+    g->hubs.in_items = g->hubs.out_items;
+    g->hubs.n_in = g->hubs.n_out;
+  }
+  LGBC_TRY(dev_alloc(&g->hubs.acc, static_cast<size_t>(nslots) * kMaxLanes));
+  LGBC_TRY(dev_alloc(&g->hubs.mask, static_cast<size_t>(nslots)));
+  LGBC_TRY(dev_alloc(&g->hubs.cnt, static_cast<size_t>(nslots)));
+  LGBC_CUDA(cudaMemset(g->hubs.acc, 0, static_cast<size_t>(nslots) * kMaxLanes * 8));
+  LGBC_CUDA(cudaMemset(g->hubs.mask, 0, static_cast<size_t>(nslots) * 8));
+  LGBC_CUDA(cudaMemset(g->hubs.cnt, 0, static_cast<size_t>(nslots) * 4));
+  return LGBC_OK;
+}
+
+// Rebuild the hub table after hub_degree changed (rowptr copied back).
+int ensure_hubs(lgbc_graph* g) {
+  if (g->hubs.built_for == g->tune.hub_degree) return LGBC_OK;
+  LGBC_CUDA(cudaStreamSynchronize(g->stream));
+  std::vector<int64_t> rp(static_cast<size_t>(g->n + 1)), irp;
+  LGBC_CUDA(cudaMemcpy(rp.data(), g->d_rowptr, rp.size() * 8, cudaMemcpyDeviceToHost));
+  const int64_t* in_rp = rp.data();
+  if (g->directed) {
+    irp.resize(rp.size());
+    LGBC_CUDA(cudaMemcpy(irp.data(), g->d_in_rowptr, irp.size() * 8, cudaMemcpyDeviceToHost));
+    in_rp = irp.data();
+  }
+  return build_hubs(g, rp.data(), in_rp, g->tune.hub_degree);
+}
+
+HubData hub_data(const lgbc_graph* g) {
+  HubData h;
+  h.out_items = g->hubs.out_items;
+  h.n_out = g->hubs.n_out;
+  h.in_items = g->hubs.in_items;
+  h.n_in = g->hubs.n_in;
+  h.acc = g->hubs.acc;
+  h.mask = g->hubs.mask;
+  h.cnt = g->hubs.cnt;
+  h.hub_degree = g->hubs.nslots > 0 ? g->hubs.built_for : INT32_MAX;
+  return h;
+}
+
 int read_ctl(lgbc_graph* g, const BatchCtl* dctl) {
   LGBC_CUDA(cudaMemcpyAsync(g->h_ctl, dctl, sizeof(BatchCtl), cudaMemcpyDeviceToHost, g->stream));
   LGBC_CUDA(cudaStreamSynchronize(g->stream));
@@ -293,6 +409,8 @@ bool choose_bottom_up(const lgbc_graph* g, const BatchCtl& c, bool was_bu) {
 int run_ms_batch(lgbc_graph* g, const int32_t* lane_src, int nl, int sigma_kind, double* bc,
                  int32_t* dist, int64_t dist_ld) {
   const DevGraph dg = g->dev();
+  LGBC_TRY(ensure_hubs(g));
+  const HubData hd = hub_data(g);
   const uint64_t act = nl >= 64 ? ~0ull : ((1ull << nl) - 1ull);
   for (;;) {
     MsBuffers b = ms_buffers(g, lane_src);
@@ -303,10 +421,10 @@ int run_ms_batch(lgbc_graph* g, const int32_t* lane_src, int nl, int sigma_kind,
     int64_t levels = 0;
     for (;;) {
       if (bu) {
-        g->launches += ms_bottomup(g->cfg, g->stream, dg, b, act, sigma_kind, dist, dist_ld);
+        g->launches += ms_bottomup(g->cfg, g->stream, dg, b, hd, act, sigma_kind, dist, dist_ld);
         g->stats.bottomup_levels++;
       } else {
-        g->launches += ms_topdown(g->cfg, g->stream, dg, b, act, sigma_kind, dist, dist_ld);
+        g->launches += ms_topdown(g->cfg, g->stream, dg, b, hd, act, sigma_kind, dist, dist_ld);
         g->stats.topdown_levels++;
       }
       g->launches += ms_advance(g->stream, dg, b);
@@ -342,7 +460,7 @@ int run_ms_batch(lgbc_graph* g, const int32_t* lane_src, int nl, int sigma_kind,
     const int maxl = g->h_ctl->maxlevel;
     g->launches += ms_begin_backward(g->stream, b);
     for (int L = maxl; L >= 0; --L)
-      g->launches += ms_backward_level(g->cfg, g->stream, dg, b, sigma_kind, bc);
+      g->launches += ms_backward_level(g->cfg, g->stream, dg, b, hd, sigma_kind, bc);
     g->launches += ms_cleanup(g->cfg, g->stream, b);
     return check_launch(g);
   }
@@ -459,7 +577,7 @@ int create_impl(lgbc_graph* g, int64_t n, int64_t nnz, const int64_t* rowptr, co
   LGBC_TRY(check_launch(g));
   if (bad & 1) return fail(LGBC_EINVAL, "rowptr must be non-decreasing");
   if (bad & 2) return fail(LGBC_EINVAL, "column index out of range");
-  return LGBC_OK;
+  return build_hubs(g, rowptr, directed ? in_rowptr : rowptr, g->tune.hub_degree);
 }
 
 }  // namespace
@@ -519,6 +637,7 @@ int lgbc_graph_destroy(lgbc_graph* g) {
   if (g->stream) cudaStreamSynchronize(g->stream);
   g->ms.release();
   g->bfs.release();
+  g->hubs.release();
   if (g->d_in_rowptr != g->d_rowptr) dev_free(g->d_in_rowptr);
   if (g->d_in_colidx != g->d_colidx) dev_free(g->d_in_colidx);
   dev_free(g->d_rowptr);

@@ -38,18 +38,41 @@ struct MsBuffers {
   unsigned long long cap;       // entries in qv / qm
 };
 
+// Vertices with more than hub_degree neighbours ("hubs") are not expanded by
+// one warp: their edge lists are cut into kHubChunk-edge work items spread over
+// the whole grid, whose partial results are combined with atomics; the last
+// item of a hub to finish (a completion counter, no waiting) finalises it.
+constexpr int kHubChunk = 256;
+struct HubItem {
+  int64_t lo, hi;      // edge range [lo, hi) in the CSR the item list belongs to
+  int32_t v;           // the hub vertex
+  int32_t slot;        // its accumulator slot
+  int32_t nitems;      // items of this hub in this list
+  int32_t pad;
+};
+struct HubData {
+  const HubItem* out_items;      // items over out-edges (top-down discovery, dependencies)
+  long long n_out;
+  const HubItem* in_items;       // items over in-edges (path-count pulls, bottom-up)
+  long long n_in;
+  unsigned long long* acc;       // slots x 64 partial sums (uint64 or FP64 bits), kept zero
+  unsigned long long* mask;      // slots: OR of discovering lanes, kept zero
+  unsigned int* cnt;             // slots: finished items, kept zero
+  int hub_degree;                // degree above which a vertex is a hub (INT32_MAX: none)
+};
+
 int ms_init(cudaStream_t s, const DevGraph& g, const MsBuffers& b, int nlanes, int sigma_kind,
             int32_t* dist, int64_t dist_ld);
 int ms_topdown(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
-               uint64_t act, int sigma_kind, int32_t* dist, int64_t dist_ld);
+               const HubData& hd, uint64_t act, int sigma_kind, int32_t* dist, int64_t dist_ld);
 int ms_bottomup(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
-                uint64_t act, int sigma_kind, int32_t* dist, int64_t dist_ld);
+                const HubData& hd, uint64_t act, int sigma_kind, int32_t* dist, int64_t dist_ld);
 int ms_advance(cudaStream_t s, const DevGraph& g, const MsBuffers& b);
 // Set ctl->level = maxlevel for the backward sweep (on the device).
 int ms_begin_backward(cudaStream_t s, const MsBuffers& b);
 // Backward (dependency) step for the level in ctl->level, then level--.
 int ms_backward_level(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
-                      int sigma_kind, double* bc);
+                      const HubData& hd, int sigma_kind, double* bc);
 // After the backward sweep: clear the masks of levels 0 and 1.
 int ms_cleanup(const LaunchCfg& c, cudaStream_t s, const MsBuffers& b);
 // After a distance-only batch: clear visit / masks of every listed vertex.

@@ -23,6 +23,9 @@
 //   qv/qm             concatenated per-level lists of (vertex, lane mask)
 // A warp owns one vertex; thread t owns lanes 2t and 2t+1, so a vertex's
 // 64 lanes are one 512-byte row read by 32 coalesced 16-byte accesses.
+// Neighbour rows are gathered four at a time so each warp keeps four row
+// loads in flight.  Hubs (more than hub_degree neighbours) are cut into
+// kHubChunk-edge items processed by the whole grid (k_ms_hub_*).
 #include "lgbc_kernels.h"
 
 namespace lgbc {
@@ -62,6 +65,20 @@ __device__ __forceinline__ void sig_add(unsigned long long& a, unsigned long lon
 }
 __device__ __forceinline__ void sig_add(double& a, double x, bool&) { a += x; }
 
+__device__ __forceinline__ void hub_add(unsigned long long* p, unsigned long long x, bool& ovf) {
+  const unsigned long long old = atomicAdd(p, x);
+  ovf |= (old + x < old);
+}
+__device__ __forceinline__ void hub_add(unsigned long long* p, double x, bool&) {
+  atomicAdd(reinterpret_cast<double*>(p), x);
+}
+
+template <class T> __device__ __forceinline__ T from_bits(unsigned long long x);
+template <> __device__ __forceinline__ unsigned long long from_bits(unsigned long long x) { return x; }
+template <> __device__ __forceinline__ double from_bits(unsigned long long x) {
+  return __longlong_as_double(static_cast<long long>(x));
+}
+
 template <class P, class T> __device__ __forceinline__ P make_pair2(T a, T b);
 template <> __device__ __forceinline__ ulonglong2 make_pair2(unsigned long long a, unsigned long long b) {
   return make_ulonglong2(a, b);
@@ -71,6 +88,8 @@ template <> __device__ __forceinline__ double2 make_pair2(double a, double b) {
 }
 
 // Store the path counts of lanes (2t, 2t+1) of w that are set in `mask`.
+// Lanes outside `mask` may be read concurrently by other warps (w sits at
+// another level for them), so they are never written.
 template <int SK>
 __device__ __forceinline__ void store_sigma(void* sigma, int32_t w, uint64_t mask,
                                             typename Sig<SK>::T a0, typename Sig<SK>::T a1) {
@@ -95,21 +114,34 @@ __device__ __forceinline__ void store_dist(int32_t* dist, int64_t ld, int32_t w,
   if (my & 2u) dist[static_cast<int64_t>(2 * ln + 1) * ld + w] = level;
 }
 
-// Pull over the in-neighbours v of w: f = front[v] & want marks the lanes for
-// which v is a predecessor of w one level up.  Accumulates the predecessors'
-// path counts into (a0, a1) for this thread's lanes and returns the OR of all
-// f (the lanes that discover w).  With SK == kSigmaNone it stops as soon as
-// every wanted lane is found.
+// Take up to four set bits of a warp-uniform ballot (-1 when exhausted).
+__device__ __forceinline__ void take4(unsigned& bal, int (&j)[4]) {
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    if (bal) {
+      j[q] = __ffs(bal) - 1;
+      bal &= bal - 1;
+    } else {
+      j[q] = -1;
+    }
+  }
+}
+
+// Path-count gather over in-edges [e0, e1) of one vertex: for every
+// in-neighbour v, f = front[v] & want marks the lanes whose predecessor it is;
+// their rows are added into (a0, a1).  Returns the OR of all f (the lanes
+// that discover the vertex).  With SK == kSigmaNone only the OR is formed,
+// and the scan stops once every wanted lane is found.
 template <int SK>
-__device__ __forceinline__ uint64_t pull_lanes(const int64_t* __restrict__ rp,
-                                               const int32_t* __restrict__ ci, int32_t w,
-                                               uint64_t want, const uint64_t* __restrict__ front,
+__device__ __forceinline__ uint64_t pull_range(const int32_t* __restrict__ ci, int64_t e0,
+                                               int64_t e1, uint64_t want,
+                                               const uint64_t* __restrict__ front,
                                                const void* __restrict__ sigma,
                                                typename Sig<SK>::T& a0, typename Sig<SK>::T& a1,
                                                bool& ovf) {
+  using T = typename Sig<SK>::T;
   using P = typename Sig<SK>::Pair;
   const int ln = lane_id();
-  const int64_t e0 = rp[w], e1 = rp[w + 1];
   uint64_t found = 0;
   for (int64_t e = e0; e < e1; e += kWarp) {
     const int64_t idx = e + ln;
@@ -119,27 +151,189 @@ __device__ __forceinline__ uint64_t pull_lanes(const int64_t* __restrict__ rp,
       v = ci[idx];
       f = front[v] & want;
     }
+    found |= f;
     if (SK == kSigmaNone) {
-      found |= f;
       if (warp_or_u64(found) == want) break;
       continue;
     }
-    found |= f;
     unsigned bal = __ballot_sync(kFull, f != 0);
     while (bal) {
-      const int j = __ffs(bal) - 1;
-      bal &= bal - 1;
-      const int32_t vj = __shfl_sync(kFull, v, j);
-      const uint64_t fj = shfl_u64(f, j);
-      const unsigned my = static_cast<unsigned>(fj >> (2 * ln)) & 3u;
-      if (my) {
-        const P p = reinterpret_cast<const P*>(sigma)[static_cast<int64_t>(vj) * 32 + ln];
-        if (my & 1u) sig_add(a0, p.x, ovf);
-        if (my & 2u) sig_add(a1, p.y, ovf);
+      int j[4];
+      take4(bal, j);
+      P p[4];
+      unsigned my[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int src = j[q] < 0 ? 0 : j[q];
+        const int32_t vj = __shfl_sync(kFull, v, src);
+        const uint64_t fj = shfl_u64(f, src);
+        my[q] = j[q] < 0 ? 0u : (static_cast<unsigned>(fj >> (2 * ln)) & 3u);
+        p[q] = make_pair2<P, T>(T(0), T(0));
+        if (my[q]) p[q] = reinterpret_cast<const P*>(sigma)[static_cast<int64_t>(vj) * 32 + ln];
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        if (my[q] & 1u) sig_add(a0, p[q].x, ovf);
+        if (my[q] & 2u) sig_add(a1, p[q].y, ovf);
       }
     }
   }
   return warp_or_u64(found);
+}
+
+// Dependency gather over out-edges [e0, e1) of v at level L: for every
+// out-neighbour w, g = succ[w] & F marks the lanes for which w is a DAG
+// successor; their psi = (1 + delta[w]) / sigma[w] are summed.
+__device__ __forceinline__ void psi_range_df(const int32_t* __restrict__ ci, int64_t e0, int64_t e1,
+                                             uint64_t F, const uint64_t* __restrict__ succ,
+                                             const void* __restrict__ psi, df32& acc0, df32& acc1) {
+  const int ln = lane_id();
+  for (int64_t e = e0; e < e1; e += kWarp) {
+    const int64_t idx = e + ln;
+    int32_t w = 0;
+    uint64_t gm = 0;
+    if (idx < e1) {
+      w = ci[idx];
+      gm = succ[w] & F;
+    }
+    unsigned bal = __ballot_sync(kFull, gm != 0);
+    while (bal) {
+      int j[4];
+      take4(bal, j);
+      float4 p[4];
+      unsigned my[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int src = j[q] < 0 ? 0 : j[q];
+        const int32_t wj = __shfl_sync(kFull, w, src);
+        const uint64_t gj = shfl_u64(gm, src);
+        my[q] = j[q] < 0 ? 0u : (static_cast<unsigned>(gj >> (2 * ln)) & 3u);
+        p[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (my[q]) p[q] = reinterpret_cast<const float4*>(psi)[static_cast<int64_t>(wj) * 32 + ln];
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        if (my[q] & 1u) acc0 = df_add(acc0, df32{p[q].x, p[q].y});
+        if (my[q] & 2u) acc1 = df_add(acc1, df32{p[q].z, p[q].w});
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ void psi_range_f64(const int32_t* __restrict__ ci, int64_t e0, int64_t e1,
+                                              uint64_t F, const uint64_t* __restrict__ succ,
+                                              const void* __restrict__ psi, double& acc0,
+                                              double& acc1) {
+  const int ln = lane_id();
+  for (int64_t e = e0; e < e1; e += kWarp) {
+    const int64_t idx = e + ln;
+    int32_t w = 0;
+    uint64_t gm = 0;
+    if (idx < e1) {
+      w = ci[idx];
+      gm = succ[w] & F;
+    }
+    unsigned bal = __ballot_sync(kFull, gm != 0);
+    while (bal) {
+      int j[4];
+      take4(bal, j);
+      double2 p[4];
+      unsigned my[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int src = j[q] < 0 ? 0 : j[q];
+        const int32_t wj = __shfl_sync(kFull, w, src);
+        const uint64_t gj = shfl_u64(gm, src);
+        my[q] = j[q] < 0 ? 0u : (static_cast<unsigned>(gj >> (2 * ln)) & 3u);
+        p[q] = make_double2(0.0, 0.0);
+        if (my[q]) p[q] = reinterpret_cast<const double2*>(psi)[static_cast<int64_t>(wj) * 32 + ln];
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        if (my[q] & 1u) acc0 += p[q].x;
+        if (my[q] & 2u) acc1 += p[q].y;
+      }
+    }
+  }
+}
+
+// Finalise the dependencies of lanes `mine` of v from the psi sums:
+// delta = sigma * acc, psi[v] = (1 + delta) / sigma; returns the lanes' delta sum.
+__device__ __forceinline__ df32 finish_df(void* psi, const void* sigma, int32_t v, unsigned mine,
+                                          df32 acc0, df32 acc1) {
+  const int ln = lane_id();
+  df32 contrib{0.f, 0.f};
+  if (!mine) return contrib;
+  const ulonglong2 s = reinterpret_cast<const ulonglong2*>(sigma)[static_cast<int64_t>(v) * 32 + ln];
+  df32 p0{0.f, 0.f}, p1{0.f, 0.f};
+  if (mine & 1u) {
+    const df32 sv = df_from_u64(s.x);
+    const df32 d = df_mul(sv, acc0);
+    p0 = df_div(df_add_f(d, 1.0f), sv);
+    contrib = d;
+  }
+  if (mine & 2u) {
+    const df32 sv = df_from_u64(s.y);
+    const df32 d = df_mul(sv, acc1);
+    p1 = df_div(df_add_f(d, 1.0f), sv);
+    contrib = df_add(contrib, d);
+  }
+  float* pf = reinterpret_cast<float*>(psi);
+  const int64_t base = (static_cast<int64_t>(v) * 64 + 2 * ln) * 2;
+  if (mine == 3u) {
+    reinterpret_cast<float4*>(psi)[static_cast<int64_t>(v) * 32 + ln] =
+        make_float4(p0.hi, p0.lo, p1.hi, p1.lo);
+  } else if (mine == 1u) {
+    *reinterpret_cast<float2*>(pf + base) = make_float2(p0.hi, p0.lo);
+  } else {
+    *reinterpret_cast<float2*>(pf + base + 2) = make_float2(p1.hi, p1.lo);
+  }
+  return contrib;
+}
+
+__device__ __forceinline__ double finish_f64(void* psi, const void* sigma, int32_t v, unsigned mine,
+                                             double acc0, double acc1) {
+  const int ln = lane_id();
+  double contrib = 0.0;
+  if (!mine) return contrib;
+  const double2 s = reinterpret_cast<const double2*>(sigma)[static_cast<int64_t>(v) * 32 + ln];
+  double p0 = 0.0, p1 = 0.0;
+  if (mine & 1u) {
+    const double d = s.x * acc0;
+    p0 = (1.0 + d) / s.x;
+    contrib += d;
+  }
+  if (mine & 2u) {
+    const double d = s.y * acc1;
+    p1 = (1.0 + d) / s.y;
+    contrib += d;
+  }
+  double* pd = reinterpret_cast<double*>(psi);
+  if (mine == 3u) {
+    reinterpret_cast<double2*>(psi)[static_cast<int64_t>(v) * 32 + ln] = make_double2(p0, p1);
+  } else if (mine == 1u) {
+    pd[static_cast<int64_t>(v) * 64 + 2 * ln] = p0;
+  } else {
+    pd[static_cast<int64_t>(v) * 64 + 2 * ln + 1] = p1;
+  }
+  return contrib;
+}
+
+__device__ __forceinline__ df32 df_from_double(double x) {
+  const float hi = __double2float_rn(x);
+  const float lo = __double2float_rn(x - static_cast<double>(hi));
+  return df32{hi, lo};
+}
+
+// Last-item handshake of a hub: fence this item's atomics, count it, and
+// report (warp-uniformly) whether it was the hub's last item.
+__device__ __forceinline__ bool hub_last(unsigned int* cnt, int nitems) {
+  __threadfence();
+  unsigned last = 0;
+  if (lane_id() == 0) last = atomicAdd(cnt, 1u) == static_cast<unsigned>(nitems - 1) ? 1u : 0u;
+  last = __shfl_sync(kFull, last, 0);
+  if (last) __threadfence();
+  return last != 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -194,41 +388,59 @@ __global__ void k_ms_init(DevGraph g, MsBuffers b, int nl, unsigned long long ca
 // Top-down, phase 1: expand Q_L over out-edges; the first lane set on a new
 // vertex appends it to Q_{L+1}.  next[w] collects the discovering lanes.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_ms_td_discover(DevGraph g, MsBuffers b) {
+__device__ __forceinline__ void discover_range(const int32_t* __restrict__ ci, int64_t e0, int64_t e1,
+                                               uint64_t F, const uint64_t* __restrict__ visit,
+                                               uint64_t* next, int32_t* qv, BatchCtl* c) {
+  const int ln = lane_id();
+  for (int64_t e = e0; e < e1; e += kWarp) {
+    const int64_t idx = e + ln;
+    bool app = false;
+    int32_t w = 0;
+    if (idx < e1) {
+      w = ci[idx];
+      const uint64_t m = F & ~visit[w];
+      if (m) {
+        const unsigned long long old = atomicOr(reinterpret_cast<unsigned long long*>(next + w), m);
+        app = (old == 0);
+      }
+    }
+    const unsigned long long slot = warp_append(app, &c->tail);
+    if (app) qv[slot] = w;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_ms_td_discover(DevGraph g, MsBuffers b, HubData hd) {
   BatchCtl* c = b.ctl;
   const unsigned long long lo = c->lo, hi = c->hi;
   const int L = c->level;
-  const uint64_t* __restrict__ visit = b.visit;
   uint64_t* next = mb_at(b, L + 1);
-  const int ln = lane_id();
   for (unsigned long long i = lo + gwarp(); i < hi; i += nwarps()) {
     const int32_t v = b.qv[i];
-    const uint64_t F = b.qm[i];
     const int64_t e0 = g.rowptr[v], e1 = g.rowptr[v + 1];
-    for (int64_t e = e0; e < e1; e += kWarp) {
-      const int64_t idx = e + ln;
-      bool app = false;
-      int32_t w = 0;
-      if (idx < e1) {
-        w = g.colidx[idx];
-        const uint64_t m = F & ~visit[w];
-        if (m) {
-          const unsigned long long old =
-              atomicOr(reinterpret_cast<unsigned long long*>(next + w), m);
-          app = (old == 0);
-        }
-      }
-      const unsigned long long slot = warp_append(app, &c->tail);
-      if (app) b.qv[slot] = w;
-    }
+    if (e1 - e0 > hd.hub_degree) continue;  // k_ms_hub_discover
+    discover_range(g.colidx, e0, e1, b.qm[i], b.visit, next, b.qv, c);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_ms_hub_discover(DevGraph g, MsBuffers b, HubData hd) {
+  BatchCtl* c = b.ctl;
+  const int L = c->level;
+  const uint64_t* front = mb_at(b, L);
+  uint64_t* next = mb_at(b, L + 1);
+  for (long long it = gwarp(); it < hd.n_out; it += nwarps()) {
+    const HubItem I = hd.out_items[it];
+    const uint64_t F = front[I.v];
+    if (!F) continue;
+    discover_range(g.colidx, I.lo, I.hi, F, b.visit, next, b.qv, c);
   }
 }
 
 // Top-down, phase 2: for every vertex appended in phase 1, record its lane
-// mask, mark it visited and pull its path counts from its predecessors.
+// mask, mark it visited and pull its path counts from its predecessors
+// (hubs: k_ms_hub_pull).
 template <int SK, bool DIST>
-__global__ void __launch_bounds__(256) k_ms_td_settle(DevGraph g, MsBuffers b, uint64_t act,
-                                                      int32_t* dist, int64_t ld) {
+__global__ void __launch_bounds__(256) k_ms_td_settle(DevGraph g, MsBuffers b, HubData hd,
+                                                      uint64_t act, int32_t* dist, int64_t ld) {
   using T = typename Sig<SK>::T;
   BatchCtl* c = b.ctl;
   const unsigned long long lo = c->hi, hi = c->tail;
@@ -241,19 +453,20 @@ __global__ void __launch_bounds__(256) k_ms_td_settle(DevGraph g, MsBuffers b, u
   for (unsigned long long i = lo + gwarp(); i < hi; i += nwarps()) {
     const int32_t w = b.qv[i];
     const uint64_t mask = next[w];
+    const int64_t e0 = g.in_rowptr[w], e1 = g.in_rowptr[w + 1];
     if (ln == 0) {
       const uint64_t nv = b.visit[w] | mask;
       b.qm[i] = mask;
       b.visit[w] = nv;
       mf += static_cast<unsigned long long>(g.rowptr[w + 1] - g.rowptr[w]);
-      if (nv == act) mu += static_cast<unsigned long long>(g.in_rowptr[w + 1] - g.in_rowptr[w]);
-    }
-    if (SK != kSigmaNone) {
-      T a0 = T(0), a1 = T(0);
-      pull_lanes<SK>(g.in_rowptr, g.in_colidx, w, mask, front, b.sigma, a0, a1, ovf);
-      store_sigma<SK>(b.sigma, w, mask, a0, a1);
+      if (nv == act) mu += static_cast<unsigned long long>(e1 - e0);
     }
     if (DIST) store_dist(dist, ld, w, mask, L + 1);
+    if (SK != kSigmaNone && e1 - e0 <= hd.hub_degree) {
+      T a0 = T(0), a1 = T(0);
+      pull_range<SK>(g.in_colidx, e0, e1, mask, front, b.sigma, a0, a1, ovf);
+      store_sigma<SK>(b.sigma, w, mask, a0, a1);
+    }
   }
   if (SK == kSigmaU64 && __any_sync(kFull, ovf) && ln == 0) c->overflow_sigma = 1;
   if (ln == 0) {
@@ -265,10 +478,11 @@ __global__ void __launch_bounds__(256) k_ms_td_settle(DevGraph g, MsBuffers b, u
 // ---------------------------------------------------------------------------
 // Bottom-up: every vertex some lane has not reached scans its in-neighbours
 // for predecessors in the current frontier.  A warp takes 32 consecutive
-// vertices, so its discoveries are appended with one atomic.
+// vertices, so its discoveries are appended with one atomic.  Hubs are left
+// to k_ms_hub_pull.
 // ---------------------------------------------------------------------------
 template <int SK, bool DIST>
-__global__ void __launch_bounds__(256) k_ms_bu(DevGraph g, MsBuffers b, uint64_t act,
+__global__ void __launch_bounds__(256) k_ms_bu(DevGraph g, MsBuffers b, HubData hd, uint64_t act,
                                                int32_t* dist, int64_t ld) {
   using T = typename Sig<SK>::T;
   BatchCtl* c = b.ctl;
@@ -285,7 +499,8 @@ __global__ void __launch_bounds__(256) k_ms_bu(DevGraph g, MsBuffers b, uint64_t
     bool cand = false;
     if (wme < n) {
       vis = b.visit[wme];
-      cand = (vis != act) && (g.in_rowptr[wme + 1] > g.in_rowptr[wme]);
+      const int64_t d = g.in_rowptr[wme + 1] - g.in_rowptr[wme];
+      cand = (vis != act) && d > 0 && d <= hd.hub_degree;
     }
     unsigned cb = __ballot_sync(kFull, cand);
     uint64_t my_nm = 0;
@@ -295,8 +510,8 @@ __global__ void __launch_bounds__(256) k_ms_bu(DevGraph g, MsBuffers b, uint64_t
       const int32_t w = static_cast<int32_t>(base + j);
       const uint64_t want = act & ~shfl_u64(vis, j);
       T a0 = T(0), a1 = T(0);
-      const uint64_t nm =
-          pull_lanes<SK>(g.in_rowptr, g.in_colidx, w, want, front, b.sigma, a0, a1, ovf);
+      const uint64_t nm = pull_range<SK>(g.in_colidx, g.in_rowptr[w], g.in_rowptr[w + 1], want,
+                                         front, b.sigma, a0, a1, ovf);
       if (nm) {
         if (SK != kSigmaNone) store_sigma<SK>(b.sigma, w, nm, a0, a1);
         if (DIST) store_dist(dist, ld, w, nm, L + 1);
@@ -318,6 +533,77 @@ __global__ void __launch_bounds__(256) k_ms_bu(DevGraph g, MsBuffers b, uint64_t
   if (SK == kSigmaU64 && __any_sync(kFull, ovf) && ln == 0) c->overflow_sigma = 1;
   mf = warp_sum_u64(mf);
   mu = warp_sum_u64(mu);
+  if (ln == 0) {
+    if (mf) atomicAdd(&c->mf, mf);
+    if (mu) atomicAdd(&c->mu_done, mu);
+  }
+}
+
+// Hub path-count pull over in-edge items, for the top-down settle phase
+// (BU == false: the hub was discovered this level, want = next[h]) or the
+// bottom-up phase (BU == true: the hub is not finished, want = unvisited
+// lanes).  Partial sums go to the hub's slot; its last item stores sigma and,
+// bottom-up, appends the hub to the next level.
+template <int SK, bool DIST, bool BU>
+__global__ void __launch_bounds__(256) k_ms_hub_pull(DevGraph g, MsBuffers b, HubData hd,
+                                                     uint64_t act, int32_t* dist, int64_t ld) {
+  using T = typename Sig<SK>::T;
+  BatchCtl* c = b.ctl;
+  const int L = c->level;
+  const uint64_t* __restrict__ front = mb_at(b, L);
+  uint64_t* next = mb_at(b, L + 1);
+  const int ln = lane_id();
+  unsigned long long mf = 0, mu = 0;
+  bool ovf = false;
+  for (long long it = gwarp(); it < hd.n_in; it += nwarps()) {
+    const HubItem I = hd.in_items[it];
+    const int32_t h = I.v;
+    uint64_t vis = 0, want;
+    if (BU) {
+      vis = b.visit[h];
+      if (vis == act) continue;
+      want = act & ~vis;
+    } else {
+      want = next[h];
+      if (!want) continue;
+    }
+    T a0 = T(0), a1 = T(0);
+    const uint64_t found = pull_range<SK>(g.in_colidx, I.lo, I.hi, want, front, b.sigma, a0, a1, ovf);
+    unsigned long long* acc = hd.acc + static_cast<int64_t>(I.slot) * 64;
+    if (SK != kSigmaNone) {
+      if (a0 != T(0)) hub_add(acc + 2 * ln, a0, ovf);
+      if (a1 != T(0)) hub_add(acc + 2 * ln + 1, a1, ovf);
+    }
+    if (BU && ln == 0 && found) atomicOr(hd.mask + I.slot, found);
+    if (!hub_last(hd.cnt + I.slot, I.nitems)) continue;
+    uint64_t nm = want;
+    if (BU) {
+      unsigned long long x = 0;
+      if (ln == 0) x = atomicExch(hd.mask + I.slot, 0ull);
+      nm = shfl_u64(x, 0);
+    }
+    T s0 = T(0), s1 = T(0);
+    if (SK != kSigmaNone) {
+      s0 = from_bits<T>(atomicExch(acc + 2 * ln, 0ull));
+      s1 = from_bits<T>(atomicExch(acc + 2 * ln + 1, 0ull));
+    }
+    if (ln == 0) hd.cnt[I.slot] = 0u;
+    if (nm) {
+      if (SK != kSigmaNone) store_sigma<SK>(b.sigma, h, nm, s0, s1);
+      if (DIST) store_dist(dist, ld, h, nm, L + 1);
+      if (BU && ln == 0) {
+        const unsigned long long slot = atomicAdd(&c->tail, 1ull);
+        b.qv[slot] = h;
+        b.qm[slot] = nm;
+        next[h] = nm;
+        const uint64_t nv = vis | nm;
+        b.visit[h] = nv;
+        mf += static_cast<unsigned long long>(g.rowptr[h + 1] - g.rowptr[h]);
+        if (nv == act) mu += static_cast<unsigned long long>(g.in_rowptr[h + 1] - g.in_rowptr[h]);
+      }
+    }
+  }
+  if (SK == kSigmaU64 && __any_sync(kFull, ovf) && ln == 0) c->overflow_sigma = 1;
   if (ln == 0) {
     if (mf) atomicAdd(&c->mf, mf);
     if (mu) atomicAdd(&c->mu_done, mu);
@@ -374,8 +660,10 @@ __global__ void k_ms_back_clear(MsBuffers b) {
 // and betweenness[v] += sum over lanes of delta (level 0 = sources: skipped,
 // as _accumulate_basic! skips w == s, betweenness.jl:102).
 // psi is the reference's `coeff` (betweenness.jl:96) stored once per vertex.
+// Writes F_L into mb[L & 1] for every v (hubs included) before
+// k_ms_hub_delta finishes the hubs.
 template <int SK>
-__global__ void __launch_bounds__(256) k_ms_delta(DevGraph g, MsBuffers b, double* bc) {
+__global__ void __launch_bounds__(256) k_ms_delta(DevGraph g, MsBuffers b, HubData hd, double* bc) {
   BatchCtl* c = b.ctl;
   const int L = c->level;
   const unsigned long long lo = b.lvl_off[L], hi = b.lvl_off[L + 1];
@@ -391,109 +679,66 @@ __global__ void __launch_bounds__(256) k_ms_delta(DevGraph g, MsBuffers b, doubl
     }
     if (L == 0) continue;
     const int64_t e0 = g.rowptr[v], e1 = g.rowptr[v + 1];
+    if (e1 - e0 > hd.hub_degree) continue;  // k_ms_hub_delta
     const unsigned mine = static_cast<unsigned>(F >> (2 * ln)) & 3u;
     if (SK == kSigmaU64) {
       df32 acc0{0.f, 0.f}, acc1{0.f, 0.f};
-      for (int64_t e = e0; e < e1; e += kWarp) {
-        const int64_t idx = e + ln;
-        int32_t w = 0;
-        uint64_t gm = 0;
-        if (idx < e1) {
-          w = g.colidx[idx];
-          gm = succ[w] & F;
-        }
-        unsigned bal = __ballot_sync(kFull, gm != 0);
-        while (bal) {
-          const int j = __ffs(bal) - 1;
-          bal &= bal - 1;
-          const int32_t wj = __shfl_sync(kFull, w, j);
-          const uint64_t gj = shfl_u64(gm, j);
-          const unsigned my = static_cast<unsigned>(gj >> (2 * ln)) & 3u;
-          if (my) {
-            const float4 p = reinterpret_cast<const float4*>(b.psi)[static_cast<int64_t>(wj) * 32 + ln];
-            if (my & 1u) acc0 = df_add(acc0, df32{p.x, p.y});
-            if (my & 2u) acc1 = df_add(acc1, df32{p.z, p.w});
-          }
-        }
-      }
-      df32 contrib{0.f, 0.f};
-      if (mine) {
-        const ulonglong2 s = reinterpret_cast<const ulonglong2*>(b.sigma)[static_cast<int64_t>(v) * 32 + ln];
-        df32 p0{0.f, 0.f}, p1{0.f, 0.f};
-        if (mine & 1u) {
-          const df32 sv = df_from_u64(s.x);
-          const df32 d = df_mul(sv, acc0);
-          p0 = df_div(df_add_f(d, 1.0f), sv);
-          contrib = d;
-        }
-        if (mine & 2u) {
-          const df32 sv = df_from_u64(s.y);
-          const df32 d = df_mul(sv, acc1);
-          p1 = df_div(df_add_f(d, 1.0f), sv);
-          contrib = df_add(contrib, d);
-        }
-        float* psi = reinterpret_cast<float*>(b.psi);
-        const int64_t base = (static_cast<int64_t>(v) * 64 + 2 * ln) * 2;
-        if (mine == 3u) {
-          reinterpret_cast<float4*>(b.psi)[static_cast<int64_t>(v) * 32 + ln] =
-              make_float4(p0.hi, p0.lo, p1.hi, p1.lo);
-        } else if (mine == 1u) {
-          *reinterpret_cast<float2*>(psi + base) = make_float2(p0.hi, p0.lo);
-        } else {
-          *reinterpret_cast<float2*>(psi + base + 2) = make_float2(p1.hi, p1.lo);
-        }
-      }
+      psi_range_df(g.colidx, e0, e1, F, succ, b.psi, acc0, acc1);
+      df32 contrib = finish_df(b.psi, b.sigma, v, mine, acc0, acc1);
       contrib = warp_sum_df(contrib);
       if (ln == 0) bc[v] += df_to_double(contrib);
-    } else if (SK == kSigmaF64) {
+    } else {
       double acc0 = 0.0, acc1 = 0.0;
-      for (int64_t e = e0; e < e1; e += kWarp) {
-        const int64_t idx = e + ln;
-        int32_t w = 0;
-        uint64_t gm = 0;
-        if (idx < e1) {
-          w = g.colidx[idx];
-          gm = succ[w] & F;
-        }
-        unsigned bal = __ballot_sync(kFull, gm != 0);
-        while (bal) {
-          const int j = __ffs(bal) - 1;
-          bal &= bal - 1;
-          const int32_t wj = __shfl_sync(kFull, w, j);
-          const uint64_t gj = shfl_u64(gm, j);
-          const unsigned my = static_cast<unsigned>(gj >> (2 * ln)) & 3u;
-          if (my) {
-            const double2 p = reinterpret_cast<const double2*>(b.psi)[static_cast<int64_t>(wj) * 32 + ln];
-            if (my & 1u) acc0 += p.x;
-            if (my & 2u) acc1 += p.y;
-          }
-        }
-      }
-      double contrib = 0.0;
-      if (mine) {
-        const double2 s = reinterpret_cast<const double2*>(b.sigma)[static_cast<int64_t>(v) * 32 + ln];
-        double p0 = 0.0, p1 = 0.0;
-        if (mine & 1u) {
-          const double d = s.x * acc0;
-          p0 = (1.0 + d) / s.x;
-          contrib += d;
-        }
-        if (mine & 2u) {
-          const double d = s.y * acc1;
-          p1 = (1.0 + d) / s.y;
-          contrib += d;
-        }
-        double* psi = reinterpret_cast<double*>(b.psi);
-        if (mine == 3u) {
-          reinterpret_cast<double2*>(b.psi)[static_cast<int64_t>(v) * 32 + ln] = make_double2(p0, p1);
-        } else if (mine == 1u) {
-          psi[static_cast<int64_t>(v) * 64 + 2 * ln] = p0;
-        } else {
-          psi[static_cast<int64_t>(v) * 64 + 2 * ln + 1] = p1;
-        }
-      }
+      psi_range_f64(g.colidx, e0, e1, F, succ, b.psi, acc0, acc1);
+      double contrib = finish_f64(b.psi, b.sigma, v, mine, acc0, acc1);
       contrib = warp_sum_f64(contrib);
       if (ln == 0) bc[v] += contrib;
+    }
+  }
+}
+
+// Hub dependencies at level L over out-edge items; partial psi sums are
+// combined in FP64 atomics, the hub's last item finalises delta / psi / bc.
+template <int SK>
+__global__ void __launch_bounds__(256) k_ms_hub_delta(DevGraph g, MsBuffers b, HubData hd, double* bc) {
+  BatchCtl* c = b.ctl;
+  const int L = c->level;
+  if (L == 0) return;
+  const uint64_t* __restrict__ succ = mb_at(b, L + 1);
+  const uint64_t* __restrict__ cur = mb_at(b, L);
+  const int ln = lane_id();
+  bool unused = false;
+  for (long long it = gwarp(); it < hd.n_out; it += nwarps()) {
+    const HubItem I = hd.out_items[it];
+    const int32_t h = I.v;
+    const uint64_t F = cur[h];
+    if (!F) continue;
+    unsigned long long* acc = hd.acc + static_cast<int64_t>(I.slot) * 64;
+    double part0, part1;
+    if (SK == kSigmaU64) {
+      df32 a0{0.f, 0.f}, a1{0.f, 0.f};
+      psi_range_df(g.colidx, I.lo, I.hi, F, succ, b.psi, a0, a1);
+      part0 = df_to_double(a0);
+      part1 = df_to_double(a1);
+    } else {
+      part0 = part1 = 0.0;
+      psi_range_f64(g.colidx, I.lo, I.hi, F, succ, b.psi, part0, part1);
+    }
+    if (part0 != 0.0) hub_add(acc + 2 * ln, part0, unused);
+    if (part1 != 0.0) hub_add(acc + 2 * ln + 1, part1, unused);
+    if (!hub_last(hd.cnt + I.slot, I.nitems)) continue;
+    const double s0 = from_bits<double>(atomicExch(acc + 2 * ln, 0ull));
+    const double s1 = from_bits<double>(atomicExch(acc + 2 * ln + 1, 0ull));
+    if (ln == 0) hd.cnt[I.slot] = 0u;
+    const unsigned mine = static_cast<unsigned>(F >> (2 * ln)) & 3u;
+    if (SK == kSigmaU64) {
+      df32 contrib = finish_df(b.psi, b.sigma, h, mine, df_from_double(s0), df_from_double(s1));
+      contrib = warp_sum_df(contrib);
+      if (ln == 0) bc[h] += df_to_double(contrib);
+    } else {
+      double contrib = finish_f64(b.psi, b.sigma, h, mine, s0, s1);
+      contrib = warp_sum_f64(contrib);
+      if (ln == 0) bc[h] += contrib;
     }
   }
 }
@@ -538,30 +783,58 @@ int ms_init(cudaStream_t s, const DevGraph& g, const MsBuffers& b, int nlanes, i
 }
 
 int ms_topdown(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
-               uint64_t act, int sigma_kind, int32_t* dist, int64_t dist_ld) {
-  k_ms_td_discover<<<c.grid, c.block, 0, s>>>(g, b);
-  if (dist) {
-    k_ms_td_settle<kSigmaNone, true><<<c.grid, c.block, 0, s>>>(g, b, act, dist, dist_ld);
-  } else if (sigma_kind == kSigmaU64) {
-    k_ms_td_settle<kSigmaU64, false><<<c.grid, c.block, 0, s>>>(g, b, act, dist, dist_ld);
-  } else {
-    k_ms_td_settle<kSigmaF64, false><<<c.grid, c.block, 0, s>>>(g, b, act, dist, dist_ld);
+               const HubData& hd, uint64_t act, int sigma_kind, int32_t* dist, int64_t dist_ld) {
+  int launches = 0;
+  k_ms_td_discover<<<c.grid, c.block, 0, s>>>(g, b, hd);
+  ++launches;
+  if (hd.n_out > 0) {
+    k_ms_hub_discover<<<c.grid, c.block, 0, s>>>(g, b, hd);
+    ++launches;
   }
+  if (dist) {
+    k_ms_td_settle<kSigmaNone, true><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
+  } else if (sigma_kind == kSigmaU64) {
+    k_ms_td_settle<kSigmaU64, false><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
+    if (hd.n_in > 0) {
+      k_ms_hub_pull<kSigmaU64, false, false><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
+      ++launches;
+    }
+  } else {
+    k_ms_td_settle<kSigmaF64, false><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
+    if (hd.n_in > 0) {
+      k_ms_hub_pull<kSigmaF64, false, false><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
+      ++launches;
+    }
+  }
+  ++launches;
   k_ms_clear_front<<<c.grid, c.block, 0, s>>>(b);
-  return 3;
+  return launches + 1;
 }
 
 int ms_bottomup(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
-                uint64_t act, int sigma_kind, int32_t* dist, int64_t dist_ld) {
+                const HubData& hd, uint64_t act, int sigma_kind, int32_t* dist, int64_t dist_ld) {
+  int launches = 1;
   if (dist) {
-    k_ms_bu<kSigmaNone, true><<<c.grid, c.block, 0, s>>>(g, b, act, dist, dist_ld);
+    k_ms_bu<kSigmaNone, true><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
+    if (hd.n_in > 0) {
+      k_ms_hub_pull<kSigmaNone, true, true><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
+      ++launches;
+    }
   } else if (sigma_kind == kSigmaU64) {
-    k_ms_bu<kSigmaU64, false><<<c.grid, c.block, 0, s>>>(g, b, act, dist, dist_ld);
+    k_ms_bu<kSigmaU64, false><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
+    if (hd.n_in > 0) {
+      k_ms_hub_pull<kSigmaU64, false, true><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
+      ++launches;
+    }
   } else {
-    k_ms_bu<kSigmaF64, false><<<c.grid, c.block, 0, s>>>(g, b, act, dist, dist_ld);
+    k_ms_bu<kSigmaF64, false><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
+    if (hd.n_in > 0) {
+      k_ms_hub_pull<kSigmaF64, false, true><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
+      ++launches;
+    }
   }
   k_ms_clear_front<<<c.grid, c.block, 0, s>>>(b);
-  return 2;
+  return launches + 1;
 }
 
 int ms_advance(cudaStream_t s, const DevGraph& g, const MsBuffers& b) {
@@ -575,14 +848,24 @@ int ms_begin_backward(cudaStream_t s, const MsBuffers& b) {
 }
 
 int ms_backward_level(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
-                      int sigma_kind, double* bc) {
+                      const HubData& hd, int sigma_kind, double* bc) {
+  int launches = 3;
   k_ms_back_clear<<<c.grid, c.block, 0, s>>>(b);
-  if (sigma_kind == kSigmaF64)
-    k_ms_delta<kSigmaF64><<<c.grid, c.block, 0, s>>>(g, b, bc);
-  else
-    k_ms_delta<kSigmaU64><<<c.grid, c.block, 0, s>>>(g, b, bc);
+  if (sigma_kind == kSigmaF64) {
+    k_ms_delta<kSigmaF64><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
+    if (hd.n_out > 0) {
+      k_ms_hub_delta<kSigmaF64><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
+      ++launches;
+    }
+  } else {
+    k_ms_delta<kSigmaU64><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
+    if (hd.n_out > 0) {
+      k_ms_hub_delta<kSigmaU64><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
+      ++launches;
+    }
+  }
   k_ms_back_advance<<<1, 1, 0, s>>>(b);
-  return 3;
+  return launches;
 }
 
 int ms_cleanup(const LaunchCfg& c, cudaStream_t s, const MsBuffers& b) {

@@ -177,7 +177,7 @@ def test_long_path_grows_level_lists():
     d = lgbc.multi_gdistances(g, list(src + 1))
     rp, ci, _ = csr_args(g)
     for i in (0, 17, 63):
-        assert np.array_equal(d[i], oracle.gdistances(rp, ci, [src[i]]).astype(np.int64))
+        assert np.array_equal(d[i], oracle.gdistances(rp, ci, [src[i]]).astype(g.eltype))
 
 
 def test_grid_path_counts_overflow_replay():
@@ -204,15 +204,16 @@ def test_gdistances_random(name, direction):
     rng = np.random.default_rng(1)
     for srcs in ([0], [5, 17, 1000], rng.choice(g.nv(), 40).tolist()):
         got = lgbc.gdistances(g, [s + 1 for s in srcs])
+        assert got.dtype == g.eltype
         exp = oracle.gdistances(rp, ci, srcs).astype(np.int64)
-        exp[exp == oracle.UNREACHED32] = np.iinfo(np.int64).max
-        assert np.array_equal(got, exp)
+        exp[exp == oracle.UNREACHED32] = np.iinfo(g.eltype).max
+        assert np.array_equal(got.astype(np.int64), exp)
     batch = rng.choice(g.nv(), 70).astype(np.int32)
     got = lgbc.multi_gdistances(g, list(batch + 1))
     for i, s in enumerate(batch):
         exp = oracle.gdistances(rp, ci, [s]).astype(np.int64)
-        exp[exp == oracle.UNREACHED32] = np.iinfo(np.int64).max
-        assert np.array_equal(got[i], exp)
+        exp[exp == oracle.UNREACHED32] = np.iinfo(g.eltype).max
+        assert np.array_equal(got[i].astype(np.int64), exp)
 
 
 def test_gdistances_inplace_semantics():
