@@ -154,6 +154,7 @@ struct lgbc_graph {
   int64_t launches_at_start = 0;
   LaunchCfg cfg{};
   size_t max_smem = 0;
+  unsigned long long sigma_limit = ~0ull;  // (2^64 - 1) / (max in-degree + 1)
   lgbc_stats stats{};
   lgbc_tuning tune{14.0, 24.0, 512, 64};
 
@@ -414,7 +415,7 @@ int run_ms_batch(lgbc_graph* g, const int32_t* lane_src, int nl, int sigma_kind,
   const uint64_t act = nl >= 64 ? ~0ull : ((1ull << nl) - 1ull);
   for (;;) {
     MsBuffers b = ms_buffers(g, lane_src);
-    g->launches += ms_init(g->stream, dg, b, nl, sigma_kind, dist, dist_ld);
+    g->launches += ms_init(g->stream, dg, b, nl, sigma_kind, g->sigma_limit, dist, dist_ld);
     LGBC_TRY(check_launch(g));
     bool bu = false;
     bool regrow = false;
@@ -566,11 +567,15 @@ int create_impl(lgbc_graph* g, int64_t n, int64_t nnz, const int64_t* rowptr, co
   cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, g->stream);
   // degree(g, v) > 0: in+out for digraphs (src/core.jl:66-67), kept on the host
   g->has_degree.assign(static_cast<size_t>(n), 0);
+  int64_t max_in = 0;
   for (int64_t v = 0; v < n; ++v) {
-    int64_t d = rowptr[v + 1] - rowptr[v];
-    if (directed) d += in_rowptr[v + 1] - in_rowptr[v];
+    const int64_t dout = rowptr[v + 1] - rowptr[v];
+    const int64_t din = directed ? in_rowptr[v + 1] - in_rowptr[v] : dout;
+    const int64_t d = directed ? dout + din : dout;
     g->has_degree[static_cast<size_t>(v)] = d > 0 ? 1 : 0;
+    max_in = std::max(max_in, din);
   }
+  g->sigma_limit = ~0ull / static_cast<unsigned long long>(max_in + 1);
   cudaError_t e = cudaStreamSynchronize(g->stream);
   cudaFree(d_bad);
   if (e != cudaSuccess) return cuda_fail(e, "graph upload");

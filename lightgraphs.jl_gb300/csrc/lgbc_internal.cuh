@@ -37,8 +37,11 @@ struct BatchCtl {
   int maxlevel;                 // deepest non-empty level (set when the forward ends)
   int done;                     // forward finished (Q_{L+1} empty)
   int overflow_list;            // list capacity exceeded (host grows + replays)
-  int overflow_sigma;           // a path count exceeded 2^64 (host replays in FP64)
+  int overflow_sigma;           // path counts may exceed 2^64 (host replays in FP64)
   int mode;                     // 0 = top-down, 1 = bottom-up (for the next level)
+  unsigned long long sigma_max;   // largest path count stored this level
+  unsigned long long sigma_limit; // (2^64 - 1) / (max in-degree + 1): a level whose
+                                  // counts stay <= this cannot overflow the next
 };
 
 // ---------------------------------------------------------------------------
@@ -57,6 +60,30 @@ __device__ __forceinline__ uint64_t warp_or_u64(uint64_t x) {
   uint32_t lo = __reduce_or_sync(kFull, static_cast<uint32_t>(x));
   uint32_t hi = __reduce_or_sync(kFull, static_cast<uint32_t>(x >> 32));
   return (static_cast<uint64_t>(hi) << 32) | lo;
+}
+
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long y = shfl_u64(x, lane_id() ^ o);
+    x = y > x ? y : x;
+  }
+  return x;
+}
+
+// 32 x 32 bit-matrix transpose across a warp: thread t enters with row t
+// (bit j = element (t, j)) and leaves with column t (bit j = element (j, t)).
+// Recursive block swap (Hacker's Delight 7-3) with one shuffle per level.
+__device__ __forceinline__ uint32_t warp_transpose32(uint32_t a) {
+  const int ln = threadIdx.x & 31;
+#pragma unroll
+  for (int s = 16; s >= 1; s >>= 1) {
+    const uint32_t m = s == 16 ? 0x0000FFFFu : s == 8 ? 0x00FF00FFu : s == 4 ? 0x0F0F0F0Fu
+                     : s == 2 ? 0x33333333u : 0x55555555u;
+    const uint32_t x = __shfl_xor_sync(0xffffffffu, a, s);
+    a = (ln & s) ? ((a & ~m) | ((x & ~m) >> s)) : ((a & m) | ((x & m) << s));
+  }
+  return a;
 }
 
 __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long x) {

@@ -61,8 +61,10 @@ struct HubData {
   int hub_degree;                // degree above which a vertex is a hub (INT32_MAX: none)
 };
 
+// sigma_limit: (2^64 - 1) / (max in-degree + 1), the largest path count a
+// level may hold without the next level risking 64-bit overflow.
 int ms_init(cudaStream_t s, const DevGraph& g, const MsBuffers& b, int nlanes, int sigma_kind,
-            int32_t* dist, int64_t dist_ld);
+            unsigned long long sigma_limit, int32_t* dist, int64_t dist_ld);
 int ms_topdown(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
                const HubData& hd, uint64_t act, int sigma_kind, int32_t* dist, int64_t dist_ld);
 int ms_bottomup(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,

@@ -21,11 +21,14 @@
 //   sigma[v*64 + l]   uint64 path count (or FP64 in the overflow replay)
 //   psi[v*64 + l]     df32 (1 + delta) / sigma (or FP64)
 //   qv/qm             concatenated per-level lists of (vertex, lane mask)
-// A warp owns one vertex; thread t owns lanes 2t and 2t+1, so a vertex's
-// 64 lanes are one 512-byte row read by 32 coalesced 16-byte accesses.
-// Neighbour rows are gathered four at a time so each warp keeps four row
-// loads in flight.  Hubs (more than hub_degree neighbours) are cut into
-// kHubChunk-edge items processed by the whole grid (k_ms_hub_*).
+// A warp owns one vertex; thread t owns lanes t and t + 32.  Edges are read
+// 32 at a time; when several of them carry lanes, the warp transposes the
+// 32 x 64 bit matrix (edge, lane) so that each thread walks only the edges
+// on which its own lanes are set, four row loads in flight at a time (each
+// useful lane-op costs one 8-byte load and one add, no broadcast).  Chunks
+// with one or two such edges take a per-edge path instead.  Hubs (more than
+// hub_degree neighbours) are cut into kHubChunk-edge items processed by the
+// whole grid (k_ms_hub_*).
 #include "lgbc_kernels.h"
 
 namespace lgbc {
@@ -58,18 +61,10 @@ template <> struct Sig<kSigmaF64> {
   using Pair = double2;
 };
 
-__device__ __forceinline__ void sig_add(unsigned long long& a, unsigned long long x, bool& ovf) {
-  unsigned long long t = a + x;
-  ovf |= (t < a);
-  a = t;
+__device__ __forceinline__ void hub_add(unsigned long long* p, unsigned long long x) {
+  atomicAdd(p, x);
 }
-__device__ __forceinline__ void sig_add(double& a, double x, bool&) { a += x; }
-
-__device__ __forceinline__ void hub_add(unsigned long long* p, unsigned long long x, bool& ovf) {
-  const unsigned long long old = atomicAdd(p, x);
-  ovf |= (old + x < old);
-}
-__device__ __forceinline__ void hub_add(unsigned long long* p, double x, bool&) {
+__device__ __forceinline__ void hub_add(unsigned long long* p, double x) {
   atomicAdd(reinterpret_cast<double*>(p), x);
 }
 
@@ -79,50 +74,127 @@ template <> __device__ __forceinline__ double from_bits(unsigned long long x) {
   return __longlong_as_double(static_cast<long long>(x));
 }
 
-template <class P, class T> __device__ __forceinline__ P make_pair2(T a, T b);
-template <> __device__ __forceinline__ ulonglong2 make_pair2(unsigned long long a, unsigned long long b) {
-  return make_ulonglong2(a, b);
-}
-template <> __device__ __forceinline__ double2 make_pair2(double a, double b) {
-  return make_double2(a, b);
+// Bits (t, t + 32) of a lane mask, as bit 0 / bit 1.
+__device__ __forceinline__ unsigned my_bits(uint64_t m) {
+  const int ln = lane_id();
+  return static_cast<unsigned>((m >> ln) & 1ull) |
+         (static_cast<unsigned>((m >> (32 + ln)) & 1ull) << 1);
 }
 
-// Store the path counts of lanes (2t, 2t+1) of w that are set in `mask`.
+__device__ __forceinline__ unsigned long long max_u64(unsigned long long a, unsigned long long b) {
+  return a > b ? a : b;
+}
+
+// Store the path counts of lanes (t, t + 32) of w that are set in `mask`.
 // Lanes outside `mask` may be read concurrently by other warps (w sits at
-// another level for them), so they are never written.
+// another level for them), so they are never written.  Tracks the largest
+// stored count (for the per-level overflow bound).
 template <int SK>
 __device__ __forceinline__ void store_sigma(void* sigma, int32_t w, uint64_t mask,
-                                            typename Sig<SK>::T a0, typename Sig<SK>::T a1) {
+                                            typename Sig<SK>::T a0, typename Sig<SK>::T a1,
+                                            unsigned long long& smax) {
   using T = typename Sig<SK>::T;
-  using P = typename Sig<SK>::Pair;
   const int ln = lane_id();
-  unsigned my = static_cast<unsigned>(mask >> (2 * ln)) & 3u;
-  if (my == 3u) {
-    reinterpret_cast<P*>(sigma)[static_cast<int64_t>(w) * 32 + ln] = make_pair2<P, T>(a0, a1);
-  } else if (my == 1u) {
-    reinterpret_cast<T*>(sigma)[static_cast<int64_t>(w) * 64 + 2 * ln] = a0;
-  } else if (my == 2u) {
-    reinterpret_cast<T*>(sigma)[static_cast<int64_t>(w) * 64 + 2 * ln + 1] = a1;
+  const unsigned my = my_bits(mask);
+  T* row = reinterpret_cast<T*>(sigma) + static_cast<int64_t>(w) * 64;
+  if (my & 1u) row[ln] = a0;
+  if (my & 2u) row[32 + ln] = a1;
+  if (SK == kSigmaU64) {
+    if (my & 1u) smax = max_u64(smax, static_cast<unsigned long long>(a0));
+    if (my & 2u) smax = max_u64(smax, static_cast<unsigned long long>(a1));
   }
 }
 
 __device__ __forceinline__ void store_dist(int32_t* dist, int64_t ld, int32_t w, uint64_t mask,
                                            int32_t level) {
   const int ln = lane_id();
-  unsigned my = static_cast<unsigned>(mask >> (2 * ln)) & 3u;
-  if (my & 1u) dist[static_cast<int64_t>(2 * ln) * ld + w] = level;
-  if (my & 2u) dist[static_cast<int64_t>(2 * ln + 1) * ld + w] = level;
+  const unsigned my = my_bits(mask);
+  if (my & 1u) dist[static_cast<int64_t>(ln) * ld + w] = level;
+  if (my & 2u) dist[static_cast<int64_t>(32 + ln) * ld + w] = level;
 }
 
-// Take up to four set bits of a warp-uniform ballot (-1 when exhausted).
-__device__ __forceinline__ void take4(unsigned& bal, int (&j)[4]) {
+// Compensated double-float accumulator: hi carries the running sum, lo the
+// exact rounding errors of the hi additions plus the addends' own lo parts;
+// normalised once at the end (acc_done).  7 FP32 additions per term.
+__device__ __forceinline__ void acc_add(df32& acc, float xh, float xl) {
+  const df32 t = two_sum(acc.hi, xh);
+  acc.hi = t.hi;
+  acc.lo = __fadd_rn(acc.lo, __fadd_rn(t.lo, xl));
+}
+__device__ __forceinline__ df32 acc_done(df32 acc) { return fast_two_sum(acc.hi, acc.lo); }
+
+// Row element types of the two gathers.
+template <int SK> struct Rows;
+template <> struct Rows<kSigmaU64> { using T = unsigned long long; };
+template <> struct Rows<kSigmaF64> { using T = double; };
+
+template <class T, class A> __device__ __forceinline__ void acc_row(A& acc, T x);
+template <> __device__ __forceinline__ void acc_row(unsigned long long& acc, unsigned long long x) { acc += x; }
+template <> __device__ __forceinline__ void acc_row(double& acc, double x) { acc += x; }
+template <> __device__ __forceinline__ void acc_row(df32& acc, float2 x) { acc_add(acc, x.x, x.y); }
+
+template <class T> __device__ __forceinline__ T zero_row();
+template <> __device__ __forceinline__ unsigned long long zero_row() { return 0ull; }
+template <> __device__ __forceinline__ double zero_row() { return 0.0; }
+template <> __device__ __forceinline__ float2 zero_row() { return make_float2(0.f, 0.f); }
+
+// Chunk gather.  Each of the 32 threads holds one edge (neighbour id `nb`,
+// lane mask `f` of the lanes that edge contributes to).  Adds, for this
+// thread's lanes t and t + 32, rows[nb_j * 64 + lane] over every edge j whose
+// mask has that lane, into (a0, a1).
+template <class T, class A>
+__device__ __forceinline__ void gather_chunk(int32_t nb, uint64_t f, const T* __restrict__ rows,
+                                             A& a0, A& a1) {
+  const int ln = lane_id();
+  const unsigned bal = __ballot_sync(kFull, f != 0);
+  if (bal == 0) return;
+  const T* r0 = rows + ln;
+  const T* r1 = rows + 32 + ln;
+  if (__popc(bal) <= 2) {
+    // per-edge path: broadcast each set edge to the warp
+    unsigned b = bal;
+    while (b) {
+      const int j = __ffs(b) - 1;
+      b &= b - 1;
+      const int32_t vj = __shfl_sync(kFull, nb, j);
+      const uint64_t fj = shfl_u64(f, j);
+      const unsigned my = my_bits(fj);
+      const int64_t off = static_cast<int64_t>(vj) * 64;
+      T x0 = zero_row<T>(), x1 = zero_row<T>();
+      if (my & 1u) x0 = r0[off];
+      if (my & 2u) x1 = r1[off];
+      if (my & 1u) acc_row<T, A>(a0, x0);
+      if (my & 2u) acc_row<T, A>(a1, x1);
+    }
+    return;
+  }
+  // transposed path: thread t gets the edges that carry lane t / lane t + 32
+  uint32_t E0 = warp_transpose32(static_cast<uint32_t>(f));
+  uint32_t E1 = warp_transpose32(static_cast<uint32_t>(f >> 32));
+  const int cnt = static_cast<int>(__reduce_max_sync(kFull, static_cast<unsigned>(__popc(E0) + __popc(E1))));
+  for (int k = 0; k < cnt; k += 4) {
+    int32_t vj[4];
+    unsigned sel[4];  // 0 = none, 1 = lane t, 2 = lane t + 32
 #pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    if (bal) {
-      j[q] = __ffs(bal) - 1;
-      bal &= bal - 1;
-    } else {
-      j[q] = -1;
+    for (int q = 0; q < 4; ++q) {
+      const bool lo = E0 != 0u;
+      uint32_t E = lo ? E0 : E1;
+      const int j = E ? __ffs(E) - 1 : 0;
+      sel[q] = E ? (lo ? 1u : 2u) : 0u;
+      E &= E - 1u;
+      if (lo) E0 = E; else E1 = E;
+      vj[q] = __shfl_sync(kFull, nb, j);
+    }
+    T x[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      x[q] = zero_row<T>();
+      if (sel[q]) x[q] = (sel[q] == 1u ? r0 : r1)[static_cast<int64_t>(vj[q]) * 64];
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      if (sel[q] == 1u) acc_row<T, A>(a0, x[q]);
+      if (sel[q] == 2u) acc_row<T, A>(a1, x[q]);
     }
   }
 }
@@ -137,10 +209,7 @@ __device__ __forceinline__ uint64_t pull_range(const int32_t* __restrict__ ci, i
                                                int64_t e1, uint64_t want,
                                                const uint64_t* __restrict__ front,
                                                const void* __restrict__ sigma,
-                                               typename Sig<SK>::T& a0, typename Sig<SK>::T& a1,
-                                               bool& ovf) {
-  using T = typename Sig<SK>::T;
-  using P = typename Sig<SK>::Pair;
+                                               typename Sig<SK>::T& a0, typename Sig<SK>::T& a1) {
   const int ln = lane_id();
   uint64_t found = 0;
   for (int64_t e = e0; e < e1; e += kWarp) {
@@ -156,27 +225,8 @@ __device__ __forceinline__ uint64_t pull_range(const int32_t* __restrict__ ci, i
       if (warp_or_u64(found) == want) break;
       continue;
     }
-    unsigned bal = __ballot_sync(kFull, f != 0);
-    while (bal) {
-      int j[4];
-      take4(bal, j);
-      P p[4];
-      unsigned my[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int src = j[q] < 0 ? 0 : j[q];
-        const int32_t vj = __shfl_sync(kFull, v, src);
-        const uint64_t fj = shfl_u64(f, src);
-        my[q] = j[q] < 0 ? 0u : (static_cast<unsigned>(fj >> (2 * ln)) & 3u);
-        p[q] = make_pair2<P, T>(T(0), T(0));
-        if (my[q]) p[q] = reinterpret_cast<const P*>(sigma)[static_cast<int64_t>(vj) * 32 + ln];
-      }
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        if (my[q] & 1u) sig_add(a0, p[q].x, ovf);
-        if (my[q] & 2u) sig_add(a1, p[q].y, ovf);
-      }
-    }
+    using T = typename Sig<SK>::T;
+    gather_chunk<T, T>(v, f, reinterpret_cast<const T*>(sigma), a0, a1);
   }
   return warp_or_u64(found);
 }
@@ -196,28 +246,10 @@ __device__ __forceinline__ void psi_range_df(const int32_t* __restrict__ ci, int
       w = ci[idx];
       gm = succ[w] & F;
     }
-    unsigned bal = __ballot_sync(kFull, gm != 0);
-    while (bal) {
-      int j[4];
-      take4(bal, j);
-      float4 p[4];
-      unsigned my[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int src = j[q] < 0 ? 0 : j[q];
-        const int32_t wj = __shfl_sync(kFull, w, src);
-        const uint64_t gj = shfl_u64(gm, src);
-        my[q] = j[q] < 0 ? 0u : (static_cast<unsigned>(gj >> (2 * ln)) & 3u);
-        p[q] = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (my[q]) p[q] = reinterpret_cast<const float4*>(psi)[static_cast<int64_t>(wj) * 32 + ln];
-      }
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        if (my[q] & 1u) acc0 = df_add(acc0, df32{p[q].x, p[q].y});
-        if (my[q] & 2u) acc1 = df_add(acc1, df32{p[q].z, p[q].w});
-      }
-    }
+    gather_chunk<float2, df32>(w, gm, reinterpret_cast<const float2*>(psi), acc0, acc1);
   }
+  acc0 = acc_done(acc0);
+  acc1 = acc_done(acc1);
 }
 
 __device__ __forceinline__ void psi_range_f64(const int32_t* __restrict__ ci, int64_t e0, int64_t e1,
@@ -233,60 +265,34 @@ __device__ __forceinline__ void psi_range_f64(const int32_t* __restrict__ ci, in
       w = ci[idx];
       gm = succ[w] & F;
     }
-    unsigned bal = __ballot_sync(kFull, gm != 0);
-    while (bal) {
-      int j[4];
-      take4(bal, j);
-      double2 p[4];
-      unsigned my[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int src = j[q] < 0 ? 0 : j[q];
-        const int32_t wj = __shfl_sync(kFull, w, src);
-        const uint64_t gj = shfl_u64(gm, src);
-        my[q] = j[q] < 0 ? 0u : (static_cast<unsigned>(gj >> (2 * ln)) & 3u);
-        p[q] = make_double2(0.0, 0.0);
-        if (my[q]) p[q] = reinterpret_cast<const double2*>(psi)[static_cast<int64_t>(wj) * 32 + ln];
-      }
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        if (my[q] & 1u) acc0 += p[q].x;
-        if (my[q] & 2u) acc1 += p[q].y;
-      }
-    }
+    gather_chunk<double, double>(w, gm, reinterpret_cast<const double*>(psi), acc0, acc1);
   }
 }
 
-// Finalise the dependencies of lanes `mine` of v from the psi sums:
-// delta = sigma * acc, psi[v] = (1 + delta) / sigma; returns the lanes' delta sum.
+// Finalise the dependencies of lanes `mine` (bit 0 = lane t, bit 1 = lane
+// t + 32) of v from the psi sums: delta = sigma * acc, psi[v] = (1 + delta) /
+// sigma; returns the lanes' delta sum.
 __device__ __forceinline__ df32 finish_df(void* psi, const void* sigma, int32_t v, unsigned mine,
                                           df32 acc0, df32 acc1) {
   const int ln = lane_id();
   df32 contrib{0.f, 0.f};
   if (!mine) return contrib;
-  const ulonglong2 s = reinterpret_cast<const ulonglong2*>(sigma)[static_cast<int64_t>(v) * 32 + ln];
-  df32 p0{0.f, 0.f}, p1{0.f, 0.f};
+  const unsigned long long* srow =
+      reinterpret_cast<const unsigned long long*>(sigma) + static_cast<int64_t>(v) * 64;
+  float2* prow = reinterpret_cast<float2*>(psi) + static_cast<int64_t>(v) * 64;
   if (mine & 1u) {
-    const df32 sv = df_from_u64(s.x);
+    const df32 sv = df_from_u64(srow[ln]);
     const df32 d = df_mul(sv, acc0);
-    p0 = df_div(df_add_f(d, 1.0f), sv);
+    const df32 p = df_div(df_add_f(d, 1.0f), sv);
+    prow[ln] = make_float2(p.hi, p.lo);
     contrib = d;
   }
   if (mine & 2u) {
-    const df32 sv = df_from_u64(s.y);
+    const df32 sv = df_from_u64(srow[32 + ln]);
     const df32 d = df_mul(sv, acc1);
-    p1 = df_div(df_add_f(d, 1.0f), sv);
+    const df32 p = df_div(df_add_f(d, 1.0f), sv);
+    prow[32 + ln] = make_float2(p.hi, p.lo);
     contrib = df_add(contrib, d);
-  }
-  float* pf = reinterpret_cast<float*>(psi);
-  const int64_t base = (static_cast<int64_t>(v) * 64 + 2 * ln) * 2;
-  if (mine == 3u) {
-    reinterpret_cast<float4*>(psi)[static_cast<int64_t>(v) * 32 + ln] =
-        make_float4(p0.hi, p0.lo, p1.hi, p1.lo);
-  } else if (mine == 1u) {
-    *reinterpret_cast<float2*>(pf + base) = make_float2(p0.hi, p0.lo);
-  } else {
-    *reinterpret_cast<float2*>(pf + base + 2) = make_float2(p1.hi, p1.lo);
   }
   return contrib;
 }
@@ -296,25 +302,19 @@ __device__ __forceinline__ double finish_f64(void* psi, const void* sigma, int32
   const int ln = lane_id();
   double contrib = 0.0;
   if (!mine) return contrib;
-  const double2 s = reinterpret_cast<const double2*>(sigma)[static_cast<int64_t>(v) * 32 + ln];
-  double p0 = 0.0, p1 = 0.0;
+  const double* srow = reinterpret_cast<const double*>(sigma) + static_cast<int64_t>(v) * 64;
+  double* prow = reinterpret_cast<double*>(psi) + static_cast<int64_t>(v) * 64;
   if (mine & 1u) {
-    const double d = s.x * acc0;
-    p0 = (1.0 + d) / s.x;
+    const double sv = srow[ln];
+    const double d = sv * acc0;
+    prow[ln] = (1.0 + d) / sv;
     contrib += d;
   }
   if (mine & 2u) {
-    const double d = s.y * acc1;
-    p1 = (1.0 + d) / s.y;
+    const double sv = srow[32 + ln];
+    const double d = sv * acc1;
+    prow[32 + ln] = (1.0 + d) / sv;
     contrib += d;
-  }
-  double* pd = reinterpret_cast<double*>(psi);
-  if (mine == 3u) {
-    reinterpret_cast<double2*>(psi)[static_cast<int64_t>(v) * 32 + ln] = make_double2(p0, p1);
-  } else if (mine == 1u) {
-    pd[static_cast<int64_t>(v) * 64 + 2 * ln] = p0;
-  } else {
-    pd[static_cast<int64_t>(v) * 64 + 2 * ln + 1] = p1;
   }
   return contrib;
 }
@@ -341,8 +341,8 @@ __device__ __forceinline__ bool hub_last(unsigned int* cnt, int nitems) {
 // source gets several lanes in one list entry).
 // ---------------------------------------------------------------------------
 template <int SK>
-__global__ void k_ms_init(DevGraph g, MsBuffers b, int nl, unsigned long long cap, int32_t* dist,
-                          int64_t ld) {
+__global__ void k_ms_init(DevGraph g, MsBuffers b, int nl, unsigned long long cap,
+                          unsigned long long sigma_limit, int32_t* dist, int64_t ld) {
   if (blockIdx.x != 0 || threadIdx.x != 0) return;
   using T = typename Sig<SK>::T;
   const uint64_t act = nl >= 64 ? ~0ull : ((1ull << nl) - 1ull);
@@ -380,6 +380,8 @@ __global__ void k_ms_init(DevGraph g, MsBuffers b, int nl, unsigned long long ca
   c->overflow_list = 0;
   c->overflow_sigma = 0;
   c->mode = 0;
+  c->sigma_max = 1;
+  c->sigma_limit = sigma_limit;
   b.lvl_off[0] = 0;
   b.lvl_off[1] = tail;
 }
@@ -448,8 +450,7 @@ __global__ void __launch_bounds__(256) k_ms_td_settle(DevGraph g, MsBuffers b, H
   const uint64_t* __restrict__ front = mb_at(b, L);
   const uint64_t* __restrict__ next = mb_at(b, L + 1);
   const int ln = lane_id();
-  unsigned long long mf = 0, mu = 0;
-  bool ovf = false;
+  unsigned long long mf = 0, mu = 0, smax = 0;
   for (unsigned long long i = lo + gwarp(); i < hi; i += nwarps()) {
     const int32_t w = b.qv[i];
     const uint64_t mask = next[w];
@@ -464,11 +465,14 @@ __global__ void __launch_bounds__(256) k_ms_td_settle(DevGraph g, MsBuffers b, H
     if (DIST) store_dist(dist, ld, w, mask, L + 1);
     if (SK != kSigmaNone && e1 - e0 <= hd.hub_degree) {
       T a0 = T(0), a1 = T(0);
-      pull_range<SK>(g.in_colidx, e0, e1, mask, front, b.sigma, a0, a1, ovf);
-      store_sigma<SK>(b.sigma, w, mask, a0, a1);
+      pull_range<SK>(g.in_colidx, e0, e1, mask, front, b.sigma, a0, a1);
+      store_sigma<SK>(b.sigma, w, mask, a0, a1, smax);
     }
   }
-  if (SK == kSigmaU64 && __any_sync(kFull, ovf) && ln == 0) c->overflow_sigma = 1;
+  if (SK == kSigmaU64) {
+    smax = warp_max_u64(smax);
+    if (ln == 0 && smax) atomicMax(&c->sigma_max, smax);
+  }
   if (ln == 0) {
     if (mf) atomicAdd(&c->mf, mf);
     if (mu) atomicAdd(&c->mu_done, mu);
@@ -491,8 +495,7 @@ __global__ void __launch_bounds__(256) k_ms_bu(DevGraph g, MsBuffers b, HubData 
   uint64_t* next = mb_at(b, L + 1);
   const int64_t n = g.n;
   const int ln = lane_id();
-  unsigned long long mf = 0, mu = 0;
-  bool ovf = false;
+  unsigned long long mf = 0, mu = 0, smax = 0;
   for (int64_t base = gwarp() * kWarp; base < n; base += nwarps() * kWarp) {
     const int64_t wme = base + ln;
     uint64_t vis = 0;
@@ -511,9 +514,9 @@ __global__ void __launch_bounds__(256) k_ms_bu(DevGraph g, MsBuffers b, HubData 
       const uint64_t want = act & ~shfl_u64(vis, j);
       T a0 = T(0), a1 = T(0);
       const uint64_t nm = pull_range<SK>(g.in_colidx, g.in_rowptr[w], g.in_rowptr[w + 1], want,
-                                         front, b.sigma, a0, a1, ovf);
+                                         front, b.sigma, a0, a1);
       if (nm) {
-        if (SK != kSigmaNone) store_sigma<SK>(b.sigma, w, nm, a0, a1);
+        if (SK != kSigmaNone) store_sigma<SK>(b.sigma, w, nm, a0, a1, smax);
         if (DIST) store_dist(dist, ld, w, nm, L + 1);
       }
       if (ln == j) my_nm = nm;
@@ -530,7 +533,10 @@ __global__ void __launch_bounds__(256) k_ms_bu(DevGraph g, MsBuffers b, HubData 
       if (nv == act) mu += static_cast<unsigned long long>(g.in_rowptr[wme + 1] - g.in_rowptr[wme]);
     }
   }
-  if (SK == kSigmaU64 && __any_sync(kFull, ovf) && ln == 0) c->overflow_sigma = 1;
+  if (SK == kSigmaU64) {
+    smax = warp_max_u64(smax);
+    if (ln == 0 && smax) atomicMax(&c->sigma_max, smax);
+  }
   mf = warp_sum_u64(mf);
   mu = warp_sum_u64(mu);
   if (ln == 0) {
@@ -553,8 +559,7 @@ __global__ void __launch_bounds__(256) k_ms_hub_pull(DevGraph g, MsBuffers b, Hu
   const uint64_t* __restrict__ front = mb_at(b, L);
   uint64_t* next = mb_at(b, L + 1);
   const int ln = lane_id();
-  unsigned long long mf = 0, mu = 0;
-  bool ovf = false;
+  unsigned long long mf = 0, mu = 0, smax = 0;
   for (long long it = gwarp(); it < hd.n_in; it += nwarps()) {
     const HubItem I = hd.in_items[it];
     const int32_t h = I.v;
@@ -568,11 +573,11 @@ __global__ void __launch_bounds__(256) k_ms_hub_pull(DevGraph g, MsBuffers b, Hu
       if (!want) continue;
     }
     T a0 = T(0), a1 = T(0);
-    const uint64_t found = pull_range<SK>(g.in_colidx, I.lo, I.hi, want, front, b.sigma, a0, a1, ovf);
+    const uint64_t found = pull_range<SK>(g.in_colidx, I.lo, I.hi, want, front, b.sigma, a0, a1);
     unsigned long long* acc = hd.acc + static_cast<int64_t>(I.slot) * 64;
     if (SK != kSigmaNone) {
-      if (a0 != T(0)) hub_add(acc + 2 * ln, a0, ovf);
-      if (a1 != T(0)) hub_add(acc + 2 * ln + 1, a1, ovf);
+      if (a0 != T(0)) hub_add(acc + ln, a0);
+      if (a1 != T(0)) hub_add(acc + 32 + ln, a1);
     }
     if (BU && ln == 0 && found) atomicOr(hd.mask + I.slot, found);
     if (!hub_last(hd.cnt + I.slot, I.nitems)) continue;
@@ -584,12 +589,12 @@ __global__ void __launch_bounds__(256) k_ms_hub_pull(DevGraph g, MsBuffers b, Hu
     }
     T s0 = T(0), s1 = T(0);
     if (SK != kSigmaNone) {
-      s0 = from_bits<T>(atomicExch(acc + 2 * ln, 0ull));
-      s1 = from_bits<T>(atomicExch(acc + 2 * ln + 1, 0ull));
+      s0 = from_bits<T>(atomicExch(acc + ln, 0ull));
+      s1 = from_bits<T>(atomicExch(acc + 32 + ln, 0ull));
     }
     if (ln == 0) hd.cnt[I.slot] = 0u;
     if (nm) {
-      if (SK != kSigmaNone) store_sigma<SK>(b.sigma, h, nm, s0, s1);
+      if (SK != kSigmaNone) store_sigma<SK>(b.sigma, h, nm, s0, s1, smax);
       if (DIST) store_dist(dist, ld, h, nm, L + 1);
       if (BU && ln == 0) {
         const unsigned long long slot = atomicAdd(&c->tail, 1ull);
@@ -603,7 +608,10 @@ __global__ void __launch_bounds__(256) k_ms_hub_pull(DevGraph g, MsBuffers b, Hu
       }
     }
   }
-  if (SK == kSigmaU64 && __any_sync(kFull, ovf) && ln == 0) c->overflow_sigma = 1;
+  if (SK == kSigmaU64) {
+    smax = warp_max_u64(smax);
+    if (ln == 0 && smax) atomicMax(&c->sigma_max, smax);
+  }
   if (ln == 0) {
     if (mf) atomicAdd(&c->mf, mf);
     if (mu) atomicAdd(&c->mu_done, mu);
@@ -626,6 +634,11 @@ __global__ void k_ms_advance(MsBuffers b, int64_t n) {
   BatchCtl* c = b.ctl;
   const int L = c->level;
   b.lvl_off[L + 2] = c->tail;
+  // every count of level L + 1 is a sum of at most max-in-degree counts of
+  // level L; once a level's largest count passes the limit, the next level
+  // could overflow 64 bits, so the batch is replayed with FP64 counts
+  if (c->sigma_max > c->sigma_limit) c->overflow_sigma = 1;
+  c->sigma_max = 0;
   if (c->tail == c->hi) {
     c->done = 1;
     c->maxlevel = L;
@@ -680,7 +693,7 @@ __global__ void __launch_bounds__(256) k_ms_delta(DevGraph g, MsBuffers b, HubDa
     if (L == 0) continue;
     const int64_t e0 = g.rowptr[v], e1 = g.rowptr[v + 1];
     if (e1 - e0 > hd.hub_degree) continue;  // k_ms_hub_delta
-    const unsigned mine = static_cast<unsigned>(F >> (2 * ln)) & 3u;
+    const unsigned mine = my_bits(F);
     if (SK == kSigmaU64) {
       df32 acc0{0.f, 0.f}, acc1{0.f, 0.f};
       psi_range_df(g.colidx, e0, e1, F, succ, b.psi, acc0, acc1);
@@ -707,7 +720,6 @@ __global__ void __launch_bounds__(256) k_ms_hub_delta(DevGraph g, MsBuffers b, H
   const uint64_t* __restrict__ succ = mb_at(b, L + 1);
   const uint64_t* __restrict__ cur = mb_at(b, L);
   const int ln = lane_id();
-  bool unused = false;
   for (long long it = gwarp(); it < hd.n_out; it += nwarps()) {
     const HubItem I = hd.out_items[it];
     const int32_t h = I.v;
@@ -724,13 +736,13 @@ __global__ void __launch_bounds__(256) k_ms_hub_delta(DevGraph g, MsBuffers b, H
       part0 = part1 = 0.0;
       psi_range_f64(g.colidx, I.lo, I.hi, F, succ, b.psi, part0, part1);
     }
-    if (part0 != 0.0) hub_add(acc + 2 * ln, part0, unused);
-    if (part1 != 0.0) hub_add(acc + 2 * ln + 1, part1, unused);
+    if (part0 != 0.0) hub_add(acc + ln, part0);
+    if (part1 != 0.0) hub_add(acc + 32 + ln, part1);
     if (!hub_last(hd.cnt + I.slot, I.nitems)) continue;
-    const double s0 = from_bits<double>(atomicExch(acc + 2 * ln, 0ull));
-    const double s1 = from_bits<double>(atomicExch(acc + 2 * ln + 1, 0ull));
+    const double s0 = from_bits<double>(atomicExch(acc + ln, 0ull));
+    const double s1 = from_bits<double>(atomicExch(acc + 32 + ln, 0ull));
     if (ln == 0) hd.cnt[I.slot] = 0u;
-    const unsigned mine = static_cast<unsigned>(F >> (2 * ln)) & 3u;
+    const unsigned mine = my_bits(F);
     if (SK == kSigmaU64) {
       df32 contrib = finish_df(b.psi, b.sigma, h, mine, df_from_double(s0), df_from_double(s1));
       contrib = warp_sum_df(contrib);
@@ -773,11 +785,17 @@ __global__ void k_ms_cleanup_all(MsBuffers b) {
 }  // namespace
 
 int ms_init(cudaStream_t s, const DevGraph& g, const MsBuffers& b, int nlanes, int sigma_kind,
-            int32_t* dist, int64_t dist_ld) {
+            unsigned long long sigma_limit, int32_t* dist, int64_t dist_ld) {
   switch (sigma_kind) {
-    case kSigmaU64: k_ms_init<kSigmaU64><<<1, 32, 0, s>>>(g, b, nlanes, b.cap, dist, dist_ld); break;
-    case kSigmaF64: k_ms_init<kSigmaF64><<<1, 32, 0, s>>>(g, b, nlanes, b.cap, dist, dist_ld); break;
-    default: k_ms_init<kSigmaNone><<<1, 32, 0, s>>>(g, b, nlanes, b.cap, dist, dist_ld); break;
+    case kSigmaU64:
+      k_ms_init<kSigmaU64><<<1, 32, 0, s>>>(g, b, nlanes, b.cap, sigma_limit, dist, dist_ld);
+      break;
+    case kSigmaF64:
+      k_ms_init<kSigmaF64><<<1, 32, 0, s>>>(g, b, nlanes, b.cap, ~0ull, dist, dist_ld);
+      break;
+    default:
+      k_ms_init<kSigmaNone><<<1, 32, 0, s>>>(g, b, nlanes, b.cap, ~0ull, dist, dist_ld);
+      break;
   }
   return 1;
 }
