@@ -135,13 +135,17 @@ int lgbc_graph_stats(const lgbc_graph *g, lgbc_stats *out);
  *                 frontier has fewer than n/beta vertices.
  *   hub_degree    vertices with more than this many neighbours ("hubs") are
  *                 cut into 256-edge work items spread over the whole GPU
- *                 instead of being expanded by one warp (default 512).
- *   lanes         sources per multi-source batch (1..64). */
+ *                 instead of being expanded by one warp (default 256).
+ *   lanes         sources per multi-source batch (1..64).
+ *   dense_edges   a 32-edge chunk with more than this many edges that carry
+ *                 lanes is gathered thread-per-lane (bit-transposed) instead
+ *                 of edge by edge (32 = always edge by edge). */
 typedef struct lgbc_tuning {
   double alpha;
   double beta;
   int32_t hub_degree;
   int32_t lanes;
+  int32_t dense_edges;
 } lgbc_tuning;
 int lgbc_get_tuning(const lgbc_graph *g, lgbc_tuning *out);
 int lgbc_set_tuning(lgbc_graph *g, const lgbc_tuning *t);

@@ -156,7 +156,7 @@ struct lgbc_graph {
   size_t max_smem = 0;
   unsigned long long sigma_limit = ~0ull;  // (2^64 - 1) / (max in-degree + 1)
   lgbc_stats stats{};
-  lgbc_tuning tune{14.0, 24.0, 512, 64};
+  lgbc_tuning tune{14.0, 24.0, 256, 64, 32};
 
   DevGraph dev() const {
     return DevGraph{n, nnz, d_rowptr, d_colidx, d_in_rowptr, d_in_colidx};
@@ -359,6 +359,7 @@ HubData hub_data(const lgbc_graph* g) {
   h.mask = g->hubs.mask;
   h.cnt = g->hubs.cnt;
   h.hub_degree = g->hubs.nslots > 0 ? g->hubs.built_for : INT32_MAX;
+  h.dense_edges = g->tune.dense_edges;
   return h;
 }
 
@@ -822,8 +823,10 @@ int lgbc_get_tuning(const lgbc_graph* g, lgbc_tuning* out) {
 int lgbc_set_tuning(lgbc_graph* g, const lgbc_tuning* t) {
   LGBC_TRY(check_graph(g));
   if (!t) return fail(LGBC_EINVAL, "null tuning");
-  if (!(t->alpha > 0) || !(t->beta > 0) || t->lanes < 1 || t->lanes > kMaxLanes || t->hub_degree < 1)
-    return fail(LGBC_EINVAL, "tuning out of range (alpha, beta > 0; 1 <= lanes <= 64; hub_degree >= 1)");
+  if (!(t->alpha > 0) || !(t->beta > 0) || t->lanes < 1 || t->lanes > kMaxLanes ||
+      t->hub_degree < 1 || t->dense_edges < 0)
+    return fail(LGBC_EINVAL,
+                "tuning out of range (alpha, beta > 0; 1 <= lanes <= 64; hub_degree >= 1; dense_edges >= 0)");
   std::lock_guard<std::mutex> lock(g->mu);
   g->tune = *t;
   return LGBC_OK;

@@ -59,6 +59,7 @@ struct HubData {
   unsigned long long* mask;      // slots: OR of discovering lanes, kept zero
   unsigned int* cnt;             // slots: finished items, kept zero
   int hub_degree;                // degree above which a vertex is a hub (INT32_MAX: none)
+  int dense_edges;               // chunks with more contributing edges use the transposed gather
 };
 
 // sigma_limit: (2^64 - 1) / (max in-degree + 1), the largest path count a

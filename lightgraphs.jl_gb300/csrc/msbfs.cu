@@ -138,63 +138,94 @@ template <> __device__ __forceinline__ unsigned long long zero_row() { return 0u
 template <> __device__ __forceinline__ double zero_row() { return 0.0; }
 template <> __device__ __forceinline__ float2 zero_row() { return make_float2(0.f, 0.f); }
 
+// Per-warp staging of one chunk's contributing edges (compacted).
+struct ChunkStage {
+  uint64_t f[kWarp];
+  int32_t v[kWarp];
+};
+constexpr int kWarpsPerBlock = 8;  // every gather kernel runs 256-thread blocks
+
+__device__ __forceinline__ ChunkStage& my_stage() {
+  __shared__ ChunkStage stage[kWarpsPerBlock];
+  return stage[threadIdx.x >> 5];
+}
+
 // Chunk gather.  Each of the 32 threads holds one edge (neighbour id `nb`,
 // lane mask `f` of the lanes that edge contributes to).  Adds, for this
 // thread's lanes t and t + 32, rows[nb_j * 64 + lane] over every edge j whose
 // mask has that lane, into (a0, a1).
+//  * at most `dense` contributing edges: the edges are compacted into shared
+//    memory and the warp walks them, each edge's row read by coalesced loads;
+//  * more: the (edge, lane) bit matrix is transposed so each thread walks only
+//    the edges that carry its own lanes.
 template <class T, class A>
 __device__ __forceinline__ void gather_chunk(int32_t nb, uint64_t f, const T* __restrict__ rows,
-                                             A& a0, A& a1) {
+                                             int dense, A& a0, A& a1) {
   const int ln = lane_id();
   const unsigned bal = __ballot_sync(kFull, f != 0);
   if (bal == 0) return;
   const T* r0 = rows + ln;
   const T* r1 = rows + 32 + ln;
-  if (__popc(bal) <= 2) {
-    // per-edge path: broadcast each set edge to the warp
-    unsigned b = bal;
-    while (b) {
-      const int j = __ffs(b) - 1;
-      b &= b - 1;
-      const int32_t vj = __shfl_sync(kFull, nb, j);
-      const uint64_t fj = shfl_u64(f, j);
-      const unsigned my = my_bits(fj);
-      const int64_t off = static_cast<int64_t>(vj) * 64;
-      T x0 = zero_row<T>(), x1 = zero_row<T>();
-      if (my & 1u) x0 = r0[off];
-      if (my & 2u) x1 = r1[off];
-      if (my & 1u) acc_row<T, A>(a0, x0);
-      if (my & 2u) acc_row<T, A>(a1, x1);
+  const int S = __popc(bal);
+  if (S <= dense) {
+    ChunkStage& st = my_stage();
+    if (f) {
+      const int r = __popc(bal & ((1u << ln) - 1u));
+      st.v[r] = nb;
+      st.f[r] = f;
     }
+    __syncwarp();
+    for (int r = 0; r < S; r += 4) {
+      T x0[4], x1[4];
+      unsigned my[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const bool ok = r + q < S;
+        const uint64_t fj = ok ? st.f[r + q] : 0ull;
+        const int64_t off = static_cast<int64_t>(ok ? st.v[r + q] : 0) * 64;
+        my[q] = my_bits(fj);
+        x0[q] = zero_row<T>();
+        x1[q] = zero_row<T>();
+        if (my[q] & 1u) x0[q] = r0[off];
+        if (my[q] & 2u) x1[q] = r1[off];
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        if (my[q] & 1u) acc_row<T, A>(a0, x0[q]);
+        if (my[q] & 2u) acc_row<T, A>(a1, x1[q]);
+      }
+    }
+    __syncwarp();
     return;
   }
   // transposed path: thread t gets the edges that carry lane t / lane t + 32
-  uint32_t E0 = warp_transpose32(static_cast<uint32_t>(f));
-  uint32_t E1 = warp_transpose32(static_cast<uint32_t>(f >> 32));
-  const int cnt = static_cast<int>(__reduce_max_sync(kFull, static_cast<unsigned>(__popc(E0) + __popc(E1))));
-  for (int k = 0; k < cnt; k += 4) {
-    int32_t vj[4];
-    unsigned sel[4];  // 0 = none, 1 = lane t, 2 = lane t + 32
+  uint32_t E[2] = {warp_transpose32(static_cast<uint32_t>(f)),
+                   warp_transpose32(static_cast<uint32_t>(f >> 32))};
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const bool lo = E0 != 0u;
-      uint32_t E = lo ? E0 : E1;
-      const int j = E ? __ffs(E) - 1 : 0;
-      sel[q] = E ? (lo ? 1u : 2u) : 0u;
-      E &= E - 1u;
-      if (lo) E0 = E; else E1 = E;
-      vj[q] = __shfl_sync(kFull, nb, j);
-    }
-    T x[4];
+  for (int h = 0; h < 2; ++h) {
+    const T* rb = h ? r1 : r0;
+    A& acc = h ? a1 : a0;
+    uint32_t m = E[h];
+    const int cnt = static_cast<int>(__reduce_max_sync(kFull, static_cast<unsigned>(__popc(m))));
+    for (int k = 0; k < cnt; k += 4) {
+      int32_t vj[4];
+      bool ok[4];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      x[q] = zero_row<T>();
-      if (sel[q]) x[q] = (sel[q] == 1u ? r0 : r1)[static_cast<int64_t>(vj[q]) * 64];
-    }
+      for (int q = 0; q < 4; ++q) {
+        ok[q] = m != 0u;
+        const int j = ok[q] ? __ffs(m) - 1 : 0;
+        m &= m - 1u;
+        vj[q] = __shfl_sync(kFull, nb, j);
+      }
+      T x[4];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      if (sel[q] == 1u) acc_row<T, A>(a0, x[q]);
-      if (sel[q] == 2u) acc_row<T, A>(a1, x[q]);
+      for (int q = 0; q < 4; ++q) {
+        x[q] = zero_row<T>();
+        if (ok[q]) x[q] = rb[static_cast<int64_t>(vj[q]) * 64];
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (ok[q]) acc_row<T, A>(acc, x[q]);
     }
   }
 }
@@ -208,7 +239,7 @@ template <int SK>
 __device__ __forceinline__ uint64_t pull_range(const int32_t* __restrict__ ci, int64_t e0,
                                                int64_t e1, uint64_t want,
                                                const uint64_t* __restrict__ front,
-                                               const void* __restrict__ sigma,
+                                               const void* __restrict__ sigma, int dense,
                                                typename Sig<SK>::T& a0, typename Sig<SK>::T& a1) {
   const int ln = lane_id();
   uint64_t found = 0;
@@ -226,7 +257,7 @@ __device__ __forceinline__ uint64_t pull_range(const int32_t* __restrict__ ci, i
       continue;
     }
     using T = typename Sig<SK>::T;
-    gather_chunk<T, T>(v, f, reinterpret_cast<const T*>(sigma), a0, a1);
+    gather_chunk<T, T>(v, f, reinterpret_cast<const T*>(sigma), dense, a0, a1);
   }
   return warp_or_u64(found);
 }
@@ -236,7 +267,8 @@ __device__ __forceinline__ uint64_t pull_range(const int32_t* __restrict__ ci, i
 // successor; their psi = (1 + delta[w]) / sigma[w] are summed.
 __device__ __forceinline__ void psi_range_df(const int32_t* __restrict__ ci, int64_t e0, int64_t e1,
                                              uint64_t F, const uint64_t* __restrict__ succ,
-                                             const void* __restrict__ psi, df32& acc0, df32& acc1) {
+                                             const void* __restrict__ psi, int dense, df32& acc0,
+                                             df32& acc1) {
   const int ln = lane_id();
   for (int64_t e = e0; e < e1; e += kWarp) {
     const int64_t idx = e + ln;
@@ -246,7 +278,7 @@ __device__ __forceinline__ void psi_range_df(const int32_t* __restrict__ ci, int
       w = ci[idx];
       gm = succ[w] & F;
     }
-    gather_chunk<float2, df32>(w, gm, reinterpret_cast<const float2*>(psi), acc0, acc1);
+    gather_chunk<float2, df32>(w, gm, reinterpret_cast<const float2*>(psi), dense, acc0, acc1);
   }
   acc0 = acc_done(acc0);
   acc1 = acc_done(acc1);
@@ -254,8 +286,8 @@ __device__ __forceinline__ void psi_range_df(const int32_t* __restrict__ ci, int
 
 __device__ __forceinline__ void psi_range_f64(const int32_t* __restrict__ ci, int64_t e0, int64_t e1,
                                               uint64_t F, const uint64_t* __restrict__ succ,
-                                              const void* __restrict__ psi, double& acc0,
-                                              double& acc1) {
+                                              const void* __restrict__ psi, int dense,
+                                              double& acc0, double& acc1) {
   const int ln = lane_id();
   for (int64_t e = e0; e < e1; e += kWarp) {
     const int64_t idx = e + ln;
@@ -265,7 +297,7 @@ __device__ __forceinline__ void psi_range_f64(const int32_t* __restrict__ ci, in
       w = ci[idx];
       gm = succ[w] & F;
     }
-    gather_chunk<double, double>(w, gm, reinterpret_cast<const double*>(psi), acc0, acc1);
+    gather_chunk<double, double>(w, gm, reinterpret_cast<const double*>(psi), dense, acc0, acc1);
   }
 }
 
@@ -465,7 +497,7 @@ __global__ void __launch_bounds__(256) k_ms_td_settle(DevGraph g, MsBuffers b, H
     if (DIST) store_dist(dist, ld, w, mask, L + 1);
     if (SK != kSigmaNone && e1 - e0 <= hd.hub_degree) {
       T a0 = T(0), a1 = T(0);
-      pull_range<SK>(g.in_colidx, e0, e1, mask, front, b.sigma, a0, a1);
+      pull_range<SK>(g.in_colidx, e0, e1, mask, front, b.sigma, hd.dense_edges, a0, a1);
       store_sigma<SK>(b.sigma, w, mask, a0, a1, smax);
     }
   }
@@ -514,7 +546,7 @@ __global__ void __launch_bounds__(256) k_ms_bu(DevGraph g, MsBuffers b, HubData 
       const uint64_t want = act & ~shfl_u64(vis, j);
       T a0 = T(0), a1 = T(0);
       const uint64_t nm = pull_range<SK>(g.in_colidx, g.in_rowptr[w], g.in_rowptr[w + 1], want,
-                                         front, b.sigma, a0, a1);
+                                         front, b.sigma, hd.dense_edges, a0, a1);
       if (nm) {
         if (SK != kSigmaNone) store_sigma<SK>(b.sigma, w, nm, a0, a1, smax);
         if (DIST) store_dist(dist, ld, w, nm, L + 1);
@@ -573,7 +605,8 @@ __global__ void __launch_bounds__(256) k_ms_hub_pull(DevGraph g, MsBuffers b, Hu
       if (!want) continue;
     }
     T a0 = T(0), a1 = T(0);
-    const uint64_t found = pull_range<SK>(g.in_colidx, I.lo, I.hi, want, front, b.sigma, a0, a1);
+    const uint64_t found =
+        pull_range<SK>(g.in_colidx, I.lo, I.hi, want, front, b.sigma, hd.dense_edges, a0, a1);
     unsigned long long* acc = hd.acc + static_cast<int64_t>(I.slot) * 64;
     if (SK != kSigmaNone) {
       if (a0 != T(0)) hub_add(acc + ln, a0);
@@ -696,13 +729,13 @@ __global__ void __launch_bounds__(256) k_ms_delta(DevGraph g, MsBuffers b, HubDa
     const unsigned mine = my_bits(F);
     if (SK == kSigmaU64) {
       df32 acc0{0.f, 0.f}, acc1{0.f, 0.f};
-      psi_range_df(g.colidx, e0, e1, F, succ, b.psi, acc0, acc1);
+      psi_range_df(g.colidx, e0, e1, F, succ, b.psi, hd.dense_edges, acc0, acc1);
       df32 contrib = finish_df(b.psi, b.sigma, v, mine, acc0, acc1);
       contrib = warp_sum_df(contrib);
       if (ln == 0) bc[v] += df_to_double(contrib);
     } else {
       double acc0 = 0.0, acc1 = 0.0;
-      psi_range_f64(g.colidx, e0, e1, F, succ, b.psi, acc0, acc1);
+      psi_range_f64(g.colidx, e0, e1, F, succ, b.psi, hd.dense_edges, acc0, acc1);
       double contrib = finish_f64(b.psi, b.sigma, v, mine, acc0, acc1);
       contrib = warp_sum_f64(contrib);
       if (ln == 0) bc[v] += contrib;
@@ -729,12 +762,12 @@ __global__ void __launch_bounds__(256) k_ms_hub_delta(DevGraph g, MsBuffers b, H
     double part0, part1;
     if (SK == kSigmaU64) {
       df32 a0{0.f, 0.f}, a1{0.f, 0.f};
-      psi_range_df(g.colidx, I.lo, I.hi, F, succ, b.psi, a0, a1);
+      psi_range_df(g.colidx, I.lo, I.hi, F, succ, b.psi, hd.dense_edges, a0, a1);
       part0 = df_to_double(a0);
       part1 = df_to_double(a1);
     } else {
       part0 = part1 = 0.0;
-      psi_range_f64(g.colidx, I.lo, I.hi, F, succ, b.psi, part0, part1);
+      psi_range_f64(g.colidx, I.lo, I.hi, F, succ, b.psi, hd.dense_edges, part0, part1);
     }
     if (part0 != 0.0) hub_add(acc + ln, part0);
     if (part1 != 0.0) hub_add(acc + 32 + ln, part1);

@@ -134,6 +134,17 @@ def test_lane_widths(lanes):
     assert_bc_close(z, oracle_bc(g, np.arange(199), normalize=False))
 
 
+@pytest.mark.parametrize("dense", [0, 2, 32])
+@pytest.mark.parametrize("name", ["rmat10", "er_directed", "ba"])
+def test_gather_paths(name, dense):
+    # dense_edges selects, per 32-edge chunk, the edge-by-edge gather or the
+    # bit-transposed one; both must give the oracle's result
+    g = GRAPHS[name]()
+    g.device_handle().set_tuning(dense_edges=dense, hub_degree=64)
+    z = lgbc.betweenness_centrality(g, list(range(1, 300)), normalize=False)
+    assert_bc_close(z, oracle_bc(g, np.arange(299), normalize=False))
+
+
 def test_sampled_k_uses_distinct_sources():
     g = GRAPHS["ba"]()
     rng = np.random.default_rng(123)
