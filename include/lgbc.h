@@ -150,6 +150,29 @@ typedef struct lgbc_tuning {
 int lgbc_get_tuning(const lgbc_graph *g, lgbc_tuning *out);
 int lgbc_set_tuning(lgbc_graph *g, const lgbc_tuning *t);
 
+/* gdistances for callers that cannot allocate device memory: no counterpart
+ * in the reference.  Some callers cannot call cudaMalloc -- code that runs
+ * while a CUDA graph is being captured on its stream, or hosts whose device
+ * memory belongs to another allocator with a fixed budget -- so this entry
+ * point allocates nothing.  Every input and output is a caller-owned DEVICE
+ * pointer: the CSR (in_rowptr / in_colidx NULL for an undirected graph), the
+ * nsrc sources, and dist (n int32, LGBC_UNREACHED where no source reaches).
+ * Results equal lgbc_gdistances'.  The BFS queue, frontier bitmaps and control
+ * block live in one static device array of about 17 MB that every GPU which
+ * loads the library holds until exit, so n is limited to
+ * LGBC_NOALLOC_MAX_VERTICES (larger graphs get LGBC_EINVAL).  The first call on
+ * a device looks up that array's address (cudaGetSymbolAddress) and the
+ * device's launch shape; make that first call before any stream capture.
+ * `stream` is a cudaStream_t (NULL = default stream); the call returns when
+ * dist is complete.  All calls share the one array: calls that overlap on the
+ * GPU (from several host threads or streams at once) race and must not be
+ * issued. */
+#define LGBC_NOALLOC_MAX_VERTICES (1 << 22)
+int lgbc_gdistances_noalloc(int64_t n, int64_t nnz, const int64_t *rowptr,
+                            const int32_t *colidx, const int64_t *in_rowptr,
+                            const int32_t *in_colidx, const int32_t *src, int64_t nsrc,
+                            int32_t *dist, void *stream);
+
 /* Device / pinned-host memory helpers for callers without their own CUDA
  * allocator (bench and test harnesses).  lgbc_memcpy kinds: 1 = host to
  * device, 2 = device to host, 3 = device to device. */

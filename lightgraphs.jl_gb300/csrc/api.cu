@@ -128,6 +128,10 @@ struct BfsWorkspace {
 
 }  // namespace
 
+// Lets the other translation units of the library report errors through
+// lgbc_last_error().
+void lgbc::set_last_error(const char* msg) { g_last_error = msg ? msg : ""; }
+
 struct lgbc_graph {
   int device = 0;
   int64_t n = 0;

@@ -99,6 +99,9 @@ int bfs_advance(cudaStream_t s, const BfsBuffers& b);
 // Largest dynamic shared memory the bottom-up kernel may stage (bytes).
 int bfs_configure(size_t max_dyn_smem);
 
+// Set the thread-local message returned by lgbc_last_error() (api.cu).
+void set_last_error(const char* msg);
+
 // ---- small utilities: util.cu ----------------------------------------------
 // ORs into *bad: 1 = rowptr decreases somewhere, 2 = a column index is not in [0, n).
 int validate_csr(const LaunchCfg& c, cudaStream_t s, const int64_t* rowptr, const int32_t* colidx,

@@ -86,6 +86,7 @@ def _declare(lib) -> None:
         "lgbc_host_alloc": ([pp, i64], c_int),
         "lgbc_host_free": ([p], c_int),
         "lgbc_memcpy": ([p, p, i64, c_int], c_int),
+        "lgbc_gdistances_noalloc": ([i64, i64, p, p, p, p, p, i64, p, p], c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
