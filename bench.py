@@ -171,18 +171,46 @@ def traffic_per_step() -> float | None:
     return None
 
 
-def workload(rank: int, k: int, scale: int):
+WORKLOADS = {
+    "c1": "ER G(n=10000, m=50000) undirected, exact BC (all sources)",
+    "c2": "R-MAT scale 20 undirected, sampled BC k=4096",
+    "c3": "4096 Barabasi-Albert graphs n~U[200,20000], k=3, exact BC for every graph",
+    "c4": "R-MAT scale 22 directed, sampled BC k=16384",
+}
+
+
+def workload(rank: int, args):
+    """(graph, 0-based sources, active source count, generation seconds, name)."""
     from lgbc import generators as G
     import lgbc
     t = time.perf_counter()
-    g = G.rmat(scale, 16, seed=1)
+    if args.workload == "c1":
+        g = G.erdos_renyi_nm(10000, 50000, seed=1, eltype=np.int64)
+        src = np.arange(g.nv(), dtype=np.int32)
+        name = "er10k_m50k_exact_bc"
+    elif args.workload == "c4":
+        g = G.rmat(22, 16, seed=1, directed=True)
+        src1 = lgbc.sample(g.vertices(), args.k or 16384, rng=np.random.default_rng(2 + rank))
+        src = (np.asarray(src1, np.int64) - 1).astype(np.int32)
+        name = f"rmat22_directed_sampled_bc_k{len(src)}"
+    else:
+        g = G.rmat(args.scale, 16, seed=1)
+        src1 = lgbc.sample(g.vertices(), args.k or 4096, rng=np.random.default_rng(2 + rank))
+        src = (np.asarray(src1, np.int64) - 1).astype(np.int32)
+        name = f"rmat{args.scale}_sampled_bc_k{len(src)}"
     gen_s = time.perf_counter() - t
-    src1 = lgbc.sample(g.vertices(), k, rng=np.random.default_rng(2 + rank))
-    src = (np.asarray(src1, np.int64) - 1).astype(np.int32)
-    rp, ci = g.csr()
-    deg = np.diff(rp)
+    deg = g.degrees()
     k_act = int(np.count_nonzero(deg[src] > 0))
-    return g, src, k_act, gen_s
+    return g, src, k_act, gen_s, name
+
+
+def many_graphs(rank: int, count: int):
+    """Config C3: `count` BA graphs, n uniform in [200, 20000] (seed 0), k = 3,
+    graph i seeded 1000 + i."""
+    from lgbc import generators as G
+    rng = np.random.default_rng(0 + rank)
+    ns = rng.integers(200, 20001, count)
+    return [G.barabasi_albert(int(n), 3, seed=1000 + i) for i, n in enumerate(ns)]
 
 
 # ----------------------------------------------------------------------------- CPU arms
@@ -191,20 +219,24 @@ def cpu_betweenness_sample(g, src: np.ndarray, nthreads: int, target_s: float, s
     sample of the workload's sources; returns (GTEPS, sample description)."""
     from oracle import oracle
     rp, ci = g.csr()
-    deg = np.diff(rp)
+    kw = {}
+    if g.is_directed():
+        irp, ici = g.in_csr()
+        kw = dict(directed=True, in_rowptr=irp, in_colidx=ici)
+    deg = g.degrees()
     act = src[deg[src] > 0]
     rng = np.random.default_rng(seed)
     # calibrate with one source per thread
     cal = rng.choice(act, size=min(len(act), nthreads), replace=False)
     t = time.perf_counter()
-    oracle.betweenness_raw(rp, ci, cal, mode="faithful", nthreads=nthreads)
+    oracle.betweenness_raw(rp, ci, cal, mode="faithful", nthreads=nthreads, **kw)
     dt = max(time.perf_counter() - t, 1e-3)
     per_round = dt
     rounds = max(1, int(target_s / per_round))
     count = min(len(act), rounds * nthreads)
     samp = rng.choice(act, size=count, replace=False)
     t = time.perf_counter()
-    oracle.betweenness_raw(rp, ci, samp, mode="faithful", nthreads=nthreads)
+    oracle.betweenness_raw(rp, ci, samp, mode="faithful", nthreads=nthreads, **kw)
     dt = time.perf_counter() - t
     m = g.ne()
     return count * m / dt / 1e9, dt, count
@@ -215,9 +247,15 @@ def run_reference(args, dist: Dist):
     if dist.rank != 0:
         return
     nthreads = os.cpu_count() or 1
-    g, src, k_act, _ = workload(0, args.k, args.scale)
+    if args.workload == "c3":
+        return run_reference_many(args, nthreads)
+    g, src, k_act, _, wname = workload(0, args)
     rp, ci = g.csr()
-    deg = np.diff(rp)
+    kw = {}
+    if g.is_directed():
+        irp, ici = g.in_csr()
+        kw = dict(directed=True, in_rowptr=irp, in_colidx=ici)
+    deg = g.degrees()
     act = src[deg[src] > 0]
     from oracle import oracle
     oracle.build()
@@ -229,14 +267,14 @@ def run_reference(args, dist: Dist):
             # size one step to about 10 s of CPU work
             cal = act[:nthreads]
             t = time.perf_counter()
-            oracle.betweenness_raw(rp, ci, cal, mode="faithful", nthreads=nthreads)
+            oracle.betweenness_raw(rp, ci, cal, mode="faithful", nthreads=nthreads, **kw)
             dt = max(time.perf_counter() - t, 1e-3)
             count = min(len(act), max(nthreads, int(10.0 / dt) * nthreads))
         samp = act[(it * count) % len(act):][:count]
         if len(samp) < count:
             samp = np.concatenate([samp, act[:count - len(samp)]])
         t = time.perf_counter()
-        oracle.betweenness_raw(rp, ci, samp, mode="faithful", nthreads=nthreads)
+        oracle.betweenness_raw(rp, ci, samp, mode="faithful", nthreads=nthreads, **kw)
         dt = time.perf_counter() - t
         if it >= args.warmup:
             per_step.append(dt)
@@ -247,9 +285,7 @@ def run_reference(args, dist: Dist):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"rmat{args.scale}_sampled_bc_k{args.k}", "scale": args.scale,
-                   "edgefactor": 16, "k": args.k, "n": g.nv(), "m": m,
-                   "active_sources": k_act},
+        "config": {"workload": wname, "n": g.nv(), "m": m, "active_sources": k_act},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
                          "sample": f"{count} of the {k_act} active sources per step "
                                    "(heap Dijkstra + predecessor lists, as "
@@ -272,12 +308,17 @@ def run_ours(args, dist: Dist):
     import lgbc
     from lgbc import _lib
     lib = _lib.lib()
-    g, src, k_act, gen_s = workload(dist.rank, args.k, args.scale)
+    if args.workload == "c3":
+        return run_ours_many(args, dist)
+    g, src, k_act, gen_s, wname = workload(dist.rank, args)
     n, m = g.nv(), g.ne()
     rp, ci = g.csr()
     nnz = len(ci)
-    log(f"[rank {dist.rank}] R-MAT scale {args.scale}: n={n} m={m} nnz={nnz} "
-        f"k={args.k} active={k_act} (generated in {gen_s:.1f}s)")
+    directed = g.is_directed()
+    if directed:
+        irp, ici = g.in_csr()
+    log(f"[rank {dist.rank}] {wname}: n={n} m={m} nnz={nnz} "
+        f"sources={len(src)} active={k_act} (generated in {gen_s:.1f}s)")
 
     dg = g.device_handle()
     h = dg.handle
@@ -322,17 +363,22 @@ def run_ours(args, dist: Dist):
     assert np.all(np.isfinite(host_bc)) and host_bc.min() >= 0
 
     # ---- end to end through the C ABI with host buffers ----------------------------
-    prp = ctypes.c_void_p()
-    pci = ctypes.c_void_p()
-    _lib.check(lib.lgbc_host_alloc(ctypes.byref(prp), 8 * (n + 1)))
-    _lib.check(lib.lgbc_host_alloc(ctypes.byref(pci), 4 * nnz))
-    ctypes.memmove(prp, rp.ctypes.data, 8 * (n + 1))
-    ctypes.memmove(pci, ci.ctypes.data, 4 * nnz)
+    def pinned(a):
+        p = ctypes.c_void_p()
+        _lib.check(lib.lgbc_host_alloc(ctypes.byref(p), max(a.nbytes, 1)))
+        ctypes.memmove(p, a.ctypes.data, a.nbytes)
+        return p
+
+    prp, pci = pinned(rp), pinned(ci)
+    pirp = pici = None
+    if directed:
+        pirp, pici = pinned(irp), pinned(ici)
     out = np.empty(n, np.float64)
 
     def step_e2e():
         hh = ctypes.c_void_p()
-        _lib.check(lib.lgbc_graph_create(ctypes.byref(hh), n, nnz, prp, pci, None, None, 0))
+        _lib.check(lib.lgbc_graph_create(ctypes.byref(hh), n, nnz, prp, pci, pirp, pici,
+                                         int(directed)))
         try:
             _lib.check(lib.lgbc_betweenness(hh, srcp, len(src), 0, _lib.ptr(out)))
         finally:
@@ -346,8 +392,9 @@ def run_ours(args, dist: Dist):
         step_e2e()
     t_e2e = dist.max((time.perf_counter() - t0) / e2e_steps)
     e2e_value = dist.sum(te_step) / t_e2e / 1e9
-    lib.lgbc_host_free(prp)
-    lib.lgbc_host_free(pci)
+    for p_ in (prp, pci, pirp, pici):
+        if p_ is not None:
+            lib.lgbc_host_free(p_)
 
     # ---- gdistances from 64 sources (the workload's BFS part) ----------------------
     rng = np.random.default_rng(3 + dist.rank)
@@ -385,13 +432,16 @@ def run_ours(args, dist: Dist):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "u64 path counts, df32/f64 dependencies", "data": "synthetic",
-            "config": {"workload": f"rmat{args.scale}_sampled_bc_k{args.k}", "scale": args.scale,
-                       "edgefactor": 16, "abcd": [0.57, 0.19, 0.19, 0.05], "k": args.k,
-                       "n": n, "m": m, "nnz": nnz, "active_sources": k_act,
-                       "lanes": LANES, "parallelism": f"replicas x{dist.world}",
-                       "l2": "inputs larger than L2 (CSR 134 MB, lane state 1 GB); no flush"},
+            "config": {"workload": wname, "description": WORKLOADS[args.workload],
+                       "n": n, "m": m, "nnz": nnz, "directed": directed, "sources": len(src),
+                       "active_sources": k_act, "lanes": LANES,
+                       "parallelism": f"replicas x{dist.world}",
+                       "l2": ("inputs larger than L2 (CSR + lane state); no flush"
+                              if nnz * 4 + n * 1024 > 129e6 else
+                              "small graph: inputs fit in L2, no flush (parity config)")},
             "e2e": {"value": e2e_value, "unit": UNIT,
-                    "h2d_bytes_per_step": 8 * (n + 1) + 4 * nnz + 4 * len(src),
+                    "h2d_bytes_per_step": (8 * (n + 1) + 4 * nnz) * (2 if directed else 1)
+                    + 4 * len(src),
                     "d2h_bytes_per_step": 8 * n,
                     "ms_per_step": t_e2e * 1e3},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -411,14 +461,80 @@ def run_ours(args, dist: Dist):
     lib.lgbc_device_free(bc_dev)
 
 
+def run_ours_many(args, dist: Dist):
+    """Config C3: exact BC of many BA graphs in one lgbc_betweenness_many call
+    per step (host buffers in, raw vectors out)."""
+    import lgbc
+    graphs = many_graphs(dist.rank, args.graphs)
+    te = sum(g.nv() * g.ne() for g in graphs)  # every vertex is an active source
+    log(f"[rank {dist.rank}] {len(graphs)} BA graphs, sum n = {sum(g.nv() for g in graphs)}, "
+        f"traversed edges per step = {te:.3g}")
+    for _ in range(args.warmup):
+        lgbc.betweenness_centrality_many(graphs, normalize=False)
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        lgbc.betweenness_centrality_many(graphs, normalize=False)
+    t = dist.max((time.perf_counter() - t0) / args.steps)
+    value = dist.sum(te) / t / 1e9
+    if dist.rank == 0:
+        print(json.dumps({
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "u64 path counts, df32/f64 dependencies", "data": "synthetic",
+            "config": {"workload": f"ba_many_{len(graphs)}_exact_bc", "description": WORKLOADS["c3"],
+                       "graphs": len(graphs), "graphs_per_s": len(graphs) / t},
+            "e2e": {"value": value, "unit": UNIT,
+                    "h2d_bytes_per_step": sum(8 * (g.nv() + 1) + 4 * 2 * g.ne() for g in graphs),
+                    "d2h_bytes_per_step": 8 * sum(g.nv() for g in graphs)},
+        }), flush=True)
+
+
+def run_reference_many(args, nthreads: int):
+    """C3 on the host cores: the faithful oracle on a bounded sample of graphs."""
+    from oracle import oracle
+    graphs = many_graphs(0, args.graphs)
+    rng = np.random.default_rng(5)
+    per_step = []
+    for it in range(args.warmup + args.steps):
+        idx = rng.choice(len(graphs), 2, replace=False)
+        te = 0
+        t = time.perf_counter()
+        for i in idx:
+            g = graphs[i]
+            rp, ci = g.csr()
+            srcs = np.arange(min(g.nv(), 16 * nthreads), dtype=np.int32)
+            oracle.betweenness_raw(rp, ci, srcs, mode="faithful", nthreads=nthreads)
+            te += len(srcs) * g.ne()
+        dt = time.perf_counter() - t
+        if it >= args.warmup:
+            per_step.append((te, dt))
+    te = sum(a for a, _ in per_step)
+    dt = sum(b for _, b in per_step)
+    value = te / dt / 1e9
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": {"workload": f"ba_many_{len(graphs)}_exact_bc"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
+                         "sample": "2 graphs per step, 16 sources per thread each"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawTextHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="c2",
+                    help="; ".join(f"{k}: {v}" for k, v in WORKLOADS.items()))
     ap.add_argument("--scale", type=int, default=20)
-    ap.add_argument("--k", type=int, default=4096)
+    ap.add_argument("--k", type=int, default=0, help="sampled sources (0 = the workload's)")
+    ap.add_argument("--graphs", type=int, default=4096, help="c3: number of graphs")
     ap.add_argument("--cpu-seconds", type=float, default=15.0,
                     help="approximate CPU-baseline sample length")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")

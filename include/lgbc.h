@@ -107,6 +107,20 @@ int lgbc_betweenness(lgbc_graph *g, const int32_t *src, int64_t nsrc,
 int lgbc_betweenness_dev(lgbc_graph *g, const int32_t *src, int64_t nsrc,
                          int endpoints, double *bc_raw_dev);
 
+/* Exact betweenness (all sources) of many undirected graphs in one call:
+ * betweenness_centrality(g) (src/centrality/betweenness.jl:46-75, before
+ * _rescale!) for every graph g_i.  Graph i has n[i] vertices; its local
+ * 0-based CSR is rowptr[rowptr_off[i] .. rowptr_off[i] + n[i]] (n[i] + 1
+ * entries starting at 0) and colidx[col_off[i] ..] (local ids).  bc_raw_out
+ * receives the graphs' raw vectors concatenated in input order (sum n[i]
+ * doubles); the caller rescales each with _rescale!(bc_i, n[i], ...).
+ * Graphs are grouped by size into disjoint unions; one 64-lane batch seeds
+ * source index b*64 + l of every graph of a group in lane l, so each level
+ * launch covers every graph of the group. */
+int lgbc_betweenness_many(int64_t ngraphs, const int64_t *n, const int64_t *rowptr_off,
+                          const int64_t *col_off, const int64_t *rowptr, const int32_t *colidx,
+                          int endpoints, double *bc_raw_out);
+
 /* Wait for all work queued on the handle's stream. */
 int lgbc_graph_sync(lgbc_graph *g);
 
@@ -139,13 +153,18 @@ int lgbc_graph_stats(const lgbc_graph *g, lgbc_stats *out);
  *   lanes         sources per multi-source batch (1..64).
  *   dense_edges   a 32-edge chunk with more than this many edges that carry
  *                 lanes is gathered thread-per-lane (bit-transposed) instead
- *                 of edge by edge (32 = always edge by edge). */
+ *                 of edge by edge (32 = always edge by edge).
+ *   segment_degree graphs whose mean degree (stored entries / n) is below
+ *                 this run the low-degree kernels, in which a warp streams the
+ *                 edges of 32 vertices at once (default 0 = never: on the
+ *                 measured workloads the warp-per-vertex kernels were faster). */
 typedef struct lgbc_tuning {
   double alpha;
   double beta;
   int32_t hub_degree;
   int32_t lanes;
   int32_t dense_edges;
+  int32_t segment_degree;
 } lgbc_tuning;
 int lgbc_get_tuning(const lgbc_graph *g, lgbc_tuning *out);
 int lgbc_set_tuning(lgbc_graph *g, const lgbc_tuning *t);

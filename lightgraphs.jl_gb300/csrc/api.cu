@@ -160,7 +160,7 @@ struct lgbc_graph {
   size_t max_smem = 0;
   unsigned long long sigma_limit = ~0ull;  // (2^64 - 1) / (max in-degree + 1)
   lgbc_stats stats{};
-  lgbc_tuning tune{14.0, 24.0, 256, 64, 32};
+  lgbc_tuning tune{14.0, 24.0, 256, 64, 32, 0};
 
   DevGraph dev() const {
     return DevGraph{n, nnz, d_rowptr, d_colidx, d_in_rowptr, d_in_colidx};
@@ -364,6 +364,8 @@ HubData hub_data(const lgbc_graph* g) {
   h.cnt = g->hubs.cnt;
   h.hub_degree = g->hubs.nslots > 0 ? g->hubs.built_for : INT32_MAX;
   h.dense_edges = g->tune.dense_edges;
+  // low-degree graphs: segmented warps when the mean degree is below the cut
+  h.segmented = g->n > 0 && g->nnz < static_cast<int64_t>(g->tune.segment_degree) * g->n ? 1 : 0;
   return h;
 }
 
@@ -412,15 +414,32 @@ bool choose_bottom_up(const lgbc_graph* g, const BatchCtl& c, bool was_bu) {
 // One multi-source batch: forward level loop, then (with sigma) the backward
 // dependency sweep into bc.  Returns LGBC_OK, or 1 when the batch must be
 // replayed with FP64 path counts.
+// Explicit (vertex, lane) seeds on the device, for unions of graphs.
+struct Seeds {
+  const int32_t* v = nullptr;
+  const int32_t* lane = nullptr;
+  int64_t count = 0;
+  // optional premark of seedless lanes per component (unions of graphs)
+  const int64_t* seg_off = nullptr;
+  const uint64_t* seg_mark = nullptr;
+  int64_t nseg = 0;
+};
+
 int run_ms_batch(lgbc_graph* g, const int32_t* lane_src, int nl, int sigma_kind, double* bc,
-                 int32_t* dist, int64_t dist_ld) {
+                 int32_t* dist, int64_t dist_ld, const Seeds& seeds = Seeds()) {
   const DevGraph dg = g->dev();
   LGBC_TRY(ensure_hubs(g));
   const HubData hd = hub_data(g);
   const uint64_t act = nl >= 64 ? ~0ull : ((1ull << nl) - 1ull);
   for (;;) {
     MsBuffers b = ms_buffers(g, lane_src);
-    g->launches += ms_init(g->stream, dg, b, nl, sigma_kind, g->sigma_limit, dist, dist_ld);
+    if (seeds.seg_mark) g->launches += ms_premark(g->cfg, g->stream, b, seeds.seg_off, seeds.seg_mark,
+                                                  seeds.nseg);
+    if (seeds.v)
+      g->launches += ms_init_seeds(g->cfg, g->stream, dg, b, seeds.v, seeds.lane, seeds.count,
+                                   sigma_kind, g->sigma_limit, dist, dist_ld);
+    else
+      g->launches += ms_init(g->stream, dg, b, nl, sigma_kind, g->sigma_limit, dist, dist_ld);
     LGBC_TRY(check_launch(g));
     bool bu = false;
     bool regrow = false;
@@ -468,6 +487,8 @@ int run_ms_batch(lgbc_graph* g, const int32_t* lane_src, int nl, int sigma_kind,
     for (int L = maxl; L >= 0; --L)
       g->launches += ms_backward_level(g->cfg, g->stream, dg, b, hd, sigma_kind, bc);
     g->launches += ms_cleanup(g->cfg, g->stream, b);
+    if (seeds.seg_mark)  // premarked vertices were never listed: clear visit outright
+      LGBC_CUDA(cudaMemsetAsync(b.visit, 0, static_cast<size_t>(g->n) * 8, g->stream));
     return check_launch(g);
   }
 }
@@ -828,7 +849,7 @@ int lgbc_set_tuning(lgbc_graph* g, const lgbc_tuning* t) {
   LGBC_TRY(check_graph(g));
   if (!t) return fail(LGBC_EINVAL, "null tuning");
   if (!(t->alpha > 0) || !(t->beta > 0) || t->lanes < 1 || t->lanes > kMaxLanes ||
-      t->hub_degree < 1 || t->dense_edges < 0)
+      t->hub_degree < 1 || t->dense_edges < 0 || t->segment_degree < 0)
     return fail(LGBC_EINVAL,
                 "tuning out of range (alpha, beta > 0; 1 <= lanes <= 64; hub_degree >= 1; dense_edges >= 0)");
   std::lock_guard<std::mutex> lock(g->mu);
@@ -882,3 +903,190 @@ int lgbc_memcpy(void* dst, const void* src, int64_t bytes, int kind) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Exact betweenness of many graphs (disjoint unions, one lane per source
+// index in every graph of a group).
+// ---------------------------------------------------------------------------
+namespace {
+
+struct ManyGraph {
+  int64_t idx, n, nnz;
+  const int64_t* rowptr;  // n + 1 entries, local
+  const int32_t* colidx;  // local ids
+  int64_t out_off;        // position of its first vertex in bc_raw_out
+};
+
+int many_group(const std::vector<ManyGraph>& grp, int endpoints, double* bc_raw_out) {
+  // union CSR on the host
+  int64_t N = 0, NNZ = 0;
+  for (const auto& m : grp) {
+    N += m.n;
+    NNZ += m.nnz;
+  }
+  std::vector<int64_t> rp(static_cast<size_t>(N + 1));
+  std::vector<int32_t> ci(static_cast<size_t>(NNZ));
+  std::vector<int64_t> voff(grp.size() + 1);
+  int64_t vo = 0, eo = 0;
+  for (size_t k = 0; k < grp.size(); ++k) {
+    const ManyGraph& m = grp[k];
+    voff[k] = vo;
+    for (int64_t v = 0; v < m.n; ++v) rp[static_cast<size_t>(vo + v)] = eo + m.rowptr[v];
+    for (int64_t e = 0; e < m.nnz; ++e) {
+      // a local id outside [0, n) would land in a neighbouring graph of the union
+      if (m.colidx[e] < 0 || m.colidx[e] >= m.n)
+        return fail(LGBC_EINVAL, "graph " + std::to_string(m.idx) + ": column index outside [0, n)");
+      ci[static_cast<size_t>(eo + e)] = static_cast<int32_t>(vo + m.colidx[e]);
+    }
+    vo += m.n;
+    eo += m.nnz;
+  }
+  voff[grp.size()] = vo;
+  rp[static_cast<size_t>(N)] = NNZ;
+  lgbc_graph* g = nullptr;
+  LGBC_TRY(lgbc_graph_create(&g, N, NNZ, rp.data(), ci.data(), nullptr, nullptr, 0));
+  std::unique_ptr<lgbc_graph, int (*)(lgbc_graph*)> guard(g, lgbc_graph_destroy);
+  std::lock_guard<std::mutex> lock(g->mu);
+
+  // seeds of every batch, and the endpoint terms
+  int64_t maxn = 0;
+  for (const auto& m : grp) maxn = std::max(maxn, m.n);
+  std::vector<int32_t> sv, sl, act_src;
+  std::vector<double> seg_add(grp.size()), src_add;
+  for (size_t k = 0; k < grp.size(); ++k) {
+    int64_t a = 0;
+    for (int64_t v = 0; v < grp[k].n; ++v)
+      if (g->has_degree[static_cast<size_t>(voff[k] + v)]) {
+        ++a;
+        act_src.push_back(static_cast<int32_t>(voff[k] + v));
+        src_add.push_back(static_cast<double>(grp[k].n) - 2.0);
+      }
+    seg_add[k] = static_cast<double>(a);
+  }
+  const int64_t nb = (maxn + kMaxLanes - 1) / kMaxLanes;
+  std::vector<int64_t> bstart(static_cast<size_t>(nb + 1), 0);
+  std::vector<uint64_t> marks(static_cast<size_t>(nb) * grp.size());
+  for (int64_t b = 0; b < nb; ++b) {
+    for (size_t k = 0; k < grp.size(); ++k) {
+      uint64_t seeded = 0;
+      for (int l = 0; l < kMaxLanes; ++l) {
+        const int64_t s = b * kMaxLanes + l;
+        if (s < grp[k].n && g->has_degree[static_cast<size_t>(voff[k] + s)]) {
+          sv.push_back(static_cast<int32_t>(voff[k] + s));
+          sl.push_back(l);
+          seeded |= 1ull << l;
+        }
+      }
+      marks[static_cast<size_t>(b) * grp.size() + k] = ~seeded;
+    }
+    bstart[static_cast<size_t>(b + 1)] = static_cast<int64_t>(sv.size());
+  }
+  int64_t* d_voff = nullptr;
+  uint64_t* d_marks = nullptr;
+  LGBC_TRY(dev_alloc(&d_voff, voff.size()));
+  std::unique_ptr<int64_t, cudaError_t (*)(void*)> g7(d_voff, cudaFree);
+  LGBC_TRY(dev_alloc(&d_marks, marks.size()));
+  std::unique_ptr<uint64_t, cudaError_t (*)(void*)> g8(d_marks, cudaFree);
+  LGBC_CUDA(cudaMemcpyAsync(d_voff, voff.data(), voff.size() * 8, cudaMemcpyHostToDevice, g->stream));
+  if (!marks.empty())
+    LGBC_CUDA(cudaMemcpyAsync(d_marks, marks.data(), marks.size() * 8, cudaMemcpyHostToDevice,
+                              g->stream));
+  int32_t* d_sv = nullptr;
+  int32_t* d_sl = nullptr;
+  LGBC_TRY(dev_alloc(&d_sv, sv.size()));
+  std::unique_ptr<int32_t, cudaError_t (*)(void*)> g1(d_sv, cudaFree);
+  LGBC_TRY(dev_alloc(&d_sl, sl.size()));
+  std::unique_ptr<int32_t, cudaError_t (*)(void*)> g2(d_sl, cudaFree);
+  if (!sv.empty()) {
+    LGBC_CUDA(cudaMemcpyAsync(d_sv, sv.data(), sv.size() * 4, cudaMemcpyHostToDevice, g->stream));
+    LGBC_CUDA(cudaMemcpyAsync(d_sl, sl.data(), sl.size() * 4, cudaMemcpyHostToDevice, g->stream));
+  }
+  if (!g->d_bc) LGBC_TRY(dev_alloc(&g->d_bc, static_cast<size_t>(N)));
+  g->launches += fill_f64(g->cfg, g->stream, g->d_bc, N, 0.0);
+  if (!sv.empty()) LGBC_TRY(ensure_ms(g, true));
+  for (int64_t b = 0; b < nb; ++b) {
+    Seeds sd;
+    sd.v = d_sv + bstart[static_cast<size_t>(b)];
+    sd.lane = d_sl + bstart[static_cast<size_t>(b)];
+    sd.count = bstart[static_cast<size_t>(b + 1)] - bstart[static_cast<size_t>(b)];
+    if (sd.count == 0) continue;
+    sd.seg_off = d_voff;
+    sd.seg_mark = d_marks + static_cast<size_t>(b) * grp.size();
+    sd.nseg = static_cast<int64_t>(grp.size());
+    int rc = run_ms_batch(g, nullptr, kMaxLanes, kSigmaU64, g->d_bc, nullptr, 0, sd);
+    if (rc == 1) rc = run_ms_batch(g, nullptr, kMaxLanes, kSigmaF64, g->d_bc, nullptr, 0, sd);
+    if (rc != LGBC_OK) return rc;
+  }
+  if (endpoints && !act_src.empty()) {
+    int64_t* d_off = nullptr;
+    double* d_add = nullptr;
+    int32_t* d_src = nullptr;
+    double* d_sadd = nullptr;
+    LGBC_TRY(dev_alloc(&d_off, voff.size()));
+    std::unique_ptr<int64_t, cudaError_t (*)(void*)> g3(d_off, cudaFree);
+    LGBC_TRY(dev_alloc(&d_add, seg_add.size()));
+    std::unique_ptr<double, cudaError_t (*)(void*)> g4(d_add, cudaFree);
+    LGBC_TRY(dev_alloc(&d_src, act_src.size()));
+    std::unique_ptr<int32_t, cudaError_t (*)(void*)> g5(d_src, cudaFree);
+    LGBC_TRY(dev_alloc(&d_sadd, src_add.size()));
+    std::unique_ptr<double, cudaError_t (*)(void*)> g6(d_sadd, cudaFree);
+    LGBC_CUDA(cudaMemcpyAsync(d_off, voff.data(), voff.size() * 8, cudaMemcpyHostToDevice, g->stream));
+    LGBC_CUDA(cudaMemcpyAsync(d_add, seg_add.data(), seg_add.size() * 8, cudaMemcpyHostToDevice, g->stream));
+    LGBC_CUDA(cudaMemcpyAsync(d_src, act_src.data(), act_src.size() * 4, cudaMemcpyHostToDevice, g->stream));
+    LGBC_CUDA(cudaMemcpyAsync(d_sadd, src_add.data(), src_add.size() * 8, cudaMemcpyHostToDevice, g->stream));
+    g->launches += add_endpoints_many(g->cfg, g->stream, g->d_bc, d_off, d_add,
+                                      static_cast<int64_t>(grp.size()), d_src, d_sadd,
+                                      static_cast<int64_t>(act_src.size()));
+    LGBC_CUDA(cudaStreamSynchronize(g->stream));
+  }
+  std::vector<double> out(static_cast<size_t>(N));
+  LGBC_CUDA(cudaMemcpyAsync(out.data(), g->d_bc, static_cast<size_t>(N) * 8, cudaMemcpyDeviceToHost,
+                            g->stream));
+  LGBC_CUDA(cudaStreamSynchronize(g->stream));
+  for (size_t k = 0; k < grp.size(); ++k)
+    std::memcpy(bc_raw_out + grp[k].out_off, out.data() + voff[k],
+                static_cast<size_t>(grp[k].n) * 8);
+  return LGBC_OK;
+}
+
+}  // namespace
+
+extern "C" int lgbc_betweenness_many(int64_t ngraphs, const int64_t* n, const int64_t* rowptr_off,
+                                     const int64_t* col_off, const int64_t* rowptr,
+                                     const int32_t* colidx, int endpoints, double* bc_raw_out) {
+  if (ngraphs < 0) return fail(LGBC_EINVAL, "negative graph count");
+  if (ngraphs == 0) return LGBC_OK;
+  if (!n || !rowptr_off || !col_off || !rowptr || !bc_raw_out)
+    return fail(LGBC_EINVAL, "null argument");
+  std::vector<ManyGraph> gs(static_cast<size_t>(ngraphs));
+  int64_t out = 0;
+  for (int64_t i = 0; i < ngraphs; ++i) {
+    if (n[i] < 0 || rowptr_off[i] < 0 || col_off[i] < 0) return fail(LGBC_EINVAL, "negative offset");
+    const int64_t* rp = rowptr + rowptr_off[i];
+    if (rp[0] != 0) return fail(LGBC_EINVAL, "each graph's rowptr must start at 0");
+    gs[static_cast<size_t>(i)] =
+        ManyGraph{i, n[i], rp[n[i]], rp, colidx ? colidx + col_off[i] : nullptr, out};
+    if (gs[static_cast<size_t>(i)].nnz > 0 && !colidx) return fail(LGBC_EINVAL, "null colidx");
+    out += n[i];
+  }
+  // size-sorted groups of at most kGroupVertices vertices (one big graph alone)
+  std::vector<size_t> order(gs.size());
+  for (size_t i = 0; i < order.size(); ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](size_t a, size_t b) { return gs[a].n > gs[b].n; });
+  const int64_t kGroupVertices = int64_t(1) << 21;
+  std::vector<ManyGraph> grp;
+  int64_t gv = 0;
+  for (size_t oi = 0; oi < order.size(); ++oi) {
+    const ManyGraph& m = gs[order[oi]];
+    if (!grp.empty() && gv + m.n > kGroupVertices) {
+      LGBC_TRY(many_group(grp, endpoints, bc_raw_out));
+      grp.clear();
+      gv = 0;
+    }
+    grp.push_back(m);
+    gv += m.n;
+  }
+  if (!grp.empty()) LGBC_TRY(many_group(grp, endpoints, bc_raw_out));
+  return LGBC_OK;
+}

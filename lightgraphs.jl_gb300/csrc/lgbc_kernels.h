@@ -60,12 +60,22 @@ struct HubData {
   unsigned int* cnt;             // slots: finished items, kept zero
   int hub_degree;                // degree above which a vertex is a hub (INT32_MAX: none)
   int dense_edges;               // chunks with more contributing edges use the transposed gather
+  int segmented;                 // 1: low-degree kernels (a warp streams 32 vertices' edges)
 };
 
 // sigma_limit: (2^64 - 1) / (max in-degree + 1), the largest path count a
 // level may hold without the next level risking 64-bit overflow.
 int ms_init(cudaStream_t s, const DevGraph& g, const MsBuffers& b, int nlanes, int sigma_kind,
             unsigned long long sigma_limit, int32_t* dist, int64_t dist_ld);
+// Level 0 from explicit (vertex, lane) seeds (distinct vertices); for disjoint
+// unions of graphs, where one lane holds a source in every component.
+int ms_init_seeds(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
+                  const int32_t* seed_v, const int32_t* seed_lane, int64_t nseeds, int sigma_kind,
+                  unsigned long long sigma_limit, int32_t* dist, int64_t dist_ld);
+// visit[v] = seg_mark[k] for every vertex of segment k (vertices
+// [seg_off[k], seg_off[k+1])): the lanes with no source in that component.
+int ms_premark(const LaunchCfg& c, cudaStream_t s, const MsBuffers& b, const int64_t* seg_off,
+               const uint64_t* seg_mark, int64_t nseg);
 int ms_topdown(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
                const HubData& hd, uint64_t act, int sigma_kind, int32_t* dist, int64_t dist_ld);
 int ms_bottomup(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
@@ -112,5 +122,11 @@ int fill_f64(const LaunchCfg& c, cudaStream_t s, double* p, int64_t count, doubl
 // the endpoint terms of _accumulate_endpoints! summed over the sources.
 int add_endpoints(const LaunchCfg& c, cudaStream_t s, double* bc, int64_t n,
                   const int32_t* active_src, int64_t k_act);
+// The same for a disjoint union of graphs: segment i = vertices [seg_off[i],
+// seg_off[i+1]) gets seg_add[i] (its active-source count) everywhere, and each
+// active source src[j] gets src_add[j] (its graph's n - 2) more.
+int add_endpoints_many(const LaunchCfg& c, cudaStream_t s, double* bc, const int64_t* seg_off,
+                       const double* seg_add, int64_t nseg, const int32_t* src,
+                       const double* src_add, int64_t nsrc);
 
 }  // namespace lgbc

@@ -29,6 +29,8 @@
 // with one or two such edges take a per-edge path instead.  Hubs (more than
 // hub_degree neighbours) are cut into kHubChunk-edge items processed by the
 // whole grid (k_ms_hub_*).
+#include <algorithm>
+
 #include "lgbc_kernels.h"
 
 namespace lgbc {
@@ -142,6 +144,7 @@ template <> __device__ __forceinline__ float2 zero_row() { return make_float2(0.
 struct ChunkStage {
   uint64_t f[kWarp];
   int32_t v[kWarp];
+  int32_t j[kWarp];  // owner segment (seg_gather)
 };
 constexpr int kWarpsPerBlock = 8;  // every gather kernel runs 256-thread blocks
 
@@ -298,6 +301,128 @@ __device__ __forceinline__ void psi_range_f64(const int32_t* __restrict__ ci, in
       gm = succ[w] & F;
     }
     gather_chunk<double, double>(w, gm, reinterpret_cast<const double*>(psi), dense, acc0, acc1);
+  }
+}
+
+__device__ __forceinline__ int64_t shfl_i64(int64_t x, int src) {
+  return static_cast<int64_t>(shfl_u64(static_cast<uint64_t>(x), src));
+}
+
+template <class A> __device__ __forceinline__ A zero_acc();
+template <> __device__ __forceinline__ unsigned long long zero_acc() { return 0ull; }
+template <> __device__ __forceinline__ double zero_acc() { return 0.0; }
+template <> __device__ __forceinline__ df32 zero_acc() { return df32{0.f, 0.f}; }
+
+// Segmented gather for low-degree graphs: lane j of the warp holds one
+// vertex ("segment"): `valid`, its edge range [e0, e0 + deg) in `ci`, and a
+// lane mask `mask`.  The warp streams the concatenation of the valid
+// segments' edges 32 at a time, so a vertex with a handful of edges does not
+// occupy a whole warp pass; for an edge to neighbour x of segment j, the
+// lanes f = gate[x] & mask_j contribute rows[x * 64 + lane].  Contributing
+// edges are compacted into shared memory with their segment, read four at a
+// time into per-thread accumulators for lanes t and t + 32; when the segment
+// changes, flush(j, nm_j, acc_lo, acc_hi) runs (warp-uniformly) with nm_j the
+// OR of segment j's f.  With VISIT_ALL every valid segment is flushed once,
+// contributions or not.
+template <class T, class A, bool VISIT_ALL, class Flush>
+__device__ __forceinline__ void seg_gather(bool valid, int64_t e0, int deg, uint64_t mask,
+                                           const int32_t* __restrict__ ci,
+                                           const uint64_t* __restrict__ gate,
+                                           const T* __restrict__ rows, Flush&& flush) {
+  const int ln = lane_id();
+  const int d = valid ? deg : 0;
+  int incl = d;
+#pragma unroll
+  for (int o = 1; o < kWarp; o <<= 1) {
+    const int y = __shfl_up_sync(kFull, incl, o);
+    if (ln >= o) incl += y;
+  }
+  const int total = __shfl_sync(kFull, incl, kWarp - 1);
+  const int off = incl - d;
+  const unsigned vmask = __ballot_sync(kFull, valid);
+  const T* r0 = rows + ln;
+  const T* r1 = rows + 32 + ln;
+  ChunkStage& st = my_stage();
+  int cur = -1;
+  unsigned done = 0;
+  uint64_t nm = 0;
+  A a0 = zero_acc<A>(), a1 = zero_acc<A>();
+  for (int c = 0; c < total; c += kWarp) {
+    const int gi = c + ln;
+    int pos = 0;
+#pragma unroll
+    for (int step = 16; step >= 1; step >>= 1) {
+      const int iv = __shfl_sync(kFull, incl, pos + step - 1);
+      if (iv <= gi) pos += step;
+    }
+    const bool ok = gi < total;
+    const int j = ok ? pos : 0;
+    const int64_t ej = shfl_i64(e0, j);
+    const int oj = __shfl_sync(kFull, off, j);
+    const uint64_t mj = shfl_u64(mask, j);
+    int32_t x = 0;
+    uint64_t f = 0;
+    if (ok) {
+      x = ci[ej + (gi - oj)];
+      f = gate[x] & mj;
+    }
+    const unsigned bal = __ballot_sync(kFull, f != 0);
+    if (f) {
+      const int r = __popc(bal & ((1u << ln) - 1u));
+      st.v[r] = x;
+      st.f[r] = f;
+      st.j[r] = j;
+    }
+    __syncwarp();
+    const int S = __popc(bal);
+    for (int r = 0; r < S; r += 4) {
+      T x0[4], x1[4];
+      unsigned my[4];
+      uint64_t fq[4];
+      int jq[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const bool okq = r + q < S;
+        fq[q] = okq ? st.f[r + q] : 0ull;
+        jq[q] = okq ? st.j[r + q] : -1;
+        const int64_t o = static_cast<int64_t>(okq ? st.v[r + q] : 0) * 64;
+        my[q] = my_bits(fq[q]);
+        x0[q] = zero_row<T>();
+        x1[q] = zero_row<T>();
+        if (my[q] & 1u) x0[q] = r0[o];
+        if (my[q] & 2u) x1[q] = r1[o];
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        if (jq[q] < 0) continue;
+        if (jq[q] != cur) {
+          if (cur >= 0) {
+            flush(cur, nm, a0, a1);
+            done |= 1u << cur;
+          }
+          cur = jq[q];
+          nm = 0;
+          a0 = zero_acc<A>();
+          a1 = zero_acc<A>();
+        }
+        nm |= fq[q];
+        if (my[q] & 1u) acc_row<T, A>(a0, x0[q]);
+        if (my[q] & 2u) acc_row<T, A>(a1, x1[q]);
+      }
+    }
+    __syncwarp();
+  }
+  if (cur >= 0) {
+    flush(cur, nm, a0, a1);
+    done |= 1u << cur;
+  }
+  if (VISIT_ALL) {
+    unsigned rem = vmask & ~done;
+    while (rem) {
+      const int j = __ffs(rem) - 1;
+      rem &= rem - 1;
+      flush(j, 0ull, zero_acc<A>(), zero_acc<A>());
+    }
   }
 }
 
@@ -788,6 +913,165 @@ __global__ void __launch_bounds__(256) k_ms_hub_delta(DevGraph g, MsBuffers b, H
   }
 }
 
+// ---------------------------------------------------------------------------
+// Low-degree variants (segmented warps): a warp takes 32 vertices / list
+// entries and streams their concatenated edge lists (seg_gather), instead of
+// giving each vertex a whole warp pass.  Same results as k_ms_td_settle,
+// k_ms_bu and k_ms_delta.
+// ---------------------------------------------------------------------------
+template <int SK>
+__global__ void __launch_bounds__(256) k_ms_td_settle_seg(DevGraph g, MsBuffers b, HubData hd,
+                                                          uint64_t act) {
+  using T = typename Sig<SK>::T;
+  BatchCtl* c = b.ctl;
+  const unsigned long long lo = c->hi, hi = c->tail;
+  const int L = c->level;
+  const uint64_t* __restrict__ front = mb_at(b, L);
+  const uint64_t* __restrict__ next = mb_at(b, L + 1);
+  const int ln = lane_id();
+  unsigned long long mf = 0, mu = 0, smax = 0;
+  for (unsigned long long base = lo + static_cast<unsigned long long>(gwarp()) * kWarp; base < hi;
+       base += static_cast<unsigned long long>(nwarps()) * kWarp) {
+    const unsigned long long i = base + ln;
+    const bool ve = i < hi;
+    int32_t w = 0;
+    uint64_t mask = 0;
+    int64_t e0 = 0, deg = 0;
+    if (ve) {
+      w = b.qv[i];
+      mask = next[w];
+      e0 = g.in_rowptr[w];
+      deg = g.in_rowptr[w + 1] - e0;
+      const uint64_t nv = b.visit[w] | mask;
+      b.qm[i] = mask;
+      b.visit[w] = nv;
+      mf += static_cast<unsigned long long>(g.rowptr[w + 1] - g.rowptr[w]);
+      if (nv == act) mu += static_cast<unsigned long long>(deg);
+    }
+    const bool mine = ve && deg <= hd.hub_degree;  // hubs: k_ms_hub_pull
+    seg_gather<T, T, false>(mine, e0, static_cast<int>(mine ? deg : 0), mask, g.in_colidx, front,
+                            reinterpret_cast<const T*>(b.sigma),
+                            [&](int j, uint64_t nm, T a0, T a1) {
+                              store_sigma<SK>(b.sigma, __shfl_sync(kFull, w, j), nm, a0, a1, smax);
+                            });
+  }
+  if (SK == kSigmaU64) {
+    smax = warp_max_u64(smax);
+    if (ln == 0 && smax) atomicMax(&c->sigma_max, smax);
+  }
+  mf = warp_sum_u64(mf);
+  mu = warp_sum_u64(mu);
+  if (ln == 0) {
+    if (mf) atomicAdd(&c->mf, mf);
+    if (mu) atomicAdd(&c->mu_done, mu);
+  }
+}
+
+template <int SK>
+__global__ void __launch_bounds__(256) k_ms_bu_seg(DevGraph g, MsBuffers b, HubData hd, uint64_t act) {
+  using T = typename Sig<SK>::T;
+  BatchCtl* c = b.ctl;
+  const int L = c->level;
+  const uint64_t* __restrict__ front = mb_at(b, L);
+  uint64_t* next = mb_at(b, L + 1);
+  const int64_t n = g.n;
+  const int ln = lane_id();
+  unsigned long long mf = 0, mu = 0, smax = 0;
+  for (int64_t base = gwarp() * kWarp; base < n; base += nwarps() * kWarp) {
+    const int64_t wme = base + ln;
+    uint64_t vis = 0;
+    int64_t e0 = 0, deg = 0;
+    bool cand = false;
+    if (wme < n) {
+      vis = b.visit[wme];
+      e0 = g.in_rowptr[wme];
+      deg = g.in_rowptr[wme + 1] - e0;
+      cand = (vis != act) && deg > 0 && deg <= hd.hub_degree;
+    }
+    uint64_t my_nm = 0;
+    seg_gather<T, T, false>(cand, e0, static_cast<int>(cand ? deg : 0), act & ~vis, g.in_colidx,
+                            front, reinterpret_cast<const T*>(b.sigma),
+                            [&](int j, uint64_t nm, T a0, T a1) {
+                              if (nm)
+                                store_sigma<SK>(b.sigma, static_cast<int32_t>(base + j), nm, a0, a1,
+                                                smax);
+                              if (ln == j) my_nm = nm;
+                            });
+    const bool app = my_nm != 0;
+    const unsigned long long slot = warp_append(app, &c->tail);
+    if (app) {
+      b.qv[slot] = static_cast<int32_t>(wme);
+      b.qm[slot] = my_nm;
+      next[wme] = my_nm;
+      const uint64_t nv = vis | my_nm;
+      b.visit[wme] = nv;
+      mf += static_cast<unsigned long long>(g.rowptr[wme + 1] - g.rowptr[wme]);
+      if (nv == act) mu += static_cast<unsigned long long>(deg);
+    }
+  }
+  if (SK == kSigmaU64) {
+    smax = warp_max_u64(smax);
+    if (ln == 0 && smax) atomicMax(&c->sigma_max, smax);
+  }
+  mf = warp_sum_u64(mf);
+  mu = warp_sum_u64(mu);
+  if (ln == 0) {
+    if (mf) atomicAdd(&c->mf, mf);
+    if (mu) atomicAdd(&c->mu_done, mu);
+  }
+}
+
+template <int SK>
+__global__ void __launch_bounds__(256) k_ms_delta_seg(DevGraph g, MsBuffers b, HubData hd, double* bc) {
+  BatchCtl* c = b.ctl;
+  const int L = c->level;
+  const unsigned long long lo = b.lvl_off[L], hi = b.lvl_off[L + 1];
+  const uint64_t* __restrict__ succ = mb_at(b, L + 1);
+  uint64_t* other = mb_at(b, L);
+  const int ln = lane_id();
+  for (unsigned long long base = lo + static_cast<unsigned long long>(gwarp()) * kWarp; base < hi;
+       base += static_cast<unsigned long long>(nwarps()) * kWarp) {
+    const unsigned long long i = base + ln;
+    const bool ve = i < hi;
+    int32_t v = 0;
+    uint64_t F = 0;
+    int64_t e0 = 0, deg = 0;
+    if (ve) {
+      v = b.qv[i];
+      F = b.qm[i];
+      other[v] = F;
+      b.visit[v] = 0;
+      e0 = g.rowptr[v];
+      deg = g.rowptr[v + 1] - e0;
+    }
+    if (L == 0) continue;
+    const bool mine = ve && deg <= hd.hub_degree;  // hubs: k_ms_hub_delta
+    const int dg = static_cast<int>(mine ? deg : 0);
+    if (SK == kSigmaU64) {
+      seg_gather<float2, df32, true>(mine, e0, dg, F, g.colidx, succ,
+                                     reinterpret_cast<const float2*>(b.psi),
+                                     [&](int j, uint64_t, df32 a0, df32 a1) {
+                                       const int32_t vj = __shfl_sync(kFull, v, j);
+                                       df32 contrib = finish_df(b.psi, b.sigma, vj,
+                                                                my_bits(shfl_u64(F, j)),
+                                                                acc_done(a0), acc_done(a1));
+                                       contrib = warp_sum_df(contrib);
+                                       if (ln == 0 && contrib.hi != 0.f) bc[vj] += df_to_double(contrib);
+                                     });
+    } else {
+      seg_gather<double, double, true>(mine, e0, dg, F, g.colidx, succ,
+                                       reinterpret_cast<const double*>(b.psi),
+                                       [&](int j, uint64_t, double a0, double a1) {
+                                         const int32_t vj = __shfl_sync(kFull, v, j);
+                                         double contrib = finish_f64(b.psi, b.sigma, vj,
+                                                                     my_bits(shfl_u64(F, j)), a0, a1);
+                                         contrib = warp_sum_f64(contrib);
+                                         if (ln == 0 && contrib != 0.0) bc[vj] += contrib;
+                                       });
+    }
+  }
+}
+
 __global__ void k_ms_back_advance(MsBuffers b) { b.ctl->level -= 1; }
 
 // End of a Brandes batch: the backward sweep cleared visit for every listed
@@ -815,6 +1099,66 @@ __global__ void k_ms_cleanup_all(MsBuffers b) {
   }
 }
 
+// Batch initialisation with explicit seeds: seed i puts vertex seed_v[i] at
+// level 0 of lane seed_lane[i].  Used for disjoint unions of graphs, where a
+// lane may hold one source in every component: BFS trees of different
+// components never meet, so each component sees a single-source traversal.
+// Seed vertices must be distinct.  The host zeroes the control block first.
+template <int SK>
+__global__ void k_ms_init_seeds(DevGraph g, MsBuffers b, const int32_t* seed_v,
+                                const int32_t* seed_lane, long long nseeds, int32_t* dist,
+                                int64_t ld) {
+  using T = typename Sig<SK>::T;
+  unsigned long long mf = 0;
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < nseeds;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const int32_t v = seed_v[i];
+    const int l = seed_lane[i];
+    const uint64_t m = 1ull << l;
+    b.mb[0][v] = m;
+    b.visit[v] |= m;
+    b.qv[i] = v;
+    b.qm[i] = m;
+    if (SK != kSigmaNone) reinterpret_cast<T*>(b.sigma)[static_cast<int64_t>(v) * 64 + l] = T(1);
+    if (dist) dist[static_cast<int64_t>(l) * ld + v] = 0;
+    mf += static_cast<unsigned long long>(g.rowptr[v + 1] - g.rowptr[v]);
+  }
+  mf = warp_sum_u64(mf);
+  if (lane_id() == 0 && mf) atomicAdd(&b.ctl->mf_cur, mf);
+}
+
+// Union batches: lanes that hold no source in a component can never reach
+// its vertices; marking them visited there keeps bottom-up levels from
+// rescanning those vertices.  Block k covers component k.
+__global__ void k_ms_premark(uint64_t* visit, const int64_t* seg_off, const uint64_t* seg_mark,
+                             int64_t nseg) {
+  for (int64_t k = blockIdx.x; k < nseg; k += gridDim.x) {
+    const uint64_t m = seg_mark[k];
+    for (int64_t v = seg_off[k] + threadIdx.x; v < seg_off[k + 1]; v += blockDim.x) visit[v] = m;
+  }
+}
+
+__global__ void k_ms_init_seeds_ctl(MsBuffers b, long long nseeds, unsigned long long cap,
+                                    unsigned long long sigma_limit) {
+  BatchCtl* c = b.ctl;
+  c->lo = 0;
+  c->hi = static_cast<unsigned long long>(nseeds);
+  c->tail = static_cast<unsigned long long>(nseeds);
+  c->mf = 0;
+  c->mu_done = 0;
+  c->cap = cap;
+  c->level = 0;
+  c->maxlevel = 0;
+  c->done = 0;
+  c->overflow_list = 0;
+  c->overflow_sigma = 0;
+  c->mode = 0;
+  c->sigma_max = 1;
+  c->sigma_limit = sigma_limit;
+  b.lvl_off[0] = 0;
+  b.lvl_off[1] = static_cast<unsigned long long>(nseeds);
+}
+
 }  // namespace
 
 int ms_init(cudaStream_t s, const DevGraph& g, const MsBuffers& b, int nlanes, int sigma_kind,
@@ -833,6 +1177,34 @@ int ms_init(cudaStream_t s, const DevGraph& g, const MsBuffers& b, int nlanes, i
   return 1;
 }
 
+int ms_init_seeds(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
+                  const int32_t* seed_v, const int32_t* seed_lane, int64_t nseeds, int sigma_kind,
+                  unsigned long long sigma_limit, int32_t* dist, int64_t dist_ld) {
+  cudaMemsetAsync(b.ctl, 0, sizeof(BatchCtl), s);
+  const int grid = static_cast<int>(std::min<int64_t>((nseeds + 255) / 256, c.grid));
+  switch (sigma_kind) {
+    case kSigmaU64:
+      k_ms_init_seeds<kSigmaU64><<<grid, 256, 0, s>>>(g, b, seed_v, seed_lane, nseeds, dist, dist_ld);
+      k_ms_init_seeds_ctl<<<1, 1, 0, s>>>(b, nseeds, b.cap, sigma_limit);
+      break;
+    case kSigmaF64:
+      k_ms_init_seeds<kSigmaF64><<<grid, 256, 0, s>>>(g, b, seed_v, seed_lane, nseeds, dist, dist_ld);
+      k_ms_init_seeds_ctl<<<1, 1, 0, s>>>(b, nseeds, b.cap, ~0ull);
+      break;
+    default:
+      k_ms_init_seeds<kSigmaNone><<<grid, 256, 0, s>>>(g, b, seed_v, seed_lane, nseeds, dist, dist_ld);
+      k_ms_init_seeds_ctl<<<1, 1, 0, s>>>(b, nseeds, b.cap, ~0ull);
+      break;
+  }
+  return 2;
+}
+
+int ms_premark(const LaunchCfg& c, cudaStream_t s, const MsBuffers& b, const int64_t* seg_off,
+               const uint64_t* seg_mark, int64_t nseg) {
+  k_ms_premark<<<c.grid, c.block, 0, s>>>(b.visit, seg_off, seg_mark, nseg);
+  return 1;
+}
+
 int ms_topdown(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
                const HubData& hd, uint64_t act, int sigma_kind, int32_t* dist, int64_t dist_ld) {
   int launches = 0;
@@ -845,13 +1217,19 @@ int ms_topdown(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBu
   if (dist) {
     k_ms_td_settle<kSigmaNone, true><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
   } else if (sigma_kind == kSigmaU64) {
-    k_ms_td_settle<kSigmaU64, false><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
+    if (hd.segmented)
+      k_ms_td_settle_seg<kSigmaU64><<<c.grid, c.block, 0, s>>>(g, b, hd, act);
+    else
+      k_ms_td_settle<kSigmaU64, false><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
     if (hd.n_in > 0) {
       k_ms_hub_pull<kSigmaU64, false, false><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
       ++launches;
     }
   } else {
-    k_ms_td_settle<kSigmaF64, false><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
+    if (hd.segmented)
+      k_ms_td_settle_seg<kSigmaF64><<<c.grid, c.block, 0, s>>>(g, b, hd, act);
+    else
+      k_ms_td_settle<kSigmaF64, false><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
     if (hd.n_in > 0) {
       k_ms_hub_pull<kSigmaF64, false, false><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
       ++launches;
@@ -872,13 +1250,19 @@ int ms_bottomup(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsB
       ++launches;
     }
   } else if (sigma_kind == kSigmaU64) {
-    k_ms_bu<kSigmaU64, false><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
+    if (hd.segmented)
+      k_ms_bu_seg<kSigmaU64><<<c.grid, c.block, 0, s>>>(g, b, hd, act);
+    else
+      k_ms_bu<kSigmaU64, false><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
     if (hd.n_in > 0) {
       k_ms_hub_pull<kSigmaU64, false, true><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
       ++launches;
     }
   } else {
-    k_ms_bu<kSigmaF64, false><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
+    if (hd.segmented)
+      k_ms_bu_seg<kSigmaF64><<<c.grid, c.block, 0, s>>>(g, b, hd, act);
+    else
+      k_ms_bu<kSigmaF64, false><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
     if (hd.n_in > 0) {
       k_ms_hub_pull<kSigmaF64, false, true><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
       ++launches;
@@ -903,13 +1287,19 @@ int ms_backward_level(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, con
   int launches = 3;
   k_ms_back_clear<<<c.grid, c.block, 0, s>>>(b);
   if (sigma_kind == kSigmaF64) {
-    k_ms_delta<kSigmaF64><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
+    if (hd.segmented)
+      k_ms_delta_seg<kSigmaF64><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
+    else
+      k_ms_delta<kSigmaF64><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
     if (hd.n_out > 0) {
       k_ms_hub_delta<kSigmaF64><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
       ++launches;
     }
   } else {
-    k_ms_delta<kSigmaU64><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
+    if (hd.segmented)
+      k_ms_delta_seg<kSigmaU64><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
+    else
+      k_ms_delta<kSigmaU64><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
     if (hd.n_out > 0) {
       k_ms_hub_delta<kSigmaU64><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
       ++launches;

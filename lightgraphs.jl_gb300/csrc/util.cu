@@ -43,7 +43,37 @@ __global__ void k_validate_csr(const int64_t* rowptr, const int32_t* colidx, int
   if (__any_sync(kFull, local != 0) && local) atomicOr(bad, local);
 }
 
+__global__ void k_add_segments(double* bc, const int64_t* seg_off, const double* seg_add,
+                               int64_t nseg) {
+  for (int64_t sgi = blockIdx.x; sgi < nseg; sgi += gridDim.x) {
+    const double a = seg_add[sgi];
+    if (a == 0.0) continue;
+    for (int64_t v = seg_off[sgi] + threadIdx.x; v < seg_off[sgi + 1]; v += blockDim.x) bc[v] += a;
+  }
+}
+
+__global__ void k_add_sources_var(double* bc, const int32_t* src, const double* add, int64_t k) {
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < k;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    atomicAdd(bc + src[i], add[i]);
+}
+
 }  // namespace
+
+int add_endpoints_many(const LaunchCfg& c, cudaStream_t s, double* bc, const int64_t* seg_off,
+                       const double* seg_add, int64_t nseg, const int32_t* src,
+                       const double* src_add, int64_t nsrc) {
+  int launches = 0;
+  if (nseg > 0) {
+    k_add_segments<<<c.grid, c.block, 0, s>>>(bc, seg_off, seg_add, nseg);
+    ++launches;
+  }
+  if (nsrc > 0) {
+    k_add_sources_var<<<c.grid, c.block, 0, s>>>(bc, src, src_add, nsrc);
+    ++launches;
+  }
+  return launches;
+}
 
 int validate_csr(const LaunchCfg& c, cudaStream_t s, const int64_t* rowptr, const int32_t* colidx,
                  int64_t n, int64_t nnz, int* bad) {

@@ -19,7 +19,8 @@ a GPU or without the built library the calls raise ``LGBCError``.
 """
 from . import Parallel
 from ._lib import ArgumentError, BoundsError, LGBCError, MethodError
-from .centrality import betweenness_centrality, betweenness_raw, sample, sample_, _rescale_
+from .centrality import (betweenness_centrality, betweenness_centrality_many, betweenness_raw,
+                         sample, sample_, _rescale_)
 from .graphs import (DefaultDistance, DeviceGraph, SimpleDiGraph, SimpleGraph, degree,
                      is_directed, ne, nv, vertices, weights)
 from .persistence import loadgraph
@@ -27,7 +28,7 @@ from .traversals import gdistances, gdistances_, multi_gdistances
 
 __all__ = [
     "Parallel", "ArgumentError", "BoundsError", "LGBCError", "MethodError",
-    "betweenness_centrality", "betweenness_raw", "sample", "sample_", "_rescale_",
+    "betweenness_centrality", "betweenness_centrality_many", "betweenness_raw", "sample", "sample_", "_rescale_",
     "DefaultDistance", "DeviceGraph", "SimpleDiGraph", "SimpleGraph", "degree", "is_directed",
     "ne", "nv", "vertices", "weights", "loadgraph", "gdistances", "gdistances_",
     "multi_gdistances",

@@ -57,7 +57,7 @@ class LgbcStats(ctypes.Structure):
 class LgbcTuning(ctypes.Structure):
     _fields_ = [("alpha", ctypes.c_double), ("beta", ctypes.c_double),
                 ("hub_degree", ctypes.c_int32), ("lanes", ctypes.c_int32),
-                ("dense_edges", ctypes.c_int32)]
+                ("dense_edges", ctypes.c_int32), ("segment_degree", ctypes.c_int32)]
 
 
 def _declare(lib) -> None:
@@ -87,6 +87,7 @@ def _declare(lib) -> None:
         "lgbc_host_free": ([p], c_int),
         "lgbc_memcpy": ([p, p, i64, c_int], c_int),
         "lgbc_gdistances_noalloc": ([i64, i64, p, p, p, p, p, i64, p, p], c_int),
+        "lgbc_betweenness_many": ([i64, p, p, p, p, p, c_int, p], c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

@@ -145,6 +145,18 @@ def test_gather_paths(name, dense):
     assert_bc_close(z, oracle_bc(g, np.arange(299), normalize=False))
 
 
+@pytest.mark.parametrize("segment_degree", [0, 1000])
+@pytest.mark.parametrize("name", ["rmat10", "er_directed", "ba", "sparse_er"])
+def test_kernel_families(name, segment_degree):
+    # segment_degree 0 forces the warp-per-vertex kernels, 1000 the
+    # segmented (32 vertices per warp) kernels; both match the oracle
+    g = GRAPHS[name]()
+    g.device_handle().set_tuning(segment_degree=segment_degree, hub_degree=64)
+    for ep in (False, True):
+        z = lgbc.betweenness_centrality(g, list(range(1, 400)), normalize=False, endpoints=ep)
+        assert_bc_close(z, oracle_bc(g, np.arange(399), normalize=False, endpoints=ep))
+
+
 def test_sampled_k_uses_distinct_sources():
     g = GRAPHS["ba"]()
     rng = np.random.default_rng(123)
@@ -259,3 +271,20 @@ def test_rmat20_properties():
         e = oracle.gdistances(rp, ci, [s]).astype(np.int64)
         e[e == oracle.UNREACHED32] = np.iinfo(g.eltype).max
         assert np.array_equal(got, e)
+
+
+# ---------------------------------------------------------------- many graphs
+def test_betweenness_many_matches_per_graph():
+    # uneven Barabasi-Albert graphs (plus a star, a path, an empty and an
+    # edgeless graph) in one call; each graph against the oracle
+    rng = np.random.default_rng(4)
+    graphs = [G.barabasi_albert(int(n), 3, seed=1000 + i)
+              for i, n in enumerate(rng.integers(20, 700, 40))]
+    graphs += [lgbc.SimpleGraph.from_edges(70, [(1, j) for j in range(2, 71)]),
+               lgbc.SimpleGraph.from_edge_arrays(300, np.arange(299), np.arange(1, 300)),
+               lgbc.SimpleGraph(0), lgbc.SimpleGraph(5)]
+    for endpoints in (False, True):
+        res = lgbc.betweenness_centrality_many(graphs, normalize=False, endpoints=endpoints)
+        assert len(res) == len(graphs)
+        for g, z in zip(graphs, res):
+            assert_bc_close(z, oracle_bc(g, normalize=False, endpoints=endpoints))
