@@ -192,6 +192,97 @@ int lgbc_gdistances_noalloc(int64_t n, int64_t nnz, const int64_t *rowptr,
                             const int32_t *in_colidx, const int32_t *src, int64_t nsrc,
                             int32_t *dist, void *stream);
 
+/* ---- Learned source proposal (no counterpart in the reference) -----------
+ *
+ * Sampled betweenness with an importance-sampling proposal learned from
+ * structure: raw(v) = sum_i w_i delta_{s_i}(v) with s_i drawn i.i.d. from p
+ * and w_i = 1 / (k p_{s_i}), an unbiased estimate of the exact raw vector.
+ * Passing it to _rescale!(raw, n, normalize, directed, n) gives the same
+ * scale as betweenness_centrality(g) (uniform p = 1/n reproduces the n / k
+ * factor of the k-sampled call).  p = (1 - eps) softmax(y) + eps / n, y the
+ * output of a 4 -> 64 -> 64 -> 1 ReLU MLP over per-vertex features, trained
+ * to predict log(1 + dependency mass).
+ *
+ * Undirected graphs only for the features and the proposal. */
+
+/* Core numbers, as core_number(g) (src/degeneracy.jl:38-80): LGBC_EINVAL
+ * for a directed graph or one with a self-loop (the reference throws
+ * ArgumentError for self-loops).  core_out: n int32. */
+int lgbc_core_number(lgbc_graph *g, int32_t *core_out);
+
+/* Per-vertex features, n x 4 float32 row-major: log(1 + degree),
+ * log(1 + core number), mean of log(1 + degree) over the neighbours, and
+ * log(1 + sum of the neighbours' degrees).  Degree = length(fadjlist[v]);
+ * the core number is that of the graph without its self-loops. */
+int lgbc_features(lgbc_graph *g, float *feat_out);
+
+/* Dependency mass of each source, mass_out[i] = sum_{v != s_i} delta_{s_i}(v):
+ * the total that _accumulate_basic! (src/centrality/betweenness.jl:81-107)
+ * adds to the betweenness vector for source s_i.  Computed exactly as
+ * sum over reached t != s of (d(s, t) - 1), from the multi-source BFS. */
+int lgbc_dependency_mass(lgbc_graph *g, const int32_t *src, int64_t nsrc, double *mass_out);
+
+/* Weighted raw betweenness: bc_raw_out[v] = sum_i w[i] delta_{src[i]}(v)
+ * (repeats allowed; degree-0 sources contribute nothing).  endpoints=false
+ * accumulation only. */
+int lgbc_betweenness_weighted(lgbc_graph *g, const int32_t *src, const double *w, int64_t nsrc,
+                              double *bc_raw_out);
+
+/* The MLP.  Parameters, in order: W1[64][4], b1[64], W2[64][64] (row = output
+ * unit), b2[64], W3[64], b3 -- LGBC_MLP_PARAMS floats.  The network computes
+ * with BF16 copies of FP32 master parameters and accumulates in FP32; inputs
+ * are standardised as (x - mean) / stdev first. */
+#define LGBC_MLP_FEATURES 4
+#define LGBC_MLP_HIDDEN 64
+#define LGBC_MLP_PARAMS 4545
+typedef struct lgbc_mlp lgbc_mlp;
+/* PyTorch-style uniform(-1/sqrt(fan_in), 1/sqrt(fan_in)) initialisation from
+ * a seed; mean 0 / stdev 1 standardisation; fresh Adam state. */
+int lgbc_mlp_create(lgbc_mlp **out, uint64_t seed);
+int lgbc_mlp_destroy(lgbc_mlp *m);
+/* master (LGBC_MLP_PARAMS float32) and / or bf16 (LGBC_MLP_PARAMS uint16 bit
+ * patterns); either may be NULL. */
+int lgbc_mlp_get_params(const lgbc_mlp *m, float *master, uint16_t *bf16);
+/* Sets the master parameters (and their BF16 copies); resets Adam state. */
+int lgbc_mlp_set_params(lgbc_mlp *m, const float *master);
+int lgbc_mlp_set_norm(lgbc_mlp *m, const float *mean, const float *stdev);
+int lgbc_mlp_get_norm(const lgbc_mlp *m, float *mean, float *stdev);
+/* y[r] = MLP(x[r]) for rows x rows of 4 floats (host buffers). */
+int lgbc_mlp_forward(lgbc_mlp *m, const float *x, int64_t rows, float *y);
+/* Gradient (LGBC_MLP_PARAMS floats) and value of the centred squared error
+ * (1/B) sum_r (e_r - mean e)^2, e_r = MLP(x_r) - target_r, over B = rows. */
+int lgbc_mlp_grad(lgbc_mlp *m, const float *x, const float *target, int64_t rows, float *grad,
+                  float *loss);
+/* Adam training on the GPU.  Rows are grouped (group g = rows
+ * [group_off[g], group_off[g + 1]), one graph each); every step takes one
+ * group, chosen at random, and a random window of at most `batch` of its rows.
+ * The learning rate warms up linearly over `warmup` steps, then decays by a
+ * cosine to lr_final.  loss_out (steps floats, may be NULL) gets each step's
+ * loss. */
+typedef struct lgbc_train_cfg {
+  int32_t steps;
+  int32_t batch;
+  int32_t warmup;
+  float lr;
+  float lr_final;
+  float beta1;
+  float beta2;
+  float eps;
+  uint64_t seed;
+} lgbc_train_cfg;
+int lgbc_mlp_train(lgbc_mlp *m, const float *x, const float *target, int64_t rows,
+                   const int64_t *group_off, int64_t ngroups, const lgbc_train_cfg *cfg,
+                   float *loss_out);
+
+/* Build the proposal of graph g on the device: features, MLP scores, p and its
+ * CDF (kept in the handle until the next build).  p_out (n doubles, may be
+ * NULL) receives p. */
+int lgbc_proposal_build(lgbc_graph *g, lgbc_mlp *m, double eps, double *p_out);
+/* Draw k sources i.i.d. from the built proposal (SplitMix64 stream `seed`)
+ * with weights 1 / (k p). */
+int lgbc_proposal_sample(lgbc_graph *g, int64_t k, uint64_t seed, int32_t *src_out,
+                         double *w_out);
+
 /* Device / pinned-host memory helpers for callers without their own CUDA
  * allocator (bench and test harnesses).  lgbc_memcpy kinds: 1 = host to
  * device, 2 = device to host, 3 = device to device. */

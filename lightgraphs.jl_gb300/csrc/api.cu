@@ -2,6 +2,7 @@
 // host side of the level loops.  All arithmetic runs in the kernels of
 // msbfs.cu / bfs.cu / util.cu; there is no CPU fallback.
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <memory>
@@ -126,6 +127,46 @@ struct BfsWorkspace {
   }
 };
 
+// Learned-proposal state of a graph (learned.cu): core numbers, features,
+// scores, the proposal p and its CDF, and scan scratch.
+struct LearnedWorkspace {
+  int32_t* core = nullptr;
+  uint8_t* flag = nullptr;
+  int32_t* list = nullptr;
+  unsigned long long* counters = nullptr;  // [0] self-loop flag, [1] lowered, [2] list size
+  float4* feat = nullptr;
+  float* y = nullptr;
+  float* fscr = nullptr;
+  double* e = nullptr;
+  double* tsum = nullptr;
+  double* scal = nullptr;
+  double* p = nullptr;
+  double* cdf = nullptr;
+  int32_t* samp = nullptr;
+  double* samp_w = nullptr;
+  int64_t samp_cap = 0;
+  bool built = false;
+  int64_t core_passes = 0;
+  void release() {
+    dev_free(core);
+    dev_free(flag);
+    dev_free(list);
+    dev_free(counters);
+    dev_free(feat);
+    dev_free(y);
+    dev_free(fscr);
+    dev_free(e);
+    dev_free(tsum);
+    dev_free(scal);
+    dev_free(p);
+    dev_free(cdf);
+    dev_free(samp);
+    dev_free(samp_w);
+    samp_cap = 0;
+    built = false;
+  }
+};
+
 }  // namespace
 
 // Lets the other translation units of the library report errors through
@@ -147,6 +188,7 @@ struct lgbc_graph {
   MsWorkspace ms;
   BfsWorkspace bfs;
   HubTable hubs;
+  LearnedWorkspace learned;
   int32_t* d_src = nullptr;         // device copy of a call's source list
   int64_t d_src_cap = 0;
   double* d_bc = nullptr;           // device result buffer for host-buffer calls
@@ -382,7 +424,7 @@ int check_launch(lgbc_graph* g) {
   return LGBC_OK;
 }
 
-MsBuffers ms_buffers(lgbc_graph* g, const int32_t* lane_src) {
+MsBuffers ms_buffers(lgbc_graph* g, const int32_t* lane_src, const double* lane_w = nullptr) {
   MsWorkspace& w = g->ms;
   MsBuffers b;
   b.visit = w.visit;
@@ -396,6 +438,7 @@ MsBuffers ms_buffers(lgbc_graph* g, const int32_t* lane_src) {
   b.ctl = w.ctl;
   b.lane_src = lane_src;
   b.cap = w.cap;
+  b.lane_w = lane_w;
   return b;
 }
 
@@ -425,14 +468,17 @@ struct Seeds {
   int64_t nseg = 0;
 };
 
+// lane_w (sigma batches): per-lane weights of the accumulation into bc.
+// mass (distance-only batches): per-lane dependency mass, accumulated.
 int run_ms_batch(lgbc_graph* g, const int32_t* lane_src, int nl, int sigma_kind, double* bc,
-                 int32_t* dist, int64_t dist_ld, const Seeds& seeds = Seeds()) {
+                 int32_t* dist, int64_t dist_ld, const Seeds& seeds = Seeds(),
+                 const double* lane_w = nullptr, unsigned long long* mass = nullptr) {
   const DevGraph dg = g->dev();
   LGBC_TRY(ensure_hubs(g));
   const HubData hd = hub_data(g);
   const uint64_t act = nl >= 64 ? ~0ull : ((1ull << nl) - 1ull);
   for (;;) {
-    MsBuffers b = ms_buffers(g, lane_src);
+    MsBuffers b = ms_buffers(g, lane_src, lane_w);
     if (seeds.seg_mark) g->launches += ms_premark(g->cfg, g->stream, b, seeds.seg_off, seeds.seg_mark,
                                                   seeds.nseg);
     if (seeds.v)
@@ -479,6 +525,7 @@ int run_ms_batch(lgbc_graph* g, const int32_t* lane_src, int nl, int sigma_kind,
       return 1;
     }
     if (sigma_kind == kSigmaNone) {
+      if (mass) g->launches += ms_level_mass(g->cfg, g->stream, b, mass);
       g->launches += ms_cleanup_all(g->cfg, g->stream, b);
       return check_launch(g);
     }
@@ -494,17 +541,20 @@ int run_ms_batch(lgbc_graph* g, const int32_t* lane_src, int nl, int sigma_kind,
 }
 
 // Brandes over the active sources already on the device (g->d_src[0, k)),
-// accumulating into bc_dev (zeroed here).
-int run_betweenness(lgbc_graph* g, int64_t k_act, int endpoints, double* bc_dev) {
+// accumulating into bc_dev (zeroed here); with d_w, source i's dependencies
+// are scaled by d_w[i].
+int run_betweenness(lgbc_graph* g, int64_t k_act, int endpoints, double* bc_dev,
+                    const double* d_w = nullptr) {
   g->launches += fill_f64(g->cfg, g->stream, bc_dev, g->n, 0.0);
   if (k_act > 0) LGBC_TRY(ensure_ms(g, true));
   const int lanes = std::max(1, std::min<int>(kMaxLanes, g->tune.lanes));
   for (int64_t s0 = 0; s0 < k_act; s0 += lanes) {
     const int nl = static_cast<int>(std::min<int64_t>(lanes, k_act - s0));
-    int rc = run_ms_batch(g, g->d_src + s0, nl, kSigmaU64, bc_dev, nullptr, 0);
+    const double* lw = d_w ? d_w + s0 : nullptr;
+    int rc = run_ms_batch(g, g->d_src + s0, nl, kSigmaU64, bc_dev, nullptr, 0, Seeds(), lw);
     if (rc == 1) {
       g->stats.wide_batches++;
-      rc = run_ms_batch(g, g->d_src + s0, nl, kSigmaF64, bc_dev, nullptr, 0);
+      rc = run_ms_batch(g, g->d_src + s0, nl, kSigmaF64, bc_dev, nullptr, 0, Seeds(), lw);
     }
     if (rc != LGBC_OK) return rc;
     g->stats.batches++;
@@ -669,6 +719,7 @@ int lgbc_graph_destroy(lgbc_graph* g) {
   g->ms.release();
   g->bfs.release();
   g->hubs.release();
+  g->learned.release();
   if (g->d_in_rowptr != g->d_rowptr) dev_free(g->d_in_rowptr);
   if (g->d_in_colidx != g->d_colidx) dev_free(g->d_in_colidx);
   dev_free(g->d_rowptr);
@@ -1090,3 +1141,253 @@ extern "C" int lgbc_betweenness_many(int64_t ngraphs, const int64_t* n, const in
   if (!grp.empty()) LGBC_TRY(many_group(grp, endpoints, bc_raw_out));
   return LGBC_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Learned source proposal (learned.cu, mlp.cu)
+// ---------------------------------------------------------------------------
+namespace {
+
+int ensure_learned(lgbc_graph* g) {
+  LearnedWorkspace& w = g->learned;
+  if (w.core) return LGBC_OK;
+  const size_t n = static_cast<size_t>(g->n);
+  const size_t tiles = static_cast<size_t>(proposal_tiles(g->n));
+  LGBC_TRY(dev_alloc(&w.core, n));
+  LGBC_TRY(dev_alloc(&w.flag, n));
+  LGBC_TRY(dev_alloc(&w.list, n));
+  LGBC_TRY(dev_alloc(&w.counters, 4));
+  LGBC_TRY(dev_alloc(&w.feat, n));
+  LGBC_TRY(dev_alloc(&w.y, n));
+  LGBC_TRY(dev_alloc(&w.fscr, tiles + 1));
+  LGBC_TRY(dev_alloc(&w.e, n));
+  LGBC_TRY(dev_alloc(&w.tsum, tiles));
+  LGBC_TRY(dev_alloc(&w.scal, 1));
+  LGBC_TRY(dev_alloc(&w.p, n));
+  LGBC_TRY(dev_alloc(&w.cdf, n));
+  LGBC_CUDA(cudaMemsetAsync(w.flag, 0, n, g->stream));
+  return LGBC_OK;
+}
+
+unsigned long long read_counter(lgbc_graph* g, int i, int* rc) {
+  unsigned long long v = 0;
+  cudaError_t e = cudaMemcpyAsync(&v, g->learned.counters + i, 8, cudaMemcpyDeviceToHost, g->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+  *rc = e == cudaSuccess ? LGBC_OK : cuda_fail(e, "reading a device counter");
+  return v;
+}
+
+// Core numbers into learned.core: degrees without self-loops, then h-index
+// passes over the flagged vertices until none is lowered.  strict: a
+// self-loop is an error (core_number's ArgumentError).
+int compute_core(lgbc_graph* g, bool strict) {
+  LearnedWorkspace& w = g->learned;
+  const DevGraph dg = g->dev();
+  LGBC_CUDA(cudaMemsetAsync(w.counters, 0, 4 * 8, g->stream));
+  g->launches += core_degree(g->cfg, g->stream, dg, w.core, reinterpret_cast<int*>(w.counters));
+  LGBC_TRY(check_launch(g));
+  int rc = LGBC_OK;
+  const unsigned long long loops = read_counter(g, 0, &rc);
+  LGBC_TRY(rc);
+  if (strict && (loops & 0xffffffffull))
+    return fail(LGBC_EINVAL, "core_number: graph must not have self-loops");
+  const int32_t* list = nullptr;
+  int64_t nlist = g->n;
+  w.core_passes = 0;
+  while (nlist > 0) {
+    g->launches += core_pass(g->cfg, g->stream, dg, list, nlist, w.core, w.flag, w.counters + 1);
+    LGBC_CUDA(cudaMemsetAsync(w.counters + 2, 0, 8, g->stream));
+    g->launches += core_compact(g->cfg, g->stream, g->n, w.flag, w.list, w.counters + 2);
+    LGBC_TRY(check_launch(g));
+    nlist = static_cast<int64_t>(read_counter(g, 2, &rc));
+    LGBC_TRY(rc);
+    list = w.list;
+    // every pass with work lowers some value by at least one; the values
+    // start at the degrees, so more passes than stored entries means a fault
+    if (++w.core_passes > g->nnz + 2) return fail(LGBC_ETIMEOUT, "core iteration did not settle");
+  }
+  return LGBC_OK;
+}
+
+int compute_features(lgbc_graph* g) {
+  LGBC_TRY(ensure_learned(g));
+  LGBC_TRY(compute_core(g, false));
+  g->launches += features(g->cfg, g->stream, g->dev(), g->learned.core, g->learned.feat);
+  return check_launch(g);
+}
+
+int need_undirected(const lgbc_graph* g, const char* what) {
+  if (g->directed) return fail(LGBC_EINVAL, std::string(what) + " covers undirected graphs");
+  return LGBC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lgbc_core_number(lgbc_graph* g, int32_t* core_out) {
+  LGBC_TRY(check_graph(g));
+  std::lock_guard<std::mutex> lock(g->mu);
+  LGBC_TRY(use_device(g));
+  LGBC_TRY(need_undirected(g, "core_number"));
+  if (!core_out && g->n > 0) return fail(LGBC_EINVAL, "null output");
+  reset_stats(g);
+  if (g->n == 0) return LGBC_OK;
+  LGBC_TRY(ensure_learned(g));
+  LGBC_TRY(compute_core(g, true));
+  LGBC_CUDA(cudaMemcpyAsync(core_out, g->learned.core, static_cast<size_t>(g->n) * 4,
+                            cudaMemcpyDeviceToHost, g->stream));
+  LGBC_CUDA(cudaStreamSynchronize(g->stream));
+  g->stats.levels = g->learned.core_passes;
+  finish_stats(g);
+  return LGBC_OK;
+}
+
+int lgbc_features(lgbc_graph* g, float* feat_out) {
+  LGBC_TRY(check_graph(g));
+  std::lock_guard<std::mutex> lock(g->mu);
+  LGBC_TRY(use_device(g));
+  LGBC_TRY(need_undirected(g, "lgbc_features"));
+  if (!feat_out && g->n > 0) return fail(LGBC_EINVAL, "null output");
+  reset_stats(g);
+  if (g->n == 0) return LGBC_OK;
+  LGBC_TRY(compute_features(g));
+  LGBC_CUDA(cudaMemcpyAsync(feat_out, g->learned.feat, static_cast<size_t>(g->n) * 16,
+                            cudaMemcpyDeviceToHost, g->stream));
+  LGBC_CUDA(cudaStreamSynchronize(g->stream));
+  g->stats.levels = g->learned.core_passes;
+  finish_stats(g);
+  return LGBC_OK;
+}
+
+int lgbc_dependency_mass(lgbc_graph* g, const int32_t* src, int64_t nsrc, double* mass_out) {
+  LGBC_TRY(check_graph(g));
+  std::lock_guard<std::mutex> lock(g->mu);
+  LGBC_TRY(use_device(g));
+  LGBC_TRY(check_sources(g, src, nsrc));
+  if (nsrc > 0 && !mass_out) return fail(LGBC_EINVAL, "null output");
+  reset_stats(g);
+  if (nsrc == 0) return LGBC_OK;
+  LGBC_TRY(ensure_ms(g, false));
+  LGBC_TRY(ensure_src(g, nsrc));
+  unsigned long long* d_mass = nullptr;
+  LGBC_TRY(dev_alloc(&d_mass, static_cast<size_t>(nsrc)));
+  std::unique_ptr<unsigned long long, void (*)(unsigned long long*)> guard(
+      d_mass, [](unsigned long long* q) { cudaFree(q); });
+  LGBC_CUDA(cudaMemsetAsync(d_mass, 0, static_cast<size_t>(nsrc) * 8, g->stream));
+  LGBC_CUDA(cudaMemcpyAsync(g->d_src, src, static_cast<size_t>(nsrc) * 4, cudaMemcpyHostToDevice,
+                            g->stream));
+  for (int64_t s0 = 0; s0 < nsrc; s0 += kMaxLanes) {
+    const int nl = static_cast<int>(std::min<int64_t>(kMaxLanes, nsrc - s0));
+    LGBC_TRY(run_ms_batch(g, g->d_src + s0, nl, kSigmaNone, nullptr, nullptr, 0, Seeds(), nullptr,
+                          d_mass + s0));
+    g->stats.batches++;
+  }
+  std::vector<unsigned long long> h(static_cast<size_t>(nsrc));
+  LGBC_CUDA(cudaMemcpyAsync(h.data(), d_mass, static_cast<size_t>(nsrc) * 8, cudaMemcpyDeviceToHost,
+                            g->stream));
+  LGBC_CUDA(cudaStreamSynchronize(g->stream));
+  for (int64_t i = 0; i < nsrc; ++i) mass_out[i] = static_cast<double>(h[static_cast<size_t>(i)]);
+  finish_stats(g);
+  return LGBC_OK;
+}
+
+int lgbc_betweenness_weighted(lgbc_graph* g, const int32_t* src, const double* w, int64_t nsrc,
+                              double* bc_raw_out) {
+  LGBC_TRY(check_graph(g));
+  std::lock_guard<std::mutex> lock(g->mu);
+  LGBC_TRY(use_device(g));
+  if (!bc_raw_out && g->n > 0) return fail(LGBC_EINVAL, "null output");
+  LGBC_TRY(check_sources(g, src, nsrc));
+  if (nsrc > 0 && !w) return fail(LGBC_EINVAL, "null weights");
+  for (int64_t i = 0; i < nsrc; ++i)
+    if (!std::isfinite(w[i])) return fail(LGBC_EINVAL, "non-finite weight");
+  reset_stats(g);
+  if (g->n == 0) return LGBC_OK;
+  // degree-0 sources contribute nothing (betweenness.jl:58); drop them with
+  // their weights
+  std::vector<int32_t> act;
+  std::vector<double> aw;
+  act.reserve(static_cast<size_t>(nsrc));
+  aw.reserve(static_cast<size_t>(nsrc));
+  for (int64_t i = 0; i < nsrc; ++i)
+    if (g->has_degree[static_cast<size_t>(src[i])]) {
+      act.push_back(src[i]);
+      aw.push_back(w[i]);
+    }
+  const int64_t k_act = static_cast<int64_t>(act.size());
+  g->stats.active_sources = k_act;
+  LGBC_TRY(ensure_src(g, k_act));
+  double* d_w = nullptr;
+  LGBC_TRY(dev_alloc(&d_w, static_cast<size_t>(std::max<int64_t>(k_act, 1))));
+  std::unique_ptr<double, void (*)(double*)> guard(d_w, [](double* q) { cudaFree(q); });
+  if (k_act > 0) {
+    LGBC_CUDA(cudaMemcpyAsync(g->d_src, act.data(), static_cast<size_t>(k_act) * 4,
+                              cudaMemcpyHostToDevice, g->stream));
+    LGBC_CUDA(cudaMemcpyAsync(d_w, aw.data(), static_cast<size_t>(k_act) * 8, cudaMemcpyHostToDevice,
+                              g->stream));
+  }
+  if (!g->d_bc) LGBC_TRY(dev_alloc(&g->d_bc, static_cast<size_t>(g->n)));
+  LGBC_TRY(run_betweenness(g, k_act, 0, g->d_bc, d_w));
+  LGBC_CUDA(cudaMemcpyAsync(bc_raw_out, g->d_bc, static_cast<size_t>(g->n) * 8,
+                            cudaMemcpyDeviceToHost, g->stream));
+  LGBC_CUDA(cudaStreamSynchronize(g->stream));
+  finish_stats(g);
+  return LGBC_OK;
+}
+
+int lgbc_proposal_build(lgbc_graph* g, lgbc_mlp* m, double eps, double* p_out) {
+  LGBC_TRY(check_graph(g));
+  std::lock_guard<std::mutex> lock(g->mu);
+  LGBC_TRY(use_device(g));
+  LGBC_TRY(need_undirected(g, "the learned proposal"));
+  if (!(eps >= 0.0 && eps <= 1.0)) return fail(LGBC_EINVAL, "eps must be in [0, 1]");
+  MlpView mv;
+  LGBC_TRY(mlp_view(m, &mv));
+  if (mv.device != g->device) return fail(LGBC_EINVAL, "MLP and graph live on different devices");
+  reset_stats(g);
+  if (g->n == 0) return fail(LGBC_EINVAL, "empty graph");
+  g->learned.built = false;
+  LGBC_TRY(compute_features(g));
+  LearnedWorkspace& w = g->learned;
+  g->launches += mlp_forward(g->cfg, g->stream, w.feat, g->n, mv.P, mv.norm, w.y);
+  g->launches += proposal_build(g->stream, w.y, g->n, eps, w.fscr, w.e, w.tsum, w.scal, w.p, w.cdf);
+  LGBC_TRY(check_launch(g));
+  if (p_out)
+    LGBC_CUDA(cudaMemcpyAsync(p_out, w.p, static_cast<size_t>(g->n) * 8, cudaMemcpyDeviceToHost,
+                              g->stream));
+  LGBC_CUDA(cudaStreamSynchronize(g->stream));
+  w.built = true;
+  g->stats.levels = w.core_passes;
+  finish_stats(g);
+  return LGBC_OK;
+}
+
+int lgbc_proposal_sample(lgbc_graph* g, int64_t k, uint64_t seed, int32_t* src_out, double* w_out) {
+  LGBC_TRY(check_graph(g));
+  std::lock_guard<std::mutex> lock(g->mu);
+  LGBC_TRY(use_device(g));
+  LearnedWorkspace& w = g->learned;
+  if (!w.built) return fail(LGBC_EINVAL, "no proposal built for this graph");
+  if (k < 0 || (k > 0 && (!src_out || !w_out))) return fail(LGBC_EINVAL, "bad sample count or null output");
+  reset_stats(g);
+  if (k == 0) return LGBC_OK;
+  if (k > w.samp_cap) {
+    dev_free(w.samp);
+    dev_free(w.samp_w);
+    w.samp_cap = 0;
+    LGBC_TRY(dev_alloc(&w.samp, static_cast<size_t>(k)));
+    LGBC_TRY(dev_alloc(&w.samp_w, static_cast<size_t>(k)));
+    w.samp_cap = k;
+  }
+  g->launches += proposal_sample(g->stream, w.cdf, w.p, g->n, k, seed, w.samp, w.samp_w);
+  LGBC_TRY(check_launch(g));
+  LGBC_CUDA(cudaMemcpyAsync(src_out, w.samp, static_cast<size_t>(k) * 4, cudaMemcpyDeviceToHost,
+                            g->stream));
+  LGBC_CUDA(cudaMemcpyAsync(w_out, w.samp_w, static_cast<size_t>(k) * 8, cudaMemcpyDeviceToHost,
+                            g->stream));
+  LGBC_CUDA(cudaStreamSynchronize(g->stream));
+  finish_stats(g);
+  return LGBC_OK;
+}
+
+}  // extern "C"

@@ -3,10 +3,14 @@
 // queued, which the API layer counts for lgbc_stats / lgbc_timer_stop.
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
+#include <stddef.h>
 #include <stdint.h>
 
 #include "lgbc_internal.cuh"
+
+struct lgbc_mlp;
 
 namespace lgbc {
 
@@ -36,6 +40,7 @@ struct MsBuffers {
   BatchCtl* ctl;       // control block
   const int32_t* lane_src;      // sources of the batch (device)
   unsigned long long cap;       // entries in qv / qm
+  const double* lane_w;         // 64 lane weights (weighted accumulation) or nullptr
 };
 
 // Vertices with more than hub_degree neighbours ("hubs") are not expanded by
@@ -88,6 +93,11 @@ int ms_backward_level(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, con
                       const HubData& hd, int sigma_kind, double* bc);
 // After the backward sweep: clear the masks of levels 0 and 1.
 int ms_cleanup(const LaunchCfg& c, cudaStream_t s, const MsBuffers& b);
+// After a distance-only forward sweep (before ms_cleanup_all):
+// mass[lane] += sum over the lane's reached vertices t != source of (d - 1),
+// the lane's dependency mass sum_v delta_s(v).
+int ms_level_mass(const LaunchCfg& c, cudaStream_t s, const MsBuffers& b,
+                  unsigned long long* mass);
 // After a distance-only batch: clear visit / masks of every listed vertex.
 int ms_cleanup_all(const LaunchCfg& c, cudaStream_t s, const MsBuffers& b);
 // Zero visit and both mask buffers outright (after an aborted batch).
@@ -128,5 +138,67 @@ int add_endpoints(const LaunchCfg& c, cudaStream_t s, double* bc, int64_t n,
 int add_endpoints_many(const LaunchCfg& c, cudaStream_t s, double* bc, const int64_t* seg_off,
                        const double* seg_add, int64_t nseg, const int32_t* src,
                        const double* src_add, int64_t nsrc);
+
+// ---- learned source proposal: learned.cu ----------------------------------
+// deg[v] = neighbours other than v; *loops |= 1 if v has a self-loop.
+int core_degree(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, int32_t* deg, int* loops);
+// One h-index pass over list[0, nlist) (all vertices when list is null);
+// lowered vertices flag their neighbours; *changed counts the lowered ones.
+int core_pass(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const int32_t* list,
+              int64_t nlist, int32_t* core, uint8_t* flag, unsigned long long* changed);
+// list <- flagged vertices (flags cleared), *count += their number.
+int core_compact(const LaunchCfg& c, cudaStream_t s, int64_t n, uint8_t* flag, int32_t* list,
+                 unsigned long long* count);
+int features(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const int32_t* core,
+             float4* feat);
+
+// MLP parameter layout (floats): W1[64][4], b1[64], W2[64][64], b2[64], W3[64], b3.
+constexpr int kMlpHidden = 64;
+constexpr int kMlpW1 = 0;
+constexpr int kMlpB1 = kMlpW1 + kMlpHidden * 4;
+constexpr int kMlpW2 = kMlpB1 + kMlpHidden;
+constexpr int kMlpB2 = kMlpW2 + kMlpHidden * kMlpHidden;
+constexpr int kMlpW3 = kMlpB2 + kMlpHidden;
+constexpr int kMlpB3 = kMlpW3 + kMlpHidden;
+constexpr int kMlpParams = kMlpB3 + 1;                  // 4545
+constexpr int kMlpParamsPadded = (kMlpParams + 3) & ~3;
+constexpr int kGradRows = 2 * kMlpHidden;               // rows (threads) per gradient block
+static_assert(kMlpParams == 4545, "parameter count");
+
+struct MlpNorm {
+  float mu[4];
+  float isd[4];   // 1 / stdev
+};
+struct AdamStep {
+  float lr, beta1, beta2, eps;
+  float bc1, bc2;  // bias corrections 1 - beta^t
+};
+int mlp_forward(const LaunchCfg& c, cudaStream_t s, const float4* x, int64_t rows,
+                const __nv_bfloat16* P, const MlpNorm& nm, float* y);
+// Opt the gradient kernel into its dynamic shared memory (once per device).
+int mlp_configure();
+// One step on rows [r0, r0 + B): residuals e, block partials part, the loss,
+// the reduced gradient (grad may be null) and, when master is not null, an
+// Adam update of master / Pw / m1 / m2.
+int mlp_train_step(cudaStream_t s, const float4* x, const float* target, int64_t r0, int B,
+                   const __nv_bfloat16* P, const MlpNorm& nm, float* e, float* part, float* loss,
+                   float* grad, float* master, __nv_bfloat16* Pw, float* m1, float* m2,
+                   const AdamStep& st);
+int mlp_to_bf16(cudaStream_t s, const float* master, __nv_bfloat16* P);
+// Weights and standardisation of an MLP handle (mlp.cu), for graph calls.
+struct MlpView {
+  const __nv_bfloat16* P;
+  MlpNorm norm;
+  int device;
+};
+int mlp_view(const lgbc_mlp* m, MlpView* out);
+
+// Proposal scratch: tiles of the scan; fscratch needs tiles + 1 floats, tsum
+// tiles doubles, scal 1 double.
+int64_t proposal_tiles(int64_t n);
+int proposal_build(cudaStream_t s, const float* y, int64_t n, double eps, float* fscratch,
+                   double* e, double* tsum, double* scal, double* p, double* cdf);
+int proposal_sample(cudaStream_t s, const double* cdf, const double* p, int64_t n, int64_t k,
+                    uint64_t seed, int32_t* src, double* w);
 
 }  // namespace lgbc

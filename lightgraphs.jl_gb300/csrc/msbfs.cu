@@ -426,9 +426,27 @@ __device__ __forceinline__ void seg_gather(bool valid, int64_t e0, int deg, uint
   }
 }
 
+// Finalise one lane l of v from its psi sum: delta = sigma * acc,
+// psi[v] = (1 + delta) / sigma; returns delta.
+__device__ __forceinline__ df32 finish_lane_df(const unsigned long long* srow, float2* prow, int l,
+                                               df32 acc) {
+  const df32 sv = df_from_u64(srow[l]);
+  const df32 d = df_mul(sv, acc);
+  const df32 p = df_div(df_add_f(d, 1.0f), sv);
+  prow[l] = make_float2(p.hi, p.lo);
+  return d;
+}
+
+__device__ __forceinline__ double finish_lane_f64(const double* srow, double* prow, int l,
+                                                  double acc) {
+  const double sv = srow[l];
+  const double d = sv * acc;
+  prow[l] = (1.0 + d) / sv;
+  return d;
+}
+
 // Finalise the dependencies of lanes `mine` (bit 0 = lane t, bit 1 = lane
-// t + 32) of v from the psi sums: delta = sigma * acc, psi[v] = (1 + delta) /
-// sigma; returns the lanes' delta sum.
+// t + 32) of v from the psi sums; returns the lanes' delta sum.
 __device__ __forceinline__ df32 finish_df(void* psi, const void* sigma, int32_t v, unsigned mine,
                                           df32 acc0, df32 acc1) {
   const int ln = lane_id();
@@ -437,20 +455,8 @@ __device__ __forceinline__ df32 finish_df(void* psi, const void* sigma, int32_t 
   const unsigned long long* srow =
       reinterpret_cast<const unsigned long long*>(sigma) + static_cast<int64_t>(v) * 64;
   float2* prow = reinterpret_cast<float2*>(psi) + static_cast<int64_t>(v) * 64;
-  if (mine & 1u) {
-    const df32 sv = df_from_u64(srow[ln]);
-    const df32 d = df_mul(sv, acc0);
-    const df32 p = df_div(df_add_f(d, 1.0f), sv);
-    prow[ln] = make_float2(p.hi, p.lo);
-    contrib = d;
-  }
-  if (mine & 2u) {
-    const df32 sv = df_from_u64(srow[32 + ln]);
-    const df32 d = df_mul(sv, acc1);
-    const df32 p = df_div(df_add_f(d, 1.0f), sv);
-    prow[32 + ln] = make_float2(p.hi, p.lo);
-    contrib = df_add(contrib, d);
-  }
+  if (mine & 1u) contrib = finish_lane_df(srow, prow, ln, acc0);
+  if (mine & 2u) contrib = df_add(contrib, finish_lane_df(srow, prow, 32 + ln, acc1));
   return contrib;
 }
 
@@ -461,18 +467,37 @@ __device__ __forceinline__ double finish_f64(void* psi, const void* sigma, int32
   if (!mine) return contrib;
   const double* srow = reinterpret_cast<const double*>(sigma) + static_cast<int64_t>(v) * 64;
   double* prow = reinterpret_cast<double*>(psi) + static_cast<int64_t>(v) * 64;
-  if (mine & 1u) {
-    const double sv = srow[ln];
-    const double d = sv * acc0;
-    prow[ln] = (1.0 + d) / sv;
-    contrib += d;
-  }
-  if (mine & 2u) {
-    const double sv = srow[32 + ln];
-    const double d = sv * acc1;
-    prow[32 + ln] = (1.0 + d) / sv;
-    contrib += d;
-  }
+  if (mine & 1u) contrib += finish_lane_f64(srow, prow, ln, acc0);
+  if (mine & 2u) contrib += finish_lane_f64(srow, prow, 32 + ln, acc1);
+  return contrib;
+}
+
+// Weighted finalisation (importance-sampled estimators): the same psi
+// updates, returning sum over the lanes of w[lane] * delta in FP64.
+__device__ __forceinline__ double finish_df_w(void* psi, const void* sigma, int32_t v,
+                                              unsigned mine, df32 acc0, df32 acc1,
+                                              const double* __restrict__ lw) {
+  const int ln = lane_id();
+  double contrib = 0.0;
+  if (!mine) return contrib;
+  const unsigned long long* srow =
+      reinterpret_cast<const unsigned long long*>(sigma) + static_cast<int64_t>(v) * 64;
+  float2* prow = reinterpret_cast<float2*>(psi) + static_cast<int64_t>(v) * 64;
+  if (mine & 1u) contrib = lw[ln] * df_to_double(finish_lane_df(srow, prow, ln, acc0));
+  if (mine & 2u) contrib += lw[32 + ln] * df_to_double(finish_lane_df(srow, prow, 32 + ln, acc1));
+  return contrib;
+}
+
+__device__ __forceinline__ double finish_f64_w(void* psi, const void* sigma, int32_t v,
+                                               unsigned mine, double acc0, double acc1,
+                                               const double* __restrict__ lw) {
+  const int ln = lane_id();
+  double contrib = 0.0;
+  if (!mine) return contrib;
+  const double* srow = reinterpret_cast<const double*>(sigma) + static_cast<int64_t>(v) * 64;
+  double* prow = reinterpret_cast<double*>(psi) + static_cast<int64_t>(v) * 64;
+  if (mine & 1u) contrib = lw[ln] * finish_lane_f64(srow, prow, ln, acc0);
+  if (mine & 2u) contrib += lw[32 + ln] * finish_lane_f64(srow, prow, 32 + ln, acc1);
   return contrib;
 }
 
@@ -855,13 +880,20 @@ __global__ void __launch_bounds__(256) k_ms_delta(DevGraph g, MsBuffers b, HubDa
     if (SK == kSigmaU64) {
       df32 acc0{0.f, 0.f}, acc1{0.f, 0.f};
       psi_range_df(g.colidx, e0, e1, F, succ, b.psi, hd.dense_edges, acc0, acc1);
-      df32 contrib = finish_df(b.psi, b.sigma, v, mine, acc0, acc1);
-      contrib = warp_sum_df(contrib);
-      if (ln == 0) bc[v] += df_to_double(contrib);
+      if (b.lane_w) {
+        const double contrib =
+            warp_sum_f64(finish_df_w(b.psi, b.sigma, v, mine, acc0, acc1, b.lane_w));
+        if (ln == 0) bc[v] += contrib;
+      } else {
+        df32 contrib = finish_df(b.psi, b.sigma, v, mine, acc0, acc1);
+        contrib = warp_sum_df(contrib);
+        if (ln == 0) bc[v] += df_to_double(contrib);
+      }
     } else {
       double acc0 = 0.0, acc1 = 0.0;
       psi_range_f64(g.colidx, e0, e1, F, succ, b.psi, hd.dense_edges, acc0, acc1);
-      double contrib = finish_f64(b.psi, b.sigma, v, mine, acc0, acc1);
+      double contrib = b.lane_w ? finish_f64_w(b.psi, b.sigma, v, mine, acc0, acc1, b.lane_w)
+                                : finish_f64(b.psi, b.sigma, v, mine, acc0, acc1);
       contrib = warp_sum_f64(contrib);
       if (ln == 0) bc[v] += contrib;
     }
@@ -902,11 +934,18 @@ __global__ void __launch_bounds__(256) k_ms_hub_delta(DevGraph g, MsBuffers b, H
     if (ln == 0) hd.cnt[I.slot] = 0u;
     const unsigned mine = my_bits(F);
     if (SK == kSigmaU64) {
-      df32 contrib = finish_df(b.psi, b.sigma, h, mine, df_from_double(s0), df_from_double(s1));
-      contrib = warp_sum_df(contrib);
-      if (ln == 0) bc[h] += df_to_double(contrib);
+      if (b.lane_w) {
+        const double contrib = warp_sum_f64(finish_df_w(
+            b.psi, b.sigma, h, mine, df_from_double(s0), df_from_double(s1), b.lane_w));
+        if (ln == 0) bc[h] += contrib;
+      } else {
+        df32 contrib = finish_df(b.psi, b.sigma, h, mine, df_from_double(s0), df_from_double(s1));
+        contrib = warp_sum_df(contrib);
+        if (ln == 0) bc[h] += df_to_double(contrib);
+      }
     } else {
-      double contrib = finish_f64(b.psi, b.sigma, h, mine, s0, s1);
+      double contrib = b.lane_w ? finish_f64_w(b.psi, b.sigma, h, mine, s0, s1, b.lane_w)
+                                : finish_f64(b.psi, b.sigma, h, mine, s0, s1);
       contrib = warp_sum_f64(contrib);
       if (ln == 0) bc[h] += contrib;
     }
@@ -1099,6 +1138,49 @@ __global__ void k_ms_cleanup_all(MsBuffers b) {
   }
 }
 
+// Dependency mass of every lane after a forward sweep, from the identity
+//   sum_{v != s} delta_s(v) = sum_{t reachable from s, t != s} (d(s, t) - 1)
+// (delta_s(v) = sum_t sigma_st(v) / sigma_st, and sum_v sigma_st(v) / sigma_st
+// is the number of interior vertices of a shortest s-t path).  Level L >= 1
+// entries add L - 1 to each of their lanes; exact in 64-bit integers.  A warp
+// loads 32 entries, then walks them by broadcast; thread t owns lanes t and
+// t + 32; block sums go to mass[lane] with one atomic per lane per block.
+__global__ void __launch_bounds__(256) k_ms_level_mass(MsBuffers b, unsigned long long* mass) {
+  __shared__ unsigned long long part[64];
+  const int ln = lane_id();
+  if (threadIdx.x < 64) part[threadIdx.x] = 0ull;
+  __syncthreads();
+  const int maxl = b.ctl->maxlevel;
+  const unsigned long long lo = b.lvl_off[1], hi = b.lvl_off[maxl + 1];
+  unsigned long long a0 = 0, a1 = 0;
+  const unsigned long long stride = static_cast<unsigned long long>(nwarps()) * 32;
+  for (unsigned long long base = lo + static_cast<unsigned long long>(gwarp()) * 32; base < hi;
+       base += stride) {
+    const unsigned long long i = base + ln;
+    uint64_t m = 0;
+    int lev = 0;
+    if (i < hi) {
+      m = b.qm[i];
+      int l = 1, r = maxl;  // largest L in [1, maxl] with lvl_off[L] <= i
+      while (l < r) {
+        const int mid = (l + r + 1) >> 1;
+        if (b.lvl_off[mid] <= i) l = mid; else r = mid - 1;
+      }
+      lev = l;
+    }
+    for (int j = 0; j < 32; ++j) {
+      const uint64_t mj = shfl_u64(m, j);
+      const unsigned long long dj = static_cast<unsigned long long>(__shfl_sync(kFull, lev, j) - 1);
+      if ((mj >> ln) & 1ull) a0 += dj;
+      if ((mj >> (32 + ln)) & 1ull) a1 += dj;
+    }
+  }
+  if (a0) atomicAdd(&part[ln], a0);
+  if (a1) atomicAdd(&part[32 + ln], a1);
+  __syncthreads();
+  if (threadIdx.x < 64 && part[threadIdx.x]) atomicAdd(mass + threadIdx.x, part[threadIdx.x]);
+}
+
 // Batch initialisation with explicit seeds: seed i puts vertex seed_v[i] at
 // level 0 of lane seed_lane[i].  Used for disjoint unions of graphs, where a
 // lane may hold one source in every component: BFS trees of different
@@ -1214,8 +1296,11 @@ int ms_topdown(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBu
     k_ms_hub_discover<<<c.grid, c.block, 0, s>>>(g, b, hd);
     ++launches;
   }
-  if (dist) {
-    k_ms_td_settle<kSigmaNone, true><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
+  if (sigma_kind == kSigmaNone) {
+    if (dist)
+      k_ms_td_settle<kSigmaNone, true><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
+    else
+      k_ms_td_settle<kSigmaNone, false><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
   } else if (sigma_kind == kSigmaU64) {
     if (hd.segmented)
       k_ms_td_settle_seg<kSigmaU64><<<c.grid, c.block, 0, s>>>(g, b, hd, act);
@@ -1243,10 +1328,16 @@ int ms_topdown(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBu
 int ms_bottomup(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
                 const HubData& hd, uint64_t act, int sigma_kind, int32_t* dist, int64_t dist_ld) {
   int launches = 1;
-  if (dist) {
-    k_ms_bu<kSigmaNone, true><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
+  if (sigma_kind == kSigmaNone) {
+    if (dist)
+      k_ms_bu<kSigmaNone, true><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
+    else
+      k_ms_bu<kSigmaNone, false><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
     if (hd.n_in > 0) {
-      k_ms_hub_pull<kSigmaNone, true, true><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
+      if (dist)
+        k_ms_hub_pull<kSigmaNone, true, true><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
+      else
+        k_ms_hub_pull<kSigmaNone, false, true><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
       ++launches;
     }
   } else if (sigma_kind == kSigmaU64) {
@@ -1286,8 +1377,10 @@ int ms_backward_level(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, con
                       const HubData& hd, int sigma_kind, double* bc) {
   int launches = 3;
   k_ms_back_clear<<<c.grid, c.block, 0, s>>>(b);
+  // the segmented variant has no weighted finalisation
+  const bool seg = hd.segmented && !b.lane_w;
   if (sigma_kind == kSigmaF64) {
-    if (hd.segmented)
+    if (seg)
       k_ms_delta_seg<kSigmaF64><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
     else
       k_ms_delta<kSigmaF64><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
@@ -1296,7 +1389,7 @@ int ms_backward_level(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, con
       ++launches;
     }
   } else {
-    if (hd.segmented)
+    if (seg)
       k_ms_delta_seg<kSigmaU64><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
     else
       k_ms_delta<kSigmaU64><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
@@ -1311,6 +1404,12 @@ int ms_backward_level(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, con
 
 int ms_cleanup(const LaunchCfg& c, cudaStream_t s, const MsBuffers& b) {
   k_ms_cleanup<<<c.grid, c.block, 0, s>>>(b);
+  return 1;
+}
+
+int ms_level_mass(const LaunchCfg& c, cudaStream_t s, const MsBuffers& b,
+                  unsigned long long* mass) {
+  k_ms_level_mass<<<c.sms * 2, 256, 0, s>>>(b, mass);
   return 1;
 }
 

@@ -13,17 +13,23 @@ CUDA library ``liblgbc.so`` through its C ABI (include/lgbc.h):
     Parallel.gdistances / Parallel.gdistances_
         src/Parallel/traversals/gdistances.jl:36-139
 
+    core_number(g)                                  src/degeneracy.jl:38-80
+    learned.* -- importance-sampled betweenness with a learned source
+        proposal (no counterpart in the reference)
+
 Graphs are ``SimpleGraph`` / ``SimpleDiGraph`` (CSR-backed mirrors of
 LightGraphs' fadjlist storage).  Every computation runs on the GPU; without
 a GPU or without the built library the calls raise ``LGBCError``.
 """
-from . import Parallel
+from . import Parallel, learned
 from ._lib import ArgumentError, BoundsError, LGBCError, MethodError
 from .centrality import (betweenness_centrality, betweenness_centrality_many, betweenness_raw,
                          sample, sample_, _rescale_)
 from .graphs import (DefaultDistance, DeviceGraph, SimpleDiGraph, SimpleGraph, degree,
                      is_directed, ne, nv, vertices, weights)
 from .persistence import loadgraph
+from .learned import (SourceProposal, betweenness_centrality_learned, core_number,
+                      dependency_mass, features)
 from .traversals import gdistances, gdistances_, multi_gdistances
 
 __all__ = [
@@ -31,5 +37,6 @@ __all__ = [
     "betweenness_centrality", "betweenness_centrality_many", "betweenness_raw", "sample", "sample_", "_rescale_",
     "DefaultDistance", "DeviceGraph", "SimpleDiGraph", "SimpleGraph", "degree", "is_directed",
     "ne", "nv", "vertices", "weights", "loadgraph", "gdistances", "gdistances_",
-    "multi_gdistances",
+    "multi_gdistances", "learned", "SourceProposal", "betweenness_centrality_learned",
+    "core_number", "dependency_mass", "features",
 ]

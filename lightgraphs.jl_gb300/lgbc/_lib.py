@@ -60,6 +60,17 @@ class LgbcTuning(ctypes.Structure):
                 ("dense_edges", ctypes.c_int32), ("segment_degree", ctypes.c_int32)]
 
 
+class LgbcTrainCfg(ctypes.Structure):
+    _fields_ = [("steps", ctypes.c_int32), ("batch", ctypes.c_int32), ("warmup", ctypes.c_int32),
+                ("lr", ctypes.c_float), ("lr_final", ctypes.c_float), ("beta1", ctypes.c_float),
+                ("beta2", ctypes.c_float), ("eps", ctypes.c_float), ("seed", ctypes.c_uint64)]
+
+
+MLP_PARAMS = 4545
+MLP_HIDDEN = 64
+MLP_FEATURES = 4
+
+
 def _declare(lib) -> None:
     c_int, i64, p = ctypes.c_int, ctypes.c_int64, ctypes.c_void_p
     pp = ctypes.POINTER(ctypes.c_void_p)
@@ -88,6 +99,21 @@ def _declare(lib) -> None:
         "lgbc_memcpy": ([p, p, i64, c_int], c_int),
         "lgbc_gdistances_noalloc": ([i64, i64, p, p, p, p, p, i64, p, p], c_int),
         "lgbc_betweenness_many": ([i64, p, p, p, p, p, c_int, p], c_int),
+        "lgbc_core_number": ([p, p], c_int),
+        "lgbc_features": ([p, p], c_int),
+        "lgbc_dependency_mass": ([p, p, i64, p], c_int),
+        "lgbc_betweenness_weighted": ([p, p, p, i64, p], c_int),
+        "lgbc_mlp_create": ([pp, ctypes.c_uint64], c_int),
+        "lgbc_mlp_destroy": ([p], c_int),
+        "lgbc_mlp_get_params": ([p, p, p], c_int),
+        "lgbc_mlp_set_params": ([p, p], c_int),
+        "lgbc_mlp_set_norm": ([p, p, p], c_int),
+        "lgbc_mlp_get_norm": ([p, p, p], c_int),
+        "lgbc_mlp_forward": ([p, p, i64, p], c_int),
+        "lgbc_mlp_grad": ([p, p, p, i64, p, p], c_int),
+        "lgbc_mlp_train": ([p, p, p, i64, p, i64, ctypes.POINTER(LgbcTrainCfg), p], c_int),
+        "lgbc_proposal_build": ([p, p, ctypes.c_double, p], c_int),
+        "lgbc_proposal_sample": ([p, i64, ctypes.c_uint64, p, p], c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

@@ -401,4 +401,87 @@ void orc_rescale(double* bc, int64_t n, int normalize, int directed, int64_t k) 
   }
 }
 
+// Per-source dependency mass sum_{v != s} delta_s(v) (the total that
+// _accumulate_basic!, src/centrality/betweenness.jl:81-107, adds to the
+// betweenness vector for source s; 0 for sources of degree 0, :58), and the
+// weighted accumulation sum_i w_i * delta_{s_i}(v) used by importance-sampled
+// estimators.  Either output may be NULL.
+int orc_dependency(int64_t n, const int64_t* rowptr, const int32_t* colidx,
+                   const int64_t* in_rowptr, const int32_t* in_colidx, int directed,
+                   const int32_t* src, const double* w, int64_t nsrc, double* mass_out,
+                   double* bc_weighted_out) {
+  for (int64_t i = 0; i < nsrc; ++i)
+    if (src[i] < 0 || src[i] >= n) return -1;
+  if (directed && (!in_rowptr || !in_colidx)) return -1;
+  Csr out{n, rowptr, colidx};
+  Csr in = directed ? Csr{n, in_rowptr, in_colidx} : out;
+  BfsWork wk;
+  std::vector<double> tmp(n, 0.0);
+  if (bc_weighted_out) std::fill(bc_weighted_out, bc_weighted_out + n, 0.0);
+  for (int64_t i = 0; i < nsrc; ++i) {
+    const int32_t s = src[i];
+    double mass = 0.0;
+    if (degree_of(out, &in, directed, s) > 0) {
+      std::fill(tmp.begin(), tmp.end(), 0.0);
+      brandes_bfs(out, in, s, 0, wk, tmp.data());
+      for (int64_t v = 0; v < n; ++v) {
+        mass += tmp[v];
+        if (bc_weighted_out) bc_weighted_out[v] += (w ? w[i] : 1.0) * tmp[v];
+      }
+    }
+    if (mass_out) mass_out[i] = mass;
+  }
+  return 0;
+}
+
+// core_number(g) for a graph without self-loops: the bin-sort cores
+// decomposition of Batagelj & Zaversnik (2003) as in src/degeneracy.jl:38-80,
+// with degree(g, v) = length(fadjlist[v]) (undirected).  Returns -1 when a
+// self-loop is present (the reference throws ArgumentError, :39).
+int orc_core_number(int64_t n, const int64_t* rowptr, const int32_t* colidx, int32_t* core) {
+  for (int64_t v = 0; v < n; ++v)
+    for (int64_t e = rowptr[v]; e < rowptr[v + 1]; ++e)
+      if (colidx[e] == v) return -1;
+  std::vector<int64_t> deg(n), pos(n), vert(n);
+  int64_t maxdeg = 0;
+  for (int64_t v = 0; v < n; ++v) {
+    deg[v] = rowptr[v + 1] - rowptr[v];
+    maxdeg = std::max(maxdeg, deg[v]);
+  }
+  std::vector<int64_t> bin(maxdeg + 1, 0);
+  for (int64_t v = 0; v < n; ++v) bin[deg[v]]++;
+  int64_t start = 0;
+  for (int64_t d = 0; d <= maxdeg; ++d) {
+    const int64_t num = bin[d];
+    bin[d] = start;
+    start += num;
+  }
+  for (int64_t v = 0; v < n; ++v) {
+    pos[v] = bin[deg[v]];
+    vert[pos[v]] = v;
+    bin[deg[v]]++;
+  }
+  for (int64_t d = maxdeg; d >= 1; --d) bin[d] = bin[d - 1];
+  if (maxdeg >= 0) bin[0] = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    const int64_t v = vert[i];
+    for (int64_t e = rowptr[v]; e < rowptr[v + 1]; ++e) {
+      const int64_t u = colidx[e];
+      if (deg[u] > deg[v]) {
+        const int64_t du = deg[u], pu = pos[u], pw = bin[du], w = vert[pw];
+        if (u != w) {
+          pos[u] = pw;
+          vert[pu] = w;
+          pos[w] = pu;
+          vert[pw] = u;
+        }
+        bin[du]++;
+        deg[u]--;
+      }
+    }
+  }
+  for (int64_t v = 0; v < n; ++v) core[v] = static_cast<int32_t>(deg[v]);
+  return 0;
+}
+
 }  // extern "C"

@@ -66,6 +66,10 @@ def _load():
         lib.orc_betweenness.restype = ctypes.c_int
         lib.orc_rescale.argtypes = [p, i64, ctypes.c_int, ctypes.c_int, i64]
         lib.orc_rescale.restype = None
+        lib.orc_dependency.argtypes = [i64, p, p, p, p, ctypes.c_int, p, p, i64, p, p]
+        lib.orc_dependency.restype = ctypes.c_int
+        lib.orc_core_number.argtypes = [i64, p, p, p]
+        lib.orc_core_number.restype = ctypes.c_int
         _lib = lib
         return lib
 
@@ -151,3 +155,54 @@ def betweenness_centrality(rowptr, colidx, sources=None, *, directed=False, in_r
                           in_colidx=in_colidx, endpoints=endpoints, mode=mode,
                           nthreads=nthreads)
     return rescale(raw, n, normalize, directed, len(src))
+
+
+def dependency(rowptr, colidx, sources, weights=None, *, directed=False, in_rowptr=None,
+               in_colidx=None):
+    """(mass per source, weighted accumulation sum_i w_i delta_{s_i})."""
+    lib = _load()
+    rowptr, colidx = _csr(rowptr, colidx)
+    n = len(rowptr) - 1
+    if directed:
+        in_rowptr, in_colidx = _csr(in_rowptr, in_colidx)
+    else:
+        in_rowptr = in_colidx = None
+    src = np.ascontiguousarray(np.asarray(sources, dtype=np.int32).ravel())
+    w = None if weights is None else np.ascontiguousarray(weights, np.float64)
+    mass = np.empty(len(src), np.float64)
+    bcw = np.empty(n, np.float64)
+    rc = lib.orc_dependency(n, _ptr(rowptr), _ptr(colidx), _ptr(in_rowptr), _ptr(in_colidx),
+                            int(bool(directed)), _ptr(src), _ptr(w), len(src), _ptr(mass), _ptr(bcw))
+    if rc != 0:
+        raise ValueError("oracle dependency: bad arguments")
+    return mass, bcw
+
+
+def core_number(rowptr, colidx) -> np.ndarray:
+    """core_number(g) (src/degeneracy.jl:38-80) of an undirected graph."""
+    lib = _load()
+    rowptr, colidx = _csr(rowptr, colidx)
+    n = len(rowptr) - 1
+    out = np.empty(n, np.int32)
+    if lib.orc_core_number(n, _ptr(rowptr), _ptr(colidx), _ptr(out)) != 0:
+        raise ValueError("core_number: graph must not have self-loops")
+    return out
+
+
+def features(rowptr, colidx) -> np.ndarray:
+    """The four source features of the learned proposal, per vertex:
+    log(1+deg), log(1+core number), mean log(1+deg) of the neighbours, and
+    log(1 + sum of the neighbours' degrees) (a two-hop count estimate)."""
+    rowptr, colidx = _csr(rowptr, colidx)
+    n = len(rowptr) - 1
+    deg = np.diff(rowptr).astype(np.float64)
+    ld = np.log1p(deg)
+    src = np.repeat(np.arange(n), np.diff(rowptr))
+    s_ld = np.bincount(src, weights=ld[colidx], minlength=n)
+    s_d = np.bincount(src, weights=deg[colidx], minlength=n)
+    f = np.empty((n, 4), np.float64)
+    f[:, 0] = ld
+    f[:, 1] = np.log1p(core_number(rowptr, colidx).astype(np.float64))
+    f[:, 2] = np.where(deg > 0, s_ld / np.maximum(deg, 1.0), 0.0)
+    f[:, 3] = np.log1p(s_d)
+    return f
