@@ -176,6 +176,8 @@ WORKLOADS = {
     "c2": "R-MAT scale 20 undirected, sampled BC k=4096",
     "c3": "4096 Barabasi-Albert graphs n~U[200,20000], k=3, exact BC for every graph",
     "c4": "R-MAT scale 22 directed, sampled BC k=16384",
+    "c5": "learned vs uniform source sampling: R-MAT scale 20 copy and a 10^5-vertex BFS ball "
+          "of R-MAT scale 24, k in {1024, 4096, 16384}, 8 seeds",
 }
 
 
@@ -524,6 +526,93 @@ def run_reference_many(args, nthreads: int):
     }), flush=True)
 
 
+def run_c5(args, dist: Dist):
+    """Config C5: train the proposal on 128 R-MAT scale-14 + 128 BA graphs,
+    then compare uniform and learned sampling against exact BC on (a) the
+    R-MAT scale-20 graph and (b) the induced subgraph of a 10^5-vertex BFS
+    ball of R-MAT scale 24 (plus the proposal build and one sampled BC on the
+    whole scale-24 graph, time only)."""
+    import lgbc
+    from lgbc import compare
+    from lgbc import generators as G
+    if dist.rank != 0:
+        return
+    out = {}
+    t = time.perf_counter()
+    train = compare.training_graphs(args.c5_train, args.c5_train, args.c5_train_scale)
+    prop, info = compare.train_default(train, steps=args.c5_steps)
+    info["generate_s"] = time.perf_counter() - t - info["fit_s"]
+    out["training"] = info
+    log(f"trained: {info}")
+    kt = [1024, 4096, 16384]
+    ks_u = [1024, 2048, 4096, 8192, 16384]
+    ks_l = [256, 512, 1024, 2048, 4096, 8192, 16384]
+    evals = {}
+    # (a) R-MAT scale 20, the same graph as the sampled-BC workload
+    g = G.rmat(args.scale, 16, seed=1)
+    ex, ex_ms = compare.exact(g)
+    st = g.device_handle().stats()
+    log(f"exact BC on rmat{args.scale}: {ex_ms / 1e3:.1f} s, {st['active_sources']} active sources")
+    recs, build_ms = compare.run_estimators(g, ex, prop, ks_u, ks_l, seeds=args.c5_seeds)
+    evals[f"rmat{args.scale}"] = dict(n=g.nv(), m=g.ne(), exact_ms=ex_ms,
+                                      **compare.summarise(recs, build_ms, kt))
+    log(json.dumps(evals[f"rmat{args.scale}"]["equal_error"]))
+    g.device_handle().close()
+    del g
+    # (b) BFS ball of R-MAT scale 24 around a random non-isolated vertex
+    if args.c5_ball_scale > 0:
+        t = time.perf_counter()
+        big = G.rmat(args.c5_ball_scale, 16, seed=1)
+        gen_s = time.perf_counter() - t
+        deg = big.degrees()
+        rng = np.random.default_rng(24)
+        cand = np.flatnonzero(deg > 0)
+        center = int(cand[rng.integers(len(cand))])
+        # proposal build and one sampled BC per method on the whole graph (time only)
+        with compare._Timer(big) as tb:
+            prop.build(big, 0.1)
+        src = np.asarray(lgbc.sample(big.vertices(), 1024, rng=np.random.default_rng(3)))
+        with compare._Timer(big) as tu:
+            lgbc.betweenness_centrality(big, src)
+        k_act_u = big.device_handle().stats()["active_sources"]
+        with compare._Timer(big) as tl:
+            lgbc.betweenness_centrality_learned(big, 1024, prop, seed=3, build=False)
+        k_act_l = big.device_handle().stats()["active_sources"]
+        whole = dict(n=big.nv(), m=big.ne(), generate_s=gen_s, proposal_build_ms=tb.ms,
+                     uniform_k1024_ms=tu.ms, uniform_active=k_act_u,
+                     uniform_gteps=k_act_u * big.ne() / (tu.ms * 1e-3) / 1e9,
+                     learned_k1024_ms=tl.ms, learned_active=k_act_l,
+                     learned_gteps=k_act_l * big.ne() / (tl.ms * 1e-3) / 1e9)
+        log(f"rmat{args.c5_ball_scale}: {whole}")
+        sub, _ = compare.bfs_ball(big, center, args.c5_ball)
+        big.device_handle().close()
+        del big
+        ex, ex_ms = compare.exact(sub)
+        recs, build_ms = compare.run_estimators(sub, ex, prop, ks_u, ks_l, seeds=args.c5_seeds)
+        evals[f"rmat{args.c5_ball_scale}_ball{args.c5_ball}"] = dict(
+            n=sub.nv(), m=sub.ne(), center=center, exact_ms=ex_ms, whole_graph=whole,
+            **compare.summarise(recs, build_ms, kt))
+        log(json.dumps(evals[f"rmat{args.c5_ball_scale}_ball{args.c5_ball}"]["equal_error"]))
+    out["evaluations"] = evals
+    main_eval = evals[f"rmat{args.scale}"]
+    head = next(r for r in main_eval["equal_error"] if r["k_uniform"] == 4096)
+    head_sys = next(r for r in main_eval["equal_error_systematic"] if r["k_uniform"] == 4096)
+    print(json.dumps({
+        "metric": "GPU time of learned sampling at uniform sampling's L1 error, relative to uniform",
+        "value": head["time_ratio_with_build"], "unit": "ratio", "n_gpus": 1,
+        "steps": sum(len(e["uniform"]) + len(e["learned"]) + len(e["learned_systematic"])
+                     for e in evals.values()) * args.c5_seeds,
+        "warmup": 0, "ms_per_step": None, "higher_is_better": False, "scaling": "none",
+        "vs_baseline": None, "dtype": "u64 path counts, f64 weighted dependencies; MLP bf16/f32",
+        "data": "synthetic",
+        "config": {"workload": f"learned_vs_uniform_rmat{args.scale}_k4096",
+                   "description": WORKLOADS["c5"], "seeds": args.c5_seeds,
+                   "proposal_eps": 0.1, "sampling": "iid (value); systematic in c5",
+                   "systematic_time_ratio_with_build": head_sys["time_ratio_with_build"]},
+        "c5": out,
+    }), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawTextHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -535,6 +624,12 @@ def main():
     ap.add_argument("--scale", type=int, default=20)
     ap.add_argument("--k", type=int, default=0, help="sampled sources (0 = the workload's)")
     ap.add_argument("--graphs", type=int, default=4096, help="c3: number of graphs")
+    ap.add_argument("--c5-train", type=int, default=128, help="c5: training graphs per family")
+    ap.add_argument("--c5-train-scale", type=int, default=14)
+    ap.add_argument("--c5-steps", type=int, default=3000, help="c5: training steps")
+    ap.add_argument("--c5-seeds", type=int, default=8)
+    ap.add_argument("--c5-ball-scale", type=int, default=24, help="c5: 0 skips the ball graph")
+    ap.add_argument("--c5-ball", type=int, default=100000)
     ap.add_argument("--cpu-seconds", type=float, default=15.0,
                     help="approximate CPU-baseline sample length")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
@@ -545,6 +640,8 @@ def main():
     try:
         if args.impl == "reference":
             run_reference(args, dist)
+        elif args.workload == "c5":
+            run_c5(args, dist)
         else:
             run_ours(args, dist)
     finally:

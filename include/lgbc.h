@@ -169,6 +169,19 @@ typedef struct lgbc_tuning {
 int lgbc_get_tuning(const lgbc_graph *g, lgbc_tuning *out);
 int lgbc_set_tuning(lgbc_graph *g, const lgbc_tuning *t);
 
+/* Autotuner (no counterpart in the reference).  Times Brandes passes over
+ * 128 active sources spread over the vertex ids and picks, by coordinate
+ * descent (two passes; a change must win by 2 %), the degree-bin cut
+ * (hub_degree), the source-batch width (lanes), the direction-switch
+ * thresholds (alpha, beta) and the gather cuts (dense_edges, segment_degree);
+ * the result stays set on the handle (read it with lgbc_get_tuning).  Every
+ * setting gives the same results; only the speed differs.  cache_path (may be
+ * NULL) is a text file of "signature alpha beta hub_degree lanes dense_edges
+ * segment_degree" lines, keyed by n, nnz, directedness and the device's SM
+ * count: a matching line is applied without measuring, and a new result is
+ * appended. */
+int lgbc_tune(lgbc_graph *g, const char *cache_path);
+
 /* gdistances for callers that cannot allocate device memory: no counterpart
  * in the reference.  Some callers cannot call cudaMalloc -- code that runs
  * while a CUDA graph is being captured on its stream, or hosts whose device
@@ -216,6 +229,38 @@ int lgbc_core_number(lgbc_graph *g, int32_t *core_out);
  * the core number is that of the graph without its self-loops. */
 int lgbc_features(lgbc_graph *g, float *feat_out);
 
+/* bfs_parents(g, s; dir) (src/traversals/bfs.jl:35-66): parents_out[v] is
+ * the vertex from which the BFS from s first reaches v -- the smallest
+ * neighbour one level closer, as the reference's sorted levels pick it --
+ * parents_out[s] = s, and -1 where s does not reach (the reference's 0 in
+ * 1-based ids).  dir 0 follows out-edges (:out), 1 in-edges (:in). */
+int lgbc_bfs_parents(lgbc_graph *g, int32_t s, int dir, int32_t *parents_out);
+
+/* has_path(g, u, v; exclude_vertices) (src/traversals/bfs.jl:150-172):
+ * *result = 1 when v is reachable from u along out-edges without entering an
+ * excluded vertex, or u == v; 0 when u or v is excluded or no path exists. */
+int lgbc_has_path(lgbc_graph *g, int32_t u, int32_t v, const int32_t *exclude, int64_t nexclude,
+                  int *result);
+
+/* Stress centrality, unscaled, as stress_centrality(g, vs)
+ * (src/centrality/stress.jl:33-77): for every source of degree > 0 the
+ * reference's integer recursion over its shortest-path DAG, summed, in
+ * wrapping Int64 arithmetic (bit-identical to Julia's, overflow included).
+ * src NULL = every vertex; repeats count repeatedly.  stress_out: n int64. */
+int lgbc_stress(lgbc_graph *g, const int32_t *src, int64_t nsrc, int64_t *stress_out);
+
+/* Per-source BFS distance statistics (unit weights, along out-edges): for
+ * source s_i, reached_out[i] = vertices reachable from s_i including itself,
+ * dsum_out[i] = the sum of their distances, dmax_out[i] = the largest one
+ * (any output may be NULL).  These are the reductions of the distance vector
+ * of dijkstra_shortest_paths(g, s) (src/shortestpaths/dijkstra.jl:59-141)
+ * that closeness_centrality (src/centrality/closeness.jl:33-55),
+ * radiality_centrality (src/centrality/radiality.jl:36-49) and eccentricity
+ * (src/distance.jl:73-79) take; the host finishes each metric from them.
+ * Sources run as bit lanes of the multi-source BFS, 64 per batch. */
+int lgbc_distance_stats(lgbc_graph *g, const int32_t *src, int64_t nsrc, int64_t *reached_out,
+                        int64_t *dsum_out, int32_t *dmax_out);
+
 /* Dependency mass of each source, mass_out[i] = sum_{v != s_i} delta_{s_i}(v):
  * the total that _accumulate_basic! (src/centrality/betweenness.jl:81-107)
  * adds to the betweenness vector for source s_i.  Computed exactly as
@@ -223,8 +268,8 @@ int lgbc_features(lgbc_graph *g, float *feat_out);
 int lgbc_dependency_mass(lgbc_graph *g, const int32_t *src, int64_t nsrc, double *mass_out);
 
 /* Weighted raw betweenness: bc_raw_out[v] = sum_i w[i] delta_{src[i]}(v)
- * (repeats allowed; degree-0 sources contribute nothing).  endpoints=false
- * accumulation only. */
+ * (repeats allowed and merged into one traversal with the summed weight;
+ * degree-0 sources contribute nothing).  endpoints=false accumulation only. */
 int lgbc_betweenness_weighted(lgbc_graph *g, const int32_t *src, const double *w, int64_t nsrc,
                               double *bc_raw_out);
 
@@ -278,9 +323,16 @@ int lgbc_mlp_train(lgbc_mlp *m, const float *x, const float *target, int64_t row
  * CDF (kept in the handle until the next build).  p_out (n doubles, may be
  * NULL) receives p. */
 int lgbc_proposal_build(lgbc_graph *g, lgbc_mlp *m, double eps, double *p_out);
-/* Draw k sources i.i.d. from the built proposal (SplitMix64 stream `seed`)
- * with weights 1 / (k p). */
-int lgbc_proposal_sample(lgbc_graph *g, int64_t k, uint64_t seed, int32_t *src_out,
+/* Draw k sources from the built proposal with weights 1 / (k p), seeded by
+ * `seed` (SplitMix64).  LGBC_SAMPLE_IID: k independent draws.
+ * LGBC_SAMPLE_SYSTEMATIC: systematic sampling on the CDF (draw i at
+ * (i + U) / k, one uniform U), which draws source s floor or ceil of k p_s
+ * times -- k p_s on average, so the weighted estimate stays unbiased -- with
+ * lower variance.  Results come back in draw order (systematic draws in
+ * vertex order). */
+#define LGBC_SAMPLE_IID 0
+#define LGBC_SAMPLE_SYSTEMATIC 1
+int lgbc_proposal_sample(lgbc_graph *g, int64_t k, uint64_t seed, int scheme, int32_t *src_out,
                          double *w_out);
 
 /* Device / pinned-host memory helpers for callers without their own CUDA

@@ -9,6 +9,7 @@
 #include <mutex>
 #include <new>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "lgbc.h"
@@ -469,10 +470,11 @@ struct Seeds {
 };
 
 // lane_w (sigma batches): per-lane weights of the accumulation into bc.
-// mass (distance-only batches): per-lane dependency mass, accumulated.
+// stats (distance-only batches): per-lane distance statistics, accumulated.
 int run_ms_batch(lgbc_graph* g, const int32_t* lane_src, int nl, int sigma_kind, double* bc,
                  int32_t* dist, int64_t dist_ld, const Seeds& seeds = Seeds(),
-                 const double* lane_w = nullptr, unsigned long long* mass = nullptr) {
+                 const double* lane_w = nullptr, const LevelStats* stats = nullptr,
+                 unsigned long long* stress = nullptr) {
   const DevGraph dg = g->dev();
   LGBC_TRY(ensure_hubs(g));
   const HubData hd = hub_data(g);
@@ -524,8 +526,17 @@ int run_ms_batch(lgbc_graph* g, const int32_t* lane_src, int nl, int sigma_kind,
       g->launches += ms_reset_all(g->stream, dg, b);
       return 1;
     }
+    if (sigma_kind == kSigmaNone && stress) {
+      // stress sweep (distance-only forward, integer backward)
+      const int maxl = g->h_ctl->maxlevel;
+      g->launches += ms_begin_backward(g->stream, b);
+      for (int L = maxl; L >= 0; --L)
+        g->launches += st_backward_level(g->cfg, g->stream, dg, b, hd, stress);
+      g->launches += ms_cleanup(g->cfg, g->stream, b);
+      return check_launch(g);
+    }
     if (sigma_kind == kSigmaNone) {
-      if (mass) g->launches += ms_level_mass(g->cfg, g->stream, b, mass);
+      if (stats) g->launches += ms_level_stats(g->cfg, g->stream, b, *stats);
       g->launches += ms_cleanup_all(g->cfg, g->stream, b);
       return check_launch(g);
     }
@@ -743,23 +754,15 @@ int lgbc_graph_info(const lgbc_graph* g, int64_t* n, int64_t* nnz, int* directed
   return LGBC_OK;
 }
 
-int lgbc_gdistances(lgbc_graph* g, const int32_t* src, int64_t nsrc, int32_t* dist_out) {
-  LGBC_TRY(check_graph(g));
-  std::lock_guard<std::mutex> lock(g->mu);
-  LGBC_TRY(use_device(g));
-  if (!dist_out && g->n > 0) return fail(LGBC_EINVAL, "null output");
-  LGBC_TRY(check_sources(g, src, nsrc));
-  reset_stats(g);
-  if (g->n == 0) return LGBC_OK;
-  LGBC_TRY(ensure_bfs(g));
-  LGBC_TRY(ensure_dist(g, g->n));
-  LGBC_TRY(ensure_src(g, nsrc));
-  if (nsrc > 0)
-    LGBC_CUDA(cudaMemcpyAsync(g->d_src, src, static_cast<size_t>(nsrc) * 4, cudaMemcpyHostToDevice,
-                              g->stream));
-  const DevGraph dg = g->dev();
+}  // extern "C"
+
+namespace {
+
+// Level-synchronous BFS over dg from d_src[0, nsrc) into d_dist, which the
+// caller has filled (kUnreached, and any other value on vertices the search
+// must treat as already visited).
+int run_bfs(lgbc_graph* g, const DevGraph& dg, int64_t nsrc) {
   BfsBuffers b{g->bfs.queue, {g->bfs.bm0, g->bfs.bm1}, g->bfs.ctl};
-  g->launches += fill_i32(g->cfg, g->stream, g->d_dist, g->n, kUnreached);
   g->launches += bfs_init(g->cfg, g->stream, dg, b, g->d_src, nsrc, g->d_dist);
   LGBC_TRY(check_launch(g));
   LGBC_TRY(read_ctl(g, b.ctl));
@@ -785,6 +788,35 @@ int lgbc_gdistances(lgbc_graph* g, const int32_t* src, int64_t nsrc, int32_t* di
     g->stats.levels++;
     if (g->stats.levels > g->n + 1) return fail(LGBC_ETIMEOUT, "BFS exceeded n + 1 levels");
   }
+  return LGBC_OK;
+}
+
+// Upload nsrc sources and fill the distance buffer with kUnreached.
+int prepare_bfs(lgbc_graph* g, const int32_t* src, int64_t nsrc) {
+  LGBC_TRY(ensure_bfs(g));
+  LGBC_TRY(ensure_dist(g, g->n));
+  LGBC_TRY(ensure_src(g, nsrc));
+  if (nsrc > 0)
+    LGBC_CUDA(cudaMemcpyAsync(g->d_src, src, static_cast<size_t>(nsrc) * 4, cudaMemcpyHostToDevice,
+                              g->stream));
+  g->launches += fill_i32(g->cfg, g->stream, g->d_dist, g->n, kUnreached);
+  return LGBC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lgbc_gdistances(lgbc_graph* g, const int32_t* src, int64_t nsrc, int32_t* dist_out) {
+  LGBC_TRY(check_graph(g));
+  std::lock_guard<std::mutex> lock(g->mu);
+  LGBC_TRY(use_device(g));
+  if (!dist_out && g->n > 0) return fail(LGBC_EINVAL, "null output");
+  LGBC_TRY(check_sources(g, src, nsrc));
+  reset_stats(g);
+  if (g->n == 0) return LGBC_OK;
+  LGBC_TRY(prepare_bfs(g, src, nsrc));
+  LGBC_TRY(run_bfs(g, g->dev(), nsrc));
   LGBC_CUDA(cudaMemcpyAsync(dist_out, g->d_dist, static_cast<size_t>(g->n) * 4,
                             cudaMemcpyDeviceToHost, g->stream));
   LGBC_CUDA(cudaStreamSynchronize(g->stream));
@@ -1215,6 +1247,42 @@ int compute_features(lgbc_graph* g) {
   return check_launch(g);
 }
 
+// Per-source distance statistics over the multi-source BFS (no path counts):
+// vertices reached at levels >= 1, the sum and the maximum of their levels.
+int distance_stats(lgbc_graph* g, const int32_t* src, int64_t nsrc,
+                   std::vector<unsigned long long>* cnt, std::vector<unsigned long long>* dsum,
+                   std::vector<int>* dmax) {
+  cnt->assign(static_cast<size_t>(nsrc), 0ull);
+  dsum->assign(static_cast<size_t>(nsrc), 0ull);
+  dmax->assign(static_cast<size_t>(nsrc), 0);
+  if (nsrc == 0) return LGBC_OK;
+  LGBC_TRY(ensure_ms(g, false));
+  LGBC_TRY(ensure_src(g, nsrc));
+  unsigned long long* buf = nullptr;  // cnt | dsum | dmax (as int)
+  LGBC_TRY(dev_alloc(&buf, static_cast<size_t>(nsrc) * 3));
+  std::unique_ptr<unsigned long long, void (*)(unsigned long long*)> guard(
+      buf, [](unsigned long long* q) { cudaFree(q); });
+  LGBC_CUDA(cudaMemsetAsync(buf, 0, static_cast<size_t>(nsrc) * 24, g->stream));
+  LGBC_CUDA(cudaMemcpyAsync(g->d_src, src, static_cast<size_t>(nsrc) * 4, cudaMemcpyHostToDevice,
+                            g->stream));
+  int* dm = reinterpret_cast<int*>(buf + 2 * nsrc);
+  for (int64_t s0 = 0; s0 < nsrc; s0 += kMaxLanes) {
+    const int nl = static_cast<int>(std::min<int64_t>(kMaxLanes, nsrc - s0));
+    const LevelStats st{buf + s0, buf + nsrc + s0, dm + s0};
+    LGBC_TRY(run_ms_batch(g, g->d_src + s0, nl, kSigmaNone, nullptr, nullptr, 0, Seeds(), nullptr,
+                          &st));
+    g->stats.batches++;
+  }
+  LGBC_CUDA(cudaMemcpyAsync(cnt->data(), buf, static_cast<size_t>(nsrc) * 8, cudaMemcpyDeviceToHost,
+                            g->stream));
+  LGBC_CUDA(cudaMemcpyAsync(dsum->data(), buf + nsrc, static_cast<size_t>(nsrc) * 8,
+                            cudaMemcpyDeviceToHost, g->stream));
+  LGBC_CUDA(cudaMemcpyAsync(dmax->data(), dm, static_cast<size_t>(nsrc) * 4, cudaMemcpyDeviceToHost,
+                            g->stream));
+  LGBC_CUDA(cudaStreamSynchronize(g->stream));
+  return LGBC_OK;
+}
+
 int need_undirected(const lgbc_graph* g, const char* what) {
   if (g->directed) return fail(LGBC_EINVAL, std::string(what) + " covers undirected graphs");
   return LGBC_OK;
@@ -1259,6 +1327,26 @@ int lgbc_features(lgbc_graph* g, float* feat_out) {
   return LGBC_OK;
 }
 
+int lgbc_distance_stats(lgbc_graph* g, const int32_t* src, int64_t nsrc, int64_t* reached_out,
+                        int64_t* dsum_out, int32_t* dmax_out) {
+  LGBC_TRY(check_graph(g));
+  std::lock_guard<std::mutex> lock(g->mu);
+  LGBC_TRY(use_device(g));
+  LGBC_TRY(check_sources(g, src, nsrc));
+  reset_stats(g);
+  std::vector<unsigned long long> cnt, dsum;
+  std::vector<int> dmax;
+  LGBC_TRY(distance_stats(g, src, nsrc, &cnt, &dsum, &dmax));
+  for (int64_t i = 0; i < nsrc; ++i) {
+    const size_t k = static_cast<size_t>(i);
+    if (reached_out) reached_out[i] = static_cast<int64_t>(cnt[k]) + 1;
+    if (dsum_out) dsum_out[i] = static_cast<int64_t>(dsum[k]);
+    if (dmax_out) dmax_out[i] = dmax[k];
+  }
+  finish_stats(g);
+  return LGBC_OK;
+}
+
 int lgbc_dependency_mass(lgbc_graph* g, const int32_t* src, int64_t nsrc, double* mass_out) {
   LGBC_TRY(check_graph(g));
   std::lock_guard<std::mutex> lock(g->mu);
@@ -1266,27 +1354,12 @@ int lgbc_dependency_mass(lgbc_graph* g, const int32_t* src, int64_t nsrc, double
   LGBC_TRY(check_sources(g, src, nsrc));
   if (nsrc > 0 && !mass_out) return fail(LGBC_EINVAL, "null output");
   reset_stats(g);
-  if (nsrc == 0) return LGBC_OK;
-  LGBC_TRY(ensure_ms(g, false));
-  LGBC_TRY(ensure_src(g, nsrc));
-  unsigned long long* d_mass = nullptr;
-  LGBC_TRY(dev_alloc(&d_mass, static_cast<size_t>(nsrc)));
-  std::unique_ptr<unsigned long long, void (*)(unsigned long long*)> guard(
-      d_mass, [](unsigned long long* q) { cudaFree(q); });
-  LGBC_CUDA(cudaMemsetAsync(d_mass, 0, static_cast<size_t>(nsrc) * 8, g->stream));
-  LGBC_CUDA(cudaMemcpyAsync(g->d_src, src, static_cast<size_t>(nsrc) * 4, cudaMemcpyHostToDevice,
-                            g->stream));
-  for (int64_t s0 = 0; s0 < nsrc; s0 += kMaxLanes) {
-    const int nl = static_cast<int>(std::min<int64_t>(kMaxLanes, nsrc - s0));
-    LGBC_TRY(run_ms_batch(g, g->d_src + s0, nl, kSigmaNone, nullptr, nullptr, 0, Seeds(), nullptr,
-                          d_mass + s0));
-    g->stats.batches++;
-  }
-  std::vector<unsigned long long> h(static_cast<size_t>(nsrc));
-  LGBC_CUDA(cudaMemcpyAsync(h.data(), d_mass, static_cast<size_t>(nsrc) * 8, cudaMemcpyDeviceToHost,
-                            g->stream));
-  LGBC_CUDA(cudaStreamSynchronize(g->stream));
-  for (int64_t i = 0; i < nsrc; ++i) mass_out[i] = static_cast<double>(h[static_cast<size_t>(i)]);
+  std::vector<unsigned long long> cnt, dsum;
+  std::vector<int> dmax;
+  LGBC_TRY(distance_stats(g, src, nsrc, &cnt, &dsum, &dmax));
+  // sum over reached t != s of (d - 1)
+  for (int64_t i = 0; i < nsrc; ++i)
+    mass_out[i] = static_cast<double>(dsum[static_cast<size_t>(i)] - cnt[static_cast<size_t>(i)]);
   finish_stats(g);
   return LGBC_OK;
 }
@@ -1303,17 +1376,30 @@ int lgbc_betweenness_weighted(lgbc_graph* g, const int32_t* src, const double* w
     if (!std::isfinite(w[i])) return fail(LGBC_EINVAL, "non-finite weight");
   reset_stats(g);
   if (g->n == 0) return LGBC_OK;
-  // degree-0 sources contribute nothing (betweenness.jl:58); drop them with
-  // their weights
+  // degree-0 sources contribute nothing (betweenness.jl:58): drop them with
+  // their weights.  Repeats of a source are merged into one lane carrying the
+  // summed weight (sum_i w_i delta_{s_i} is unchanged; a sample drawn with
+  // replacement repeats its likeliest sources).
+  std::vector<std::pair<int32_t, double>> sw;
+  sw.reserve(static_cast<size_t>(nsrc));
+  for (int64_t i = 0; i < nsrc; ++i)
+    if (g->has_degree[static_cast<size_t>(src[i])]) sw.emplace_back(src[i], w[i]);
+  std::stable_sort(sw.begin(), sw.end(),
+                   [](const std::pair<int32_t, double>& a, const std::pair<int32_t, double>& b) {
+                     return a.first < b.first;
+                   });
   std::vector<int32_t> act;
   std::vector<double> aw;
-  act.reserve(static_cast<size_t>(nsrc));
-  aw.reserve(static_cast<size_t>(nsrc));
-  for (int64_t i = 0; i < nsrc; ++i)
-    if (g->has_degree[static_cast<size_t>(src[i])]) {
-      act.push_back(src[i]);
-      aw.push_back(w[i]);
+  act.reserve(sw.size());
+  aw.reserve(sw.size());
+  for (const auto& e : sw) {
+    if (!act.empty() && act.back() == e.first) {
+      aw.back() += e.second;
+    } else {
+      act.push_back(e.first);
+      aw.push_back(e.second);
     }
+  }
   const int64_t k_act = static_cast<int64_t>(act.size());
   g->stats.active_sources = k_act;
   LGBC_TRY(ensure_src(g, k_act));
@@ -1362,13 +1448,16 @@ int lgbc_proposal_build(lgbc_graph* g, lgbc_mlp* m, double eps, double* p_out) {
   return LGBC_OK;
 }
 
-int lgbc_proposal_sample(lgbc_graph* g, int64_t k, uint64_t seed, int32_t* src_out, double* w_out) {
+int lgbc_proposal_sample(lgbc_graph* g, int64_t k, uint64_t seed, int scheme, int32_t* src_out,
+                         double* w_out) {
   LGBC_TRY(check_graph(g));
   std::lock_guard<std::mutex> lock(g->mu);
   LGBC_TRY(use_device(g));
   LearnedWorkspace& w = g->learned;
   if (!w.built) return fail(LGBC_EINVAL, "no proposal built for this graph");
   if (k < 0 || (k > 0 && (!src_out || !w_out))) return fail(LGBC_EINVAL, "bad sample count or null output");
+  if (scheme != LGBC_SAMPLE_IID && scheme != LGBC_SAMPLE_SYSTEMATIC)
+    return fail(LGBC_EINVAL, "unknown sampling scheme");
   reset_stats(g);
   if (k == 0) return LGBC_OK;
   if (k > w.samp_cap) {
@@ -1379,7 +1468,8 @@ int lgbc_proposal_sample(lgbc_graph* g, int64_t k, uint64_t seed, int32_t* src_o
     LGBC_TRY(dev_alloc(&w.samp_w, static_cast<size_t>(k)));
     w.samp_cap = k;
   }
-  g->launches += proposal_sample(g->stream, w.cdf, w.p, g->n, k, seed, w.samp, w.samp_w);
+  g->launches += proposal_sample(g->stream, w.cdf, w.p, g->n, k, seed,
+                                 scheme == LGBC_SAMPLE_SYSTEMATIC, w.samp, w.samp_w);
   LGBC_TRY(check_launch(g));
   LGBC_CUDA(cudaMemcpyAsync(src_out, w.samp, static_cast<size_t>(k) * 4, cudaMemcpyDeviceToHost,
                             g->stream));
@@ -1391,3 +1481,235 @@ int lgbc_proposal_sample(lgbc_graph* g, int64_t k, uint64_t seed, int32_t* src_o
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Autotuner
+// ---------------------------------------------------------------------------
+namespace {
+
+// Identifies a graph shape and device for the tuning cache.
+std::string tune_signature(const lgbc_graph* g) {
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, g->device) != cudaSuccess) prop.multiProcessorCount = 0;
+  char buf[256];
+  std::snprintf(buf, sizeof buf, "n=%lld,nnz=%lld,dir=%d,sms=%d", static_cast<long long>(g->n),
+                static_cast<long long>(g->nnz), g->directed, prop.multiProcessorCount);
+  return buf;
+}
+
+bool tune_from_cache(const char* path, const std::string& sig, lgbc_tuning* out) {
+  if (!path) return false;
+  FILE* f = std::fopen(path, "r");
+  if (!f) return false;
+  char line[512];
+  bool found = false;
+  while (std::fgets(line, sizeof line, f)) {
+    char key[256];
+    lgbc_tuning t{};
+    if (std::sscanf(line, "%255s %lf %lf %d %d %d %d", key, &t.alpha, &t.beta, &t.hub_degree,
+                    &t.lanes, &t.dense_edges, &t.segment_degree) == 7 &&
+        sig == key && t.alpha > 0 && t.beta > 0 && t.lanes >= 1 && t.lanes <= kMaxLanes &&
+        t.hub_degree >= 1 && t.dense_edges >= 0 && t.segment_degree >= 0) {
+      *out = t;  // the last matching line wins
+      found = true;
+    }
+  }
+  std::fclose(f);
+  return found;
+}
+
+// Milliseconds of one Brandes pass over the k sources already in d_src with
+// tuning t (best of `reps`, after one unmeasured pass).
+int tune_measure(lgbc_graph* g, const lgbc_tuning& t, int64_t k, double* bc_dev, int reps,
+                 double* ms_out) {
+  g->tune = t;
+  LGBC_TRY(ensure_hubs(g));
+  double best = 1e300;
+  for (int r = 0; r <= reps; ++r) {
+    LGBC_CUDA(cudaEventRecord(g->ev_start, g->stream));
+    LGBC_TRY(run_betweenness(g, k, 0, bc_dev));
+    LGBC_CUDA(cudaEventRecord(g->ev_stop, g->stream));
+    LGBC_CUDA(cudaEventSynchronize(g->ev_stop));
+    float ms = 0.f;
+    LGBC_CUDA(cudaEventElapsedTime(&ms, g->ev_start, g->ev_stop));
+    if (r > 0) best = std::min(best, static_cast<double>(ms));
+  }
+  *ms_out = best;
+  return LGBC_OK;
+}
+
+}  // namespace
+
+extern "C" int lgbc_tune(lgbc_graph* g, const char* cache_path) {
+  LGBC_TRY(check_graph(g));
+  std::lock_guard<std::mutex> lock(g->mu);
+  LGBC_TRY(use_device(g));
+  reset_stats(g);
+  const std::string sig = tune_signature(g);
+  lgbc_tuning cached{};
+  if (tune_from_cache(cache_path, sig, &cached)) {
+    g->tune = cached;
+    return LGBC_OK;
+  }
+  // sample: 128 active sources spread evenly over the vertex ids
+  std::vector<int32_t> act;
+  for (int64_t v = 0; v < g->n; ++v)
+    if (g->has_degree[static_cast<size_t>(v)]) act.push_back(static_cast<int32_t>(v));
+  if (act.empty()) return LGBC_OK;  // nothing to traverse: keep the defaults
+  const int64_t k = std::min<int64_t>(128, static_cast<int64_t>(act.size()));
+  std::vector<int32_t> sample(static_cast<size_t>(k));
+  for (int64_t i = 0; i < k; ++i)
+    sample[static_cast<size_t>(i)] = act[static_cast<size_t>(i * static_cast<int64_t>(act.size()) / k)];
+  LGBC_TRY(ensure_src(g, k));
+  LGBC_CUDA(cudaMemcpyAsync(g->d_src, sample.data(), static_cast<size_t>(k) * 4,
+                            cudaMemcpyHostToDevice, g->stream));
+  LGBC_CUDA(cudaStreamSynchronize(g->stream));
+  LGBC_TRY(ensure_ms(g, true));
+  if (!g->d_bc) LGBC_TRY(dev_alloc(&g->d_bc, static_cast<size_t>(g->n)));
+  // coordinate descent over the degree-bin cut, the batch width, the
+  // direction-switch thresholds and the two gather-strategy cuts
+  lgbc_tuning best = g->tune;
+  double best_ms = 0.0;
+  LGBC_TRY(tune_measure(g, best, k, g->d_bc, 2, &best_ms));
+  const int reps = 2;
+  for (int pass = 0; pass < 2; ++pass) {
+    auto try_field = [&](auto setter, const auto& values) -> int {
+      for (const auto& val : values) {
+        lgbc_tuning c = best;
+        setter(c, val);
+        if (std::memcmp(&c, &best, sizeof c) == 0) continue;
+        double ms = 0.0;
+        LGBC_TRY(tune_measure(g, c, k, g->d_bc, reps, &ms));
+        if (ms < best_ms * 0.98) {  // a change must win by 2 %
+          best = c;
+          best_ms = ms;
+        }
+      }
+      return LGBC_OK;
+    };
+    const int hubs[] = {64, 128, 256, 512, 1024, 4096, INT32_MAX};
+    const int lanes[] = {32, 48, 64};
+    const double alphas[] = {2.0, 4.0, 8.0, 14.0, 24.0, 48.0};
+    const double betas[] = {6.0, 12.0, 24.0, 48.0, 96.0};
+    const int dense[] = {4, 8, 16, 32};
+    const int segs[] = {0, 1 << 30};
+    LGBC_TRY(try_field([](lgbc_tuning& c, int v) { c.hub_degree = v; }, hubs));
+    LGBC_TRY(try_field([](lgbc_tuning& c, int v) { c.lanes = v; }, lanes));
+    LGBC_TRY(try_field([](lgbc_tuning& c, double v) { c.alpha = v; }, alphas));
+    LGBC_TRY(try_field([](lgbc_tuning& c, double v) { c.beta = v; }, betas));
+    LGBC_TRY(try_field([](lgbc_tuning& c, int v) { c.dense_edges = v; }, dense));
+    LGBC_TRY(try_field([](lgbc_tuning& c, int v) { c.segment_degree = v; }, segs));
+  }
+  g->tune = best;
+  LGBC_TRY(ensure_hubs(g));
+  if (cache_path) {
+    FILE* f = std::fopen(cache_path, "a");
+    if (!f) return fail(LGBC_EINVAL, std::string("cannot append to tuning cache ") + cache_path);
+    std::fprintf(f, "%s %.17g %.17g %d %d %d %d\n", sig.c_str(), best.alpha, best.beta,
+                 best.hub_degree, best.lanes, best.dense_edges, best.segment_degree);
+    std::fclose(f);
+  }
+  finish_stats(g);
+  return LGBC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Stress centrality
+// ---------------------------------------------------------------------------
+extern "C" int lgbc_stress(lgbc_graph* g, const int32_t* src, int64_t nsrc, int64_t* stress_out) {
+  LGBC_TRY(check_graph(g));
+  std::lock_guard<std::mutex> lock(g->mu);
+  LGBC_TRY(use_device(g));
+  if (!stress_out && g->n > 0) return fail(LGBC_EINVAL, "null output");
+  reset_stats(g);
+  int64_t k_act = 0;
+  LGBC_TRY(prepare_sources(g, src, nsrc, &k_act));
+  g->stats.active_sources = k_act;
+  if (g->n == 0) return LGBC_OK;
+  unsigned long long* d_st = nullptr;
+  LGBC_TRY(dev_alloc(&d_st, static_cast<size_t>(g->n)));
+  std::unique_ptr<unsigned long long, void (*)(unsigned long long*)> guard(
+      d_st, [](unsigned long long* q) { cudaFree(q); });
+  LGBC_CUDA(cudaMemsetAsync(d_st, 0, static_cast<size_t>(g->n) * 8, g->stream));
+  if (k_act > 0) LGBC_TRY(ensure_ms(g, true));  // the path-count rows hold E
+  for (int64_t s0 = 0; s0 < k_act; s0 += kMaxLanes) {
+    const int nl = static_cast<int>(std::min<int64_t>(kMaxLanes, k_act - s0));
+    LGBC_TRY(run_ms_batch(g, g->d_src + s0, nl, kSigmaNone, nullptr, nullptr, 0, Seeds(), nullptr,
+                          nullptr, d_st));
+    g->stats.batches++;
+  }
+  LGBC_CUDA(cudaMemcpyAsync(stress_out, d_st, static_cast<size_t>(g->n) * 8, cudaMemcpyDeviceToHost,
+                            g->stream));
+  LGBC_CUDA(cudaStreamSynchronize(g->stream));
+  finish_stats(g);
+  return LGBC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// BFS parents and reachability
+// ---------------------------------------------------------------------------
+extern "C" int lgbc_bfs_parents(lgbc_graph* g, int32_t s, int dir, int32_t* parents_out) {
+  LGBC_TRY(check_graph(g));
+  std::lock_guard<std::mutex> lock(g->mu);
+  LGBC_TRY(use_device(g));
+  if (dir != 0 && dir != 1) return fail(LGBC_EINVAL, "dir must be 0 (out) or 1 (in)");
+  if (!parents_out && g->n > 0) return fail(LGBC_EINVAL, "null output");
+  LGBC_TRY(check_sources(g, &s, 1));
+  reset_stats(g);
+  DevGraph dg = g->dev();
+  if (dir == 1) {  // follow in-edges: swap the two CSRs
+    std::swap(dg.rowptr, dg.in_rowptr);
+    std::swap(dg.colidx, dg.in_colidx);
+  }
+  LGBC_TRY(prepare_bfs(g, &s, 1));
+  LGBC_TRY(run_bfs(g, dg, 1));
+  int32_t* d_par = nullptr;
+  LGBC_TRY(dev_alloc(&d_par, static_cast<size_t>(g->n)));
+  std::unique_ptr<int32_t, void (*)(int32_t*)> guard(d_par, [](int32_t* q) { cudaFree(q); });
+  g->launches += bfs_parents(g->cfg, g->stream, dg, g->d_dist, d_par);
+  LGBC_TRY(check_launch(g));
+  LGBC_CUDA(cudaMemcpyAsync(parents_out, d_par, static_cast<size_t>(g->n) * 4,
+                            cudaMemcpyDeviceToHost, g->stream));
+  LGBC_CUDA(cudaStreamSynchronize(g->stream));
+  finish_stats(g);
+  return LGBC_OK;
+}
+
+extern "C" int lgbc_has_path(lgbc_graph* g, int32_t u, int32_t v, const int32_t* exclude,
+                             int64_t nexclude, int* result) {
+  LGBC_TRY(check_graph(g));
+  std::lock_guard<std::mutex> lock(g->mu);
+  LGBC_TRY(use_device(g));
+  if (!result) return fail(LGBC_EINVAL, "null output");
+  LGBC_TRY(check_sources(g, &u, 1));
+  LGBC_TRY(check_sources(g, &v, 1));
+  LGBC_TRY(check_sources(g, exclude, nexclude));
+  reset_stats(g);
+  for (int64_t i = 0; i < nexclude; ++i)
+    if (exclude[i] == u || exclude[i] == v) {
+      *result = 0;
+      return LGBC_OK;
+    }
+  if (u == v) {
+    *result = 1;
+    return LGBC_OK;
+  }
+  LGBC_TRY(prepare_bfs(g, &u, 1));
+  int32_t* d_ex = nullptr;
+  if (nexclude > 0) {
+    // excluded vertices count as visited from the start (a distance the BFS
+    // never writes), so the search neither claims nor expands them
+    LGBC_TRY(dev_alloc(&d_ex, static_cast<size_t>(nexclude)));
+    LGBC_CUDA(cudaMemcpyAsync(d_ex, exclude, static_cast<size_t>(nexclude) * 4,
+                              cudaMemcpyHostToDevice, g->stream));
+    g->launches += scatter_i32(g->cfg, g->stream, g->d_dist, d_ex, nexclude, -2);
+  }
+  std::unique_ptr<int32_t, void (*)(int32_t*)> guard(d_ex, [](int32_t* q) { if (q) cudaFree(q); });
+  LGBC_TRY(run_bfs(g, g->dev(), 1));
+  int32_t dv = kUnreached;
+  LGBC_CUDA(cudaMemcpyAsync(&dv, g->d_dist + v, 4, cudaMemcpyDeviceToHost, g->stream));
+  LGBC_CUDA(cudaStreamSynchronize(g->stream));
+  *result = dv != kUnreached ? 1 : 0;
+  finish_stats(g);
+  return LGBC_OK;
+}

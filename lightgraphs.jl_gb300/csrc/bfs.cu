@@ -185,6 +185,47 @@ __global__ void k_bfs_advance(BatchCtl* c) {
   c->mf = 0;
 }
 
+// _bfs_parents (src/traversals/bfs.jl:40-66) visits each level in sorted
+// vertex order and gives a newly reached vertex the first level vertex that
+// lists it, i.e. the smallest in-neighbour one level closer; the source is
+// its own parent, unreached vertices get -1 (0 in 1-based ids).  One warp
+// per vertex scans its in-list (sorted ascending) for the first neighbour at
+// distance d - 1.
+__global__ void __launch_bounds__(256) k_bfs_parents(DevGraph g, const int32_t* dist,
+                                                     int32_t* parents) {
+  const int ln = lane_id();
+  for (long long v = gwarp(); v < g.n; v += nwarps()) {
+    const int32_t d = dist[v];
+    if (d == kUnreached || d <= 0) {
+      if (ln == 0) parents[v] = d == 0 ? static_cast<int32_t>(v) : -1;
+      continue;
+    }
+    const int64_t e0 = g.in_rowptr[v], e1 = g.in_rowptr[v + 1];
+    int32_t p = -1;
+    for (int64_t e = e0; e < e1; e += kWarp) {
+      const int64_t idx = e + ln;
+      int32_t u = 0;
+      bool hit = false;
+      if (idx < e1) {
+        u = g.in_colidx[idx];
+        hit = dist[u] == d - 1;
+      }
+      const unsigned bal = __ballot_sync(kFull, hit);
+      if (bal) {
+        p = __shfl_sync(kFull, u, __ffs(bal) - 1);
+        break;
+      }
+    }
+    if (ln == 0) parents[v] = p;
+  }
+}
+
+__global__ void k_scatter_i32(int32_t* p, const int32_t* idx, int64_t count, int32_t value) {
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < count;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    p[idx[i]] = value;
+}
+
 }  // namespace
 
 int bfs_configure(size_t max_dyn_smem) {
@@ -227,6 +268,19 @@ int bfs_bottomup(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const Bf
   } else {
     k_bfs_bu<false><<<c.grid, c.block, 0, s>>>(g, b, dist);
   }
+  return 1;
+}
+
+int bfs_parents(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const int32_t* dist,
+                int32_t* parents) {
+  k_bfs_parents<<<c.grid, c.block, 0, s>>>(g, dist, parents);
+  return 1;
+}
+
+int scatter_i32(const LaunchCfg& c, cudaStream_t s, int32_t* p, const int32_t* idx, int64_t count,
+                int32_t value) {
+  if (count <= 0) return 0;
+  k_scatter_i32<<<c.grid, c.block, 0, s>>>(p, idx, count, value);
   return 1;
 }
 

@@ -529,14 +529,23 @@ __device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
   return x ^ (x >> 31);
 }
 
-// Sample i: u uniform in [0, cdf[n - 1]) from SplitMix64(seed, i); the
-// vertex is the first index with cdf > u; weight 1 / (k p).
+// Sample i: u in [0, cdf[n - 1]); the vertex is the first index with
+// cdf > u; weight 1 / (k p).  Independent draws take u from SplitMix64(seed,
+// i); systematic draws take u = (i + U) / k of the total with one U from the
+// seed, so vertex s is drawn floor or ceil of k p_s times (Madow 1949), still
+// k p_s on average, which keeps the weighted sum unbiased.
 __global__ void k_sample(const double* cdf, const double* p, int64_t n, int64_t k, uint64_t seed,
-                         int32_t* src, double* w) {
+                         bool systematic, int32_t* src, double* w) {
   const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= k) return;
-  const uint64_t r = splitmix64(seed ^ splitmix64(static_cast<uint64_t>(i)));
-  const double u = static_cast<double>(r >> 11) * 0x1.0p-53 * cdf[n - 1];
+  double u;
+  if (systematic) {
+    const double U = static_cast<double>(splitmix64(seed ^ 0x5851F42D4C957F2Dull) >> 11) * 0x1.0p-53;
+    u = fmin((static_cast<double>(i) + U) / static_cast<double>(k), 1.0 - 0x1.0p-53) * cdf[n - 1];
+  } else {
+    const uint64_t r = splitmix64(seed ^ splitmix64(static_cast<uint64_t>(i)));
+    u = static_cast<double>(r >> 11) * 0x1.0p-53 * cdf[n - 1];
+  }
   int64_t lo = 0, hi = n - 1;
   while (lo < hi) {
     const int64_t mid = (lo + hi) >> 1;
@@ -628,9 +637,10 @@ int proposal_build(cudaStream_t s, const float* y, int64_t n, double eps, float*
 }
 
 int proposal_sample(cudaStream_t s, const double* cdf, const double* p, int64_t n, int64_t k,
-                    uint64_t seed, int32_t* src, double* w) {
+                    uint64_t seed, bool systematic, int32_t* src, double* w) {
   if (k <= 0) return 0;
-  k_sample<<<static_cast<unsigned>((k + 255) / 256), 256, 0, s>>>(cdf, p, n, k, seed, src, w);
+  k_sample<<<static_cast<unsigned>((k + 255) / 256), 256, 0, s>>>(cdf, p, n, k, seed, systematic,
+                                                                  src, w);
   return 1;
 }
 

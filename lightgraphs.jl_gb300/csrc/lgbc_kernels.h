@@ -91,13 +91,22 @@ int ms_begin_backward(cudaStream_t s, const MsBuffers& b);
 // Backward (dependency) step for the level in ctl->level, then level--.
 int ms_backward_level(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
                       const HubData& hd, int sigma_kind, double* bc);
+// Stress step for the level in ctl->level after a distance-only forward
+// sweep (E = 1 + D per (vertex, lane) in the path-count rows), adding the
+// stress of level + 1 into `stress` (wrapping uint64); then level--.
+int st_backward_level(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
+                      const HubData& hd, unsigned long long* stress);
 // After the backward sweep: clear the masks of levels 0 and 1.
 int ms_cleanup(const LaunchCfg& c, cudaStream_t s, const MsBuffers& b);
-// After a distance-only forward sweep (before ms_cleanup_all):
-// mass[lane] += sum over the lane's reached vertices t != source of (d - 1),
-// the lane's dependency mass sum_v delta_s(v).
-int ms_level_mass(const LaunchCfg& c, cudaStream_t s, const MsBuffers& b,
-                  unsigned long long* mass);
+// Per-lane distance statistics of a batch (64 entries each, accumulated):
+// vertices reached at levels >= 1, the sum of their levels, the deepest level.
+struct LevelStats {
+  unsigned long long* cnt;
+  unsigned long long* dsum;
+  int* dmax;
+};
+// After a distance-only forward sweep (before ms_cleanup_all).
+int ms_level_stats(const LaunchCfg& c, cudaStream_t s, const MsBuffers& b, const LevelStats& st);
 // After a distance-only batch: clear visit / masks of every listed vertex.
 int ms_cleanup_all(const LaunchCfg& c, cudaStream_t s, const MsBuffers& b);
 // Zero visit and both mask buffers outright (after an aborted batch).
@@ -116,6 +125,13 @@ int bfs_topdown(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const Bfs
 int bfs_bottomup(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const BfsBuffers& b,
                  int32_t* dist, int stage_smem);
 int bfs_advance(cudaStream_t s, const BfsBuffers& b);
+// parents[v] = smallest in-neighbour of v at distance dist[v] - 1 (the
+// source: itself; unreached: -1).
+int bfs_parents(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const int32_t* dist,
+                int32_t* parents);
+// p[idx[i]] = value for i < count.
+int scatter_i32(const LaunchCfg& c, cudaStream_t s, int32_t* p, const int32_t* idx, int64_t count,
+                int32_t value);
 // Largest dynamic shared memory the bottom-up kernel may stage (bytes).
 int bfs_configure(size_t max_dyn_smem);
 
@@ -198,7 +214,9 @@ int mlp_view(const lgbc_mlp* m, MlpView* out);
 int64_t proposal_tiles(int64_t n);
 int proposal_build(cudaStream_t s, const float* y, int64_t n, double eps, float* fscratch,
                    double* e, double* tsum, double* scal, double* p, double* cdf);
+// systematic: draw i uses u_i = (i + U) / k with one uniform U, else k
+// independent uniforms.
 int proposal_sample(cudaStream_t s, const double* cdf, const double* p, int64_t n, int64_t k,
-                    uint64_t seed, int32_t* src, double* w);
+                    uint64_t seed, bool systematic, int32_t* src, double* w);
 
 }  // namespace lgbc

@@ -1111,6 +1111,177 @@ __global__ void __launch_bounds__(256) k_ms_delta_seg(DevGraph g, MsBuffers b, H
   }
 }
 
+// ---------------------------------------------------------------------------
+// Stress centrality (src/centrality/stress.jl:51-77).  For source s the
+// reference walks the vertices by decreasing distance and, per w,
+//   delta[v] += delta[w] + 1 for every predecessor v of w;
+//   delta[w] *= length(P[w]);  stress[w] += delta[w] (w != s),
+// all in wrapping Int64.  With D[w] = delta[w] before its multiplication,
+//   D[v] = sum over successors c of v of (D[c] + 1),
+//   stress[w] += D[w] * |P[w]|,
+// where the successors of v are its out-neighbours one level deeper and P[w]
+// its in-neighbours one level closer.  The sweep keeps E = D + 1 per (vertex,
+// lane) in the path-count rows and uses wrapping uint64 arithmetic, which is
+// bit-identical to Julia's Int64.  Level L's step computes E for level L
+// (k_st_delta, pull over out-edges against F_{L+1}) and then, with F_L
+// complete, the predecessor counts and stress of level L + 1 (k_st_count,
+// pull over in-edges against F_L).
+// ---------------------------------------------------------------------------
+
+// Per-lane count, over in-edges [e0, e1), of the neighbours u whose mask
+// front[u] & want carries the lane (lanes t and t + 32 of this thread).
+__device__ __forceinline__ void count_range(const int32_t* __restrict__ ci, int64_t e0, int64_t e1,
+                                            uint64_t want, const uint64_t* __restrict__ front,
+                                            unsigned long long& c0, unsigned long long& c1) {
+  const int ln = lane_id();
+  for (int64_t e = e0; e < e1; e += kWarp) {
+    const int64_t idx = e + ln;
+    uint64_t f = 0;
+    if (idx < e1) f = front[ci[idx]] & want;
+    if (!__any_sync(kFull, f != 0)) continue;
+    c0 += __popc(warp_transpose32(static_cast<uint32_t>(f)));
+    c1 += __popc(warp_transpose32(static_cast<uint32_t>(f >> 32)));
+  }
+}
+
+// stress[w] += sum over the lanes `mine` of w of (E - 1) * count.
+__device__ __forceinline__ void stress_finish(const unsigned long long* __restrict__ erow,
+                                              uint64_t mask, unsigned long long c0,
+                                              unsigned long long c1, unsigned long long* stress,
+                                              int32_t w) {
+  const int ln = lane_id();
+  const unsigned mine = my_bits(mask);
+  unsigned long long x = 0;
+  if (mine & 1u) x += (erow[ln] - 1ull) * c0;
+  if (mine & 2u) x += (erow[32 + ln] - 1ull) * c1;
+  x = warp_sum_u64(x);
+  if (ln == 0) stress[w] += x;
+}
+
+// Level L entries: record F_L, clear visit, and for L >= 1 set E = 1 + sum
+// of the successors' E (hubs: k_st_hub_delta).
+__global__ void __launch_bounds__(256) k_st_delta(DevGraph g, MsBuffers b, HubData hd) {
+  BatchCtl* c = b.ctl;
+  const int L = c->level;
+  const unsigned long long lo = b.lvl_off[L], hi = b.lvl_off[L + 1];
+  const uint64_t* __restrict__ succ = mb_at(b, L + 1);
+  uint64_t* other = mb_at(b, L);
+  unsigned long long* E = reinterpret_cast<unsigned long long*>(b.sigma);
+  const int ln = lane_id();
+  for (unsigned long long i = lo + gwarp(); i < hi; i += nwarps()) {
+    const int32_t v = b.qv[i];
+    const uint64_t F = b.qm[i];
+    if (ln == 0) {
+      other[v] = F;
+      b.visit[v] = 0;
+    }
+    if (L == 0) continue;
+    const int64_t e0 = g.rowptr[v], e1 = g.rowptr[v + 1];
+    if (e1 - e0 > hd.hub_degree) continue;
+    unsigned long long a0 = 0, a1 = 0;
+    for (int64_t e = e0; e < e1; e += kWarp) {
+      const int64_t idx = e + ln;
+      int32_t w = 0;
+      uint64_t gm = 0;
+      if (idx < e1) {
+        w = g.colidx[idx];
+        gm = succ[w] & F;
+      }
+      gather_chunk<unsigned long long, unsigned long long>(w, gm, E, hd.dense_edges, a0, a1);
+    }
+    const unsigned mine = my_bits(F);
+    unsigned long long* row = E + static_cast<int64_t>(v) * 64;
+    if (mine & 1u) row[ln] = a0 + 1ull;
+    if (mine & 2u) row[32 + ln] = a1 + 1ull;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_st_hub_delta(DevGraph g, MsBuffers b, HubData hd) {
+  BatchCtl* c = b.ctl;
+  const int L = c->level;
+  if (L == 0) return;
+  const uint64_t* __restrict__ succ = mb_at(b, L + 1);
+  const uint64_t* __restrict__ cur = mb_at(b, L);
+  unsigned long long* E = reinterpret_cast<unsigned long long*>(b.sigma);
+  const int ln = lane_id();
+  for (long long it = gwarp(); it < hd.n_out; it += nwarps()) {
+    const HubItem I = hd.out_items[it];
+    const int32_t h = I.v;
+    const uint64_t F = cur[h];
+    if (!F) continue;
+    unsigned long long* acc = hd.acc + static_cast<int64_t>(I.slot) * 64;
+    unsigned long long a0 = 0, a1 = 0;
+    for (int64_t e = I.lo; e < I.hi; e += kWarp) {
+      const int64_t idx = e + ln;
+      int32_t w = 0;
+      uint64_t gm = 0;
+      if (idx < I.hi) {
+        w = g.colidx[idx];
+        gm = succ[w] & F;
+      }
+      gather_chunk<unsigned long long, unsigned long long>(w, gm, E, hd.dense_edges, a0, a1);
+    }
+    if (a0) atomicAdd(acc + ln, a0);
+    if (a1) atomicAdd(acc + 32 + ln, a1);
+    if (!hub_last(hd.cnt + I.slot, I.nitems)) continue;
+    const unsigned long long s0 = atomicExch(acc + ln, 0ull);
+    const unsigned long long s1 = atomicExch(acc + 32 + ln, 0ull);
+    if (ln == 0) hd.cnt[I.slot] = 0u;
+    const unsigned mine = my_bits(F);
+    unsigned long long* row = E + static_cast<int64_t>(h) * 64;
+    if (mine & 1u) row[ln] = s0 + 1ull;
+    if (mine & 2u) row[32 + ln] = s1 + 1ull;
+  }
+}
+
+// Level L + 1 entries (after k_st_delta of level L wrote F_L): predecessor
+// counts over in-edges and the stress contribution (hubs: k_st_hub_count).
+__global__ void __launch_bounds__(256) k_st_count(DevGraph g, MsBuffers b, HubData hd,
+                                                  unsigned long long* stress) {
+  BatchCtl* c = b.ctl;
+  const int L = c->level;
+  if (L + 1 > c->maxlevel) return;
+  const unsigned long long lo = b.lvl_off[L + 1], hi = b.lvl_off[L + 2];
+  const uint64_t* __restrict__ front = mb_at(b, L);
+  const unsigned long long* E = reinterpret_cast<const unsigned long long*>(b.sigma);
+  for (unsigned long long i = lo + gwarp(); i < hi; i += nwarps()) {
+    const int32_t w = b.qv[i];
+    const uint64_t F = b.qm[i];
+    const int64_t e0 = g.in_rowptr[w], e1 = g.in_rowptr[w + 1];
+    if (e1 - e0 > hd.hub_degree) continue;
+    unsigned long long c0 = 0, c1 = 0;
+    count_range(g.in_colidx, e0, e1, F, front, c0, c1);
+    stress_finish(E + static_cast<int64_t>(w) * 64, F, c0, c1, stress, w);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_st_hub_count(DevGraph g, MsBuffers b, HubData hd,
+                                                      unsigned long long* stress) {
+  BatchCtl* c = b.ctl;
+  const int L = c->level;
+  if (L + 1 > c->maxlevel) return;
+  const uint64_t* __restrict__ front = mb_at(b, L);
+  const uint64_t* __restrict__ nxt = mb_at(b, L + 1);
+  const unsigned long long* E = reinterpret_cast<const unsigned long long*>(b.sigma);
+  const int ln = lane_id();
+  for (long long it = gwarp(); it < hd.n_in; it += nwarps()) {
+    const HubItem I = hd.in_items[it];
+    const int32_t h = I.v;
+    const uint64_t F = nxt[h];
+    if (!F) continue;
+    unsigned long long* acc = hd.acc + static_cast<int64_t>(I.slot) * 64;
+    unsigned long long c0 = 0, c1 = 0;
+    count_range(g.in_colidx, I.lo, I.hi, F, front, c0, c1);
+    if (c0) atomicAdd(acc + ln, c0);
+    if (c1) atomicAdd(acc + 32 + ln, c1);
+    if (!hub_last(hd.cnt + I.slot, I.nitems)) continue;
+    const unsigned long long s0 = atomicExch(acc + ln, 0ull);
+    const unsigned long long s1 = atomicExch(acc + 32 + ln, 0ull);
+    if (ln == 0) hd.cnt[I.slot] = 0u;
+    stress_finish(E + static_cast<int64_t>(h) * 64, F, s0, s1, stress, h);
+  }
+}
+
 __global__ void k_ms_back_advance(MsBuffers b) { b.ctl->level -= 1; }
 
 // End of a Brandes batch: the backward sweep cleared visit for every listed
@@ -1138,21 +1309,31 @@ __global__ void k_ms_cleanup_all(MsBuffers b) {
   }
 }
 
-// Dependency mass of every lane after a forward sweep, from the identity
+// Distance statistics of every lane after a forward sweep: cnt[lane] +=
+// vertices the lane reached at levels >= 1, dsum[lane] += the sum of those
+// levels, dmax[lane] = max(dmax[lane], deepest level).  A warp loads 32 list
+// entries, then walks them by broadcast; thread t owns lanes t and t + 32;
+// block sums go out with one atomic per lane per block.
+//
+// The dependency mass of a source follows from them exactly:
 //   sum_{v != s} delta_s(v) = sum_{t reachable from s, t != s} (d(s, t) - 1)
 // (delta_s(v) = sum_t sigma_st(v) / sigma_st, and sum_v sigma_st(v) / sigma_st
-// is the number of interior vertices of a shortest s-t path).  Level L >= 1
-// entries add L - 1 to each of their lanes; exact in 64-bit integers.  A warp
-// loads 32 entries, then walks them by broadcast; thread t owns lanes t and
-// t + 32; block sums go to mass[lane] with one atomic per lane per block.
-__global__ void __launch_bounds__(256) k_ms_level_mass(MsBuffers b, unsigned long long* mass) {
-  __shared__ unsigned long long part[64];
+// is the number of interior vertices of a shortest s-t path).
+__global__ void __launch_bounds__(256) k_ms_level_stats(MsBuffers b, unsigned long long* cnt,
+                                                        unsigned long long* dsum, int* dmax) {
+  __shared__ unsigned long long pc[64], ps[64];
+  __shared__ int pm[64];
   const int ln = lane_id();
-  if (threadIdx.x < 64) part[threadIdx.x] = 0ull;
+  if (threadIdx.x < 64) {
+    pc[threadIdx.x] = 0ull;
+    ps[threadIdx.x] = 0ull;
+    pm[threadIdx.x] = 0;
+  }
   __syncthreads();
   const int maxl = b.ctl->maxlevel;
   const unsigned long long lo = b.lvl_off[1], hi = b.lvl_off[maxl + 1];
-  unsigned long long a0 = 0, a1 = 0;
+  unsigned long long c0 = 0, c1 = 0, s0 = 0, s1 = 0;
+  int m0 = 0, m1 = 0;
   const unsigned long long stride = static_cast<unsigned long long>(nwarps()) * 32;
   for (unsigned long long base = lo + static_cast<unsigned long long>(gwarp()) * 32; base < hi;
        base += stride) {
@@ -1170,15 +1351,35 @@ __global__ void __launch_bounds__(256) k_ms_level_mass(MsBuffers b, unsigned lon
     }
     for (int j = 0; j < 32; ++j) {
       const uint64_t mj = shfl_u64(m, j);
-      const unsigned long long dj = static_cast<unsigned long long>(__shfl_sync(kFull, lev, j) - 1);
-      if ((mj >> ln) & 1ull) a0 += dj;
-      if ((mj >> (32 + ln)) & 1ull) a1 += dj;
+      const int lj = __shfl_sync(kFull, lev, j);
+      if ((mj >> ln) & 1ull) {
+        c0 += 1;
+        s0 += static_cast<unsigned long long>(lj);
+        m0 = max(m0, lj);
+      }
+      if ((mj >> (32 + ln)) & 1ull) {
+        c1 += 1;
+        s1 += static_cast<unsigned long long>(lj);
+        m1 = max(m1, lj);
+      }
     }
   }
-  if (a0) atomicAdd(&part[ln], a0);
-  if (a1) atomicAdd(&part[32 + ln], a1);
+  if (c0) {
+    atomicAdd(&pc[ln], c0);
+    atomicAdd(&ps[ln], s0);
+    atomicMax(&pm[ln], m0);
+  }
+  if (c1) {
+    atomicAdd(&pc[32 + ln], c1);
+    atomicAdd(&ps[32 + ln], s1);
+    atomicMax(&pm[32 + ln], m1);
+  }
   __syncthreads();
-  if (threadIdx.x < 64 && part[threadIdx.x]) atomicAdd(mass + threadIdx.x, part[threadIdx.x]);
+  if (threadIdx.x < 64 && pc[threadIdx.x]) {
+    atomicAdd(cnt + threadIdx.x, pc[threadIdx.x]);
+    atomicAdd(dsum + threadIdx.x, ps[threadIdx.x]);
+    atomicMax(dmax + threadIdx.x, pm[threadIdx.x]);
+  }
 }
 
 // Batch initialisation with explicit seeds: seed i puts vertex seed_v[i] at
@@ -1402,14 +1603,31 @@ int ms_backward_level(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, con
   return launches;
 }
 
+int st_backward_level(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
+                      const HubData& hd, unsigned long long* stress) {
+  int launches = 4;
+  k_ms_back_clear<<<c.grid, c.block, 0, s>>>(b);
+  k_st_delta<<<c.grid, c.block, 0, s>>>(g, b, hd);
+  if (hd.n_out > 0) {
+    k_st_hub_delta<<<c.grid, c.block, 0, s>>>(g, b, hd);
+    ++launches;
+  }
+  k_st_count<<<c.grid, c.block, 0, s>>>(g, b, hd, stress);
+  if (hd.n_in > 0) {
+    k_st_hub_count<<<c.grid, c.block, 0, s>>>(g, b, hd, stress);
+    ++launches;
+  }
+  k_ms_back_advance<<<1, 1, 0, s>>>(b);
+  return launches;
+}
+
 int ms_cleanup(const LaunchCfg& c, cudaStream_t s, const MsBuffers& b) {
   k_ms_cleanup<<<c.grid, c.block, 0, s>>>(b);
   return 1;
 }
 
-int ms_level_mass(const LaunchCfg& c, cudaStream_t s, const MsBuffers& b,
-                  unsigned long long* mass) {
-  k_ms_level_mass<<<c.sms * 2, 256, 0, s>>>(b, mass);
+int ms_level_stats(const LaunchCfg& c, cudaStream_t s, const MsBuffers& b, const LevelStats& st) {
+  k_ms_level_stats<<<c.sms * 2, 256, 0, s>>>(b, st.cnt, st.dsum, st.dmax);
   return 1;
 }
 

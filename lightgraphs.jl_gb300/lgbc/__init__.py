@@ -13,7 +13,11 @@ CUDA library ``liblgbc.so`` through its C ABI (include/lgbc.h):
     Parallel.gdistances / Parallel.gdistances_
         src/Parallel/traversals/gdistances.jl:36-139
 
+    stress_centrality(g[, vs | k])                  src/centrality/stress.jl:33-49
+    bfs_parents, bfs_tree, tree, has_path           src/traversals/bfs.jl:10-76,150-172
     core_number(g)                                  src/degeneracy.jl:38-80
+    closeness_centrality, radiality_centrality      src/centrality/{closeness,radiality}.jl
+    eccentricity, diameter, radius, periphery, center  src/distance.jl:73-170
     learned.* -- importance-sampled betweenness with a learned source
         proposal (no counterpart in the reference)
 
@@ -24,13 +28,16 @@ a GPU or without the built library the calls raise ``LGBCError``.
 from . import Parallel, learned
 from ._lib import ArgumentError, BoundsError, LGBCError, MethodError
 from .centrality import (betweenness_centrality, betweenness_centrality_many, betweenness_raw,
-                         sample, sample_, _rescale_)
+                         sample, sample_, stress_centrality, _rescale_)
 from .graphs import (DefaultDistance, DeviceGraph, SimpleDiGraph, SimpleGraph, degree,
                      is_directed, ne, nv, vertices, weights)
 from .persistence import loadgraph
+from .distance import (center, closeness_centrality, diameter, eccentricity, periphery,
+                       radiality_centrality, radius)
 from .learned import (SourceProposal, betweenness_centrality_learned, core_number,
                       dependency_mass, features)
-from .traversals import gdistances, gdistances_, multi_gdistances
+from .traversals import (bfs_parents, bfs_tree, gdistances, gdistances_, has_path,
+                         multi_gdistances, tree)
 
 __all__ = [
     "Parallel", "ArgumentError", "BoundsError", "LGBCError", "MethodError",
@@ -38,5 +45,7 @@ __all__ = [
     "DefaultDistance", "DeviceGraph", "SimpleDiGraph", "SimpleGraph", "degree", "is_directed",
     "ne", "nv", "vertices", "weights", "loadgraph", "gdistances", "gdistances_",
     "multi_gdistances", "learned", "SourceProposal", "betweenness_centrality_learned",
-    "core_number", "dependency_mass", "features",
+    "core_number", "dependency_mass", "features", "closeness_centrality", "radiality_centrality",
+    "eccentricity", "diameter", "radius", "periphery", "center", "stress_centrality",
+    "bfs_parents", "bfs_tree", "tree", "has_path",
 ]

@@ -66,6 +66,8 @@ class LgbcTrainCfg(ctypes.Structure):
                 ("beta2", ctypes.c_float), ("eps", ctypes.c_float), ("seed", ctypes.c_uint64)]
 
 
+SAMPLE_IID = 0
+SAMPLE_SYSTEMATIC = 1
 MLP_PARAMS = 4545
 MLP_HIDDEN = 64
 MLP_FEATURES = 4
@@ -92,6 +94,7 @@ def _declare(lib) -> None:
         "lgbc_graph_stats": ([p, ctypes.POINTER(LgbcStats)], c_int),
         "lgbc_get_tuning": ([p, ctypes.POINTER(LgbcTuning)], c_int),
         "lgbc_set_tuning": ([p, ctypes.POINTER(LgbcTuning)], c_int),
+        "lgbc_tune": ([p, ctypes.c_char_p], c_int),
         "lgbc_device_alloc": ([pp, i64], c_int),
         "lgbc_device_free": ([p], c_int),
         "lgbc_host_alloc": ([pp, i64], c_int),
@@ -102,6 +105,10 @@ def _declare(lib) -> None:
         "lgbc_core_number": ([p, p], c_int),
         "lgbc_features": ([p, p], c_int),
         "lgbc_dependency_mass": ([p, p, i64, p], c_int),
+        "lgbc_distance_stats": ([p, p, i64, p, p, p], c_int),
+        "lgbc_stress": ([p, p, i64, p], c_int),
+        "lgbc_bfs_parents": ([p, ctypes.c_int32, c_int, p], c_int),
+        "lgbc_has_path": ([p, ctypes.c_int32, ctypes.c_int32, p, i64, ctypes.POINTER(c_int)], c_int),
         "lgbc_betweenness_weighted": ([p, p, p, i64, p], c_int),
         "lgbc_mlp_create": ([pp, ctypes.c_uint64], c_int),
         "lgbc_mlp_destroy": ([p], c_int),
@@ -113,7 +120,7 @@ def _declare(lib) -> None:
         "lgbc_mlp_grad": ([p, p, p, i64, p, p], c_int),
         "lgbc_mlp_train": ([p, p, p, i64, p, i64, ctypes.POINTER(LgbcTrainCfg), p], c_int),
         "lgbc_proposal_build": ([p, p, ctypes.c_double, p], c_int),
-        "lgbc_proposal_sample": ([p, i64, ctypes.c_uint64, p, p], c_int),
+        "lgbc_proposal_sample": ([p, i64, ctypes.c_uint64, c_int, p, p], c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

@@ -1,6 +1,7 @@
 """betweenness_centrality with LightGraphs' signature, computed by the CUDA library.
 
-Reference: src/centrality/betweenness.jl (LightGraphs.jl v1.3.5).
+Reference: src/centrality/betweenness.jl and src/centrality/stress.jl
+(LightGraphs.jl v1.3.5).
   betweenness_centrality(g, vs=vertices(g), distmx=weights(g); normalize=true,
                          endpoints=false)                          :46-75
   betweenness_centrality(g, k::Integer, distmx=weights(g); ...)    :77-78
@@ -176,3 +177,21 @@ def betweenness_centrality_many(graphs, *, normalize: bool = True,
         res.append(v)
         o += n
     return res
+
+
+def stress_centrality(g, vs=None, *, rng=None) -> np.ndarray:
+    """Drop-in for LightGraphs.stress_centrality (src/centrality/stress.jl:33-49):
+    ``vs`` a collection of 1-based vertices (default all) or an integer k for
+    ``sample(vertices(g), k)``.  Returns the Int64 stress vector (vertex - 1),
+    with the reference's wrapping Int64 arithmetic."""
+    if _is_count(vs):
+        vs = sample(g.vertices(), int(vs), rng=rng)
+    n = g.nv()
+    out = np.zeros(n, np.int64)
+    if n == 0:
+        return out
+    src = None if vs is None else np.ascontiguousarray(_sources0(g, vs), np.int32)
+    nsrc = 0 if src is None else len(src)
+    _lib.check(_lib.lib().lgbc_stress(g.device_handle().handle, _lib.ptr(src), nsrc,
+                                      _lib.ptr(out)))
+    return out

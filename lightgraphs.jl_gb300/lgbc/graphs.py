@@ -114,6 +114,15 @@ class _GraphBase:
             self._build()
         return self._in_csr
 
+    def has_edge(self, u: int, v: int) -> bool:
+        """has_edge(g, u, v) with 1-based ids (sorted out-list search)."""
+        if not (1 <= u <= self._n and 1 <= v <= self._n):
+            return False
+        rp, ci = self.csr()
+        row = ci[rp[u - 1]:rp[u]]
+        i = int(np.searchsorted(row, v - 1))
+        return i < len(row) and int(row[i]) == v - 1
+
     def outneighbors(self, v: int) -> np.ndarray:
         rp, ci = self.csr()
         return ci[rp[v - 1]:rp[v]].astype(np.int64) + 1
@@ -288,6 +297,13 @@ class DeviceGraph:
         for k, v in kw.items():
             setattr(t, k, v)
         _lib.check(_lib.lib().lgbc_set_tuning(self.handle, ctypes.byref(t)))
+
+    def tune(self, cache_path: str | None = None) -> dict:
+        """Run the autotuner (lgbc_tune) and return the chosen settings."""
+        path = None if cache_path is None else str(cache_path).encode()
+        _lib.check(_lib.lib().lgbc_tune(self.handle, path))
+        t = self.tuning()
+        return {name: getattr(t, name) for name, _ in t._fields_}
 
     def close(self) -> None:
         if getattr(self, "_h", None) is not None:

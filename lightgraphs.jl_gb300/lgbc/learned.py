@@ -219,29 +219,35 @@ class SourceProposal:
         return p
 
     @staticmethod
-    def sample(g, k: int, seed: int = 0):
-        """k i.i.d. 0-based sources from g's built proposal and their weights 1/(k p)."""
+    def sample(g, k: int, seed: int = 0, scheme: str = "iid"):
+        """k 0-based sources from g's built proposal and their weights 1/(k p):
+        ``scheme`` "iid" (independent draws) or "systematic" (one random
+        offset, draw i at (i + U)/k of the CDF; unbiased, lower variance)."""
+        code = {"iid": _lib.SAMPLE_IID, "systematic": _lib.SAMPLE_SYSTEMATIC}.get(scheme)
+        if code is None:
+            raise _lib.ArgumentError(f"unknown sampling scheme {scheme!r}")
         src = np.empty(int(k), np.int32)
         w = np.empty(int(k), np.float64)
         _lib.check(_lib.lib().lgbc_proposal_sample(g.device_handle().handle, int(k),
-                                                   int(seed) & (2**64 - 1), _lib.ptr(src),
+                                                   int(seed) & (2**64 - 1), code, _lib.ptr(src),
                                                    _lib.ptr(w)))
         return src, w
 
 
 def betweenness_centrality_learned(g, k: int, proposal: SourceProposal, *, normalize: bool = True,
                                    eps: float = 0.1, seed: int = 0, build: bool = True,
-                                   timings: dict | None = None) -> np.ndarray:
+                                   scheme: str = "iid", timings: dict | None = None) -> np.ndarray:
     """Importance-sampled betweenness with k sources drawn from the learned
-    proposal, scaled like betweenness_centrality(g; normalize).  With
-    ``build=False`` the proposal already built for g is reused.  ``timings``
-    (a dict) receives wall-clock seconds of the build and sampled parts."""
+    proposal (``scheme`` "iid" or "systematic"), scaled like
+    betweenness_centrality(g; normalize).  With ``build=False`` the proposal
+    already built for g is reused.  ``timings`` (a dict) receives wall-clock
+    seconds of the build and sampled parts."""
     n = g.nv()
     t0 = time.perf_counter()
     if build:
         proposal.build(g, eps)
     t1 = time.perf_counter()
-    src, w = proposal.sample(g, k, seed)
+    src, w = proposal.sample(g, k, seed, scheme)
     raw = betweenness_raw_weighted(g, src, w)
     _rescale_(raw, n, normalize, g.is_directed(), n)
     t2 = time.perf_counter()

@@ -3,6 +3,8 @@
 Reference: src/traversals/bfs.jl (LightGraphs.jl v1.3.5)
   gdistances!(g, source, vert_level; sort_alg=QuickSort)   :95-124
   gdistances(g, source; sort_alg=QuickSort)                :141
+  bfs_parents / bfs_tree / tree                            :10-19, :35-76
+  has_path(g, u, v; exclude_vertices)                      :150-172
 ``source`` is one vertex or a collection (a multi-source BFS: distance to the
 nearest source).  Unreachable vertices hold typemax(eltype(g)).  The
 ``sort_alg`` keyword only orders the reference's level queue and is accepted
@@ -10,6 +12,7 @@ and ignored.
 """
 from __future__ import annotations
 
+import ctypes
 import numbers
 
 import numpy as np
@@ -75,3 +78,43 @@ def multi_gdistances(g, sources) -> np.ndarray:
         _lib.check(_lib.lib().lgbc_gdistances_batch(h.handle, _lib.ptr(src), len(src),
                                                     _lib.ptr(out)))
     return _to_eltype(out, g.eltype)
+
+
+def bfs_parents(g, s: int, *, dir: str = "out") -> np.ndarray:
+    """Drop-in for bfs_parents(g, s; dir=:out) (src/traversals/bfs.jl:35-66):
+    1-based parent of every vertex (the smallest neighbour one level closer,
+    as the reference's sorted levels choose), s for s, 0 where unreached."""
+    d = {"out": 0, ":out": 0, "in": 1, ":in": 1}.get(str(dir))
+    if d is None:
+        raise _lib.ArgumentError(f"dir must be :out or :in, got {dir!r}")
+    src = _sources0(g, [s])
+    out = np.empty(g.nv(), np.int32)
+    _lib.check(_lib.lib().lgbc_bfs_parents(g.device_handle().handle, int(src[0]), d,
+                                           _lib.ptr(out)))
+    return (out.astype(np.int64) + 1).astype(g.eltype)
+
+
+def tree(parents):
+    """tree(parents) (src/traversals/bfs.jl:10-19): the DiGraph with an
+    edge u -> v for every v whose parent u is neither 0 nor v itself."""
+    from .graphs import SimpleDiGraph
+    p = np.asarray(parents, np.int64)
+    v = np.arange(1, len(p) + 1)
+    keep = (p > 0) & (p != v)
+    return SimpleDiGraph.from_edge_arrays(len(p), p[keep] - 1, v[keep] - 1, eltype=p.dtype)
+
+
+def bfs_tree(g, s: int, *, dir: str = "out"):
+    """Drop-in for bfs_tree(g, s; dir) = tree(bfs_parents(g, s; dir)) (bfs.jl:76)."""
+    return tree(bfs_parents(g, s, dir=dir))
+
+
+def has_path(g, u: int, v: int, *, exclude_vertices=()) -> bool:
+    """Drop-in for has_path(g, u, v; exclude_vertices) (bfs.jl:150-172)."""
+    uv = _sources0(g, [u, v])
+    ex = np.ascontiguousarray(_sources0(g, list(exclude_vertices)), np.int32)
+    res = ctypes.c_int()
+    _lib.check(_lib.lib().lgbc_has_path(g.device_handle().handle, int(uv[0]), int(uv[1]),
+                                        _lib.ptr(ex) if len(ex) else None, len(ex),
+                                        ctypes.byref(res)))
+    return bool(res.value)

@@ -434,6 +434,38 @@ int orc_dependency(int64_t n, const int64_t* rowptr, const int32_t* colidx,
   return 0;
 }
 
+// stress_centrality(g, vs) (src/centrality/stress.jl:33-49) with
+// _stress_accumulate_basic! (:51-77) on the Dijkstra state of every source of
+// degree > 0.  Julia's Int64 arithmetic wraps; uint64 arithmetic wraps
+// identically (two's complement), so the sums are kept in uint64.
+int orc_stress(int64_t n, const int64_t* rowptr, const int32_t* colidx,
+               const int64_t* in_rowptr, const int32_t* in_colidx, int directed,
+               const int32_t* src, int64_t nsrc, int64_t* stress_out) {
+  for (int64_t i = 0; i < nsrc; ++i)
+    if (src[i] < 0 || src[i] >= n) return -1;
+  if (directed && (!in_rowptr || !in_colidx)) return -1;
+  Csr out{n, rowptr, colidx};
+  Csr in = directed ? Csr{n, in_rowptr, in_colidx} : out;
+  std::vector<uint64_t> stress(n, 0);
+  std::vector<uint64_t> delta(n);
+  DijkstraState st;
+  for (int64_t i = 0; i < nsrc; ++i) {
+    const int32_t s = src[i];
+    if (degree_of(out, &in, directed, s) == 0) continue;        // :38
+    dijkstra_allpaths(out, s, st);                               // :39
+    std::fill(delta.begin(), delta.end(), 0);                    // :57
+    st.preds[s].clear();                                         // :62
+    for (auto it = st.closest.rbegin(); it != st.closest.rend(); ++it) {  // :64-65
+      const int32_t w = *it;
+      for (int32_t v : st.preds[w]) delta[v] += delta[w] + 1;    // :66-70
+      delta[w] *= static_cast<uint64_t>(st.preds[w].size());     // :72
+      if (w != s) stress[w] += delta[w];                         // :73-75
+    }
+  }
+  for (int64_t v = 0; v < n; ++v) stress_out[v] = static_cast<int64_t>(stress[v]);
+  return 0;
+}
+
 // core_number(g) for a graph without self-loops: the bin-sort cores
 // decomposition of Batagelj & Zaversnik (2003) as in src/degeneracy.jl:38-80,
 // with degree(g, v) = length(fadjlist[v]) (undirected).  Returns -1 when a

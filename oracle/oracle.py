@@ -12,6 +12,12 @@ The oracle restates LightGraphs.jl v1.3.5 (paths relative to that project):
                              ``_rescale!``; Parallel threaded variant
                              src/Parallel/centrality/betweenness.jl:42-72
   * ``rescale``           -- src/centrality/betweenness.jl:136-160
+  * ``closeness``, ``radiality``, ``eccentricity``
+                          -- src/centrality/closeness.jl:33-55,
+                             src/centrality/radiality.jl:36-49, src/distance.jl:73-79
+  * ``core_number``       -- src/degeneracy.jl:38-80
+  * ``stress``            -- src/centrality/stress.jl:33-77
+  * ``bfs_parents``, ``has_path`` -- src/traversals/bfs.jl:40-66, :150-172
 Parity is pinned against the reference's golden vectors (tests/golden/).
 """
 from __future__ import annotations
@@ -68,6 +74,8 @@ def _load():
         lib.orc_rescale.restype = None
         lib.orc_dependency.argtypes = [i64, p, p, p, p, ctypes.c_int, p, p, i64, p, p]
         lib.orc_dependency.restype = ctypes.c_int
+        lib.orc_stress.argtypes = [i64, p, p, p, p, ctypes.c_int, p, i64, p]
+        lib.orc_stress.restype = ctypes.c_int
         lib.orc_core_number.argtypes = [i64, p, p, p]
         lib.orc_core_number.restype = ctypes.c_int
         _lib = lib
@@ -206,3 +214,117 @@ def features(rowptr, colidx) -> np.ndarray:
     f[:, 2] = np.where(deg > 0, s_ld / np.maximum(deg, 1.0), 0.0)
     f[:, 3] = np.log1p(s_d)
     return f
+
+
+_TYPEMAX = np.iinfo(np.int64).max
+
+
+def _dists64(rowptr, colidx, s):
+    """dijkstra_shortest_paths(g, s).dists with unit weights: Int64, typemax unreached."""
+    d = gdistances(rowptr, colidx, [s]).astype(np.int64)
+    d[d == UNREACHED32] = _TYPEMAX
+    return d
+
+
+def closeness(rowptr, colidx, degrees, normalize=True) -> np.ndarray:
+    """closeness_centrality (src/centrality/closeness.jl:33-55); degrees as
+    degree(g, v) (in + out for a digraph)."""
+    n = len(rowptr) - 1
+    out = np.zeros(n)
+    for u in range(n):
+        if degrees[u] == 0:
+            continue
+        d = _dists64(rowptr, colidx, u)
+        delta = d[d != _TYPEMAX]
+        sigma = int(delta.sum())
+        l = len(delta) - 1
+        if sigma > 0:
+            out[u] = l / sigma
+            if normalize:
+                out[u] *= l / (n - 1)
+    return out
+
+
+def radiality(rowptr, colidx) -> np.ndarray:
+    """radiality_centrality (src/centrality/radiality.jl:36-49), Int64
+    sums wrapping as Julia's do."""
+    n = len(rowptr) - 1
+    meandists = np.zeros(n)
+    dmtr = 0.0
+    with np.errstate(over="ignore"):
+        for v in range(n):
+            d = _dists64(rowptr, colidx, v)
+            dmtr = max(dmtr, float(d.max()))
+            meandists[v] = float(d.sum(dtype=np.int64)) / (n - 1)
+    meandists = (dmtr + 1) - meandists
+    return meandists / dmtr
+
+
+def eccentricity(rowptr, colidx, vs=None) -> np.ndarray:
+    """eccentricity(g, vs) (src/distance.jl:73-84): Int64, typemax if unreachable."""
+    n = len(rowptr) - 1
+    vs = range(n) if vs is None else vs
+    return np.array([int(_dists64(rowptr, colidx, v).max()) for v in vs], np.int64)
+
+
+def stress(rowptr, colidx, sources=None, *, directed=False, in_rowptr=None, in_colidx=None):
+    """stress_centrality(g, vs) (src/centrality/stress.jl:33-77), Int64."""
+    lib = _load()
+    rowptr, colidx = _csr(rowptr, colidx)
+    n = len(rowptr) - 1
+    if directed:
+        in_rowptr, in_colidx = _csr(in_rowptr, in_colidx)
+    else:
+        in_rowptr = in_colidx = None
+    src = np.arange(n, dtype=np.int32) if sources is None else \
+        np.ascontiguousarray(np.asarray(sources, dtype=np.int32).ravel())
+    out = np.empty(n, np.int64)
+    if lib.orc_stress(n, _ptr(rowptr), _ptr(colidx), _ptr(in_rowptr), _ptr(in_colidx),
+                      int(bool(directed)), _ptr(src), len(src), _ptr(out)) != 0:
+        raise ValueError("oracle stress: bad arguments")
+    return out
+
+
+def bfs_parents(rowptr, colidx, s: int) -> np.ndarray:
+    """_bfs_parents(g, s, neighborfn) (src/traversals/bfs.jl:40-66) over the
+    given CSR (the out-lists for :out, the in-lists for :in); 0-based ids,
+    -1 where unreached.  Pure Python, for small graphs."""
+    n = len(rowptr) - 1
+    visited = np.zeros(n, bool)
+    parents = np.full(n, -1, np.int64)
+    cur = [s]
+    visited[s] = True
+    parents[s] = s
+    while cur:
+        nxt = []
+        for v in cur:
+            for i in colidx[rowptr[v]:rowptr[v + 1]].tolist():
+                if not visited[i]:
+                    nxt.append(i)
+                    parents[i] = v
+                    visited[i] = True
+        cur = sorted(nxt)
+    return parents
+
+
+def has_path(rowptr, colidx, u: int, v: int, exclude=()) -> bool:
+    """has_path(g, u, v; exclude_vertices) (src/traversals/bfs.jl:150-172), 0-based."""
+    n = len(rowptr) - 1
+    seen = np.zeros(n, bool)
+    for x in exclude:
+        seen[x] = True
+    if seen[u] or seen[v]:
+        return False
+    if u == v:
+        return True
+    q = [u]
+    seen[u] = True
+    while q:
+        x = q.pop(0)
+        for w in colidx[rowptr[x]:rowptr[x + 1]].tolist():
+            if w == v:
+                return True
+            if not seen[w]:
+                q.append(w)
+                seen[w] = True
+    return False

@@ -219,14 +219,41 @@ def test_proposal_matches_softmax_and_sampler():
     m.close()
 
 
+def test_systematic_sampling_counts():
+    g = gen.rmat(11, 8, seed=22)
+    m = SourceProposal(seed=5)
+    p = m.build(g, 0.1, return_p=True)
+    k = 5000
+    src, w = m.sample(g, k, seed=3, scheme="systematic")
+    assert np.all(np.diff(src) >= 0)  # draws come in CDF (vertex) order
+    counts = np.bincount(src, minlength=g.nv())
+    kp = k * p
+    assert np.all(counts >= np.floor(kp) - 1) and np.all(counts <= np.ceil(kp) + 1)
+    np.testing.assert_allclose(w, 1.0 / (k * p[src]), rtol=1e-15)
+    with pytest.raises(lgbc.ArgumentError):
+        m.sample(g, 10, scheme="stratified")
+    m.close()
+
+
+def test_weighted_repeats_merge_into_one_lane():
+    g = gen.rmat(12, 16, seed=3)
+    src = np.array([5, 9, 5, 5, 9, 77], np.int32)
+    w = np.array([1.0, 2.0, 0.5, 0.25, 1.0, 3.0])
+    a = betweenness_raw_weighted(g, src, w)
+    assert g.device_handle().stats()["active_sources"] <= 3
+    b = betweenness_raw_weighted(g, np.array([5, 9, 77], np.int32), np.array([1.75, 3.0, 3.0]))
+    np.testing.assert_allclose(a, b, rtol=1e-12, atol=1e-9)
+
+
 def test_importance_estimator_is_unbiased_on_average():
     g = gen.barabasi_albert(600, 2, seed=8)
     exact = lgbc.betweenness_centrality(g)
     m = SourceProposal(seed=2)
     m.build(g, 0.1)
-    est = np.mean([betweenness_centrality_learned(g, 64, m, seed=s, build=False)
-                   for s in range(60)], axis=0)
-    assert l1_error(est, exact) < 0.08
+    for scheme in ("iid", "systematic"):
+        est = np.mean([betweenness_centrality_learned(g, 64, m, seed=s, build=False, scheme=scheme)
+                       for s in range(60)], axis=0)
+        assert l1_error(est, exact) < 0.08
     m.close()
 
 

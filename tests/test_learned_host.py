@@ -133,7 +133,8 @@ def test_abi_argument_errors_without_gpu():
     assert lib.lgbc_mlp_create(None, 0) == _lib.LGBC_EINVAL
     assert lib.lgbc_mlp_destroy(None) == _lib.LGBC_OK
     assert lib.lgbc_mlp_forward(None, None, 0, None) == _lib.LGBC_EINVAL
-    assert lib.lgbc_proposal_sample(None, 0, 0, None, None) == _lib.LGBC_EINVAL
+    assert lib.lgbc_proposal_sample(None, 0, 0, 0, None, None) == _lib.LGBC_EINVAL
+    assert lib.lgbc_tune(None, None) == _lib.LGBC_EINVAL
 
 
 def _csr_args(g):
