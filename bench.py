@@ -181,6 +181,17 @@ WORKLOADS = {
 }
 
 
+def parse_tuning(spec: str | None) -> dict:
+    """"key=value,..." -> lgbc_tuning overrides (numbers)."""
+    out = {}
+    for item in (spec or "").split(","):
+        if not item.strip():
+            continue
+        k, v = item.split("=", 1)
+        out[k.strip()] = float(v) if k.strip() in ("alpha", "beta") else int(v)
+    return out
+
+
 def workload(rank: int, args):
     """(graph, 0-based sources, active source count, generation seconds, name)."""
     from lgbc import generators as G
@@ -324,6 +335,16 @@ def run_ours(args, dist: Dist):
 
     dg = g.device_handle()
     h = dg.handle
+    overrides = parse_tuning(args.tuning)
+    if overrides:
+        dg.set_tuning(**overrides)
+    tune_s = None
+    if args.autotune:
+        t0 = time.perf_counter()
+        dg.tune()
+        tune_s = time.perf_counter() - t0
+    tuning = {k: getattr(dg.tuning(), k) for k, _ in _lib.LgbcTuning._fields_ if k != "reserved"}
+    log(f"[rank {dist.rank}] tuning {tuning}" + (f" (autotuned in {tune_s:.2f} s)" if tune_s else ""))
     bc_dev = ctypes.c_void_p()
     _lib.check(lib.lgbc_device_alloc(ctypes.byref(bc_dev), 8 * n))
     srcp = _lib.ptr(src)
@@ -382,6 +403,11 @@ def run_ours(args, dist: Dist):
         _lib.check(lib.lgbc_graph_create(ctypes.byref(hh), n, nnz, prp, pci, pirp, pici,
                                          int(directed)))
         try:
+            t = _lib.LgbcTuning()
+            for k_, _ in _lib.LgbcTuning._fields_:
+                if k_ in tuning:
+                    setattr(t, k_, tuning[k_])
+            _lib.check(lib.lgbc_set_tuning(hh, ctypes.byref(t)))
             _lib.check(lib.lgbc_betweenness(hh, srcp, len(src), 0, _lib.ptr(out)))
         finally:
             lib.lgbc_graph_destroy(hh)
@@ -436,7 +462,8 @@ def run_ours(args, dist: Dist):
             "dtype": "u64 path counts, df32/f64 dependencies", "data": "synthetic",
             "config": {"workload": wname, "description": WORKLOADS[args.workload],
                        "n": n, "m": m, "nnz": nnz, "directed": directed, "sources": len(src),
-                       "active_sources": k_act, "lanes": LANES,
+                       "active_sources": k_act, "lanes": tuning["lanes"], "tuning": tuning,
+                       "autotune_s": tune_s,
                        "parallelism": f"replicas x{dist.world}",
                        "l2": ("inputs larger than L2 (CSR + lane state); no flush"
                               if nnz * 4 + n * 1024 > 129e6 else
@@ -624,6 +651,8 @@ def main():
     ap.add_argument("--scale", type=int, default=20)
     ap.add_argument("--k", type=int, default=0, help="sampled sources (0 = the workload's)")
     ap.add_argument("--graphs", type=int, default=4096, help="c3: number of graphs")
+    ap.add_argument("--tuning", default="", help="lgbc_tuning overrides, e.g. source_order=0,hub_degree=512")
+    ap.add_argument("--autotune", action="store_true", help="run lgbc_tune before timing")
     ap.add_argument("--c5-train", type=int, default=128, help="c5: training graphs per family")
     ap.add_argument("--c5-train-scale", type=int, default=14)
     ap.add_argument("--c5-steps", type=int, default=3000, help="c5: training steps")

@@ -157,7 +157,13 @@ int lgbc_graph_stats(const lgbc_graph *g, lgbc_stats *out);
  *   segment_degree graphs whose mean degree (stored entries / n) is below
  *                 this run the low-degree kernels, in which a warp streams the
  *                 edges of 32 vertices at once (default 0 = never: on the
- *                 measured workloads the warp-per-vertex kernels were faster). */
+ *                 measured workloads the warp-per-vertex kernels were faster).
+ *   source_order  1: before batching, sort the sources by their BFS distances
+ *                 to the 16 highest-degree vertices (computed once per
+ *                 graph), so that one batch holds sources with similar
+ *                 distance profiles and reaches each vertex at fewer
+ *                 distinct levels; 0: batch in the given order.  Results are
+ *                 the same up to floating-point summation order. */
 typedef struct lgbc_tuning {
   double alpha;
   double beta;
@@ -165,6 +171,8 @@ typedef struct lgbc_tuning {
   int32_t lanes;
   int32_t dense_edges;
   int32_t segment_degree;
+  int32_t source_order;
+  int32_t reserved;
 } lgbc_tuning;
 int lgbc_get_tuning(const lgbc_graph *g, lgbc_tuning *out);
 int lgbc_set_tuning(lgbc_graph *g, const lgbc_tuning *t);

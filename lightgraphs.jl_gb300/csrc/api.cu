@@ -203,7 +203,9 @@ struct lgbc_graph {
   size_t max_smem = 0;
   unsigned long long sigma_limit = ~0ull;  // (2^64 - 1) / (max in-degree + 1)
   lgbc_stats stats{};
-  lgbc_tuning tune{14.0, 24.0, 256, 64, 32, 0};
+  lgbc_tuning tune{14.0, 24.0, 256, 64, 32, 0, 1, 0};
+  std::vector<int32_t> landmarks;   // the highest-degree vertices (source ordering)
+  int32_t* d_lmdist = nullptr;      // landmarks x n BFS distances, computed on first use
 
   DevGraph dev() const {
     return DevGraph{n, nnz, d_rowptr, d_colidx, d_in_rowptr, d_in_colidx};
@@ -574,8 +576,74 @@ int run_betweenness(lgbc_graph* g, int64_t k_act, int endpoints, double* bc_dev,
   return check_launch(g);
 }
 
+// BFS distances from the landmarks (computed once per graph, kept on the device).
+int ensure_landmarks(lgbc_graph* g) {
+  if (g->d_lmdist || g->landmarks.empty()) return LGBC_OK;
+  const int nl = static_cast<int>(g->landmarks.size());
+  LGBC_TRY(ensure_ms(g, false));
+  int32_t* d_lm = nullptr;
+  LGBC_TRY(dev_alloc(&d_lm, static_cast<size_t>(nl)));
+  std::unique_ptr<int32_t, void (*)(int32_t*)> guard(d_lm, [](int32_t* q) { cudaFree(q); });
+  LGBC_CUDA(cudaMemcpyAsync(d_lm, g->landmarks.data(), static_cast<size_t>(nl) * 4,
+                            cudaMemcpyHostToDevice, g->stream));
+  int32_t* d = nullptr;
+  LGBC_TRY(dev_alloc(&d, static_cast<size_t>(nl) * static_cast<size_t>(g->n)));
+  g->launches += fill_i32(g->cfg, g->stream, d, static_cast<int64_t>(nl) * g->n, kUnreached);
+  const lgbc_stats saved = g->stats;  // the call's statistics describe its own sources
+  const int rc = run_ms_batch(g, d_lm, nl, kSigmaNone, nullptr, d, g->n);
+  g->stats = saved;
+  if (rc != LGBC_OK) {
+    cudaFree(d);
+    return rc;
+  }
+  LGBC_CUDA(cudaStreamSynchronize(g->stream));
+  g->d_lmdist = d;
+  return LGBC_OK;
+}
+
+// Source ordering (tuning source_order = 1): sort the active sources by
+// their distance vectors to the landmarks (lexicographically, then by id),
+// so that a 64-lane batch holds sources with similar distance profiles.  Such
+// sources reach a vertex at fewer distinct levels, and every distinct level
+// costs the vertex one pass over its edges in each sweep.  `w`, when given,
+// is permuted alongside.
+int order_active(lgbc_graph* g, std::vector<int32_t>& act, std::vector<double>* w) {
+  const int64_t k = static_cast<int64_t>(act.size());
+  if (g->tune.source_order == 0 || k <= g->tune.lanes || g->landmarks.empty()) return LGBC_OK;
+  LGBC_TRY(ensure_landmarks(g));
+  const int nl = static_cast<int>(g->landmarks.size());
+  int32_t* d_buf = nullptr;  // k sources | k x nl keys
+  LGBC_TRY(dev_alloc(&d_buf, static_cast<size_t>(k) * static_cast<size_t>(nl + 1)));
+  std::unique_ptr<int32_t, void (*)(int32_t*)> guard(d_buf, [](int32_t* q) { cudaFree(q); });
+  LGBC_CUDA(cudaMemcpyAsync(d_buf, act.data(), static_cast<size_t>(k) * 4, cudaMemcpyHostToDevice,
+                            g->stream));
+  g->launches += gather_cols(g->cfg, g->stream, g->d_lmdist, g->n, nl, d_buf, k, d_buf + k);
+  std::vector<int32_t> key(static_cast<size_t>(k) * static_cast<size_t>(nl));
+  LGBC_CUDA(cudaMemcpyAsync(key.data(), d_buf + k, key.size() * 4, cudaMemcpyDeviceToHost,
+                            g->stream));
+  LGBC_CUDA(cudaStreamSynchronize(g->stream));
+  std::vector<int64_t> perm(static_cast<size_t>(k));
+  for (int64_t i = 0; i < k; ++i) perm[static_cast<size_t>(i)] = i;
+  std::stable_sort(perm.begin(), perm.end(), [&](int64_t a, int64_t b) {
+    const int32_t* ka = key.data() + a * nl;
+    const int32_t* kb = key.data() + b * nl;
+    for (int j = 0; j < nl; ++j)
+      if (ka[j] != kb[j]) return ka[j] < kb[j];
+    return act[static_cast<size_t>(a)] < act[static_cast<size_t>(b)];
+  });
+  std::vector<int32_t> a2(static_cast<size_t>(k));
+  for (int64_t i = 0; i < k; ++i) a2[static_cast<size_t>(i)] = act[static_cast<size_t>(perm[i])];
+  act.swap(a2);
+  if (w) {
+    std::vector<double> w2(static_cast<size_t>(k));
+    for (int64_t i = 0; i < k; ++i) w2[static_cast<size_t>(i)] = (*w)[static_cast<size_t>(perm[i])];
+    w->swap(w2);
+  }
+  return LGBC_OK;
+}
+
 // Host-side part shared by the betweenness entry points: validate, filter
-// degree-0 sources (betweenness.jl:58) and upload the active list.
+// degree-0 sources (betweenness.jl:58), order and upload the active list.
 int prepare_sources(lgbc_graph* g, const int32_t* src, int64_t nsrc, int64_t* k_act) {
   std::vector<int32_t> active;
   if (!src) {
@@ -588,6 +656,7 @@ int prepare_sources(lgbc_graph* g, const int32_t* src, int64_t nsrc, int64_t* k_
     for (int64_t i = 0; i < nsrc; ++i)
       if (g->has_degree[static_cast<size_t>(src[i])]) active.push_back(src[i]);
   }
+  LGBC_TRY(order_active(g, active, nullptr));
   *k_act = static_cast<int64_t>(active.size());
   LGBC_TRY(ensure_src(g, *k_act));
   if (*k_act > 0)
@@ -663,6 +732,25 @@ int create_impl(lgbc_graph* g, int64_t n, int64_t nnz, const int64_t* rowptr, co
     max_in = std::max(max_in, din);
   }
   g->sigma_limit = ~0ull / static_cast<unsigned long long>(max_in + 1);
+  {
+    // the kLandmarks highest-degree vertices (ties: smaller id), for source ordering
+    std::vector<std::pair<int64_t, int32_t>> top;
+    for (int64_t v = 0; v < n; ++v) {
+      const int64_t d = (rowptr[v + 1] - rowptr[v]) + (directed ? in_rowptr[v + 1] - in_rowptr[v] : 0);
+      if (d == 0) continue;
+      const std::pair<int64_t, int32_t> item(-d, static_cast<int32_t>(v));
+      if (top.size() < static_cast<size_t>(kLandmarks)) {
+        top.push_back(item);
+        std::push_heap(top.begin(), top.end());
+      } else if (item < top.front()) {
+        std::pop_heap(top.begin(), top.end());
+        top.back() = item;
+        std::push_heap(top.begin(), top.end());
+      }
+    }
+    std::sort(top.begin(), top.end());
+    for (const auto& t : top) g->landmarks.push_back(t.second);
+  }
   cudaError_t e = cudaStreamSynchronize(g->stream);
   cudaFree(d_bad);
   if (e != cudaSuccess) return cuda_fail(e, "graph upload");
@@ -738,6 +826,7 @@ int lgbc_graph_destroy(lgbc_graph* g) {
   dev_free(g->d_src);
   dev_free(g->d_bc);
   dev_free(g->d_dist);
+  dev_free(g->d_lmdist);
   if (g->h_ctl) cudaFreeHost(g->h_ctl);
   if (g->ev_start) cudaEventDestroy(g->ev_start);
   if (g->ev_stop) cudaEventDestroy(g->ev_stop);
@@ -932,7 +1021,8 @@ int lgbc_set_tuning(lgbc_graph* g, const lgbc_tuning* t) {
   LGBC_TRY(check_graph(g));
   if (!t) return fail(LGBC_EINVAL, "null tuning");
   if (!(t->alpha > 0) || !(t->beta > 0) || t->lanes < 1 || t->lanes > kMaxLanes ||
-      t->hub_degree < 1 || t->dense_edges < 0 || t->segment_degree < 0)
+      t->hub_degree < 1 || t->dense_edges < 0 || t->segment_degree < 0 ||
+      (t->source_order != 0 && t->source_order != 1))
     return fail(LGBC_EINVAL,
                 "tuning out of range (alpha, beta > 0; 1 <= lanes <= 64; hub_degree >= 1; dense_edges >= 0)");
   std::lock_guard<std::mutex> lock(g->mu);
@@ -1400,6 +1490,7 @@ int lgbc_betweenness_weighted(lgbc_graph* g, const int32_t* src, const double* w
       aw.push_back(e.second);
     }
   }
+  LGBC_TRY(order_active(g, act, &aw));
   const int64_t k_act = static_cast<int64_t>(act.size());
   g->stats.active_sources = k_act;
   LGBC_TRY(ensure_src(g, k_act));
@@ -1506,10 +1597,11 @@ bool tune_from_cache(const char* path, const std::string& sig, lgbc_tuning* out)
   while (std::fgets(line, sizeof line, f)) {
     char key[256];
     lgbc_tuning t{};
-    if (std::sscanf(line, "%255s %lf %lf %d %d %d %d", key, &t.alpha, &t.beta, &t.hub_degree,
-                    &t.lanes, &t.dense_edges, &t.segment_degree) == 7 &&
+    if (std::sscanf(line, "%255s %lf %lf %d %d %d %d %d", key, &t.alpha, &t.beta, &t.hub_degree,
+                    &t.lanes, &t.dense_edges, &t.segment_degree, &t.source_order) == 8 &&
         sig == key && t.alpha > 0 && t.beta > 0 && t.lanes >= 1 && t.lanes <= kMaxLanes &&
-        t.hub_degree >= 1 && t.dense_edges >= 0 && t.segment_degree >= 0) {
+        t.hub_degree >= 1 && t.dense_edges >= 0 && t.segment_degree >= 0 &&
+        (t.source_order == 0 || t.source_order == 1)) {
       *out = t;  // the last matching line wins
       found = true;
     }
@@ -1605,8 +1697,9 @@ extern "C" int lgbc_tune(lgbc_graph* g, const char* cache_path) {
   if (cache_path) {
     FILE* f = std::fopen(cache_path, "a");
     if (!f) return fail(LGBC_EINVAL, std::string("cannot append to tuning cache ") + cache_path);
-    std::fprintf(f, "%s %.17g %.17g %d %d %d %d\n", sig.c_str(), best.alpha, best.beta,
-                 best.hub_degree, best.lanes, best.dense_edges, best.segment_degree);
+    std::fprintf(f, "%s %.17g %.17g %d %d %d %d %d\n", sig.c_str(), best.alpha, best.beta,
+                 best.hub_degree, best.lanes, best.dense_edges, best.segment_degree,
+                 best.source_order);
     std::fclose(f);
   }
   finish_stats(g);

@@ -21,6 +21,9 @@ enum SigmaKind : int {
   kSigmaF64 = 2,   // FP64 path counts and dependencies (replay after overflow)
 };
 
+// Landmark vertices (highest degree) whose BFS distances order the sources.
+constexpr int kLandmarks = 16;
+
 struct LaunchCfg {
   int grid;     // blocks for grid-stride kernels
   int block;    // threads per block
@@ -143,6 +146,9 @@ void set_last_error(const char* msg);
 int validate_csr(const LaunchCfg& c, cudaStream_t s, const int64_t* rowptr, const int32_t* colidx,
                  int64_t n, int64_t nnz, int* bad);
 int fill_i32(const LaunchCfg& c, cudaStream_t s, int32_t* p, int64_t count, int32_t value);
+// out[r * nl + j] = dist[j * ld + src[r]] for r < k, j < nl.
+int gather_cols(const LaunchCfg& c, cudaStream_t s, const int32_t* dist, int64_t ld, int nl,
+                const int32_t* src, int64_t k, int32_t* out);
 int fill_f64(const LaunchCfg& c, cudaStream_t s, double* p, int64_t count, double value);
 // bc[v] += k_act for every v, then bc[s] += n - 2 for each active source s:
 // the endpoint terms of _accumulate_endpoints! summed over the sources.

@@ -81,6 +81,26 @@ int validate_csr(const LaunchCfg& c, cudaStream_t s, const int64_t* rowptr, cons
   return 1;
 }
 
+namespace {
+__global__ void k_gather_cols(const int32_t* dist, int64_t ld, int nl, const int32_t* src,
+                              int64_t k, int32_t* out) {
+  const int64_t total = k * nl;
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < total;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int64_t r = i / nl;
+    const int j = static_cast<int>(i - r * nl);
+    out[i] = dist[static_cast<int64_t>(j) * ld + src[r]];
+  }
+}
+}  // namespace
+
+int gather_cols(const LaunchCfg& c, cudaStream_t s, const int32_t* dist, int64_t ld, int nl,
+                const int32_t* src, int64_t k, int32_t* out) {
+  if (k <= 0 || nl <= 0) return 0;
+  k_gather_cols<<<c.grid, c.block, 0, s>>>(dist, ld, nl, src, k, out);
+  return 1;
+}
+
 int fill_i32(const LaunchCfg& c, cudaStream_t s, int32_t* p, int64_t count, int32_t value) {
   if (count <= 0) return 0;
   k_fill<int32_t><<<c.grid, c.block, 0, s>>>(p, count, value);

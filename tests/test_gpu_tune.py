@@ -39,3 +39,23 @@ def test_tune_graph_without_edges():
     before = h.tuning()
     h.tune()
     assert h.tuning().lanes == before.lanes
+
+
+@pytest.mark.parametrize("directed", [False, True])
+def test_source_order_keeps_results(directed):
+    g = gen.rmat(12, 16, seed=41, directed=directed)
+    rng = np.random.default_rng(3)
+    src = rng.choice(np.arange(1, g.nv() + 1), 700, replace=False)
+    h = g.device_handle()
+    h.set_tuning(source_order=0)
+    a = lgbc.betweenness_centrality(g, src, endpoints=True)
+    s0 = lgbc.stress_centrality(g, src)
+    w = rng.uniform(0.5, 2.0, len(src))
+    wa = lgbc.learned.betweenness_raw_weighted(g, (src - 1).astype(np.int32), w)
+    h.set_tuning(source_order=1)
+    b = lgbc.betweenness_centrality(g, src, endpoints=True)
+    assert h.stats()["batches"] == (h.stats()["active_sources"] + 63) // 64
+    np.testing.assert_allclose(b, a, rtol=1e-9, atol=1e-12)
+    assert np.array_equal(lgbc.stress_centrality(g, src), s0)
+    wb = lgbc.learned.betweenness_raw_weighted(g, (src - 1).astype(np.int32), w)
+    np.testing.assert_allclose(wb, wa, rtol=1e-9, atol=1e-9)
