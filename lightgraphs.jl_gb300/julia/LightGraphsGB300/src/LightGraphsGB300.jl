@@ -9,6 +9,12 @@ gdistances.  The functions below take the same arguments as
   gdistances!(g, source, dists), gdistances(g, source)              src/traversals/bfs.jl:95-141
   Parallel.betweenness_centrality(...; parallel)                    src/Parallel/centrality/betweenness.jl:1-75
   Parallel.gdistances[!](g, source(s)[, dists])                     src/Parallel/traversals/gdistances.jl:36-139
+  stress_centrality(g[, vs | k])                                    src/centrality/stress.jl:33-49
+  closeness_centrality(g[, distmx]; normalize)                      src/centrality/closeness.jl:33-55
+  radiality_centrality(g)                                           src/centrality/radiality.jl:36-49
+  eccentricity(g[, v | vs][, distmx])                               src/distance.jl:73-84
+  bfs_parents(g, s; dir), bfs_tree(g, s; dir), has_path(g, u, v)    src/traversals/bfs.jl:35-76,150-172
+  core_number(g)                                                    src/degeneracy.jl:38-80
 
 restricted to `SimpleGraph` / `SimpleDiGraph` with unit weights (`DefaultDistance`);
 another distance matrix is a `MethodError`.  The graph's `fadjlist` (and
@@ -26,7 +32,8 @@ using LightGraphs: AbstractGraph, SimpleGraph, SimpleDiGraph, DefaultDistance, n
                    is_directed, vertices, weights, degree
 using Libdl
 
-export betweenness_centrality, gdistances, gdistances!
+export betweenness_centrality, gdistances, gdistances!, stress_centrality, closeness_centrality,
+       radiality_centrality, eccentricity, bfs_parents, bfs_tree, has_path, core_number
 
 const LGBC_OK = Cint(0)
 const LGBC_EINVAL = Cint(-1)
@@ -37,7 +44,8 @@ function __init__()
     path = get(ENV, "LGBC_LIB", normpath(joinpath(@__DIR__, "..", "..", "..", "lib", "liblgbc.so")))
     LIB[] = Libdl.dlopen(path)
     for s in (:lgbc_graph_create, :lgbc_graph_destroy, :lgbc_gdistances, :lgbc_betweenness,
-              :lgbc_last_error)
+              :lgbc_last_error, :lgbc_stress, :lgbc_distance_stats, :lgbc_bfs_parents,
+              :lgbc_has_path, :lgbc_core_number, :lgbc_tune)
         SYM[s] = Libdl.dlsym(LIB[], s)
     end
 end
@@ -188,6 +196,131 @@ GPU drop-in for `LightGraphs.gdistances`; unreachable vertices get `typemax(T)`.
 gdistances(g::Union{SimpleGraph{T},SimpleDiGraph{T}}, source; sort_alg=nothing) where {T} =
     gdistances!(g, source, fill(typemax(T), nv(g)))
 
+# ---------------------------------------------------------------- stress
+"""
+    stress_centrality(g[, vs])
+    stress_centrality(g, k)
+
+GPU drop-in for `LightGraphs.stress_centrality` (Int64, wrapping like the reference).
+"""
+function stress_centrality(g::Union{SimpleGraph,SimpleDiGraph}, vs=vertices(g))
+    src = sources0(g, vs)
+    out = zeros(Int64, nv(g))
+    if nv(g) > 0
+        d = device_graph(g)
+        GC.@preserve src out begin
+            check(ccall(SYM[:lgbc_stress], Cint, (Ptr{Cvoid}, Ptr{Int32}, Int64, Ptr{Int64}),
+                        d.ptr, src, length(src), out))
+        end
+    end
+    return out
+end
+stress_centrality(g::Union{SimpleGraph,SimpleDiGraph}, k::Integer) =
+    stress_centrality(g, LightGraphs.sample(vertices(g), k))
+
+# ---------------------------------------------------------------- distance reductions
+"""(reachable count incl. the source, distance sum, largest distance) per source."""
+function distance_stats(g, vs)
+    src = sources0(g, vs)
+    k = length(src)
+    reached = Vector{Int64}(undef, k); dsum = Vector{Int64}(undef, k); dmax = Vector{Int32}(undef, k)
+    if k > 0
+        d = device_graph(g)
+        GC.@preserve src reached dsum dmax begin
+            check(ccall(SYM[:lgbc_distance_stats], Cint,
+                        (Ptr{Cvoid}, Ptr{Int32}, Int64, Ptr{Int64}, Ptr{Int64}, Ptr{Int32}),
+                        d.ptr, src, k, reached, dsum, dmax))
+        end
+    end
+    return reached, dsum, dmax
+end
+
+"""GPU drop-in for `LightGraphs.closeness_centrality` with unit weights."""
+function closeness_centrality(g::Union{SimpleGraph,SimpleDiGraph},
+                              distmx::DefaultDistance=weights(g); normalize=true)
+    n_v = nv(g)
+    closeness = zeros(n_v)
+    act = [u for u in vertices(g) if degree(g, u) > 0]
+    reached, dsum, _ = distance_stats(g, act)
+    for (i, u) in enumerate(act)
+        σ = dsum[i]; l = reached[i] - 1
+        if σ > 0
+            closeness[u] = l / σ
+            normalize && (closeness[u] *= l / (n_v - 1))
+        end
+    end
+    return closeness
+end
+
+"""GPU drop-in for `LightGraphs.radiality_centrality` (Int64 sums over typemax distances)."""
+function radiality_centrality(g::Union{SimpleGraph,SimpleDiGraph})::Vector{Float64}
+    n_v = nv(g)
+    reached, dsum, dmax = distance_stats(g, vertices(g))
+    meandists = zeros(Float64, n_v)
+    dmtr = 0.0
+    for v in 1:n_v
+        unreached = n_v - reached[v]
+        dmtr = max(dmtr, unreached > 0 ? typemax(Int) : Int(dmax[v]))
+        meandists[v] = (dsum[v] + unreached * typemax(Int)) / (n_v - 1)
+    end
+    meandists = (dmtr + 1) .- (meandists)
+    return meandists ./ dmtr
+end
+
+"""GPU drop-in for `LightGraphs.eccentricity` with unit weights."""
+function eccentricity(g::Union{SimpleGraph,SimpleDiGraph}, vs=vertices(g),
+                      distmx::DefaultDistance=weights(g))
+    reached, _, dmax = distance_stats(g, vs)
+    e = [reached[i] < nv(g) ? typemax(Int) : Int(dmax[i]) for i in eachindex(reached)]
+    any(==(typemax(Int)), e) && @warn("Infinite path length detected")
+    return e
+end
+eccentricity(g::Union{SimpleGraph,SimpleDiGraph}, v::Integer, distmx::DefaultDistance=weights(g)) =
+    eccentricity(g, [v], distmx)[1]
+
+# ---------------------------------------------------------------- BFS trees
+"""GPU drop-in for `LightGraphs.bfs_parents` (the serial function's parents)."""
+function bfs_parents(g::Union{SimpleGraph{T},SimpleDiGraph{T}}, s::Integer; dir=:out) where {T}
+    1 <= s <= nv(g) || throw(BoundsError(vertices(g), s))
+    p = Vector{Int32}(undef, nv(g))
+    d = device_graph(g)
+    GC.@preserve p begin
+        check(ccall(SYM[:lgbc_bfs_parents], Cint, (Ptr{Cvoid}, Int32, Cint, Ptr{Int32}),
+                    d.ptr, Int32(s - 1), Cint(dir == :out ? 0 : 1), p))
+    end
+    return T[x + 1 for x in p]
+end
+bfs_tree(g::Union{SimpleGraph,SimpleDiGraph}, s::Integer; dir=:out) =
+    LightGraphs.tree(bfs_parents(g, s; dir=dir))
+
+"""GPU drop-in for `LightGraphs.has_path`."""
+function has_path(g::Union{SimpleGraph,SimpleDiGraph}, u::Integer, v::Integer;
+                  exclude_vertices::AbstractVector=Int[])
+    ex = sources0(g, exclude_vertices)
+    r = Ref{Cint}(0)
+    d = device_graph(g)
+    GC.@preserve ex begin
+        check(ccall(SYM[:lgbc_has_path], Cint, (Ptr{Cvoid}, Int32, Int32, Ptr{Int32}, Int64, Ref{Cint}),
+                    d.ptr, Int32(u - 1), Int32(v - 1), ex, length(ex), r))
+    end
+    return r[] != 0
+end
+
+"""GPU drop-in for `LightGraphs.core_number` (undirected graphs)."""
+function core_number(g::SimpleGraph{T}) where {T}
+    c = Vector{Int32}(undef, nv(g))
+    d = device_graph(g)
+    GC.@preserve c begin
+        check(ccall(SYM[:lgbc_core_number], Cint, (Ptr{Cvoid}, Ptr{Int32}), d.ptr, c))
+    end
+    return T.(c)
+end
+
+"""Run the library's autotuner for `g` (optionally with a cache file)."""
+tune!(g::Union{SimpleGraph,SimpleDiGraph}; cache::Union{Nothing,String}=nothing) =
+    check(ccall(SYM[:lgbc_tune], Cint, (Ptr{Cvoid}, Cstring), device_graph(g).ptr,
+                cache === nothing ? C_NULL : cache))
+
 module Parallel
 using ..LightGraphsGB300: LightGraphsGB300, DefaultDistance
 using LightGraphs: SimpleGraph, SimpleDiGraph, vertices, weights, nv
@@ -211,6 +344,19 @@ function gdistances!(g::Union{SimpleGraph{T},SimpleDiGraph{T}}, sources, vert_le
     fill!(vert_level, typemax(T))
     return LightGraphsGB300.gdistances!(g, sources, vert_level)
 end
+
+stress_centrality(g::Union{SimpleGraph,SimpleDiGraph}, vs=vertices(g); parallel=:distributed) =
+    LightGraphsGB300.stress_centrality(g, vs)
+stress_centrality(g::Union{SimpleGraph,SimpleDiGraph}, k::Integer; parallel=:distributed) =
+    LightGraphsGB300.stress_centrality(g, k)
+closeness_centrality(g::Union{SimpleGraph,SimpleDiGraph}, distmx::DefaultDistance=weights(g);
+                     normalize=true, parallel=:distributed) =
+    LightGraphsGB300.closeness_centrality(g, distmx; normalize=normalize)
+radiality_centrality(g::Union{SimpleGraph,SimpleDiGraph}; parallel=:distributed) =
+    LightGraphsGB300.radiality_centrality(g)
+eccentricity(g::Union{SimpleGraph,SimpleDiGraph}, vs=vertices(g), distmx::DefaultDistance=weights(g)) =
+    LightGraphsGB300.eccentricity(g, vs, distmx)
+bfs_tree(g::Union{SimpleGraph,SimpleDiGraph}, s::Integer) = LightGraphsGB300.bfs_tree(g, s)
 end # module Parallel
 
 end # module
