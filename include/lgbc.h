@@ -163,7 +163,11 @@ int lgbc_graph_stats(const lgbc_graph *g, lgbc_stats *out);
  *                 graph), so that one batch holds sources with similar
  *                 distance profiles and reaches each vertex at fewer
  *                 distinct levels; 0: batch in the given order.  Results are
- *                 the same up to floating-point summation order. */
+ *                 the same up to floating-point summation order.
+ *   graph_loop    1: run each batch's level loops as CUDA graphs with
+ *                 conditional nodes (the direction choice and the end of a
+ *                 sweep are decided on the device; the host reads the control
+ *                 block once per batch); 0: one host round trip per level. */
 typedef struct lgbc_tuning {
   double alpha;
   double beta;
@@ -172,7 +176,7 @@ typedef struct lgbc_tuning {
   int32_t dense_edges;
   int32_t segment_degree;
   int32_t source_order;
-  int32_t reserved;
+  int32_t graph_loop;
 } lgbc_tuning;
 int lgbc_get_tuning(const lgbc_graph *g, lgbc_tuning *out);
 int lgbc_set_tuning(lgbc_graph *g, const lgbc_tuning *t);

@@ -168,6 +168,34 @@ struct LearnedWorkspace {
   }
 };
 
+// A device-driven level loop instantiated for one configuration.
+struct LoopKey {
+  int backward;                 // 0 forward sweep, 1 backward (dependency) sweep
+  int sigma_kind;
+  unsigned long long act;
+  const int32_t* dist;
+  int64_t dist_ld;
+  const double* bc;
+  MsBuffers b;                  // lane_src and lane_w zeroed: not used inside the loop
+  HubData hd;
+  double alpha, beta;
+};
+struct LoopGraph {
+  LoopKey key;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int td_kernels = 0;           // kernels per top-down / bottom-up / backward level
+  int bu_kernels = 0;
+  int body_kernels = 0;
+  uint64_t last_use = 0;
+  void release() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    exec = nullptr;
+    graph = nullptr;
+  }
+};
+
 }  // namespace
 
 // Lets the other translation units of the library report errors through
@@ -203,7 +231,10 @@ struct lgbc_graph {
   size_t max_smem = 0;
   unsigned long long sigma_limit = ~0ull;  // (2^64 - 1) / (max in-degree + 1)
   lgbc_stats stats{};
-  lgbc_tuning tune{14.0, 24.0, 256, 64, 32, 0, 1, 0};
+  lgbc_tuning tune{14.0, 24.0, 256, 64, 32, 0, 1, 1};
+  cudaStream_t cap_stream = nullptr;  // stream used to capture level-loop graphs
+  std::vector<LoopGraph> loops;       // cached device-driven level loops
+  uint64_t loop_clock = 0;
   std::vector<int32_t> landmarks;   // the highest-degree vertices (source ordering)
   int32_t* d_lmdist = nullptr;      // landmarks x n BFS distances, computed on first use
 
@@ -471,6 +502,189 @@ struct Seeds {
   int64_t nseg = 0;
 };
 
+// ---------------------------------------------------------------------------
+// Device-driven level loops (tuning graph_loop = 1).  A forward sweep is one
+// graph launch: WHILE(loop) { SWITCH(dir) { top-down level | bottom-up level };
+// advance }, where the advance kernel also makes the direction choice and
+// ends the loop when the sweep is done, a list must grow, a path count may
+// overflow, or the level cap is reached.  A backward sweep is a second graph:
+// WHILE(loop) { dependency level; level-- }, then the cleanup kernel.  The host
+// reads the control block once per batch instead of once per level.
+// ---------------------------------------------------------------------------
+#define LOOP_CUDA(call)                                                              \
+  do {                                                                               \
+    cudaError_t e_ = (call);                                                         \
+    if (e_ != cudaSuccess) {                                                         \
+      if (graph) cudaGraphDestroy(graph);                                            \
+      return cuda_fail(e_, #call);                                                   \
+    }                                                                                \
+  } while (0)
+
+// Capture the kernels that `launch(stream)` queues into `into` after `deps`;
+// returns the launch count of the capture.
+template <class F>
+int capture_into(lgbc_graph* g, cudaGraph_t into, const cudaGraphNode_t* deps, size_t ndeps,
+                 F&& launch, int* count) {
+  cudaError_t e = cudaStreamBeginCaptureToGraph(g->cap_stream, into, deps, nullptr, ndeps,
+                                                cudaStreamCaptureModeRelaxed);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamBeginCaptureToGraph");
+  *count = launch(g->cap_stream);
+  cudaGraph_t out = nullptr;
+  e = cudaStreamEndCapture(g->cap_stream, &out);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+  return LGBC_OK;
+}
+
+// The sink node of `graph` (its one node without dependents).
+cudaGraphNode_t last_node(cudaGraph_t graph) {
+  size_t count = 0;
+  if (cudaGraphGetNodes(graph, nullptr, &count) != cudaSuccess || count == 0) return nullptr;
+  std::vector<cudaGraphNode_t> nodes(count);
+  if (cudaGraphGetNodes(graph, nodes.data(), &count) != cudaSuccess) return nullptr;
+  // the nodes without dependents are the sinks; a chain has exactly one
+  for (cudaGraphNode_t nd : nodes) {
+    size_t nout = 0;
+    if (cudaGraphNodeGetDependentNodes(nd, nullptr, nullptr, &nout) == cudaSuccess && nout == 0)
+      return nd;
+  }
+  return nullptr;
+}
+
+int build_loop(lgbc_graph* g, const LoopKey& k, LoopGraph* out) {
+  if (!g->cap_stream) {
+    cudaError_t e = cudaStreamCreateWithFlags(&g->cap_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamCreate (capture)");
+  }
+  cudaGraph_t graph = nullptr;
+  LOOP_CUDA(cudaGraphCreate(&graph, 0));
+  LoopParams lp{};
+  // a handle belongs to the graph that holds its conditional node: `loop` to
+  // the top-level graph, `dir` (forward) to the loop body
+  LOOP_CUDA(cudaGraphConditionalHandleCreate(&lp.loop, graph, 0, cudaGraphCondAssignDefault));
+  lp.n = g->n;
+  lp.nnz = g->nnz;
+  lp.alpha = k.alpha;
+  lp.beta = k.beta;
+  lp.sigma_kind = k.sigma_kind;
+  lp.max_levels = g->n + 1;
+  const DevGraph dg = g->dev();
+  MsBuffers b = k.b;
+  int cnt = 0;
+  // arm
+  int rc = capture_into(g, graph, nullptr, 0,
+                        [&](cudaStream_t cs) {
+                          return k.backward ? loop_back_arm(cs, b, lp) : loop_arm(cs, b, lp);
+                        },
+                        &cnt);
+  if (rc != LGBC_OK) {
+    cudaGraphDestroy(graph);
+    return rc;
+  }
+  cudaGraphNode_t arm = last_node(graph);
+  // WHILE node
+  cudaGraphNodeParams wp{};
+  wp.type = cudaGraphNodeTypeConditional;
+  wp.conditional.handle = lp.loop;
+  wp.conditional.type = cudaGraphCondTypeWhile;
+  wp.conditional.size = 1;
+  cudaGraphNode_t wnode = nullptr;
+  LOOP_CUDA(cudaGraphAddNode(&wnode, graph, &arm, nullptr, 1, &wp));
+  cudaGraph_t body = wp.conditional.phGraph_out[0];
+  if (!k.backward) {
+    LOOP_CUDA(cudaGraphConditionalHandleCreate(&lp.dir, body, 0, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams sp{};
+    sp.type = cudaGraphNodeTypeConditional;
+    sp.conditional.handle = lp.dir;
+    sp.conditional.type = cudaGraphCondTypeSwitch;
+    sp.conditional.size = 2;
+    cudaGraphNode_t snode = nullptr;
+    LOOP_CUDA(cudaGraphAddNode(&snode, body, nullptr, nullptr, 0, &sp));
+    const HubData hd = k.hd;
+    int32_t* dist = const_cast<int32_t*>(k.dist);
+    rc = capture_into(g, sp.conditional.phGraph_out[0], nullptr, 0,
+                      [&](cudaStream_t cs) {
+                        return ms_topdown(g->cfg, cs, dg, b, hd, k.act, k.sigma_kind, dist, k.dist_ld);
+                      },
+                      &out->td_kernels);
+    if (rc == LGBC_OK)
+      rc = capture_into(g, sp.conditional.phGraph_out[1], nullptr, 0,
+                        [&](cudaStream_t cs) {
+                          return ms_bottomup(g->cfg, cs, dg, b, hd, k.act, k.sigma_kind, dist,
+                                             k.dist_ld);
+                        },
+                        &out->bu_kernels);
+    if (rc == LGBC_OK)
+      rc = capture_into(g, body, &snode, 1,
+                        [&](cudaStream_t cs) { return loop_advance(cs, b, lp); }, &cnt);
+  } else {
+    const HubData hd = k.hd;
+    double* bc = const_cast<double*>(k.bc);
+    rc = capture_into(g, body, nullptr, 0,
+                      [&](cudaStream_t cs) {
+                        return ms_backward_body(g->cfg, cs, dg, b, hd, k.sigma_kind, bc) +
+                               loop_back_advance(cs, b, lp);
+                      },
+                      &out->body_kernels);
+    if (rc == LGBC_OK)
+      rc = capture_into(g, graph, &wnode, 1,
+                        [&](cudaStream_t cs) { return ms_cleanup(g->cfg, cs, b); }, &cnt);
+  }
+  if (rc != LGBC_OK) {
+    cudaGraphDestroy(graph);
+    return rc;
+  }
+  cudaGraphExec_t exec = nullptr;
+  LOOP_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+  out->key = k;
+  out->graph = graph;
+  out->exec = exec;
+  return LGBC_OK;
+}
+
+// The cached loop for key k (built on first use; at most 8 are kept).
+int get_loop(lgbc_graph* g, const LoopKey& k, LoopGraph** out) {
+  for (auto& lg : g->loops)
+    if (std::memcmp(&lg.key, &k, sizeof k) == 0) {
+      lg.last_use = ++g->loop_clock;
+      *out = &lg;
+      return LGBC_OK;
+    }
+  if (g->loops.size() >= 8) {
+    auto oldest = std::min_element(g->loops.begin(), g->loops.end(),
+                                   [](const LoopGraph& a, const LoopGraph& b2) {
+                                     return a.last_use < b2.last_use;
+                                   });
+    oldest->release();
+    g->loops.erase(oldest);
+  }
+  LoopGraph lg;
+  LGBC_TRY(build_loop(g, k, &lg));
+  lg.last_use = ++g->loop_clock;
+  g->loops.push_back(lg);
+  *out = &g->loops.back();
+  return LGBC_OK;
+}
+
+LoopKey loop_key(lgbc_graph* g, int backward, int sigma_kind, unsigned long long act,
+                 const int32_t* dist, int64_t ld, const double* bc, const MsBuffers& b,
+                 const HubData& hd) {
+  LoopKey k;
+  std::memset(&k, 0, sizeof k);  // padding bytes take part in the comparison
+  k.backward = backward;
+  k.sigma_kind = sigma_kind;
+  k.act = act;
+  k.dist = dist;
+  k.dist_ld = ld;
+  k.bc = bc;
+  k.b = b;
+  k.b.lane_src = nullptr;
+  k.b.lane_w = nullptr;
+  k.hd = hd;
+  k.alpha = g->tune.alpha;
+  k.beta = g->tune.beta;
+  return k;
+}
+
 // lane_w (sigma batches): per-lane weights of the accumulation into bc.
 // stats (distance-only batches): per-lane distance statistics, accumulated.
 int run_ms_batch(lgbc_graph* g, const int32_t* lane_src, int nl, int sigma_kind, double* bc,
@@ -491,6 +705,43 @@ int run_ms_batch(lgbc_graph* g, const int32_t* lane_src, int nl, int sigma_kind,
     else
       g->launches += ms_init(g->stream, dg, b, nl, sigma_kind, g->sigma_limit, dist, dist_ld);
     LGBC_TRY(check_launch(g));
+    // device-driven loops for plain batches (no weights, statistics or stress)
+    if (g->tune.graph_loop == 1 && !lane_w && !stats && !stress) {
+      LoopGraph* lg = nullptr;
+      LGBC_TRY(get_loop(g, loop_key(g, 0, sigma_kind, act, dist, dist_ld, nullptr, b, hd), &lg));
+      LGBC_CUDA(cudaGraphLaunch(lg->exec, g->stream));
+      LGBC_TRY(check_launch(g));
+      LGBC_TRY(read_ctl(g, b.ctl));
+      const BatchCtl& c = *g->h_ctl;
+      const int64_t lv = static_cast<int64_t>(c.td_levels + c.bu_levels);
+      g->stats.levels += lv;
+      g->stats.topdown_levels += static_cast<int64_t>(c.td_levels);
+      g->stats.bottomup_levels += static_cast<int64_t>(c.bu_levels);
+      g->launches += 1 + lv + static_cast<int64_t>(c.td_levels) * lg->td_kernels +
+                     static_cast<int64_t>(c.bu_levels) * lg->bu_kernels;
+      if (c.runaway) return fail(LGBC_ETIMEOUT, "forward sweep exceeded n + 1 levels");
+      if (c.overflow_sigma && sigma_kind == kSigmaU64) {
+        g->launches += ms_reset_all(g->stream, dg, b);
+        return 1;
+      }
+      if (c.overflow_list) {
+        LGBC_TRY(grow_ms_lists(g));
+        g->launches += ms_reset_all(g->stream, dg, ms_buffers(g, lane_src));
+        continue;
+      }
+      if (sigma_kind == kSigmaNone) {
+        g->launches += ms_cleanup_all(g->cfg, g->stream, b);
+        return check_launch(g);
+      }
+      const int maxl = c.maxlevel;
+      LoopGraph* bg = nullptr;
+      LGBC_TRY(get_loop(g, loop_key(g, 1, sigma_kind, act, nullptr, 0, bc, b, hd), &bg));
+      LGBC_CUDA(cudaGraphLaunch(bg->exec, g->stream));
+      g->launches += 2 + static_cast<int64_t>(maxl + 1) * bg->body_kernels;
+      if (seeds.seg_mark)  // premarked vertices were never listed: clear visit outright
+        LGBC_CUDA(cudaMemsetAsync(b.visit, 0, static_cast<size_t>(g->n) * 8, g->stream));
+      return check_launch(g);
+    }
     bool bu = false;
     bool regrow = false;
     int64_t levels = 0;
@@ -819,6 +1070,9 @@ int lgbc_graph_destroy(lgbc_graph* g) {
   g->bfs.release();
   g->hubs.release();
   g->learned.release();
+  for (auto& lg : g->loops) lg.release();
+  g->loops.clear();
+  if (g->cap_stream) cudaStreamDestroy(g->cap_stream);
   if (g->d_in_rowptr != g->d_rowptr) dev_free(g->d_in_rowptr);
   if (g->d_in_colidx != g->d_colidx) dev_free(g->d_in_colidx);
   dev_free(g->d_rowptr);
@@ -1022,7 +1276,7 @@ int lgbc_set_tuning(lgbc_graph* g, const lgbc_tuning* t) {
   if (!t) return fail(LGBC_EINVAL, "null tuning");
   if (!(t->alpha > 0) || !(t->beta > 0) || t->lanes < 1 || t->lanes > kMaxLanes ||
       t->hub_degree < 1 || t->dense_edges < 0 || t->segment_degree < 0 ||
-      (t->source_order != 0 && t->source_order != 1))
+      (t->source_order != 0 && t->source_order != 1) || (t->graph_loop != 0 && t->graph_loop != 1))
     return fail(LGBC_EINVAL,
                 "tuning out of range (alpha, beta > 0; 1 <= lanes <= 64; hub_degree >= 1; dense_edges >= 0)");
   std::lock_guard<std::mutex> lock(g->mu);
@@ -1597,11 +1851,12 @@ bool tune_from_cache(const char* path, const std::string& sig, lgbc_tuning* out)
   while (std::fgets(line, sizeof line, f)) {
     char key[256];
     lgbc_tuning t{};
-    if (std::sscanf(line, "%255s %lf %lf %d %d %d %d %d", key, &t.alpha, &t.beta, &t.hub_degree,
-                    &t.lanes, &t.dense_edges, &t.segment_degree, &t.source_order) == 8 &&
+    if (std::sscanf(line, "%255s %lf %lf %d %d %d %d %d %d", key, &t.alpha, &t.beta,
+                    &t.hub_degree, &t.lanes, &t.dense_edges, &t.segment_degree, &t.source_order,
+                    &t.graph_loop) == 9 &&
         sig == key && t.alpha > 0 && t.beta > 0 && t.lanes >= 1 && t.lanes <= kMaxLanes &&
         t.hub_degree >= 1 && t.dense_edges >= 0 && t.segment_degree >= 0 &&
-        (t.source_order == 0 || t.source_order == 1)) {
+        (t.source_order == 0 || t.source_order == 1) && (t.graph_loop == 0 || t.graph_loop == 1)) {
       *out = t;  // the last matching line wins
       found = true;
     }
@@ -1697,9 +1952,9 @@ extern "C" int lgbc_tune(lgbc_graph* g, const char* cache_path) {
   if (cache_path) {
     FILE* f = std::fopen(cache_path, "a");
     if (!f) return fail(LGBC_EINVAL, std::string("cannot append to tuning cache ") + cache_path);
-    std::fprintf(f, "%s %.17g %.17g %d %d %d %d %d\n", sig.c_str(), best.alpha, best.beta,
+    std::fprintf(f, "%s %.17g %.17g %d %d %d %d %d %d\n", sig.c_str(), best.alpha, best.beta,
                  best.hub_degree, best.lanes, best.dense_edges, best.segment_degree,
-                 best.source_order);
+                 best.source_order, best.graph_loop);
     std::fclose(f);
   }
   finish_stats(g);

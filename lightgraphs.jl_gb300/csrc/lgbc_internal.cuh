@@ -42,6 +42,9 @@ struct BatchCtl {
   unsigned long long sigma_max;   // largest path count stored this level
   unsigned long long sigma_limit; // (2^64 - 1) / (max in-degree + 1): a level whose
                                   // counts stay <= this cannot overflow the next
+  unsigned long long td_levels;   // levels expanded top-down / bottom-up by a
+  unsigned long long bu_levels;   //   device-driven level loop
+  int runaway;                    // a device-driven loop reached its level cap
 };
 
 // ---------------------------------------------------------------------------

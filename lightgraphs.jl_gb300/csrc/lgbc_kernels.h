@@ -94,6 +94,27 @@ int ms_begin_backward(cudaStream_t s, const MsBuffers& b);
 // Backward (dependency) step for the level in ctl->level, then level--.
 int ms_backward_level(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
                       const HubData& hd, int sigma_kind, double* bc);
+// The same without the final level decrement (the body of a device-driven loop).
+int ms_backward_body(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
+                     const HubData& hd, int sigma_kind, double* bc);
+
+// Device-driven level loops: the control kernels of a CUDA graph whose
+// conditional nodes run the forward levels (WHILE `loop` { SWITCH `dir` })
+// and the backward levels (WHILE `loop`).
+struct LoopParams {
+  cudaGraphConditionalHandle loop;  // 1: run another iteration
+  cudaGraphConditionalHandle dir;   // forward: 0 top-down, 1 bottom-up, 2 none
+  long long n;
+  long long nnz;
+  double alpha;                     // direction-switch thresholds
+  double beta;
+  int sigma_kind;
+  long long max_levels;             // runaway cap (n + 1)
+};
+int loop_arm(cudaStream_t s, const MsBuffers& b, const LoopParams& lp);
+int loop_advance(cudaStream_t s, const MsBuffers& b, const LoopParams& lp);
+int loop_back_arm(cudaStream_t s, const MsBuffers& b, const LoopParams& lp);
+int loop_back_advance(cudaStream_t s, const MsBuffers& b, const LoopParams& lp);
 // Stress step for the level in ctl->level after a distance-only forward
 // sweep (E = 1 + D per (vertex, lane) in the path-count rows), adding the
 // stress of level + 1 into `stress` (wrapping uint64); then level--.

@@ -564,6 +564,9 @@ __global__ void k_ms_init(DevGraph g, MsBuffers b, int nl, unsigned long long ca
   c->mode = 0;
   c->sigma_max = 1;
   c->sigma_limit = sigma_limit;
+  c->td_levels = 0;
+  c->bu_levels = 0;
+  c->runaway = 0;
   b.lvl_off[0] = 0;
   b.lvl_off[1] = tail;
 }
@@ -813,7 +816,60 @@ __global__ void k_ms_clear_front(MsBuffers b) {
     front[b.qv[i]] = 0;
 }
 
-__global__ void k_ms_advance(MsBuffers b, int64_t n) {
+__device__ __forceinline__ void advance_step(const MsBuffers& b, int64_t n);
+
+__global__ void k_ms_advance(MsBuffers b, int64_t n) { advance_step(b, n); }
+
+// Device-driven level loops (CUDA graphs with conditional nodes).  The
+// forward loop is WHILE(loop) { SWITCH(dir) { 0: top-down level, 1:
+// bottom-up level }; k_loop_advance }; the backward loop is WHILE(loop) {
+// dependency level; k_loop_back_advance }.  Handles default to 0 (stop) and
+// are set only by these single-thread kernels; every forward iteration either
+// raises the level or ends the loop, and the level is capped at lp.max_levels,
+// so both loops are bounded.
+// (The direction handle belongs to the loop body and starts every launch at 0:
+// the first level is expanded top-down.)
+__global__ void k_loop_arm(MsBuffers b, LoopParams lp) {
+  const BatchCtl* c = b.ctl;
+  cudaGraphSetConditional(lp.loop, c->done == 0 ? 1u : 0u);
+}
+
+__global__ void k_loop_advance(MsBuffers b, LoopParams lp) {
+  BatchCtl* c = b.ctl;
+  if (c->mode) c->bu_levels += 1; else c->td_levels += 1;
+  advance_step(b, lp.n);
+  bool stop = c->done || c->overflow_list || (lp.sigma_kind == kSigmaU64 && c->overflow_sigma);
+  if (!stop && c->level >= lp.max_levels) {
+    c->runaway = 1;
+    stop = true;
+  }
+  unsigned dir = 2u;
+  if (!stop) {
+    // Beamer's switch on the union of the lanes, as the host-driven loop does
+    const double mf = static_cast<double>(c->mf_cur);
+    const double mu = static_cast<double>(lp.nnz) - static_cast<double>(c->mu_done);
+    const double nf = static_cast<double>(c->hi - c->lo);
+    const bool bu = c->mode ? (nf >= static_cast<double>(lp.n) / lp.beta) : (mf > mu / lp.alpha);
+    c->mode = bu ? 1 : 0;
+    dir = bu ? 1u : 0u;
+  }
+  cudaGraphSetConditional(lp.loop, stop ? 0u : 1u);
+  cudaGraphSetConditional(lp.dir, dir);
+}
+
+__global__ void k_loop_back_arm(MsBuffers b, LoopParams lp) {
+  BatchCtl* c = b.ctl;
+  c->level = c->maxlevel;
+  cudaGraphSetConditional(lp.loop, c->maxlevel >= 0 ? 1u : 0u);
+}
+
+__global__ void k_loop_back_advance(MsBuffers b, LoopParams lp) {
+  BatchCtl* c = b.ctl;
+  c->level -= 1;
+  cudaGraphSetConditional(lp.loop, c->level >= 0 ? 1u : 0u);
+}
+
+__device__ __forceinline__ void advance_step(const MsBuffers& b, int64_t n) {
   BatchCtl* c = b.ctl;
   const int L = c->level;
   b.lvl_off[L + 2] = c->tail;
@@ -1438,6 +1494,9 @@ __global__ void k_ms_init_seeds_ctl(MsBuffers b, long long nseeds, unsigned long
   c->mode = 0;
   c->sigma_max = 1;
   c->sigma_limit = sigma_limit;
+  c->td_levels = 0;
+  c->bu_levels = 0;
+  c->runaway = 0;
   b.lvl_off[0] = 0;
   b.lvl_off[1] = static_cast<unsigned long long>(nseeds);
 }
@@ -1576,7 +1635,14 @@ int ms_begin_backward(cudaStream_t s, const MsBuffers& b) {
 
 int ms_backward_level(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
                       const HubData& hd, int sigma_kind, double* bc) {
-  int launches = 3;
+  const int launches = ms_backward_body(c, s, g, b, hd, sigma_kind, bc);
+  k_ms_back_advance<<<1, 1, 0, s>>>(b);
+  return launches + 1;
+}
+
+int ms_backward_body(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
+                     const HubData& hd, int sigma_kind, double* bc) {
+  int launches = 2;
   k_ms_back_clear<<<c.grid, c.block, 0, s>>>(b);
   // the segmented variant has no weighted finalisation
   const bool seg = hd.segmented && !b.lane_w;
@@ -1599,8 +1665,27 @@ int ms_backward_level(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, con
       ++launches;
     }
   }
-  k_ms_back_advance<<<1, 1, 0, s>>>(b);
   return launches;
+}
+
+int loop_arm(cudaStream_t s, const MsBuffers& b, const LoopParams& lp) {
+  k_loop_arm<<<1, 1, 0, s>>>(b, lp);
+  return 1;
+}
+
+int loop_advance(cudaStream_t s, const MsBuffers& b, const LoopParams& lp) {
+  k_loop_advance<<<1, 1, 0, s>>>(b, lp);
+  return 1;
+}
+
+int loop_back_arm(cudaStream_t s, const MsBuffers& b, const LoopParams& lp) {
+  k_loop_back_arm<<<1, 1, 0, s>>>(b, lp);
+  return 1;
+}
+
+int loop_back_advance(cudaStream_t s, const MsBuffers& b, const LoopParams& lp) {
+  k_loop_back_advance<<<1, 1, 0, s>>>(b, lp);
+  return 1;
 }
 
 int st_backward_level(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,

@@ -1,0 +1,73 @@
+"""Device-driven level loops (CUDA graphs with conditional nodes) give the
+same results as the host-driven loops, through every path that uses them:
+Brandes in both path-count kinds (with the FP64 replay), list growth,
+distance batches, landmarks and the many-graph unions."""
+import numpy as np
+import pytest
+
+import lgbc
+import lgbc.generators as gen
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _both(g, fn):
+    h = g.device_handle()
+    out = []
+    for mode in (0, 1):
+        h.set_tuning(graph_loop=mode)
+        out.append(fn())
+    h.set_tuning(graph_loop=1)
+    return out
+
+
+@pytest.mark.parametrize("kind", ["rmat", "rmat_dir", "ba", "sparse"])
+def test_betweenness_same_with_graph_loops(kind):
+    rng = np.random.default_rng(11)
+    if kind == "rmat":
+        g = gen.rmat(13, 16, seed=5)
+    elif kind == "rmat_dir":
+        g = gen.rmat(13, 8, seed=6, directed=True)
+    elif kind == "ba":
+        g = gen.barabasi_albert(4000, 3, seed=7)
+    else:
+        e = rng.integers(1, 3001, size=(2500, 2))
+        g = lgbc.SimpleGraph.from_edges(3000, [tuple(x) for x in e[e[:, 0] != e[:, 1]].tolist()])
+    src = rng.choice(np.arange(1, g.nv() + 1), 300, replace=False)
+    a, b = _both(g, lambda: lgbc.betweenness_centrality(g, src, endpoints=True))
+    np.testing.assert_allclose(b, a, rtol=1e-12, atol=1e-15)
+    rp, ci = g.csr()
+    kw = {}
+    if g.is_directed():
+        irp, ici = g.in_csr()
+        kw = dict(directed=True, in_rowptr=irp, in_colidx=ici)
+    want = oracle.betweenness_centrality(rp, ci, (src - 1).astype(np.int32), endpoints=True, **kw)
+    np.testing.assert_allclose(b, want, rtol=1e-9, atol=1e-12)
+    d0, d1 = _both(g, lambda: lgbc.multi_gdistances(g, src[:70]))
+    assert np.array_equal(d0, d1)
+
+
+def test_wide_replay_and_list_growth_with_graph_loops():
+    n = 50
+    edges = [(r * n + c + 1, r * n + c + 2) for r in range(n) for c in range(n - 1)]
+    edges += [(r * n + c + 1, (r + 1) * n + c + 1) for r in range(n - 1) for c in range(n)]
+    grid = lgbc.SimpleGraph.from_edges(n * n, edges)
+    a, b = _both(grid, lambda: lgbc.betweenness_centrality(grid, [1, 1250, 2500]))
+    np.testing.assert_allclose(b, a, rtol=1e-12)
+    assert grid.device_handle().stats()["wide_batches"] >= 1
+    path = lgbc.SimpleGraph.from_edges(6000, [(i, i + 1) for i in range(1, 6000)])
+    src = list(range(1, 6001, 97))
+    a, b = _both(path, lambda: lgbc.betweenness_centrality(path, src))
+    np.testing.assert_allclose(b, a, rtol=1e-12)
+    rp, ci = path.csr()
+    np.testing.assert_allclose(b, oracle.betweenness_centrality(rp, ci, np.array(src) - 1),
+                               rtol=1e-9)
+
+
+def test_many_graphs_with_graph_loops():
+    graphs = [gen.barabasi_albert(int(n), 3, seed=50 + i) for i, n in enumerate([300, 450, 800, 1200])]
+    h_default = [lgbc.betweenness_centrality_many(graphs)]
+    for g, got in zip(graphs, h_default[0]):
+        rp, ci = g.csr()
+        np.testing.assert_allclose(got, oracle.betweenness_centrality(rp, ci), rtol=1e-9, atol=1e-12)
