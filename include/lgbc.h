@@ -167,7 +167,11 @@ int lgbc_graph_stats(const lgbc_graph *g, lgbc_stats *out);
  *   graph_loop    1: run each batch's level loops as CUDA graphs with
  *                 conditional nodes (the direction choice and the end of a
  *                 sweep are decided on the device; the host reads the control
- *                 block once per batch); 0: one host round trip per level. */
+ *                 block once per batch); 0: one host round trip per level.
+ *   stack_vertices  small graphs run several source batches at once as a
+ *                 disjoint union of R copies of the graph, each copy holding
+ *                 its own batch of sources, with R * n <= stack_vertices
+ *                 (used when R >= 4; 0 = never).  Default 2^21. */
 typedef struct lgbc_tuning {
   double alpha;
   double beta;
@@ -177,6 +181,8 @@ typedef struct lgbc_tuning {
   int32_t segment_degree;
   int32_t source_order;
   int32_t graph_loop;
+  int32_t stack_vertices;
+  int32_t reserved;
 } lgbc_tuning;
 int lgbc_get_tuning(const lgbc_graph *g, lgbc_tuning *out);
 int lgbc_set_tuning(lgbc_graph *g, const lgbc_tuning *t);

@@ -231,7 +231,10 @@ struct lgbc_graph {
   size_t max_smem = 0;
   unsigned long long sigma_limit = ~0ull;  // (2^64 - 1) / (max in-degree + 1)
   lgbc_stats stats{};
-  lgbc_tuning tune{14.0, 24.0, 256, 64, 32, 0, 1, 1};
+  lgbc_tuning tune{14.0, 24.0, 256, 64, 32, 0, 1, 1, 1 << 21, 0};
+  lgbc_graph* stack = nullptr;        // R copies of this graph (stacked batches)
+  int64_t stack_copies = 0;
+  std::vector<int32_t> h_active;      // the last call's ordered active sources
   cudaStream_t cap_stream = nullptr;  // stream used to capture level-loop graphs
   std::vector<LoopGraph> loops;       // cached device-driven level loops
   uint64_t loop_clock = 0;
@@ -807,9 +810,19 @@ int run_ms_batch(lgbc_graph* g, const int32_t* lane_src, int nl, int sigma_kind,
 // Brandes over the active sources already on the device (g->d_src[0, k)),
 // accumulating into bc_dev (zeroed here); with d_w, source i's dependencies
 // are scaled by d_w[i].
+int run_stacked(lgbc_graph* g, int64_t copies, double* bc_dev);
+
 int run_betweenness(lgbc_graph* g, int64_t k_act, int endpoints, double* bc_dev,
                     const double* d_w = nullptr) {
   g->launches += fill_f64(g->cfg, g->stream, bc_dev, g->n, 0.0);
+  const int lanes0 = std::max(1, std::min<int>(kMaxLanes, g->tune.lanes));
+  const int64_t batches = (k_act + lanes0 - 1) / lanes0;
+  const int64_t copies = g->n > 0 ? std::min<int64_t>(g->tune.stack_vertices / g->n, batches) : 0;
+  if (!d_w && copies >= 4 && static_cast<int64_t>(g->h_active.size()) == k_act) {
+    LGBC_TRY(run_stacked(g, copies, bc_dev));
+    if (endpoints) g->launches += add_endpoints(g->cfg, g->stream, bc_dev, g->n, g->d_src, k_act);
+    return check_launch(g);
+  }
   if (k_act > 0) LGBC_TRY(ensure_ms(g, true));
   const int lanes = std::max(1, std::min<int>(kMaxLanes, g->tune.lanes));
   for (int64_t s0 = 0; s0 < k_act; s0 += lanes) {
@@ -893,6 +906,132 @@ int order_active(lgbc_graph* g, std::vector<int32_t>& act, std::vector<double>* 
   return LGBC_OK;
 }
 
+// Stacked batches for small graphs: the active sources (g->h_active, in
+// their batch order) run as a disjoint union of `copies` copies of the graph;
+// in union batch u, copy r holds the sources of ordinary batch u * copies + r
+// (one lane each, as in lgbc_betweenness_many), lanes without a source in a
+// copy are premarked there, and the copies' raw vectors are summed at the end.
+// Each union batch does the work of `copies` batches with the launches of one.
+int run_stacked(lgbc_graph* g, int64_t copies, double* bc_dev) {
+  const int64_t n = g->n, nnz = g->nnz;
+  const int L = std::max(1, std::min<int>(kMaxLanes, g->tune.lanes));
+  if (!g->stack || g->stack_copies != copies) {
+    if (g->stack) lgbc_graph_destroy(g->stack);
+    g->stack = nullptr;
+    g->stack_copies = 0;
+    // replicate the CSR(s) on the host: copy r holds vertices [r n, (r + 1) n)
+    std::vector<int64_t> rp(static_cast<size_t>(n + 1)), irp;
+    std::vector<int32_t> ci(static_cast<size_t>(nnz)), ici;
+    LGBC_CUDA(cudaMemcpy(rp.data(), g->d_rowptr, rp.size() * 8, cudaMemcpyDeviceToHost));
+    if (nnz) LGBC_CUDA(cudaMemcpy(ci.data(), g->d_colidx, ci.size() * 4, cudaMemcpyDeviceToHost));
+    if (g->directed) {
+      irp.resize(rp.size());
+      ici.resize(ci.size());
+      LGBC_CUDA(cudaMemcpy(irp.data(), g->d_in_rowptr, irp.size() * 8, cudaMemcpyDeviceToHost));
+      if (nnz)
+        LGBC_CUDA(cudaMemcpy(ici.data(), g->d_in_colidx, ici.size() * 4, cudaMemcpyDeviceToHost));
+    }
+    auto replicate = [&](const std::vector<int64_t>& r0, const std::vector<int32_t>& c0,
+                         std::vector<int64_t>& r1, std::vector<int32_t>& c1) {
+      r1.resize(static_cast<size_t>(copies * n + 1));
+      c1.resize(static_cast<size_t>(copies * nnz));
+      for (int64_t r = 0; r < copies; ++r) {
+        for (int64_t v = 0; v < n; ++v) r1[static_cast<size_t>(r * n + v)] = r * nnz + r0[static_cast<size_t>(v)];
+        for (int64_t e = 0; e < nnz; ++e)
+          c1[static_cast<size_t>(r * nnz + e)] = static_cast<int32_t>(r * n + c0[static_cast<size_t>(e)]);
+      }
+      r1[static_cast<size_t>(copies * n)] = copies * nnz;
+    };
+    std::vector<int64_t> srp, sirp;
+    std::vector<int32_t> sci, sici;
+    replicate(rp, ci, srp, sci);
+    if (g->directed) replicate(irp, ici, sirp, sici);
+    lgbc_graph* st = nullptr;
+    LGBC_TRY(lgbc_graph_create(&st, copies * n, copies * nnz, srp.data(), sci.data(),
+                               g->directed ? sirp.data() : nullptr,
+                               g->directed ? sici.data() : nullptr, g->directed));
+    g->stack = st;
+    g->stack_copies = copies;
+  }
+  lgbc_graph* st = g->stack;
+  st->tune = g->tune;
+  st->tune.source_order = 0;
+  st->tune.stack_vertices = 0;
+  LGBC_CUDA(cudaSetDevice(g->device));
+  // seeds and premarks of every union batch
+  const std::vector<int32_t>& act = g->h_active;
+  const int64_t k = static_cast<int64_t>(act.size());
+  const int64_t per = L * copies;
+  const int64_t nbu = (k + per - 1) / per;
+  std::vector<int32_t> sv, sl;
+  std::vector<int64_t> bstart(static_cast<size_t>(nbu + 1), 0), voff(static_cast<size_t>(copies + 1));
+  std::vector<uint64_t> marks(static_cast<size_t>(nbu * copies));
+  std::vector<int64_t> filled(static_cast<size_t>(nbu), 0);  // ordinary batches per union batch
+  for (int64_t r = 0; r <= copies; ++r) voff[static_cast<size_t>(r)] = r * n;
+  for (int64_t u = 0; u < nbu; ++u) {
+    for (int64_t r = 0; r < copies; ++r) {
+      if ((u * copies + r) * L < k) filled[static_cast<size_t>(u)]++;
+      uint64_t seeded = 0;
+      const int64_t i0 = (u * copies + r) * L;
+      for (int l = 0; l < L && i0 + l < k; ++l) {
+        sv.push_back(static_cast<int32_t>(r * n + act[static_cast<size_t>(i0 + l)]));
+        sl.push_back(l);
+        seeded |= 1ull << l;
+      }
+      const uint64_t all = L >= 64 ? ~0ull : ((1ull << L) - 1ull);
+      marks[static_cast<size_t>(u * copies + r)] = all & ~seeded;
+    }
+    bstart[static_cast<size_t>(u + 1)] = static_cast<int64_t>(sv.size());
+  }
+  // one device buffer: voff | marks | seed vertices | seed lanes
+  const size_t bytes = voff.size() * 8 + marks.size() * 8 + sv.size() * 4 + sl.size() * 4 + 16;
+  unsigned char* buf = nullptr;
+  LGBC_TRY(dev_alloc(&buf, bytes));
+  std::unique_ptr<unsigned char, cudaError_t (*)(void*)> guard(buf, cudaFree);
+  int64_t* d_voff = reinterpret_cast<int64_t*>(buf);
+  uint64_t* d_marks = reinterpret_cast<uint64_t*>(d_voff + voff.size());
+  int32_t* d_sv = reinterpret_cast<int32_t*>(d_marks + marks.size());
+  int32_t* d_sl = d_sv + sv.size();
+  LGBC_CUDA(cudaMemcpyAsync(d_voff, voff.data(), voff.size() * 8, cudaMemcpyHostToDevice, st->stream));
+  LGBC_CUDA(cudaMemcpyAsync(d_marks, marks.data(), marks.size() * 8, cudaMemcpyHostToDevice, st->stream));
+  LGBC_CUDA(cudaMemcpyAsync(d_sv, sv.data(), sv.size() * 4, cudaMemcpyHostToDevice, st->stream));
+  LGBC_CUDA(cudaMemcpyAsync(d_sl, sl.data(), sl.size() * 4, cudaMemcpyHostToDevice, st->stream));
+  if (!st->d_bc) LGBC_TRY(dev_alloc(&st->d_bc, static_cast<size_t>(st->n)));
+  st->launches += fill_f64(st->cfg, st->stream, st->d_bc, st->n, 0.0);
+  LGBC_TRY(ensure_ms(st, true));
+  // the caller's stream waits for nothing of ours: order the two streams
+  LGBC_CUDA(cudaStreamSynchronize(g->stream));
+  for (int64_t u = 0; u < nbu; ++u) {
+    Seeds sd;
+    sd.v = d_sv + bstart[static_cast<size_t>(u)];
+    sd.lane = d_sl + bstart[static_cast<size_t>(u)];
+    sd.count = bstart[static_cast<size_t>(u + 1)] - bstart[static_cast<size_t>(u)];
+    sd.seg_off = d_voff;
+    sd.seg_mark = d_marks + static_cast<size_t>(u * copies);
+    sd.nseg = copies;
+    int rc = run_ms_batch(st, nullptr, L, kSigmaU64, st->d_bc, nullptr, 0, sd);
+    if (rc == 1) {
+      g->stats.wide_batches++;
+      rc = run_ms_batch(st, nullptr, L, kSigmaF64, st->d_bc, nullptr, 0, sd);
+    }
+    if (rc != LGBC_OK) {
+      g->launches += st->launches;
+      st->launches = 0;
+      return rc;
+    }
+    g->stats.batches += filled[static_cast<size_t>(u)];  // counted as ordinary batches
+  }
+  LGBC_CUDA(cudaStreamSynchronize(st->stream));
+  g->stats.levels += st->stats.levels;
+  g->stats.topdown_levels += st->stats.topdown_levels;
+  g->stats.bottomup_levels += st->stats.bottomup_levels;
+  st->stats = lgbc_stats{};
+  g->launches += st->launches + 1;
+  st->launches = 0;
+  sum_copies(g->cfg, g->stream, st->d_bc, n, copies, bc_dev);
+  return check_launch(g);
+}
+
 // Host-side part shared by the betweenness entry points: validate, filter
 // degree-0 sources (betweenness.jl:58), order and upload the active list.
 int prepare_sources(lgbc_graph* g, const int32_t* src, int64_t nsrc, int64_t* k_act) {
@@ -909,6 +1048,7 @@ int prepare_sources(lgbc_graph* g, const int32_t* src, int64_t nsrc, int64_t* k_
   }
   LGBC_TRY(order_active(g, active, nullptr));
   *k_act = static_cast<int64_t>(active.size());
+  g->h_active = active;
   LGBC_TRY(ensure_src(g, *k_act));
   if (*k_act > 0)
     LGBC_CUDA(cudaMemcpyAsync(g->d_src, active.data(), active.size() * sizeof(int32_t),
@@ -1072,6 +1212,8 @@ int lgbc_graph_destroy(lgbc_graph* g) {
   g->learned.release();
   for (auto& lg : g->loops) lg.release();
   g->loops.clear();
+  if (g->stack) lgbc_graph_destroy(g->stack);
+  g->stack = nullptr;
   if (g->cap_stream) cudaStreamDestroy(g->cap_stream);
   if (g->d_in_rowptr != g->d_rowptr) dev_free(g->d_in_rowptr);
   if (g->d_in_colidx != g->d_colidx) dev_free(g->d_in_colidx);
@@ -1276,7 +1418,8 @@ int lgbc_set_tuning(lgbc_graph* g, const lgbc_tuning* t) {
   if (!t) return fail(LGBC_EINVAL, "null tuning");
   if (!(t->alpha > 0) || !(t->beta > 0) || t->lanes < 1 || t->lanes > kMaxLanes ||
       t->hub_degree < 1 || t->dense_edges < 0 || t->segment_degree < 0 ||
-      (t->source_order != 0 && t->source_order != 1) || (t->graph_loop != 0 && t->graph_loop != 1))
+      (t->source_order != 0 && t->source_order != 1) || (t->graph_loop != 0 && t->graph_loop != 1) ||
+      t->stack_vertices < 0)
     return fail(LGBC_EINVAL,
                 "tuning out of range (alpha, beta > 0; 1 <= lanes <= 64; hub_degree >= 1; dense_edges >= 0)");
   std::lock_guard<std::mutex> lock(g->mu);
@@ -1851,12 +1994,13 @@ bool tune_from_cache(const char* path, const std::string& sig, lgbc_tuning* out)
   while (std::fgets(line, sizeof line, f)) {
     char key[256];
     lgbc_tuning t{};
-    if (std::sscanf(line, "%255s %lf %lf %d %d %d %d %d %d", key, &t.alpha, &t.beta,
+    if (std::sscanf(line, "%255s %lf %lf %d %d %d %d %d %d %d", key, &t.alpha, &t.beta,
                     &t.hub_degree, &t.lanes, &t.dense_edges, &t.segment_degree, &t.source_order,
-                    &t.graph_loop) == 9 &&
+                    &t.graph_loop, &t.stack_vertices) == 10 &&
         sig == key && t.alpha > 0 && t.beta > 0 && t.lanes >= 1 && t.lanes <= kMaxLanes &&
         t.hub_degree >= 1 && t.dense_edges >= 0 && t.segment_degree >= 0 &&
-        (t.source_order == 0 || t.source_order == 1) && (t.graph_loop == 0 || t.graph_loop == 1)) {
+        (t.source_order == 0 || t.source_order == 1) && (t.graph_loop == 0 || t.graph_loop == 1) &&
+        t.stack_vertices >= 0) {
       *out = t;  // the last matching line wins
       found = true;
     }
@@ -1908,6 +2052,7 @@ extern "C" int lgbc_tune(lgbc_graph* g, const char* cache_path) {
   for (int64_t i = 0; i < k; ++i)
     sample[static_cast<size_t>(i)] = act[static_cast<size_t>(i * static_cast<int64_t>(act.size()) / k)];
   LGBC_TRY(ensure_src(g, k));
+  g->h_active = sample;
   LGBC_CUDA(cudaMemcpyAsync(g->d_src, sample.data(), static_cast<size_t>(k) * 4,
                             cudaMemcpyHostToDevice, g->stream));
   LGBC_CUDA(cudaStreamSynchronize(g->stream));
@@ -1952,9 +2097,9 @@ extern "C" int lgbc_tune(lgbc_graph* g, const char* cache_path) {
   if (cache_path) {
     FILE* f = std::fopen(cache_path, "a");
     if (!f) return fail(LGBC_EINVAL, std::string("cannot append to tuning cache ") + cache_path);
-    std::fprintf(f, "%s %.17g %.17g %d %d %d %d %d %d\n", sig.c_str(), best.alpha, best.beta,
+    std::fprintf(f, "%s %.17g %.17g %d %d %d %d %d %d %d\n", sig.c_str(), best.alpha, best.beta,
                  best.hub_degree, best.lanes, best.dense_edges, best.segment_degree,
-                 best.source_order, best.graph_loop);
+                 best.source_order, best.graph_loop, best.stack_vertices);
     std::fclose(f);
   }
   finish_stats(g);

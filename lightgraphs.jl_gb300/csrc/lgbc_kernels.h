@@ -167,6 +167,9 @@ void set_last_error(const char* msg);
 int validate_csr(const LaunchCfg& c, cudaStream_t s, const int64_t* rowptr, const int32_t* colidx,
                  int64_t n, int64_t nnz, int* bad);
 int fill_i32(const LaunchCfg& c, cudaStream_t s, int32_t* p, int64_t count, int32_t value);
+// out[v] = sum over r < copies of stacked[r * n + v] (a fixed order).
+int sum_copies(const LaunchCfg& c, cudaStream_t s, const double* stacked, int64_t n, int64_t copies,
+               double* out);
 // out[r * nl + j] = dist[j * ld + src[r]] for r < k, j < nl.
 int gather_cols(const LaunchCfg& c, cudaStream_t s, const int32_t* dist, int64_t ld, int nl,
                 const int32_t* src, int64_t k, int32_t* out);

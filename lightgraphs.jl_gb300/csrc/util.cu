@@ -101,6 +101,24 @@ int gather_cols(const LaunchCfg& c, cudaStream_t s, const int32_t* dist, int64_t
   return 1;
 }
 
+namespace {
+__global__ void k_sum_copies(const double* stacked, int64_t n, int64_t copies, double* out) {
+  for (int64_t v = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; v < n;
+       v += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    double acc = 0.0;
+    for (int64_t r = 0; r < copies; ++r) acc += stacked[r * n + v];
+    out[v] = acc;
+  }
+}
+}  // namespace
+
+int sum_copies(const LaunchCfg& c, cudaStream_t s, const double* stacked, int64_t n, int64_t copies,
+               double* out) {
+  if (n <= 0) return 0;
+  k_sum_copies<<<c.grid, c.block, 0, s>>>(stacked, n, copies, out);
+  return 1;
+}
+
 int fill_i32(const LaunchCfg& c, cudaStream_t s, int32_t* p, int64_t count, int32_t value) {
   if (count <= 0) return 0;
   k_fill<int32_t><<<c.grid, c.block, 0, s>>>(p, count, value);

@@ -71,3 +71,44 @@ def test_many_graphs_with_graph_loops():
     for g, got in zip(graphs, h_default[0]):
         rp, ci = g.csr()
         np.testing.assert_allclose(got, oracle.betweenness_centrality(rp, ci), rtol=1e-9, atol=1e-12)
+
+
+@pytest.mark.parametrize("directed,endpoints", [(False, False), (True, True)])
+def test_stacked_batches_match(directed, endpoints):
+    # 2000 vertices: 2^21 / 2000 copies allowed, so every batch of a call runs
+    # in one stacked union; compare with stacking off and with the oracle
+    g = gen.erdos_renyi_nm(2000, 7000, seed=9, directed=directed)
+    rng = np.random.default_rng(4)
+    src = rng.choice(np.arange(1, g.nv() + 1), 900, replace=False)
+    h = g.device_handle()
+    h.set_tuning(stack_vertices=0)
+    a = lgbc.betweenness_centrality(g, src, endpoints=endpoints)
+    h.set_tuning(stack_vertices=1 << 21)
+    b = lgbc.betweenness_centrality(g, src, endpoints=endpoints)
+    assert h.stats()["batches"] >= 1
+    np.testing.assert_allclose(b, a, rtol=1e-9, atol=1e-12)
+    rp, ci = g.csr()
+    kw = {}
+    if directed:
+        irp, ici = g.in_csr()
+        kw = dict(directed=True, in_rowptr=irp, in_colidx=ici)
+    want = oracle.betweenness_centrality(rp, ci, (src - 1).astype(np.int32), endpoints=endpoints,
+                                         **kw)
+    np.testing.assert_allclose(b, want, rtol=1e-9, atol=1e-12)
+    # all vertices, and a lane width that does not divide 64
+    h.set_tuning(lanes=48)
+    c = lgbc.betweenness_centrality(g)
+    h.set_tuning(lanes=64, stack_vertices=0)
+    d = lgbc.betweenness_centrality(g)
+    np.testing.assert_allclose(c, d, rtol=1e-9, atol=1e-12)
+
+
+def test_stacked_grid_replays_in_fp64():
+    n = 40  # corner-to-corner path counts C(78, 39) > 2^64
+    edges = [(r * n + c + 1, r * n + c + 2) for r in range(n) for c in range(n - 1)]
+    edges += [(r * n + c + 1, (r + 1) * n + c + 1) for r in range(n - 1) for c in range(n)]
+    g = lgbc.SimpleGraph.from_edges(n * n, edges)
+    b = lgbc.betweenness_centrality(g)
+    assert g.device_handle().stats()["wide_batches"] >= 1
+    rp, ci = g.csr()
+    np.testing.assert_allclose(b, oracle.betweenness_centrality(rp, ci), rtol=1e-9)
