@@ -246,21 +246,35 @@ __device__ __forceinline__ uint64_t pull_range(const int32_t* __restrict__ ci, i
                                                typename Sig<SK>::T& a0, typename Sig<SK>::T& a1) {
   const int ln = lane_id();
   uint64_t found = 0;
+  if (SK == kSigmaNone) {
+    for (int64_t e = e0; e < e1; e += kWarp) {
+      const int64_t idx = e + ln;
+      if (idx < e1) found |= front[ci[idx]] & want;
+      if (warp_or_u64(found) == want) break;
+    }
+    return warp_or_u64(found);
+  }
+  // software-pipelined: the next chunk's neighbour ids and masks are loaded
+  // before the current chunk's rows are gathered
+  using T = typename Sig<SK>::T;
+  int32_t v = 0;
+  uint64_t f = 0;
+  if (e0 + ln < e1) {
+    v = ci[e0 + ln];
+    f = front[v] & want;
+  }
   for (int64_t e = e0; e < e1; e += kWarp) {
-    const int64_t idx = e + ln;
-    int32_t v = 0;
-    uint64_t f = 0;
-    if (idx < e1) {
-      v = ci[idx];
-      f = front[v] & want;
+    const int64_t nidx = e + kWarp + ln;
+    int32_t vn = 0;
+    uint64_t fn = 0;
+    if (nidx < e1) {
+      vn = ci[nidx];
+      fn = front[vn] & want;
     }
     found |= f;
-    if (SK == kSigmaNone) {
-      if (warp_or_u64(found) == want) break;
-      continue;
-    }
-    using T = typename Sig<SK>::T;
     gather_chunk<T, T>(v, f, reinterpret_cast<const T*>(sigma), dense, a0, a1);
+    v = vn;
+    f = fn;
   }
   return warp_or_u64(found);
 }
@@ -268,20 +282,30 @@ __device__ __forceinline__ uint64_t pull_range(const int32_t* __restrict__ ci, i
 // Dependency gather over out-edges [e0, e1) of v at level L: for every
 // out-neighbour w, g = succ[w] & F marks the lanes for which w is a DAG
 // successor; their psi = (1 + delta[w]) / sigma[w] are summed.
+// (Software-pipelined like pull_range: the next chunk's ids and masks are in
+// flight while the current chunk's rows are gathered.)
 __device__ __forceinline__ void psi_range_df(const int32_t* __restrict__ ci, int64_t e0, int64_t e1,
                                              uint64_t F, const uint64_t* __restrict__ succ,
                                              const void* __restrict__ psi, int dense, df32& acc0,
                                              df32& acc1) {
   const int ln = lane_id();
+  int32_t w = 0;
+  uint64_t gm = 0;
+  if (e0 + ln < e1) {
+    w = ci[e0 + ln];
+    gm = succ[w] & F;
+  }
   for (int64_t e = e0; e < e1; e += kWarp) {
-    const int64_t idx = e + ln;
-    int32_t w = 0;
-    uint64_t gm = 0;
-    if (idx < e1) {
-      w = ci[idx];
-      gm = succ[w] & F;
+    const int64_t nidx = e + kWarp + ln;
+    int32_t wn = 0;
+    uint64_t gn = 0;
+    if (nidx < e1) {
+      wn = ci[nidx];
+      gn = succ[wn] & F;
     }
     gather_chunk<float2, df32>(w, gm, reinterpret_cast<const float2*>(psi), dense, acc0, acc1);
+    w = wn;
+    gm = gn;
   }
   acc0 = acc_done(acc0);
   acc1 = acc_done(acc1);
@@ -292,15 +316,23 @@ __device__ __forceinline__ void psi_range_f64(const int32_t* __restrict__ ci, in
                                               const void* __restrict__ psi, int dense,
                                               double& acc0, double& acc1) {
   const int ln = lane_id();
+  int32_t w = 0;
+  uint64_t gm = 0;
+  if (e0 + ln < e1) {
+    w = ci[e0 + ln];
+    gm = succ[w] & F;
+  }
   for (int64_t e = e0; e < e1; e += kWarp) {
-    const int64_t idx = e + ln;
-    int32_t w = 0;
-    uint64_t gm = 0;
-    if (idx < e1) {
-      w = ci[idx];
-      gm = succ[w] & F;
+    const int64_t nidx = e + kWarp + ln;
+    int32_t wn = 0;
+    uint64_t gn = 0;
+    if (nidx < e1) {
+      wn = ci[nidx];
+      gn = succ[wn] & F;
     }
     gather_chunk<double, double>(w, gm, reinterpret_cast<const double*>(psi), dense, acc0, acc1);
+    w = wn;
+    gm = gn;
   }
 }
 
