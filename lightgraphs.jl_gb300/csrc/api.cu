@@ -1487,6 +1487,62 @@ struct ManyGraph {
   int64_t out_off;        // position of its first vertex in bc_raw_out
 };
 
+// Source ordering inside a union of graphs: graph k's active sources are
+// sorted by their BFS distances to graph k's own kLandmarks highest-degree
+// vertices (one seeded kLandmarks-lane distance batch serves every graph of
+// the union at once), so that a batch lane pairs sources with similar
+// distance profiles in every component, as order_active does for one graph.
+int order_many(lgbc_graph* g, const std::vector<ManyGraph>& grp, const std::vector<int64_t>& voff,
+               std::vector<std::vector<int32_t>>& act) {
+  const int nl = kLandmarks;
+  std::vector<int32_t> sv, sl;
+  for (size_t k = 0; k < grp.size(); ++k) {
+    std::vector<std::pair<int64_t, int32_t>> deg;
+    for (int64_t v = 0; v < grp[k].n; ++v) {
+      const int64_t d = grp[k].rowptr[v + 1] - grp[k].rowptr[v];
+      if (d > 0) deg.emplace_back(-d, static_cast<int32_t>(v));
+    }
+    const size_t top = std::min<size_t>(deg.size(), static_cast<size_t>(nl));
+    std::partial_sort(deg.begin(), deg.begin() + static_cast<std::ptrdiff_t>(top), deg.end());
+    for (size_t j = 0; j < top; ++j) {
+      sv.push_back(static_cast<int32_t>(voff[k] + deg[j].second));
+      sl.push_back(static_cast<int32_t>(j));
+    }
+  }
+  if (sv.empty()) return LGBC_OK;
+  const int64_t N = g->n;
+  LGBC_TRY(ensure_ms(g, false));
+  int32_t* d_dist = nullptr;  // nl x N distances | seeds | lanes
+  LGBC_TRY(dev_alloc(&d_dist, static_cast<size_t>(nl) * static_cast<size_t>(N) + 2 * sv.size()));
+  std::unique_ptr<int32_t, cudaError_t (*)(void*)> guard(d_dist, cudaFree);
+  int32_t* d_sv = d_dist + static_cast<int64_t>(nl) * N;
+  int32_t* d_sl = d_sv + sv.size();
+  LGBC_CUDA(cudaMemcpyAsync(d_sv, sv.data(), sv.size() * 4, cudaMemcpyHostToDevice, g->stream));
+  LGBC_CUDA(cudaMemcpyAsync(d_sl, sl.data(), sl.size() * 4, cudaMemcpyHostToDevice, g->stream));
+  g->launches += fill_i32(g->cfg, g->stream, d_dist, static_cast<int64_t>(nl) * N, kUnreached);
+  Seeds sd;
+  sd.v = d_sv;
+  sd.lane = d_sl;
+  sd.count = static_cast<int64_t>(sv.size());
+  LGBC_TRY(run_ms_batch(g, nullptr, nl, kSigmaNone, nullptr, d_dist, N, sd));
+  std::vector<int32_t> dist(static_cast<size_t>(nl) * static_cast<size_t>(N));
+  LGBC_CUDA(cudaMemcpyAsync(dist.data(), d_dist, dist.size() * 4, cudaMemcpyDeviceToHost, g->stream));
+  LGBC_CUDA(cudaStreamSynchronize(g->stream));
+  for (size_t k = 0; k < grp.size(); ++k) {
+    auto& a = act[k];
+    const int64_t base = voff[k];
+    std::stable_sort(a.begin(), a.end(), [&](int32_t x, int32_t y) {
+      for (int j = 0; j < nl; ++j) {
+        const int32_t dx = dist[static_cast<size_t>(j) * N + base + x];
+        const int32_t dy = dist[static_cast<size_t>(j) * N + base + y];
+        if (dx != dy) return dx < dy;
+      }
+      return x < y;
+    });
+  }
+  return LGBC_OK;
+}
+
 int many_group(const std::vector<ManyGraph>& grp, int endpoints, double* bc_raw_out) {
   // union CSR on the host
   int64_t N = 0, NNZ = 0;
@@ -1518,31 +1574,34 @@ int many_group(const std::vector<ManyGraph>& grp, int endpoints, double* bc_raw_
   std::unique_ptr<lgbc_graph, int (*)(lgbc_graph*)> guard(g, lgbc_graph_destroy);
   std::lock_guard<std::mutex> lock(g->mu);
 
-  // seeds of every batch, and the endpoint terms
-  int64_t maxn = 0;
-  for (const auto& m : grp) maxn = std::max(maxn, m.n);
+  // every graph's active sources (degree > 0), and the endpoint terms
+  std::vector<std::vector<int32_t>> act(grp.size());
   std::vector<int32_t> sv, sl, act_src;
   std::vector<double> seg_add(grp.size()), src_add;
+  int64_t maxa = 0;
   for (size_t k = 0; k < grp.size(); ++k) {
-    int64_t a = 0;
     for (int64_t v = 0; v < grp[k].n; ++v)
       if (g->has_degree[static_cast<size_t>(voff[k] + v)]) {
-        ++a;
+        act[k].push_back(static_cast<int32_t>(v));
         act_src.push_back(static_cast<int32_t>(voff[k] + v));
         src_add.push_back(static_cast<double>(grp[k].n) - 2.0);
       }
-    seg_add[k] = static_cast<double>(a);
+    seg_add[k] = static_cast<double>(act[k].size());
+    maxa = std::max<int64_t>(maxa, static_cast<int64_t>(act[k].size()));
   }
-  const int64_t nb = (maxn + kMaxLanes - 1) / kMaxLanes;
+  if (g->tune.source_order == 1 && maxa > kMaxLanes)
+    LGBC_TRY(order_many(g, grp, voff, act));
+  // batch b, lane l holds the (64 b + l)-th ordered source of every graph
+  const int64_t nb = (maxa + kMaxLanes - 1) / kMaxLanes;
   std::vector<int64_t> bstart(static_cast<size_t>(nb + 1), 0);
   std::vector<uint64_t> marks(static_cast<size_t>(nb) * grp.size());
   for (int64_t b = 0; b < nb; ++b) {
     for (size_t k = 0; k < grp.size(); ++k) {
       uint64_t seeded = 0;
       for (int l = 0; l < kMaxLanes; ++l) {
-        const int64_t s = b * kMaxLanes + l;
-        if (s < grp[k].n && g->has_degree[static_cast<size_t>(voff[k] + s)]) {
-          sv.push_back(static_cast<int32_t>(voff[k] + s));
+        const int64_t i = b * kMaxLanes + l;
+        if (i < static_cast<int64_t>(act[k].size())) {
+          sv.push_back(static_cast<int32_t>(voff[k] + act[k][static_cast<size_t>(i)]));
           sl.push_back(l);
           seeded |= 1ull << l;
         }
