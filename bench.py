@@ -553,6 +553,33 @@ def run_reference_many(args, nthreads: int):
     }), flush=True)
 
 
+def run_c5_kernels(args):
+    """The learned proposal's kernels on one graph (for profiling): core
+    numbers and features, the MLP forward over every vertex with the softmax
+    CDF, and one training gradient over 65,536 rows; GPU times by CUDA events."""
+    import lgbc
+    from lgbc import compare
+    from lgbc import generators as G
+    g = G.rmat(args.scale, 16, seed=1)
+    with compare._Timer(g) as tf:
+        f = lgbc.features(g)
+    passes = g.device_handle().stats()["levels"]
+    m = lgbc.SourceProposal(seed=0)
+    m.set_norm(f.mean(0), np.maximum(f.std(0), 1e-6))
+    with compare._Timer(g) as tb:
+        m.build(g, 0.1)
+    rows = min(65536, g.nv())
+    x = f[:rows]
+    t = np.log1p(np.arange(rows, dtype=np.float32) % 97)
+    t0 = time.perf_counter()
+    m.grad(x, t)
+    grad_s = time.perf_counter() - t0
+    print(json.dumps({"c5_kernels": {"n": g.nv(), "m": g.ne(), "features_ms": tf.ms,
+                                     "core_passes": passes, "proposal_build_ms": tb.ms,
+                                     "grad_rows": rows, "grad_call_ms": grad_s * 1e3}}), flush=True)
+    m.close()
+
+
 def run_c5(args, dist: Dist):
     """Config C5: train the proposal on 128 R-MAT scale-14 + 128 BA graphs,
     then compare uniform and learned sampling against exact BC on (a) the
@@ -659,6 +686,8 @@ def main():
     ap.add_argument("--c5-seeds", type=int, default=8)
     ap.add_argument("--c5-ball-scale", type=int, default=24, help="c5: 0 skips the ball graph")
     ap.add_argument("--c5-ball", type=int, default=100000)
+    ap.add_argument("--c5-kernels", action="store_true",
+                    help="c5: only run the proposal's kernels once on R-MAT --scale (profiling)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0,
                     help="approximate CPU-baseline sample length")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
@@ -669,6 +698,8 @@ def main():
     try:
         if args.impl == "reference":
             run_reference(args, dist)
+        elif args.workload == "c5" and args.c5_kernels:
+            run_c5_kernels(args)
         elif args.workload == "c5":
             run_c5(args, dist)
         else:
