@@ -442,7 +442,9 @@ def run_ours(args, dist: Dist):
     t_step = t_dev / args.steps
     abytes = bc_algorithmic_bytes(n, nnz, k_act)
     achieved = abytes / t_step / 1e9
-    traffic = traffic_per_step()
+    # the committed capture is of the default workload (R-MAT 20, k = 4096) only
+    traffic = (traffic_per_step() if args.workload == "c2" and args.scale == 20
+               and len(src) == 4096 else None)
 
     # ---- CPU baseline (rank 0, N = 1 only) -------------------------------------------
     cpu = None

@@ -236,9 +236,9 @@ int lgbc_gdistances_noalloc(int64_t n, int64_t nnz, const int64_t *rowptr,
  *
  * Undirected graphs only for the features and the proposal. */
 
-/* Core numbers, as core_number(g) (src/degeneracy.jl:38-80): LGBC_EINVAL
- * for a directed graph or one with a self-loop (the reference throws
- * ArgumentError for self-loops).  core_out: n int32. */
+/* Core numbers, as core_number(g) (src/degeneracy.jl:38-96; for a digraph
+ * every arc counts at both ends, degree = out + in): LGBC_EINVAL for a graph
+ * with a self-loop (the reference throws ArgumentError).  core_out: n int32. */
 int lgbc_core_number(lgbc_graph *g, int32_t *core_out);
 
 /* Per-vertex features, n x 4 float32 row-major: log(1 + degree),

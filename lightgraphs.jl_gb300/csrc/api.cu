@@ -1842,7 +1842,6 @@ int lgbc_core_number(lgbc_graph* g, int32_t* core_out) {
   LGBC_TRY(check_graph(g));
   std::lock_guard<std::mutex> lock(g->mu);
   LGBC_TRY(use_device(g));
-  LGBC_TRY(need_undirected(g, "core_number"));
   if (!core_out && g->n > 0) return fail(LGBC_EINVAL, "null output");
   reset_stats(g);
   if (g->n == 0) return LGBC_OK;

@@ -30,31 +30,63 @@ __device__ __forceinline__ long long nwarps() {
 // Degrees and core numbers
 // ---------------------------------------------------------------------------
 
-// deg[v] = neighbours of v other than v itself; *loops |= 1 when v has a
-// self-loop.  One warp per vertex.
+// For a digraph the core decomposition counts every arc at both ends
+// (degree = out + in, src/degeneracy.jl:41,63-96), so a vertex's neighbour
+// multiset is its out-list followed by its in-list; an undirected graph's
+// in-lists alias its out-lists and only those are walked.
+__device__ __forceinline__ bool is_digraph(const DevGraph& g) { return g.in_colidx != g.colidx; }
+
+// deg[v] = neighbour-list entries of v other than v itself; *loops |= 1 when
+// v has a self-loop.  One warp per vertex.
 __global__ void __launch_bounds__(256) k_core_degree(DevGraph g, int32_t* deg, int* loops) {
   const int ln = lane_id();
+  const bool dir = is_digraph(g);
   for (long long v = gwarp(); v < g.n; v += nwarps()) {
     const int64_t e0 = g.rowptr[v], e1 = g.rowptr[v + 1];
+    int64_t total = e1 - e0;
     int self = 0;
     for (int64_t e = e0 + ln; e < e1; e += kWarp) self += g.colidx[e] == v ? 1 : 0;
+    if (dir) {
+      const int64_t i0 = g.in_rowptr[v], i1 = g.in_rowptr[v + 1];
+      total += i1 - i0;
+      for (int64_t e = i0 + ln; e < i1; e += kWarp) self += g.in_colidx[e] == v ? 1 : 0;
+    }
     self = __reduce_add_sync(kFull, self);
     if (ln == 0) {
-      deg[v] = static_cast<int32_t>(e1 - e0 - self);
+      deg[v] = static_cast<int32_t>(total - self);
       if (self) atomicOr(loops, 1);
     }
   }
 }
 
-// Neighbours u != v of v with core[u] >= h (warp-wide count).
-__device__ __forceinline__ int count_at_least(const DevGraph& g, int64_t e0, int64_t e1, int32_t v,
-                                              const int32_t* core, int32_t h) {
+// Neighbour entries u != v of v with core[u] >= h (warp-wide count).
+__device__ __forceinline__ int count_at_least(const DevGraph& g, int32_t v, const int32_t* core,
+                                              int32_t h) {
   int c = 0;
-  for (int64_t e = e0 + lane_id(); e < e1; e += kWarp) {
+  for (int64_t e = g.rowptr[v] + lane_id(); e < g.rowptr[v + 1]; e += kWarp) {
     const int32_t u = g.colidx[e];
     c += (u != v && core[u] >= h) ? 1 : 0;
   }
+  if (is_digraph(g))
+    for (int64_t e = g.in_rowptr[v] + lane_id(); e < g.in_rowptr[v + 1]; e += kWarp) {
+      const int32_t u = g.in_colidx[e];
+      c += (u != v && core[u] >= h) ? 1 : 0;
+    }
   return __reduce_add_sync(kFull, c);
+}
+
+// Flag the neighbours u != v of v whose value is above lo.
+__device__ __forceinline__ void flag_above(const DevGraph& g, int32_t v, const int32_t* core,
+                                           int32_t lo, uint8_t* flag) {
+  for (int64_t e = g.rowptr[v] + lane_id(); e < g.rowptr[v + 1]; e += kWarp) {
+    const int32_t u = g.colidx[e];
+    if (u != v && core[u] > lo) flag[u] = 1;
+  }
+  if (is_digraph(g))
+    for (int64_t e = g.in_rowptr[v] + lane_id(); e < g.in_rowptr[v + 1]; e += kWarp) {
+      const int32_t u = g.in_colidx[e];
+      if (u != v && core[u] > lo) flag[u] = 1;
+    }
 }
 
 // One h-index pass over the vertices of `list` (all vertices when list is
@@ -71,24 +103,20 @@ __global__ void __launch_bounds__(256) k_core_pass(DevGraph g, const int32_t* li
     const int32_t v = list ? list[i] : static_cast<int32_t>(i);
     const int32_t c = core[v];
     if (c == 0) continue;
-    const int64_t e0 = g.rowptr[v], e1 = g.rowptr[v + 1];
-    const int cnt = count_at_least(g, e0, e1, v, core, c);
+    const int cnt = count_at_least(g, v, core, c);
     if (cnt >= c) continue;
     // h-index: the largest h with count(>= h) >= h.  count(>= cnt) >=
     // count(>= c) = cnt, so h lies in [cnt, c - 1].
     int lo = cnt, hi = c - 1;
     while (lo < hi) {
       const int mid = (lo + hi + 1) >> 1;
-      if (count_at_least(g, e0, e1, v, core, mid) >= mid) lo = mid; else hi = mid - 1;
+      if (count_at_least(g, v, core, mid) >= mid) lo = mid; else hi = mid - 1;
     }
     if (ln == 0) {
       core[v] = lo;
       atomicAdd(changed, 1ull);
     }
-    for (int64_t e = e0 + ln; e < e1; e += kWarp) {
-      const int32_t u = g.colidx[e];
-      if (u != v && core[u] > lo) flag[u] = 1;
-    }
+    flag_above(g, v, core, lo, flag);
   }
 }
 

@@ -306,8 +306,8 @@ function has_path(g::Union{SimpleGraph,SimpleDiGraph}, u::Integer, v::Integer;
     return r[] != 0
 end
 
-"""GPU drop-in for `LightGraphs.core_number` (undirected graphs)."""
-function core_number(g::SimpleGraph{T}) where {T}
+"""GPU drop-in for `LightGraphs.core_number`."""
+function core_number(g::Union{SimpleGraph{T},SimpleDiGraph{T}}) where {T}
     c = Vector{Int32}(undef, nv(g))
     d = device_graph(g)
     GC.@preserve c begin

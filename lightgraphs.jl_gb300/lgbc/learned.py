@@ -41,10 +41,9 @@ def _need_undirected(g, what: str) -> None:
 
 
 def core_number(g) -> np.ndarray:
-    """core_number(g) (src/degeneracy.jl:38-80) on the GPU: int32 vector
-    indexed by vertex - 1.  Raises ArgumentError for a graph with self-loops,
-    as the reference does."""
-    _need_undirected(g, "core_number")
+    """core_number(g) (src/degeneracy.jl:38-96) on the GPU: int32 vector
+    indexed by vertex - 1 (digraphs: arcs count at both ends).  Raises
+    ArgumentError for a graph with self-loops, as the reference does."""
     out = np.empty(g.nv(), np.int32)
     if g.nv() == 0:
         return out

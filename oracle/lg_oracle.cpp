@@ -467,17 +467,22 @@ int orc_stress(int64_t n, const int64_t* rowptr, const int32_t* colidx,
 }
 
 // core_number(g) for a graph without self-loops: the bin-sort cores
-// decomposition of Batagelj & Zaversnik (2003) as in src/degeneracy.jl:38-80,
-// with degree(g, v) = length(fadjlist[v]) (undirected).  Returns -1 when a
-// self-loop is present (the reference throws ArgumentError, :39).
-int orc_core_number(int64_t n, const int64_t* rowptr, const int32_t* colidx, int32_t* core) {
+// decomposition of Batagelj & Zaversnik (2003) as in src/degeneracy.jl:38-96,
+// with degree(g, v) = out + in degree for a digraph, whose in-neighbours are
+// relaxed after the out-neighbours.  Returns -1 when a self-loop is present
+// (the reference throws ArgumentError, :39).
+int orc_core_number(int64_t n, const int64_t* rowptr, const int32_t* colidx,
+                    const int64_t* in_rowptr, const int32_t* in_colidx, int directed,
+                    int32_t* core) {
+  if (directed && (!in_rowptr || !in_colidx)) return -1;
   for (int64_t v = 0; v < n; ++v)
     for (int64_t e = rowptr[v]; e < rowptr[v + 1]; ++e)
       if (colidx[e] == v) return -1;
   std::vector<int64_t> deg(n), pos(n), vert(n);
   int64_t maxdeg = 0;
   for (int64_t v = 0; v < n; ++v) {
-    deg[v] = rowptr[v + 1] - rowptr[v];
+    // degree(g, v): out + in for a digraph (src/core.jl:66)
+    deg[v] = rowptr[v + 1] - rowptr[v] + (directed ? in_rowptr[v + 1] - in_rowptr[v] : 0);
     maxdeg = std::max(maxdeg, deg[v]);
   }
   std::vector<int64_t> bin(maxdeg + 1, 0);
@@ -495,10 +500,9 @@ int orc_core_number(int64_t n, const int64_t* rowptr, const int32_t* colidx, int
   }
   for (int64_t d = maxdeg; d >= 1; --d) bin[d] = bin[d - 1];
   if (maxdeg >= 0) bin[0] = 0;
-  for (int64_t i = 0; i < n; ++i) {
-    const int64_t v = vert[i];
-    for (int64_t e = rowptr[v]; e < rowptr[v + 1]; ++e) {
-      const int64_t u = colidx[e];
+  auto relax = [&](int64_t v, const int64_t* rp, const int32_t* ci) {
+    for (int64_t e = rp[v]; e < rp[v + 1]; ++e) {
+      const int64_t u = ci[e];
       if (deg[u] > deg[v]) {
         const int64_t du = deg[u], pu = pos[u], pw = bin[du], w = vert[pw];
         if (u != w) {
@@ -511,6 +515,11 @@ int orc_core_number(int64_t n, const int64_t* rowptr, const int32_t* colidx, int
         deg[u]--;
       }
     }
+  };
+  for (int64_t i = 0; i < n; ++i) {
+    const int64_t v = vert[i];
+    relax(v, rowptr, colidx);                          // outneighbors, :63-79
+    if (directed) relax(v, in_rowptr, in_colidx);      // inneighbors, :80-95
   }
   for (int64_t v = 0; v < n; ++v) core[v] = static_cast<int32_t>(deg[v]);
   return 0;

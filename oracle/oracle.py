@@ -76,7 +76,7 @@ def _load():
         lib.orc_dependency.restype = ctypes.c_int
         lib.orc_stress.argtypes = [i64, p, p, p, p, ctypes.c_int, p, i64, p]
         lib.orc_stress.restype = ctypes.c_int
-        lib.orc_core_number.argtypes = [i64, p, p, p]
+        lib.orc_core_number.argtypes = [i64, p, p, p, p, ctypes.c_int, p]
         lib.orc_core_number.restype = ctypes.c_int
         _lib = lib
         return lib
@@ -186,13 +186,18 @@ def dependency(rowptr, colidx, sources, weights=None, *, directed=False, in_rowp
     return mass, bcw
 
 
-def core_number(rowptr, colidx) -> np.ndarray:
-    """core_number(g) (src/degeneracy.jl:38-80) of an undirected graph."""
+def core_number(rowptr, colidx, *, directed=False, in_rowptr=None, in_colidx=None) -> np.ndarray:
+    """core_number(g) (src/degeneracy.jl:38-96)."""
     lib = _load()
     rowptr, colidx = _csr(rowptr, colidx)
     n = len(rowptr) - 1
+    if directed:
+        in_rowptr, in_colidx = _csr(in_rowptr, in_colidx)
+    else:
+        in_rowptr = in_colidx = None
     out = np.empty(n, np.int32)
-    if lib.orc_core_number(n, _ptr(rowptr), _ptr(colidx), _ptr(out)) != 0:
+    if lib.orc_core_number(n, _ptr(rowptr), _ptr(colidx), _ptr(in_rowptr), _ptr(in_colidx),
+                           int(bool(directed)), _ptr(out)) != 0:
         raise ValueError("core_number: graph must not have self-loops")
     return out
 

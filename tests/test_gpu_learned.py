@@ -58,8 +58,13 @@ def test_core_number_doc_example_and_errors():
     assert lgbc.core_number(g).tolist() == [1, 2, 2, 2, 2, 0]
     with pytest.raises(lgbc.ArgumentError):
         lgbc.core_number(lgbc.SimpleGraph.from_edges(3, [(1, 1), (1, 2)]))
+    d = _random_graph(800, 4000, 12, directed=True)
+    rp, ci = d.csr()
+    irp, ici = d.in_csr()
+    np.testing.assert_array_equal(
+        lgbc.core_number(d), oracle.core_number(rp, ci, directed=True, in_rowptr=irp, in_colidx=ici))
     with pytest.raises(lgbc.MethodError):
-        lgbc.core_number(lgbc.SimpleDiGraph.from_edges(3, [(1, 2)]))
+        lgbc.features(d)
 
 
 @pytest.mark.parametrize("name", ["er", "rmat12", "ba", "star"])

@@ -51,6 +51,24 @@ def test_core_number_matches_networkx(seed):
     assert oracle.core_number(rp, ci).tolist() == [want[v] for v in range(300)]
 
 
+@pytest.mark.parametrize("seed", [4, 5])
+def test_directed_core_number_matches_networkx(seed):
+    # digraph: degree = out + in, reciprocal arcs count twice (src/degeneracy.jl:41,91-96);
+    # networkx defines directed core numbers with the same in + out degree
+    nx = pytest.importorskip("networkx")
+    g = _random_graph(250, 1200, seed, directed=True)
+    rp, ci = g.csr()
+    irp, ici = g.in_csr()
+    G = nx.DiGraph()
+    G.add_nodes_from(range(250))
+    for v in range(250):
+        for u in ci[rp[v]:rp[v + 1]]:
+            G.add_edge(v, int(u))
+    want = nx.core_number(G)
+    got = oracle.core_number(rp, ci, directed=True, in_rowptr=irp, in_colidx=ici)
+    assert got.tolist() == [want[v] for v in range(250)]
+
+
 @pytest.mark.parametrize("directed", [False, True])
 def test_dependency_mass_identity(directed):
     # sum_v delta_s(v) = sum over reached t != s of (d(s, t) - 1)
@@ -121,7 +139,7 @@ def test_learned_calls_fail_loudly_without_gpu():
         lgbc.core_number(g)
     with pytest.raises(lgbc.LGBCError):
         lgbc.SourceProposal()
-    with pytest.raises(lgbc.MethodError):
+    with pytest.raises(lgbc.LGBCError):
         lgbc.core_number(lgbc.SimpleDiGraph.from_edges(3, [(1, 2)]))
 
 
