@@ -353,6 +353,21 @@ int lgbc_proposal_build(lgbc_graph *g, lgbc_mlp *m, double eps, double *p_out);
 int lgbc_proposal_sample(lgbc_graph *g, int64_t k, uint64_t seed, int scheme, int32_t *src_out,
                          double *w_out);
 
+/* Graph ingest on the device: a handle built from a 0-based edge list
+ * (src[i], dst[i]), i < m, with the storage semantics of add_edge! on
+ * SimpleGraph / SimpleDiGraph (src/SimpleGraphs/simplegraph.jl:445-461,
+ * simpledigraph.jl:414-429): neighbour lists sorted, duplicates dropped, an
+ * undirected edge stored in both lists and an undirected self-loop once.  The
+ * arcs are radix-sorted on the GPU; only the edge list crosses to the device.
+ * LGBC_EINVAL for an endpoint outside [0, n). */
+int lgbc_graph_create_from_edges(lgbc_graph **out, int64_t n, int64_t m, const int32_t *src,
+                                 const int32_t *dst, int directed);
+/* Copy a handle's CSR to the host: rowptr (n + 1 int64), colidx (nnz int32)
+ * and, for a digraph, the in-CSR; any pointer may be NULL (nnz from
+ * lgbc_graph_info). */
+int lgbc_graph_csr(const lgbc_graph *g, int64_t *rowptr, int32_t *colidx, int64_t *in_rowptr,
+                   int32_t *in_colidx);
+
 /* Device / pinned-host memory helpers for callers without their own CUDA
  * allocator (bench and test harnesses).  lgbc_memcpy kinds: 1 = host to
  * device, 2 = device to host, 3 = device to device. */

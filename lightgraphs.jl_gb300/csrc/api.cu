@@ -1066,11 +1066,10 @@ void reset_stats(lgbc_graph* g) {
 void finish_stats(lgbc_graph* g) { g->stats.kernel_launches = g->launches - g->stats.kernel_launches; }
 
 // Fills a freshly constructed handle; on failure the caller destroys it.
-int create_impl(lgbc_graph* g, int64_t n, int64_t nnz, const int64_t* rowptr, const int32_t* colidx,
-                const int64_t* in_rowptr, const int32_t* in_colidx, int directed) {
+// Device, stream, events and launch shape of a new handle.
+int init_handle(lgbc_graph* g, int64_t n, int directed) {
   LGBC_CUDA(cudaGetDevice(&g->device));
   g->n = n;
-  g->nnz = nnz;
   g->directed = directed ? 1 : 0;
   cudaDeviceProp prop;
   LGBC_CUDA(cudaGetDeviceProperties(&prop, g->device));
@@ -1083,6 +1082,17 @@ int create_impl(lgbc_graph* g, int64_t n, int64_t nnz, const int64_t* rowptr, co
   LGBC_CUDA(cudaEventCreate(&g->ev_start));
   LGBC_CUDA(cudaEventCreate(&g->ev_stop));
   LGBC_CUDA(cudaMallocHost(reinterpret_cast<void**>(&g->h_ctl), sizeof(BatchCtl)));
+  return LGBC_OK;
+}
+
+// Host-side bookkeeping from the row pointers: degree filter, path-count
+// bound, landmarks and the hub table.
+int finish_handle(lgbc_graph* g, const int64_t* rowptr, const int64_t* in_rowptr);
+
+int create_impl(lgbc_graph* g, int64_t n, int64_t nnz, const int64_t* rowptr, const int32_t* colidx,
+                const int64_t* in_rowptr, const int32_t* in_colidx, int directed) {
+  LGBC_TRY(init_handle(g, n, directed));
+  g->nnz = nnz;
 
   LGBC_TRY(dev_alloc(&g->d_rowptr, static_cast<size_t>(n + 1)));
   LGBC_TRY(dev_alloc(&g->d_colidx, static_cast<size_t>(nnz)));
@@ -1112,6 +1122,18 @@ int create_impl(lgbc_graph* g, int64_t n, int64_t nnz, const int64_t* rowptr, co
     g->launches += validate_csr(g->cfg, g->stream, g->d_in_rowptr, g->d_in_colidx, n, nnz, d_bad);
   int bad = 0;
   cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, g->stream);
+  cudaError_t e = cudaStreamSynchronize(g->stream);
+  cudaFree(d_bad);
+  if (e != cudaSuccess) return cuda_fail(e, "graph upload");
+  LGBC_TRY(check_launch(g));
+  if (bad & 1) return fail(LGBC_EINVAL, "rowptr must be non-decreasing");
+  if (bad & 2) return fail(LGBC_EINVAL, "column index out of range");
+  return finish_handle(g, rowptr, directed ? in_rowptr : rowptr);
+}
+
+int finish_handle(lgbc_graph* g, const int64_t* rowptr, const int64_t* in_rowptr) {
+  const int64_t n = g->n;
+  const int directed = g->directed;
   // degree(g, v) > 0: in+out for digraphs (src/core.jl:66-67), kept on the host
   g->has_degree.assign(static_cast<size_t>(n), 0);
   int64_t max_in = 0;
@@ -1142,12 +1164,6 @@ int create_impl(lgbc_graph* g, int64_t n, int64_t nnz, const int64_t* rowptr, co
     std::sort(top.begin(), top.end());
     for (const auto& t : top) g->landmarks.push_back(t.second);
   }
-  cudaError_t e = cudaStreamSynchronize(g->stream);
-  cudaFree(d_bad);
-  if (e != cudaSuccess) return cuda_fail(e, "graph upload");
-  LGBC_TRY(check_launch(g));
-  if (bad & 1) return fail(LGBC_EINVAL, "rowptr must be non-decreasing");
-  if (bad & 2) return fail(LGBC_EINVAL, "column index out of range");
   return build_hubs(g, rowptr, directed ? in_rowptr : rowptr, g->tune.hub_degree);
 }
 
@@ -2262,5 +2278,204 @@ extern "C" int lgbc_has_path(lgbc_graph* g, int32_t u, int32_t v, const int32_t*
   LGBC_CUDA(cudaStreamSynchronize(g->stream));
   *result = dv != kUnreached ? 1 : 0;
   finish_stats(g);
+  return LGBC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Graph ingest on the device (ingest.cu)
+// ---------------------------------------------------------------------------
+namespace {
+
+// Sort `count` keys (owned: keys / alt swap), keep the first copy of each, and
+// emit the CSR rows into colidx (allocated here) and rowptr.  With `sorted_out`
+// the kept keys are also returned compacted.
+int build_rows(lgbc_graph* g, unsigned long long*& keys, unsigned long long*& alt, int64_t count,
+               int B, int32_t** colidx, int64_t* rowptr_dev, int64_t* nnz,
+               unsigned long long** sorted_out) {
+  cudaStream_t s = g->stream;
+  const int64_t cells = radix_scratch_words(count);
+  const int64_t nsums = std::max<int64_t>(std::max(scan_tiles(cells), scan_tiles(count)),
+                                          scan_tiles(g->n)) + 1;
+  uint32_t* hist = nullptr;
+  int64_t* off = nullptr;
+  int64_t* sums = nullptr;
+  uint8_t* keep = nullptr;
+  int64_t* pos = nullptr;
+  unsigned int* deg = nullptr;
+  int64_t* d_nkept = nullptr;
+  auto cleanup = [&]() {
+    cudaFree(hist); cudaFree(off); cudaFree(sums); cudaFree(keep); cudaFree(pos); cudaFree(deg);
+    cudaFree(d_nkept);
+  };
+  int rc = LGBC_OK;
+  if ((rc = dev_alloc(&hist, static_cast<size_t>(cells))) || (rc = dev_alloc(&off, static_cast<size_t>(cells))) ||
+      (rc = dev_alloc(&sums, static_cast<size_t>(nsums))) || (rc = dev_alloc(&keep, static_cast<size_t>(count))) ||
+      (rc = dev_alloc(&pos, static_cast<size_t>(count))) || (rc = dev_alloc(&deg, static_cast<size_t>(g->n))) ||
+      (rc = dev_alloc(&d_nkept, 1))) {
+    cleanup();
+    return rc;
+  }
+  g->launches += radix_sort(s, keys, alt, count, 2 * B, hist, off, sums);
+  g->launches += ingest_unique(g->cfg, s, keys, count, keep, pos, sums, d_nkept);
+  int64_t nk = 0;
+  cudaError_t e = cudaMemcpyAsync(&nk, d_nkept, 8, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    cleanup();
+    return cuda_fail(e, "ingest: unique arcs");
+  }
+  if (count == 0) nk = 0;
+  *nnz = nk;
+  if ((rc = dev_alloc(colidx, static_cast<size_t>(std::max<int64_t>(nk, 1))))) {
+    cleanup();
+    return rc;
+  }
+  cudaMemsetAsync(deg, 0, static_cast<size_t>(g->n) * 4, s);
+  g->launches += ingest_emit(g->cfg, s, keys, count, keep, pos, B, *colidx, deg);
+  g->launches += ingest_rowptr(s, deg, g->n, sums, rowptr_dev);
+  if (g->n == 0) cudaMemsetAsync(rowptr_dev, 0, 8, s);
+  if (sorted_out) {
+    *sorted_out = alt;  // reuse the spare buffer for the compacted keys
+    alt = nullptr;
+    g->launches += ingest_compact(g->cfg, s, keys, count, keep, pos, *sorted_out);
+  }
+  e = cudaStreamSynchronize(s);
+  cleanup();
+  if (e != cudaSuccess) return cuda_fail(e, "ingest: rows");
+  return check_launch(g);
+}
+
+int create_from_edges_impl(lgbc_graph* g, int64_t n, int64_t m, const int32_t* src,
+                           const int32_t* dst, int directed) {
+  LGBC_TRY(init_handle(g, n, directed));
+  cudaStream_t s = g->stream;
+  const int B = ingest_bits(n);
+  const int64_t count = directed ? m : 2 * m;
+  int32_t* d_edges = nullptr;
+  unsigned long long* keys = nullptr;
+  unsigned long long* alt = nullptr;
+  int* d_bad = nullptr;
+  auto cleanup = [&]() { cudaFree(d_edges); cudaFree(keys); cudaFree(alt); cudaFree(d_bad); };
+  int rc = LGBC_OK;
+  if ((rc = dev_alloc(&d_edges, static_cast<size_t>(2 * std::max<int64_t>(m, 1)))) ||
+      (rc = dev_alloc(&keys, static_cast<size_t>(std::max<int64_t>(count, 1)))) ||
+      (rc = dev_alloc(&alt, static_cast<size_t>(std::max<int64_t>(count, 1)))) ||
+      (rc = dev_alloc(&d_bad, 1))) {
+    cleanup();
+    return rc;
+  }
+  cudaMemsetAsync(d_bad, 0, 4, s);
+  if (m > 0) {
+    LGBC_CUDA(cudaMemcpyAsync(d_edges, src, static_cast<size_t>(m) * 4, cudaMemcpyHostToDevice, s));
+    LGBC_CUDA(cudaMemcpyAsync(d_edges + m, dst, static_cast<size_t>(m) * 4, cudaMemcpyHostToDevice, s));
+  }
+  g->launches += ingest_make_keys(g->cfg, s, d_edges, d_edges + m, m, n, B, directed, keys, d_bad);
+  int bad = 0;
+  LGBC_CUDA(cudaMemcpyAsync(&bad, d_bad, 4, cudaMemcpyDeviceToHost, s));
+  LGBC_CUDA(cudaStreamSynchronize(s));
+  if (bad) {
+    cleanup();
+    return fail(LGBC_EINVAL, "edge endpoint outside [0, n)");
+  }
+  cudaFree(d_edges);
+  d_edges = nullptr;
+  if ((rc = dev_alloc(&g->d_rowptr, static_cast<size_t>(n + 1)))) {
+    cleanup();
+    return rc;
+  }
+  unsigned long long* sorted = nullptr;
+  int64_t nnz = 0;
+  rc = build_rows(g, keys, alt, count, B, &g->d_colidx, g->d_rowptr, &nnz, directed ? &sorted : nullptr);
+  if (rc != LGBC_OK) {
+    cudaFree(sorted);
+    cleanup();
+    return rc;
+  }
+  g->nnz = nnz;
+  std::vector<int64_t> rp(static_cast<size_t>(n + 1)), irp;
+  if (directed) {
+    // in-CSR: the kept arcs with their ends swapped, sorted again
+    cudaFree(keys);
+    keys = nullptr;
+    unsigned long long* ikeys = nullptr;
+    if ((rc = dev_alloc(&ikeys, static_cast<size_t>(std::max<int64_t>(nnz, 1))))) {
+      cudaFree(sorted);
+      cleanup();
+      return rc;
+    }
+    g->launches += ingest_swap_keys(g->cfg, s, sorted, nnz, B, ikeys);
+    unsigned long long* ialt = sorted;
+    if ((rc = dev_alloc(&g->d_in_rowptr, static_cast<size_t>(n + 1)))) {
+      cudaFree(ikeys);
+      cudaFree(ialt);
+      cleanup();
+      return rc;
+    }
+    int64_t innz = 0;
+    rc = build_rows(g, ikeys, ialt, nnz, B, &g->d_in_colidx, g->d_in_rowptr, &innz, nullptr);
+    cudaFree(ikeys);
+    cudaFree(ialt);
+    if (rc != LGBC_OK) {
+      cleanup();
+      return rc;
+    }
+    irp.resize(static_cast<size_t>(n + 1));
+    LGBC_CUDA(cudaMemcpy(irp.data(), g->d_in_rowptr, irp.size() * 8, cudaMemcpyDeviceToHost));
+  } else {
+    g->d_in_rowptr = g->d_rowptr;
+    g->d_in_colidx = g->d_colidx;
+  }
+  cleanup();
+  LGBC_CUDA(cudaMemcpy(rp.data(), g->d_rowptr, rp.size() * 8, cudaMemcpyDeviceToHost));
+  return finish_handle(g, rp.data(), directed ? irp.data() : rp.data());
+}
+
+}  // namespace
+
+extern "C" int lgbc_graph_create_from_edges(lgbc_graph** out, int64_t n, int64_t m,
+                                            const int32_t* src, const int32_t* dst, int directed) {
+  if (!out) return fail(LGBC_EINVAL, "null output handle pointer");
+  *out = nullptr;
+  if (n < 0 || m < 0) return fail(LGBC_EINVAL, "negative vertex or edge count");
+  if (n >= INT32_MAX) return fail(LGBC_EINVAL, "vertex ids must fit in int32");
+  if (m > 0 && (!src || !dst)) return fail(LGBC_EINVAL, "null edge array");
+  if (m > (int64_t{1} << 31) - 1) return fail(LGBC_EINVAL, "at most 2^31 - 1 edges per call");
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return fail(LGBC_ECUDA, std::string("no CUDA device available: ") +
+                                (e != cudaSuccess ? cudaGetErrorString(e) : "0 devices"));
+  }
+  lgbc_graph* g = new (std::nothrow) lgbc_graph();
+  if (!g) return fail(LGBC_ENOMEM, "host allocation failed");
+  const int rc = create_from_edges_impl(g, n, m, src, dst, directed);
+  if (rc != LGBC_OK) {
+    const std::string msg = g_last_error;
+    lgbc_graph_destroy(g);
+    g_last_error = msg;
+    return rc;
+  }
+  *out = g;
+  return LGBC_OK;
+}
+
+extern "C" int lgbc_graph_csr(const lgbc_graph* g, int64_t* rowptr, int32_t* colidx,
+                              int64_t* in_rowptr, int32_t* in_colidx) {
+  LGBC_TRY(check_graph(g));
+  lgbc_graph* gm = const_cast<lgbc_graph*>(g);
+  std::lock_guard<std::mutex> lock(gm->mu);
+  LGBC_TRY(use_device(gm));
+  LGBC_CUDA(cudaStreamSynchronize(g->stream));
+  if (rowptr)
+    LGBC_CUDA(cudaMemcpy(rowptr, g->d_rowptr, static_cast<size_t>(g->n + 1) * 8, cudaMemcpyDeviceToHost));
+  if (colidx && g->nnz > 0)
+    LGBC_CUDA(cudaMemcpy(colidx, g->d_colidx, static_cast<size_t>(g->nnz) * 4, cudaMemcpyDeviceToHost));
+  if (in_rowptr)
+    LGBC_CUDA(cudaMemcpy(in_rowptr, g->d_in_rowptr, static_cast<size_t>(g->n + 1) * 8,
+                         cudaMemcpyDeviceToHost));
+  if (in_colidx && g->nnz > 0)
+    LGBC_CUDA(cudaMemcpy(in_colidx, g->d_in_colidx, static_cast<size_t>(g->nnz) * 4,
+                         cudaMemcpyDeviceToHost));
   return LGBC_OK;
 }

@@ -249,4 +249,31 @@ int proposal_build(cudaStream_t s, const float* y, int64_t n, double eps, float*
 int proposal_sample(cudaStream_t s, const double* cdf, const double* p, int64_t n, int64_t k,
                     uint64_t seed, bool systematic, int32_t* src, double* w);
 
+// ---- graph ingest on the device: ingest.cu -------------------------------------
+// Bit width B of the vertex ids in the 64-bit arc keys (u << B) | v.
+int ingest_bits(int64_t n);
+// Scan tiles (int64 partial sums needed) for a scan of `count` items.
+int64_t scan_tiles(int64_t count);
+// Arc keys of an edge list (2 per edge for an undirected graph; a self-loop
+// keeps one); *bad |= 1 for ids outside [0, n).
+int ingest_make_keys(const LaunchCfg& c, cudaStream_t s, const int32_t* src, const int32_t* dst,
+                     int64_t m, int64_t n, int B, int directed, unsigned long long* keys, int* bad);
+int ingest_swap_keys(const LaunchCfg& c, cudaStream_t s, const unsigned long long* in, int64_t count,
+                     int B, unsigned long long* out);
+// Histogram cells of a radix sort of `count` keys (hist: uint32, off: int64 each).
+int64_t radix_scratch_words(int64_t count);
+// LSD radix sort of the low `bits` bits; keys / alt are swapped as passes run
+// (on return `keys` holds the sorted keys).
+int radix_sort(cudaStream_t s, unsigned long long*& keys, unsigned long long*& alt, int64_t count,
+               int bits, uint32_t* hist, int64_t* off, int64_t* sums);
+// keep[i] = first copy of key i (no sentinel); pos = exclusive scan; *nkept.
+int ingest_unique(const LaunchCfg& c, cudaStream_t s, const unsigned long long* keys, int64_t count,
+                  uint8_t* keep, int64_t* pos, int64_t* sums, int64_t* nkept);
+int ingest_emit(const LaunchCfg& c, cudaStream_t s, const unsigned long long* keys, int64_t count,
+                const uint8_t* keep, const int64_t* pos, int B, int32_t* colidx, unsigned int* deg);
+int ingest_compact(const LaunchCfg& c, cudaStream_t s, const unsigned long long* keys, int64_t count,
+                   const uint8_t* keep, const int64_t* pos, unsigned long long* out);
+// rowptr[0..n] from the row lengths.
+int ingest_rowptr(cudaStream_t s, const unsigned int* deg, int64_t n, int64_t* sums, int64_t* rowptr);
+
 }  // namespace lgbc

@@ -30,7 +30,7 @@ from ._lib import ArgumentError, BoundsError, LGBCError, MethodError
 from .centrality import (betweenness_centrality, betweenness_centrality_many, betweenness_raw,
                          sample, sample_, stress_centrality, _rescale_)
 from .graphs import (DefaultDistance, DeviceGraph, SimpleDiGraph, SimpleGraph, degree,
-                     is_directed, ne, nv, vertices, weights)
+                     graph_from_edges, is_directed, ne, nv, vertices, weights)
 from .persistence import loadgraph
 from .distance import (center, closeness_centrality, diameter, eccentricity, periphery,
                        radiality_centrality, radius)
@@ -47,5 +47,5 @@ __all__ = [
     "multi_gdistances", "learned", "SourceProposal", "betweenness_centrality_learned",
     "core_number", "dependency_mass", "features", "closeness_centrality", "radiality_centrality",
     "eccentricity", "diameter", "radius", "periphery", "center", "stress_centrality",
-    "bfs_parents", "bfs_tree", "tree", "has_path",
+    "bfs_parents", "bfs_tree", "tree", "has_path", "graph_from_edges",
 ]

@@ -103,6 +103,8 @@ def _declare(lib) -> None:
         "lgbc_host_free": ([p], c_int),
         "lgbc_memcpy": ([p, p, i64, c_int], c_int),
         "lgbc_gdistances_noalloc": ([i64, i64, p, p, p, p, p, i64, p, p], c_int),
+        "lgbc_graph_create_from_edges": ([pp, i64, i64, p, p, c_int], c_int),
+        "lgbc_graph_csr": ([p, p, p, p, p], c_int),
         "lgbc_betweenness_many": ([i64, p, p, p, p, p, c_int, p], c_int),
         "lgbc_core_number": ([p, p], c_int),
         "lgbc_features": ([p, p], c_int),

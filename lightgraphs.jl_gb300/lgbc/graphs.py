@@ -263,6 +263,16 @@ def weights(g) -> DefaultDistance:
 class DeviceGraph:
     """A graph uploaded to the GPU through lgbc_graph_create."""
 
+    @classmethod
+    def adopt(cls, handle: ctypes.c_void_p, n: int, nnz: int, directed: bool) -> "DeviceGraph":
+        """Wrap a handle the library already created (it is destroyed with the wrapper)."""
+        d = cls.__new__(cls)
+        d._h = handle
+        d.n = n
+        d.nnz = nnz
+        d.directed = directed
+        return d
+
     def __init__(self, g: _GraphBase):
         lib = _lib.lib()
         rp, ci = g.csr()
@@ -315,3 +325,43 @@ class DeviceGraph:
             self.close()
         except Exception:
             pass
+
+
+def graph_from_edges(n: int, src0, dst0, *, directed: bool = False, eltype=np.int64):
+    """SimpleGraph / SimpleDiGraph from 0-based endpoint arrays, with the CSR
+    built on the GPU (lgbc_graph_create_from_edges: radix sort of the arcs,
+    duplicates dropped, an undirected self-loop stored once -- the add_edge!
+    semantics of src/SimpleGraphs/simplegraph.jl:445-461 and
+    simpledigraph.jl:414-429).  The device copy stays attached to the graph."""
+    src = np.ascontiguousarray(np.asarray(src0).ravel(), np.int64)
+    dst = np.ascontiguousarray(np.asarray(dst0).ravel(), np.int64)
+    if src.shape != dst.shape:
+        raise _lib.ArgumentError("src and dst differ in length")
+    if len(src) and (min(src.min(), dst.min()) < 0 or max(src.max(), dst.max()) >= n):
+        raise _lib.BoundsError("edge endpoint outside 0:n-1")
+    s32 = src.astype(np.int32)
+    d32 = dst.astype(np.int32)
+    lib = _lib.lib()
+    h = ctypes.c_void_p()
+    _lib.check(lib.lgbc_graph_create_from_edges(ctypes.byref(h), int(n), len(s32), _lib.ptr(s32),
+                                                _lib.ptr(d32), int(bool(directed))))
+    dev = DeviceGraph.adopt(h, int(n), 0, bool(directed))
+    nn = ctypes.c_int64()
+    nnz = ctypes.c_int64()
+    _lib.check(lib.lgbc_graph_info(h, ctypes.byref(nn), ctypes.byref(nnz), None))
+    dev.nnz = int(nnz.value)
+    rp = np.empty(int(n) + 1, np.int64)
+    ci = np.empty(max(int(nnz.value), 1), np.int32)
+    irp = ici = None
+    if directed:
+        irp = np.empty(int(n) + 1, np.int64)
+        ici = np.empty(max(int(nnz.value), 1), np.int32)
+    _lib.check(lib.lgbc_graph_csr(h, _lib.ptr(rp), _lib.ptr(ci), _lib.ptr(irp), _lib.ptr(ici)))
+    ci = ci[:int(nnz.value)]
+    cls = SimpleDiGraph if directed else SimpleGraph
+    if directed:
+        g = cls.from_csr(rp, ci, irp, ici[:int(nnz.value)], eltype=eltype)
+    else:
+        g = cls.from_csr(rp, ci, eltype=eltype)
+    g._handle = dev
+    return g
