@@ -235,6 +235,9 @@ struct lgbc_graph {
   lgbc_graph* stack = nullptr;        // R copies of this graph (stacked batches)
   int64_t stack_copies = 0;
   std::vector<int32_t> h_active;      // the last call's ordered active sources
+  std::vector<double> h_weights;      // their weights (weighted calls; empty otherwise)
+  double* d_lw_fixed = nullptr;       // lane weights of the running batch (cached graphs)
+  int64_t d_lw_cap = 0;
   cudaStream_t cap_stream = nullptr;  // stream used to capture level-loop graphs
   std::vector<LoopGraph> loops;       // cached device-driven level loops
   uint64_t loop_clock = 0;
@@ -476,6 +479,7 @@ MsBuffers ms_buffers(lgbc_graph* g, const int32_t* lane_src, const double* lane_
   b.lane_src = lane_src;
   b.cap = w.cap;
   b.lane_w = lane_w;
+  b.lane_w_n = 0;
   return b;
 }
 
@@ -503,6 +507,10 @@ struct Seeds {
   const int64_t* seg_off = nullptr;
   const uint64_t* seg_mark = nullptr;
   int64_t nseg = 0;
+  // stacked unions with lane weights: one row of 64 weights per copy of an
+  // lane_w_n-vertex graph, lane_w_count weights in all
+  int64_t lane_w_n = 0;
+  int64_t lane_w_count = 0;
 };
 
 // ---------------------------------------------------------------------------
@@ -681,7 +689,10 @@ LoopKey loop_key(lgbc_graph* g, int backward, int sigma_kind, unsigned long long
   k.bc = bc;
   k.b = b;
   k.b.lane_src = nullptr;
-  k.b.lane_w = nullptr;
+  if (!backward) {  // the forward sweep never reads the weights
+    k.b.lane_w = nullptr;
+    k.b.lane_w_n = 0;
+  }
   k.hd = hd;
   k.alpha = g->tune.alpha;
   k.beta = g->tune.beta;
@@ -700,6 +711,7 @@ int run_ms_batch(lgbc_graph* g, const int32_t* lane_src, int nl, int sigma_kind,
   const uint64_t act = nl >= 64 ? ~0ull : ((1ull << nl) - 1ull);
   for (;;) {
     MsBuffers b = ms_buffers(g, lane_src, lane_w);
+    b.lane_w_n = seeds.lane_w_n;
     if (seeds.seg_mark) g->launches += ms_premark(g->cfg, g->stream, b, seeds.seg_off, seeds.seg_mark,
                                                   seeds.nseg);
     if (seeds.v)
@@ -709,7 +721,20 @@ int run_ms_batch(lgbc_graph* g, const int32_t* lane_src, int nl, int sigma_kind,
       g->launches += ms_init(g->stream, dg, b, nl, sigma_kind, g->sigma_limit, dist, dist_ld);
     LGBC_TRY(check_launch(g));
     // device-driven loops for plain batches (no weights, statistics or stress)
-    if (g->tune.graph_loop == 1 && !lane_w && !stats && !stress) {
+    if (g->tune.graph_loop == 1 && !stats && !stress) {
+      MsBuffers bw = b;  // the backward graph reads the weights from a fixed buffer
+      if (lane_w) {
+        const int64_t cnt = seeds.lane_w_count > 0 ? seeds.lane_w_count : nl;
+        if (cnt > g->d_lw_cap) {
+          dev_free(g->d_lw_fixed);
+          g->d_lw_cap = 0;
+          LGBC_TRY(dev_alloc(&g->d_lw_fixed, static_cast<size_t>(std::max<int64_t>(cnt, 64))));
+          g->d_lw_cap = std::max<int64_t>(cnt, 64);
+        }
+        LGBC_CUDA(cudaMemcpyAsync(g->d_lw_fixed, lane_w, static_cast<size_t>(cnt) * 8,
+                                  cudaMemcpyDeviceToDevice, g->stream));
+        bw.lane_w = g->d_lw_fixed;
+      }
       LoopGraph* lg = nullptr;
       LGBC_TRY(get_loop(g, loop_key(g, 0, sigma_kind, act, dist, dist_ld, nullptr, b, hd), &lg));
       LGBC_CUDA(cudaGraphLaunch(lg->exec, g->stream));
@@ -738,7 +763,7 @@ int run_ms_batch(lgbc_graph* g, const int32_t* lane_src, int nl, int sigma_kind,
       }
       const int maxl = c.maxlevel;
       LoopGraph* bg = nullptr;
-      LGBC_TRY(get_loop(g, loop_key(g, 1, sigma_kind, act, nullptr, 0, bc, b, hd), &bg));
+      LGBC_TRY(get_loop(g, loop_key(g, 1, sigma_kind, act, nullptr, 0, bc, bw, hd), &bg));
       LGBC_CUDA(cudaGraphLaunch(bg->exec, g->stream));
       g->launches += 2 + static_cast<int64_t>(maxl + 1) * bg->body_kernels;
       if (seeds.seg_mark)  // premarked vertices were never listed: clear visit outright
@@ -810,7 +835,7 @@ int run_ms_batch(lgbc_graph* g, const int32_t* lane_src, int nl, int sigma_kind,
 // Brandes over the active sources already on the device (g->d_src[0, k)),
 // accumulating into bc_dev (zeroed here); with d_w, source i's dependencies
 // are scaled by d_w[i].
-int run_stacked(lgbc_graph* g, int64_t copies, double* bc_dev);
+int run_stacked(lgbc_graph* g, int64_t copies, double* bc_dev, const std::vector<double>* w);
 
 int run_betweenness(lgbc_graph* g, int64_t k_act, int endpoints, double* bc_dev,
                     const double* d_w = nullptr) {
@@ -818,8 +843,9 @@ int run_betweenness(lgbc_graph* g, int64_t k_act, int endpoints, double* bc_dev,
   const int lanes0 = std::max(1, std::min<int>(kMaxLanes, g->tune.lanes));
   const int64_t batches = (k_act + lanes0 - 1) / lanes0;
   const int64_t copies = g->n > 0 ? std::min<int64_t>(g->tune.stack_vertices / g->n, batches) : 0;
-  if (!d_w && copies >= 4 && static_cast<int64_t>(g->h_active.size()) == k_act) {
-    LGBC_TRY(run_stacked(g, copies, bc_dev));
+  const bool host_w = d_w && static_cast<int64_t>(g->h_weights.size()) == k_act;
+  if ((!d_w || host_w) && copies >= 4 && static_cast<int64_t>(g->h_active.size()) == k_act) {
+    LGBC_TRY(run_stacked(g, copies, bc_dev, d_w ? &g->h_weights : nullptr));
     if (endpoints) g->launches += add_endpoints(g->cfg, g->stream, bc_dev, g->n, g->d_src, k_act);
     return check_launch(g);
   }
@@ -912,7 +938,7 @@ int order_active(lgbc_graph* g, std::vector<int32_t>& act, std::vector<double>* 
 // (one lane each, as in lgbc_betweenness_many), lanes without a source in a
 // copy are premarked there, and the copies' raw vectors are summed at the end.
 // Each union batch does the work of `copies` batches with the launches of one.
-int run_stacked(lgbc_graph* g, int64_t copies, double* bc_dev) {
+int run_stacked(lgbc_graph* g, int64_t copies, double* bc_dev, const std::vector<double>* w) {
   const int64_t n = g->n, nnz = g->nnz;
   const int L = std::max(1, std::min<int>(kMaxLanes, g->tune.lanes));
   if (!g->stack || g->stack_copies != copies) {
@@ -967,6 +993,8 @@ int run_stacked(lgbc_graph* g, int64_t copies, double* bc_dev) {
   std::vector<int64_t> bstart(static_cast<size_t>(nbu + 1), 0), voff(static_cast<size_t>(copies + 1));
   std::vector<uint64_t> marks(static_cast<size_t>(nbu * copies));
   std::vector<int64_t> filled(static_cast<size_t>(nbu), 0);  // ordinary batches per union batch
+  // lane weights: row u * copies + r holds copy r's 64 lanes of union batch u
+  std::vector<double> wrows(w ? static_cast<size_t>(nbu * copies * 64) : 0, 0.0);
   for (int64_t r = 0; r <= copies; ++r) voff[static_cast<size_t>(r)] = r * n;
   for (int64_t u = 0; u < nbu; ++u) {
     for (int64_t r = 0; r < copies; ++r) {
@@ -977,18 +1005,24 @@ int run_stacked(lgbc_graph* g, int64_t copies, double* bc_dev) {
         sv.push_back(static_cast<int32_t>(r * n + act[static_cast<size_t>(i0 + l)]));
         sl.push_back(l);
         seeded |= 1ull << l;
+        if (w) wrows[static_cast<size_t>((u * copies + r) * 64 + l)] = (*w)[static_cast<size_t>(i0 + l)];
       }
       const uint64_t all = L >= 64 ? ~0ull : ((1ull << L) - 1ull);
       marks[static_cast<size_t>(u * copies + r)] = all & ~seeded;
     }
     bstart[static_cast<size_t>(u + 1)] = static_cast<int64_t>(sv.size());
   }
-  // one device buffer: voff | marks | seed vertices | seed lanes
-  const size_t bytes = voff.size() * 8 + marks.size() * 8 + sv.size() * 4 + sl.size() * 4 + 16;
+  // one device buffer: weight rows | voff | marks | seed vertices | seed lanes
+  const size_t bytes = wrows.size() * 8 + voff.size() * 8 + marks.size() * 8 + sv.size() * 4 +
+                       sl.size() * 4 + 16;
   unsigned char* buf = nullptr;
   LGBC_TRY(dev_alloc(&buf, bytes));
   std::unique_ptr<unsigned char, cudaError_t (*)(void*)> guard(buf, cudaFree);
-  int64_t* d_voff = reinterpret_cast<int64_t*>(buf);
+  double* d_wrows = reinterpret_cast<double*>(buf);
+  if (!wrows.empty())
+    LGBC_CUDA(cudaMemcpyAsync(d_wrows, wrows.data(), wrows.size() * 8, cudaMemcpyHostToDevice,
+                              st->stream));
+  int64_t* d_voff = reinterpret_cast<int64_t*>(buf + wrows.size() * 8);
   uint64_t* d_marks = reinterpret_cast<uint64_t*>(d_voff + voff.size());
   int32_t* d_sv = reinterpret_cast<int32_t*>(d_marks + marks.size());
   int32_t* d_sl = d_sv + sv.size();
@@ -1009,10 +1043,16 @@ int run_stacked(lgbc_graph* g, int64_t copies, double* bc_dev) {
     sd.seg_off = d_voff;
     sd.seg_mark = d_marks + static_cast<size_t>(u * copies);
     sd.nseg = copies;
-    int rc = run_ms_batch(st, nullptr, L, kSigmaU64, st->d_bc, nullptr, 0, sd);
+    const double* lw = nullptr;
+    if (w) {
+      lw = d_wrows + u * copies * 64;
+      sd.lane_w_n = n;
+      sd.lane_w_count = copies * 64;
+    }
+    int rc = run_ms_batch(st, nullptr, L, kSigmaU64, st->d_bc, nullptr, 0, sd, lw);
     if (rc == 1) {
       g->stats.wide_batches++;
-      rc = run_ms_batch(st, nullptr, L, kSigmaF64, st->d_bc, nullptr, 0, sd);
+      rc = run_ms_batch(st, nullptr, L, kSigmaF64, st->d_bc, nullptr, 0, sd, lw);
     }
     if (rc != LGBC_OK) {
       g->launches += st->launches;
@@ -1049,6 +1089,7 @@ int prepare_sources(lgbc_graph* g, const int32_t* src, int64_t nsrc, int64_t* k_
   LGBC_TRY(order_active(g, active, nullptr));
   *k_act = static_cast<int64_t>(active.size());
   g->h_active = active;
+  g->h_weights.clear();
   LGBC_TRY(ensure_src(g, *k_act));
   if (*k_act > 0)
     LGBC_CUDA(cudaMemcpyAsync(g->d_src, active.data(), active.size() * sizeof(int32_t),
@@ -1239,6 +1280,7 @@ int lgbc_graph_destroy(lgbc_graph* g) {
   dev_free(g->d_bc);
   dev_free(g->d_dist);
   dev_free(g->d_lmdist);
+  dev_free(g->d_lw_fixed);
   if (g->h_ctl) cudaFreeHost(g->h_ctl);
   if (g->ev_start) cudaEventDestroy(g->ev_start);
   if (g->ev_stop) cudaEventDestroy(g->ev_stop);
@@ -1964,6 +2006,8 @@ int lgbc_betweenness_weighted(lgbc_graph* g, const int32_t* src, const double* w
   LGBC_TRY(order_active(g, act, &aw));
   const int64_t k_act = static_cast<int64_t>(act.size());
   g->stats.active_sources = k_act;
+  g->h_active = act;
+  g->h_weights = aw;
   LGBC_TRY(ensure_src(g, k_act));
   double* d_w = nullptr;
   LGBC_TRY(dev_alloc(&d_w, static_cast<size_t>(std::max<int64_t>(k_act, 1))));
@@ -2127,6 +2171,7 @@ extern "C" int lgbc_tune(lgbc_graph* g, const char* cache_path) {
     sample[static_cast<size_t>(i)] = act[static_cast<size_t>(i * static_cast<int64_t>(act.size()) / k)];
   LGBC_TRY(ensure_src(g, k));
   g->h_active = sample;
+  g->h_weights.clear();
   LGBC_CUDA(cudaMemcpyAsync(g->d_src, sample.data(), static_cast<size_t>(k) * 4,
                             cudaMemcpyHostToDevice, g->stream));
   LGBC_CUDA(cudaStreamSynchronize(g->stream));

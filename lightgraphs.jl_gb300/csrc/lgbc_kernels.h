@@ -44,6 +44,8 @@ struct MsBuffers {
   const int32_t* lane_src;      // sources of the batch (device)
   unsigned long long cap;       // entries in qv / qm
   const double* lane_w;         // 64 lane weights (weighted accumulation) or nullptr
+  int64_t lane_w_n;             // > 0: a union of copies of an n-vertex graph, one row of 64
+                                // weights per copy (vertex v uses row v / lane_w_n)
 };
 
 // Vertices with more than hub_degree neighbours ("hubs") are not expanded by

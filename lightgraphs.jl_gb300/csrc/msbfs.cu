@@ -504,6 +504,11 @@ __device__ __forceinline__ double finish_f64(void* psi, const void* sigma, int32
   return contrib;
 }
 
+// The lane weights of vertex v (its copy's row in a stacked union).
+__device__ __forceinline__ const double* weights_of(const MsBuffers& b, int32_t v) {
+  return b.lane_w_n > 0 ? b.lane_w + (static_cast<int64_t>(v) / b.lane_w_n) * 64 : b.lane_w;
+}
+
 // Weighted finalisation (importance-sampled estimators): the same psi
 // updates, returning sum over the lanes of w[lane] * delta in FP64.
 __device__ __forceinline__ double finish_df_w(void* psi, const void* sigma, int32_t v,
@@ -970,7 +975,7 @@ __global__ void __launch_bounds__(256) k_ms_delta(DevGraph g, MsBuffers b, HubDa
       psi_range_df(g.colidx, e0, e1, F, succ, b.psi, hd.dense_edges, acc0, acc1);
       if (b.lane_w) {
         const double contrib =
-            warp_sum_f64(finish_df_w(b.psi, b.sigma, v, mine, acc0, acc1, b.lane_w));
+            warp_sum_f64(finish_df_w(b.psi, b.sigma, v, mine, acc0, acc1, weights_of(b, v)));
         if (ln == 0) bc[v] += contrib;
       } else {
         df32 contrib = finish_df(b.psi, b.sigma, v, mine, acc0, acc1);
@@ -980,7 +985,7 @@ __global__ void __launch_bounds__(256) k_ms_delta(DevGraph g, MsBuffers b, HubDa
     } else {
       double acc0 = 0.0, acc1 = 0.0;
       psi_range_f64(g.colidx, e0, e1, F, succ, b.psi, hd.dense_edges, acc0, acc1);
-      double contrib = b.lane_w ? finish_f64_w(b.psi, b.sigma, v, mine, acc0, acc1, b.lane_w)
+      double contrib = b.lane_w ? finish_f64_w(b.psi, b.sigma, v, mine, acc0, acc1, weights_of(b, v))
                                 : finish_f64(b.psi, b.sigma, v, mine, acc0, acc1);
       contrib = warp_sum_f64(contrib);
       if (ln == 0) bc[v] += contrib;
@@ -1024,7 +1029,7 @@ __global__ void __launch_bounds__(256) k_ms_hub_delta(DevGraph g, MsBuffers b, H
     if (SK == kSigmaU64) {
       if (b.lane_w) {
         const double contrib = warp_sum_f64(finish_df_w(
-            b.psi, b.sigma, h, mine, df_from_double(s0), df_from_double(s1), b.lane_w));
+            b.psi, b.sigma, h, mine, df_from_double(s0), df_from_double(s1), weights_of(b, h)));
         if (ln == 0) bc[h] += contrib;
       } else {
         df32 contrib = finish_df(b.psi, b.sigma, h, mine, df_from_double(s0), df_from_double(s1));
@@ -1032,7 +1037,7 @@ __global__ void __launch_bounds__(256) k_ms_hub_delta(DevGraph g, MsBuffers b, H
         if (ln == 0) bc[h] += df_to_double(contrib);
       }
     } else {
-      double contrib = b.lane_w ? finish_f64_w(b.psi, b.sigma, h, mine, s0, s1, b.lane_w)
+      double contrib = b.lane_w ? finish_f64_w(b.psi, b.sigma, h, mine, s0, s1, weights_of(b, h))
                                 : finish_f64(b.psi, b.sigma, h, mine, s0, s1);
       contrib = warp_sum_f64(contrib);
       if (ln == 0) bc[h] += contrib;

@@ -112,3 +112,31 @@ def test_stacked_grid_replays_in_fp64():
     assert g.device_handle().stats()["wide_batches"] >= 1
     rp, ci = g.csr()
     np.testing.assert_allclose(b, oracle.betweenness_centrality(rp, ci), rtol=1e-9)
+
+
+@pytest.mark.parametrize("directed", [False, True])
+def test_weighted_batches_in_every_mode(directed):
+    # importance weights through host-driven loops, device-driven loops and
+    # stacked unions (one weight row per copy) give the same accumulation
+    from lgbc.learned import betweenness_raw_weighted
+    g = gen.erdos_renyi_nm(3000, 12000, seed=21, directed=directed)
+    rng = np.random.default_rng(8)
+    src = rng.integers(0, g.nv(), 700).astype(np.int32)
+    w = rng.uniform(0.2, 3.0, len(src))
+    h = g.device_handle()
+    out = {}
+    for loop in (0, 1):
+        for stack in (0, 1 << 21):
+            h.set_tuning(graph_loop=loop, stack_vertices=stack)
+            out[(loop, stack)] = betweenness_raw_weighted(g, src, w)
+    h.set_tuning(graph_loop=1, stack_vertices=1 << 21)
+    base = out[(0, 0)]
+    for key, val in out.items():
+        np.testing.assert_allclose(val, base, rtol=1e-9, atol=1e-9, err_msg=str(key))
+    rp, ci = g.csr()
+    kw = {}
+    if directed:
+        irp, ici = g.in_csr()
+        kw = dict(directed=True, in_rowptr=irp, in_colidx=ici)
+    _, want = oracle.dependency(rp, ci, src, w, **kw)
+    np.testing.assert_allclose(base, want, rtol=1e-9, atol=1e-9)
