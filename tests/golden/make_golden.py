@@ -10,6 +10,8 @@ It copies, in plain text, the reference's golden graph and vectors:
   * test/testdata/graph-50-500-bc.txt  -> graph-50-500-bc.txt (betweenness, normalize=true)
   * test/testdata/graph-50-500-sc.txt  -> graph-50-500-sc.txt (stress centrality)
   * test/testdata/graph-50-500-rc.txt  -> graph-50-500-rc.txt (radiality centrality)
+  * test/testdata/graph-decomposition.jgz -> graph-decomposition.lg (core numbers,
+    test/degeneracy.jl:2-6)
 and writes ``known_answers.json``: the small known-answer cases that the
 reference's tests assert (each entry carries the test file:line it restates).
 Nothing at test time reads the reference tree; the tests only read this folder.
@@ -31,6 +33,10 @@ def main(ref_root: str) -> None:
     for suffix in ("bc", "sc", "rc"):
         shutil.copyfile(os.path.join(td, f"graph-50-500-{suffix}.txt"),
                         os.path.join(here, f"graph-50-500-{suffix}.txt"))
+    with gzip.open(os.path.join(td, "graph-decomposition.jgz"), "rt") as f:
+        text = f.read()
+    with open(os.path.join(here, "graph-decomposition.lg"), "w") as f:
+        f.write(text)
 
     # Known answers asserted by the reference's tests (1-based vertex ids).
     known = {
@@ -67,6 +73,9 @@ def main(ref_root: str) -> None:
             "graph": "graph-50-500", "normalize": False, "endpoints": True,
             "first3": [122.10760591498584, 159.0072453120582, 176.39547945994505],
             "digits": 4},
+        "core_number": {
+            "cite": "test/degeneracy.jl:2-6", "graph": "graph-decomposition",
+            "expected": [3, 3, 3, 3, 3, 3, 3, 3, 2, 2, 2, 2, 2, 2, 2, 2, 1, 1, 1, 1, 0]},
         "dijkstra": [
             {"cite": "test/shortestpaths/dijkstra.jl:77-93",
              "n": 5, "directed": False,

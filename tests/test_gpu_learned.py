@@ -283,3 +283,9 @@ def test_learned_proposal_beats_uniform_at_equal_samples():
     l_uniform = [l1_error(lgbc.betweenness_centrality(g, k, rng=rng), exact) for _ in range(8)]
     assert np.mean(l_learned) < 0.95 * np.mean(l_uniform), (np.mean(l_learned), np.mean(l_uniform))
     m.close()
+
+
+def test_core_number_golden_decomposition(known):
+    from conftest import golden_path
+    g = lgbc.loadgraph(golden_path("graph-decomposition.lg"))
+    assert lgbc.core_number(g).tolist() == known["core_number"]["expected"]

@@ -162,3 +162,11 @@ def _csr_args(g):
         irp, ici = g.in_csr()
         kw.update(in_rowptr=irp, in_colidx=ici)
     return rp, ci, kw
+
+
+def test_core_number_golden_decomposition(known):
+    # test/degeneracy.jl:2-6: the reference's decomposition graph and its core numbers
+    from conftest import golden_path
+    g = lgbc.loadgraph(golden_path("graph-decomposition.lg"))
+    rp, ci = g.csr()
+    assert oracle.core_number(rp, ci).tolist() == known["core_number"]["expected"]
