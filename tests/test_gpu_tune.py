@@ -59,3 +59,15 @@ def test_source_order_keeps_results(directed):
     assert np.array_equal(lgbc.stress_centrality(g, src), s0)
     wb = lgbc.learned.betweenness_raw_weighted(g, (src - 1).astype(np.int32), w)
     np.testing.assert_allclose(wb, wa, rtol=1e-9, atol=1e-9)
+
+
+def test_tuning_validation():
+    g = gen.rmat(8, 4, seed=2)
+    h = g.device_handle()
+    for bad in (dict(source_order=2), dict(graph_loop=-1), dict(stack_vertices=-5),
+                dict(lanes=0), dict(lanes=65), dict(alpha=0.0), dict(hub_degree=0)):
+        with pytest.raises(lgbc.ArgumentError):
+            h.set_tuning(**bad)
+    h.set_tuning(lanes=7, source_order=0, graph_loop=0, stack_vertices=0)
+    t = h.tuning()
+    assert (t.lanes, t.source_order, t.graph_loop, t.stack_vertices) == (7, 0, 0, 0)
