@@ -1,255 +1,17 @@
 // api.cu -- the C ABI of include/lgbc.h: graph handles, workspaces and the
 // host side of the level loops.  All arithmetic runs in the kernels of
-// msbfs.cu / bfs.cu / util.cu; there is no CPU fallback.
-#include <algorithm>
-#include <cmath>
-#include <cstdio>
-#include <cstring>
-#include <memory>
-#include <mutex>
-#include <new>
-#include <string>
-#include <utility>
-#include <vector>
-
-#include "lgbc.h"
-#include "lgbc_kernels.h"
+// msbfs.cu / bfs.cu / util.cu; there is no CPU fallback.  The other entry
+// points live in api_many.cu, api_learned.cu and api_more.cu.
+#include "api_internal.h"
 
 using namespace lgbc;
-
-namespace {
-
-thread_local std::string g_last_error;
-
-int fail(int code, const std::string& msg) {
-  g_last_error = msg;
-  return code;
-}
-
-int cuda_fail(cudaError_t e, const char* what) {
-  return fail(LGBC_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
-}
-
-#define LGBC_CUDA(call)                                   \
-  do {                                                    \
-    cudaError_t _e = (call);                              \
-    if (_e != cudaSuccess) return cuda_fail(_e, #call);   \
-  } while (0)
-
-#define LGBC_TRY(expr)          \
-  do {                          \
-    int _rc = (expr);           \
-    if (_rc != LGBC_OK) return _rc; \
-  } while (0)
-
-template <class T>
-int dev_alloc(T** p, size_t count) {
-  *p = nullptr;
-  if (count == 0) count = 1;
-  cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(T));
-  if (e != cudaSuccess) {
-    cudaGetLastError();
-    *p = nullptr;
-    return fail(LGBC_ENOMEM, std::string("cudaMalloc of ") + std::to_string(count * sizeof(T)) +
-                                 " bytes failed: " + cudaGetErrorString(e));
-  }
-  return LGBC_OK;
-}
-
-template <class T>
-void dev_free(T*& p) {
-  if (p) cudaFree(p);
-  p = nullptr;
-}
-
-// Multi-source workspace (msbfs.cu), sized for one batch of 64 lanes.
-struct MsWorkspace {
-  uint64_t* visit = nullptr;
-  uint64_t* mb0 = nullptr;
-  uint64_t* mb1 = nullptr;
-  void* sigma = nullptr;
-  void* psi = nullptr;
-  int32_t* qv = nullptr;
-  uint64_t* qm = nullptr;
-  unsigned long long* lvl_off = nullptr;
-  BatchCtl* ctl = nullptr;
-  unsigned long long cap = 0;
-  bool have_sigma = false;
-
-  void release() {
-    dev_free(visit);
-    dev_free(mb0);
-    dev_free(mb1);
-    if (sigma) cudaFree(sigma);
-    if (psi) cudaFree(psi);
-    sigma = psi = nullptr;
-    dev_free(qv);
-    dev_free(qm);
-    dev_free(lvl_off);
-    dev_free(ctl);
-    cap = 0;
-    have_sigma = false;
-  }
-};
-
-// Hub work items (see HubItem in lgbc_kernels.h) and their accumulators.
-struct HubTable {
-  HubItem* out_items = nullptr;
-  int64_t n_out = 0;
-  HubItem* in_items = nullptr;   // == out_items for undirected graphs
-  int64_t n_in = 0;
-  unsigned long long* acc = nullptr;
-  unsigned long long* mask = nullptr;
-  unsigned int* cnt = nullptr;
-  int64_t nslots = 0;
-  int built_for = -1;            // hub_degree the table was built with
-  void release() {
-    if (in_items && in_items != out_items) cudaFree(in_items);
-    dev_free(out_items);
-    in_items = nullptr;
-    dev_free(acc);
-    dev_free(mask);
-    dev_free(cnt);
-    n_out = n_in = nslots = 0;
-    built_for = -1;
-  }
-};
-
-struct BfsWorkspace {
-  int32_t* queue = nullptr;
-  uint32_t* bm0 = nullptr;
-  uint32_t* bm1 = nullptr;
-  BatchCtl* ctl = nullptr;
-  void release() {
-    dev_free(queue);
-    dev_free(bm0);
-    dev_free(bm1);
-    dev_free(ctl);
-  }
-};
-
-// Learned-proposal state of a graph (learned.cu): core numbers, features,
-// scores, the proposal p and its CDF, and scan scratch.
-struct LearnedWorkspace {
-  int32_t* core = nullptr;
-  uint8_t* flag = nullptr;
-  int32_t* list = nullptr;
-  unsigned long long* counters = nullptr;  // [0] self-loop flag, [1] lowered, [2] list size
-  float4* feat = nullptr;
-  float* y = nullptr;
-  float* fscr = nullptr;
-  double* e = nullptr;
-  double* tsum = nullptr;
-  double* scal = nullptr;
-  double* p = nullptr;
-  double* cdf = nullptr;
-  int32_t* samp = nullptr;
-  double* samp_w = nullptr;
-  int64_t samp_cap = 0;
-  bool built = false;
-  int64_t core_passes = 0;
-  void release() {
-    dev_free(core);
-    dev_free(flag);
-    dev_free(list);
-    dev_free(counters);
-    dev_free(feat);
-    dev_free(y);
-    dev_free(fscr);
-    dev_free(e);
-    dev_free(tsum);
-    dev_free(scal);
-    dev_free(p);
-    dev_free(cdf);
-    dev_free(samp);
-    dev_free(samp_w);
-    samp_cap = 0;
-    built = false;
-  }
-};
-
-// A device-driven level loop instantiated for one configuration.
-struct LoopKey {
-  int backward;                 // 0 forward sweep, 1 backward (dependency) sweep
-  int sigma_kind;
-  unsigned long long act;
-  const int32_t* dist;
-  int64_t dist_ld;
-  const double* bc;
-  MsBuffers b;                  // lane_src and lane_w zeroed: not used inside the loop
-  HubData hd;
-  double alpha, beta;
-};
-struct LoopGraph {
-  LoopKey key;
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
-  int td_kernels = 0;           // kernels per top-down / bottom-up / backward level
-  int bu_kernels = 0;
-  int body_kernels = 0;
-  uint64_t last_use = 0;
-  void release() {
-    if (exec) cudaGraphExecDestroy(exec);
-    if (graph) cudaGraphDestroy(graph);
-    exec = nullptr;
-    graph = nullptr;
-  }
-};
-
-}  // namespace
+using namespace lgbc::api;
 
 // Lets the other translation units of the library report errors through
 // lgbc_last_error().
 void lgbc::set_last_error(const char* msg) { g_last_error = msg ? msg : ""; }
 
-struct lgbc_graph {
-  int device = 0;
-  int64_t n = 0;
-  int64_t nnz = 0;
-  int directed = 0;
-  cudaStream_t stream = nullptr;
-  int64_t* d_rowptr = nullptr;
-  int32_t* d_colidx = nullptr;
-  int64_t* d_in_rowptr = nullptr;   // == d_rowptr for undirected graphs
-  int32_t* d_in_colidx = nullptr;
-  std::vector<uint8_t> has_degree;  // degree(g, v) > 0, host copy for filtering
-  std::mutex mu;
-  MsWorkspace ms;
-  BfsWorkspace bfs;
-  HubTable hubs;
-  LearnedWorkspace learned;
-  int32_t* d_src = nullptr;         // device copy of a call's source list
-  int64_t d_src_cap = 0;
-  double* d_bc = nullptr;           // device result buffer for host-buffer calls
-  int32_t* d_dist = nullptr;        // device distance buffer (gdistances)
-  int64_t d_dist_cap = 0;
-  BatchCtl* h_ctl = nullptr;        // pinned mirror of a control block
-  cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
-  int64_t launches = 0;             // running count of kernels launched
-  int64_t launches_at_start = 0;
-  LaunchCfg cfg{};
-  size_t max_smem = 0;
-  unsigned long long sigma_limit = ~0ull;  // (2^64 - 1) / (max in-degree + 1)
-  lgbc_stats stats{};
-  lgbc_tuning tune{14.0, 24.0, 256, 64, 32, 0, 1, 1, 1 << 21, 0};
-  lgbc_graph* stack = nullptr;        // R copies of this graph (stacked batches)
-  int64_t stack_copies = 0;
-  std::vector<int32_t> h_active;      // the last call's ordered active sources
-  std::vector<double> h_weights;      // their weights (weighted calls; empty otherwise)
-  double* d_lw_fixed = nullptr;       // lane weights of the running batch (cached graphs)
-  int64_t d_lw_cap = 0;
-  cudaStream_t cap_stream = nullptr;  // stream used to capture level-loop graphs
-  std::vector<LoopGraph> loops;       // cached device-driven level loops
-  uint64_t loop_clock = 0;
-  std::vector<int32_t> landmarks;   // the highest-degree vertices (source ordering)
-  int32_t* d_lmdist = nullptr;      // landmarks x n BFS distances, computed on first use
-
-  DevGraph dev() const {
-    return DevGraph{n, nnz, d_rowptr, d_colidx, d_in_rowptr, d_in_colidx};
-  }
-};
-
-namespace {
+namespace lgbc::api {
 
 int check_graph(const lgbc_graph* g) {
   if (!g) return fail(LGBC_EINVAL, "null graph handle");
@@ -464,7 +226,7 @@ int check_launch(lgbc_graph* g) {
   return LGBC_OK;
 }
 
-MsBuffers ms_buffers(lgbc_graph* g, const int32_t* lane_src, const double* lane_w = nullptr) {
+MsBuffers ms_buffers(lgbc_graph* g, const int32_t* lane_src, const double* lane_w) {
   MsWorkspace& w = g->ms;
   MsBuffers b;
   b.visit = w.visit;
@@ -498,20 +260,6 @@ bool choose_bottom_up(const lgbc_graph* g, const BatchCtl& c, bool was_bu) {
 // One multi-source batch: forward level loop, then (with sigma) the backward
 // dependency sweep into bc.  Returns LGBC_OK, or 1 when the batch must be
 // replayed with FP64 path counts.
-// Explicit (vertex, lane) seeds on the device, for unions of graphs.
-struct Seeds {
-  const int32_t* v = nullptr;
-  const int32_t* lane = nullptr;
-  int64_t count = 0;
-  // optional premark of seedless lanes per component (unions of graphs)
-  const int64_t* seg_off = nullptr;
-  const uint64_t* seg_mark = nullptr;
-  int64_t nseg = 0;
-  // stacked unions with lane weights: one row of 64 weights per copy of an
-  // lane_w_n-vertex graph, lane_w_count weights in all
-  int64_t lane_w_n = 0;
-  int64_t lane_w_count = 0;
-};
 
 // ---------------------------------------------------------------------------
 // Device-driven level loops (tuning graph_loop = 1).  A forward sweep is one
@@ -702,9 +450,8 @@ LoopKey loop_key(lgbc_graph* g, int backward, int sigma_kind, unsigned long long
 // lane_w (sigma batches): per-lane weights of the accumulation into bc.
 // stats (distance-only batches): per-lane distance statistics, accumulated.
 int run_ms_batch(lgbc_graph* g, const int32_t* lane_src, int nl, int sigma_kind, double* bc,
-                 int32_t* dist, int64_t dist_ld, const Seeds& seeds = Seeds(),
-                 const double* lane_w = nullptr, const LevelStats* stats = nullptr,
-                 unsigned long long* stress = nullptr) {
+                 int32_t* dist, int64_t dist_ld, const Seeds& seeds, const double* lane_w,
+                 const LevelStats* stats, unsigned long long* stress) {
   const DevGraph dg = g->dev();
   LGBC_TRY(ensure_hubs(g));
   const HubData hd = hub_data(g);
@@ -838,7 +585,7 @@ int run_ms_batch(lgbc_graph* g, const int32_t* lane_src, int nl, int sigma_kind,
 int run_stacked(lgbc_graph* g, int64_t copies, double* bc_dev, const std::vector<double>* w);
 
 int run_betweenness(lgbc_graph* g, int64_t k_act, int endpoints, double* bc_dev,
-                    const double* d_w = nullptr) {
+                    const double* d_w) {
   g->launches += fill_f64(g->cfg, g->stream, bc_dev, g->n, 0.0);
   const int lanes0 = std::max(1, std::min<int>(kMaxLanes, g->tune.lanes));
   const int64_t batches = (k_act + lanes0 - 1) / lanes0;
@@ -1208,7 +955,7 @@ int finish_handle(lgbc_graph* g, const int64_t* rowptr, const int64_t* in_rowptr
   return build_hubs(g, rowptr, directed ? in_rowptr : rowptr, g->tune.hub_degree);
 }
 
-}  // namespace
+}  // namespace lgbc::api
 
 extern "C" {
 
@@ -1299,7 +1046,7 @@ int lgbc_graph_info(const lgbc_graph* g, int64_t* n, int64_t* nnz, int* directed
 
 }  // extern "C"
 
-namespace {
+namespace lgbc::api {
 
 // Level-synchronous BFS over dg from d_src[0, nsrc) into d_dist, which the
 // caller has filled (kUnreached, and any other value on vertices the search
@@ -1346,7 +1093,7 @@ int prepare_bfs(lgbc_graph* g, const int32_t* src, int64_t nsrc) {
   return LGBC_OK;
 }
 
-}  // namespace
+}  // namespace lgbc::api
 
 extern "C" {
 
@@ -1531,996 +1278,3 @@ int lgbc_memcpy(void* dst, const void* src, int64_t bytes, int kind) {
 }
 
 }  // extern "C"
-
-// ---------------------------------------------------------------------------
-// Exact betweenness of many graphs (disjoint unions, one lane per source
-// index in every graph of a group).
-// ---------------------------------------------------------------------------
-namespace {
-
-struct ManyGraph {
-  int64_t idx, n, nnz;
-  const int64_t* rowptr;  // n + 1 entries, local
-  const int32_t* colidx;  // local ids
-  int64_t out_off;        // position of its first vertex in bc_raw_out
-};
-
-// Source ordering inside a union of graphs: graph k's active sources are
-// sorted by their BFS distances to graph k's own kLandmarks highest-degree
-// vertices (one seeded kLandmarks-lane distance batch serves every graph of
-// the union at once), so that a batch lane pairs sources with similar
-// distance profiles in every component, as order_active does for one graph.
-int order_many(lgbc_graph* g, const std::vector<ManyGraph>& grp, const std::vector<int64_t>& voff,
-               std::vector<std::vector<int32_t>>& act) {
-  const int nl = kLandmarks;
-  std::vector<int32_t> sv, sl;
-  for (size_t k = 0; k < grp.size(); ++k) {
-    std::vector<std::pair<int64_t, int32_t>> deg;
-    for (int64_t v = 0; v < grp[k].n; ++v) {
-      const int64_t d = grp[k].rowptr[v + 1] - grp[k].rowptr[v];
-      if (d > 0) deg.emplace_back(-d, static_cast<int32_t>(v));
-    }
-    const size_t top = std::min<size_t>(deg.size(), static_cast<size_t>(nl));
-    std::partial_sort(deg.begin(), deg.begin() + static_cast<std::ptrdiff_t>(top), deg.end());
-    for (size_t j = 0; j < top; ++j) {
-      sv.push_back(static_cast<int32_t>(voff[k] + deg[j].second));
-      sl.push_back(static_cast<int32_t>(j));
-    }
-  }
-  if (sv.empty()) return LGBC_OK;
-  const int64_t N = g->n;
-  LGBC_TRY(ensure_ms(g, false));
-  int32_t* d_dist = nullptr;  // nl x N distances | seeds | lanes
-  LGBC_TRY(dev_alloc(&d_dist, static_cast<size_t>(nl) * static_cast<size_t>(N) + 2 * sv.size()));
-  std::unique_ptr<int32_t, cudaError_t (*)(void*)> guard(d_dist, cudaFree);
-  int32_t* d_sv = d_dist + static_cast<int64_t>(nl) * N;
-  int32_t* d_sl = d_sv + sv.size();
-  LGBC_CUDA(cudaMemcpyAsync(d_sv, sv.data(), sv.size() * 4, cudaMemcpyHostToDevice, g->stream));
-  LGBC_CUDA(cudaMemcpyAsync(d_sl, sl.data(), sl.size() * 4, cudaMemcpyHostToDevice, g->stream));
-  g->launches += fill_i32(g->cfg, g->stream, d_dist, static_cast<int64_t>(nl) * N, kUnreached);
-  Seeds sd;
-  sd.v = d_sv;
-  sd.lane = d_sl;
-  sd.count = static_cast<int64_t>(sv.size());
-  LGBC_TRY(run_ms_batch(g, nullptr, nl, kSigmaNone, nullptr, d_dist, N, sd));
-  std::vector<int32_t> dist(static_cast<size_t>(nl) * static_cast<size_t>(N));
-  LGBC_CUDA(cudaMemcpyAsync(dist.data(), d_dist, dist.size() * 4, cudaMemcpyDeviceToHost, g->stream));
-  LGBC_CUDA(cudaStreamSynchronize(g->stream));
-  for (size_t k = 0; k < grp.size(); ++k) {
-    auto& a = act[k];
-    const int64_t base = voff[k];
-    std::stable_sort(a.begin(), a.end(), [&](int32_t x, int32_t y) {
-      for (int j = 0; j < nl; ++j) {
-        const int32_t dx = dist[static_cast<size_t>(j) * N + base + x];
-        const int32_t dy = dist[static_cast<size_t>(j) * N + base + y];
-        if (dx != dy) return dx < dy;
-      }
-      return x < y;
-    });
-  }
-  return LGBC_OK;
-}
-
-int many_group(const std::vector<ManyGraph>& grp, int endpoints, double* bc_raw_out) {
-  // union CSR on the host
-  int64_t N = 0, NNZ = 0;
-  for (const auto& m : grp) {
-    N += m.n;
-    NNZ += m.nnz;
-  }
-  std::vector<int64_t> rp(static_cast<size_t>(N + 1));
-  std::vector<int32_t> ci(static_cast<size_t>(NNZ));
-  std::vector<int64_t> voff(grp.size() + 1);
-  int64_t vo = 0, eo = 0;
-  for (size_t k = 0; k < grp.size(); ++k) {
-    const ManyGraph& m = grp[k];
-    voff[k] = vo;
-    for (int64_t v = 0; v < m.n; ++v) rp[static_cast<size_t>(vo + v)] = eo + m.rowptr[v];
-    for (int64_t e = 0; e < m.nnz; ++e) {
-      // a local id outside [0, n) would land in a neighbouring graph of the union
-      if (m.colidx[e] < 0 || m.colidx[e] >= m.n)
-        return fail(LGBC_EINVAL, "graph " + std::to_string(m.idx) + ": column index outside [0, n)");
-      ci[static_cast<size_t>(eo + e)] = static_cast<int32_t>(vo + m.colidx[e]);
-    }
-    vo += m.n;
-    eo += m.nnz;
-  }
-  voff[grp.size()] = vo;
-  rp[static_cast<size_t>(N)] = NNZ;
-  lgbc_graph* g = nullptr;
-  LGBC_TRY(lgbc_graph_create(&g, N, NNZ, rp.data(), ci.data(), nullptr, nullptr, 0));
-  std::unique_ptr<lgbc_graph, int (*)(lgbc_graph*)> guard(g, lgbc_graph_destroy);
-  std::lock_guard<std::mutex> lock(g->mu);
-
-  // every graph's active sources (degree > 0), and the endpoint terms
-  std::vector<std::vector<int32_t>> act(grp.size());
-  std::vector<int32_t> sv, sl, act_src;
-  std::vector<double> seg_add(grp.size()), src_add;
-  int64_t maxa = 0;
-  for (size_t k = 0; k < grp.size(); ++k) {
-    for (int64_t v = 0; v < grp[k].n; ++v)
-      if (g->has_degree[static_cast<size_t>(voff[k] + v)]) {
-        act[k].push_back(static_cast<int32_t>(v));
-        act_src.push_back(static_cast<int32_t>(voff[k] + v));
-        src_add.push_back(static_cast<double>(grp[k].n) - 2.0);
-      }
-    seg_add[k] = static_cast<double>(act[k].size());
-    maxa = std::max<int64_t>(maxa, static_cast<int64_t>(act[k].size()));
-  }
-  if (g->tune.source_order == 1 && maxa > kMaxLanes)
-    LGBC_TRY(order_many(g, grp, voff, act));
-  // batch b, lane l holds the (64 b + l)-th ordered source of every graph
-  const int64_t nb = (maxa + kMaxLanes - 1) / kMaxLanes;
-  std::vector<int64_t> bstart(static_cast<size_t>(nb + 1), 0);
-  std::vector<uint64_t> marks(static_cast<size_t>(nb) * grp.size());
-  for (int64_t b = 0; b < nb; ++b) {
-    for (size_t k = 0; k < grp.size(); ++k) {
-      uint64_t seeded = 0;
-      for (int l = 0; l < kMaxLanes; ++l) {
-        const int64_t i = b * kMaxLanes + l;
-        if (i < static_cast<int64_t>(act[k].size())) {
-          sv.push_back(static_cast<int32_t>(voff[k] + act[k][static_cast<size_t>(i)]));
-          sl.push_back(l);
-          seeded |= 1ull << l;
-        }
-      }
-      marks[static_cast<size_t>(b) * grp.size() + k] = ~seeded;
-    }
-    bstart[static_cast<size_t>(b + 1)] = static_cast<int64_t>(sv.size());
-  }
-  int64_t* d_voff = nullptr;
-  uint64_t* d_marks = nullptr;
-  LGBC_TRY(dev_alloc(&d_voff, voff.size()));
-  std::unique_ptr<int64_t, cudaError_t (*)(void*)> g7(d_voff, cudaFree);
-  LGBC_TRY(dev_alloc(&d_marks, marks.size()));
-  std::unique_ptr<uint64_t, cudaError_t (*)(void*)> g8(d_marks, cudaFree);
-  LGBC_CUDA(cudaMemcpyAsync(d_voff, voff.data(), voff.size() * 8, cudaMemcpyHostToDevice, g->stream));
-  if (!marks.empty())
-    LGBC_CUDA(cudaMemcpyAsync(d_marks, marks.data(), marks.size() * 8, cudaMemcpyHostToDevice,
-                              g->stream));
-  int32_t* d_sv = nullptr;
-  int32_t* d_sl = nullptr;
-  LGBC_TRY(dev_alloc(&d_sv, sv.size()));
-  std::unique_ptr<int32_t, cudaError_t (*)(void*)> g1(d_sv, cudaFree);
-  LGBC_TRY(dev_alloc(&d_sl, sl.size()));
-  std::unique_ptr<int32_t, cudaError_t (*)(void*)> g2(d_sl, cudaFree);
-  if (!sv.empty()) {
-    LGBC_CUDA(cudaMemcpyAsync(d_sv, sv.data(), sv.size() * 4, cudaMemcpyHostToDevice, g->stream));
-    LGBC_CUDA(cudaMemcpyAsync(d_sl, sl.data(), sl.size() * 4, cudaMemcpyHostToDevice, g->stream));
-  }
-  if (!g->d_bc) LGBC_TRY(dev_alloc(&g->d_bc, static_cast<size_t>(N)));
-  g->launches += fill_f64(g->cfg, g->stream, g->d_bc, N, 0.0);
-  if (!sv.empty()) LGBC_TRY(ensure_ms(g, true));
-  for (int64_t b = 0; b < nb; ++b) {
-    Seeds sd;
-    sd.v = d_sv + bstart[static_cast<size_t>(b)];
-    sd.lane = d_sl + bstart[static_cast<size_t>(b)];
-    sd.count = bstart[static_cast<size_t>(b + 1)] - bstart[static_cast<size_t>(b)];
-    if (sd.count == 0) continue;
-    sd.seg_off = d_voff;
-    sd.seg_mark = d_marks + static_cast<size_t>(b) * grp.size();
-    sd.nseg = static_cast<int64_t>(grp.size());
-    int rc = run_ms_batch(g, nullptr, kMaxLanes, kSigmaU64, g->d_bc, nullptr, 0, sd);
-    if (rc == 1) rc = run_ms_batch(g, nullptr, kMaxLanes, kSigmaF64, g->d_bc, nullptr, 0, sd);
-    if (rc != LGBC_OK) return rc;
-  }
-  if (endpoints && !act_src.empty()) {
-    int64_t* d_off = nullptr;
-    double* d_add = nullptr;
-    int32_t* d_src = nullptr;
-    double* d_sadd = nullptr;
-    LGBC_TRY(dev_alloc(&d_off, voff.size()));
-    std::unique_ptr<int64_t, cudaError_t (*)(void*)> g3(d_off, cudaFree);
-    LGBC_TRY(dev_alloc(&d_add, seg_add.size()));
-    std::unique_ptr<double, cudaError_t (*)(void*)> g4(d_add, cudaFree);
-    LGBC_TRY(dev_alloc(&d_src, act_src.size()));
-    std::unique_ptr<int32_t, cudaError_t (*)(void*)> g5(d_src, cudaFree);
-    LGBC_TRY(dev_alloc(&d_sadd, src_add.size()));
-    std::unique_ptr<double, cudaError_t (*)(void*)> g6(d_sadd, cudaFree);
-    LGBC_CUDA(cudaMemcpyAsync(d_off, voff.data(), voff.size() * 8, cudaMemcpyHostToDevice, g->stream));
-    LGBC_CUDA(cudaMemcpyAsync(d_add, seg_add.data(), seg_add.size() * 8, cudaMemcpyHostToDevice, g->stream));
-    LGBC_CUDA(cudaMemcpyAsync(d_src, act_src.data(), act_src.size() * 4, cudaMemcpyHostToDevice, g->stream));
-    LGBC_CUDA(cudaMemcpyAsync(d_sadd, src_add.data(), src_add.size() * 8, cudaMemcpyHostToDevice, g->stream));
-    g->launches += add_endpoints_many(g->cfg, g->stream, g->d_bc, d_off, d_add,
-                                      static_cast<int64_t>(grp.size()), d_src, d_sadd,
-                                      static_cast<int64_t>(act_src.size()));
-    LGBC_CUDA(cudaStreamSynchronize(g->stream));
-  }
-  std::vector<double> out(static_cast<size_t>(N));
-  LGBC_CUDA(cudaMemcpyAsync(out.data(), g->d_bc, static_cast<size_t>(N) * 8, cudaMemcpyDeviceToHost,
-                            g->stream));
-  LGBC_CUDA(cudaStreamSynchronize(g->stream));
-  for (size_t k = 0; k < grp.size(); ++k)
-    std::memcpy(bc_raw_out + grp[k].out_off, out.data() + voff[k],
-                static_cast<size_t>(grp[k].n) * 8);
-  return LGBC_OK;
-}
-
-}  // namespace
-
-extern "C" int lgbc_betweenness_many(int64_t ngraphs, const int64_t* n, const int64_t* rowptr_off,
-                                     const int64_t* col_off, const int64_t* rowptr,
-                                     const int32_t* colidx, int endpoints, double* bc_raw_out) {
-  if (ngraphs < 0) return fail(LGBC_EINVAL, "negative graph count");
-  if (ngraphs == 0) return LGBC_OK;
-  if (!n || !rowptr_off || !col_off || !rowptr || !bc_raw_out)
-    return fail(LGBC_EINVAL, "null argument");
-  std::vector<ManyGraph> gs(static_cast<size_t>(ngraphs));
-  int64_t out = 0;
-  for (int64_t i = 0; i < ngraphs; ++i) {
-    if (n[i] < 0 || rowptr_off[i] < 0 || col_off[i] < 0) return fail(LGBC_EINVAL, "negative offset");
-    const int64_t* rp = rowptr + rowptr_off[i];
-    if (rp[0] != 0) return fail(LGBC_EINVAL, "each graph's rowptr must start at 0");
-    gs[static_cast<size_t>(i)] =
-        ManyGraph{i, n[i], rp[n[i]], rp, colidx ? colidx + col_off[i] : nullptr, out};
-    if (gs[static_cast<size_t>(i)].nnz > 0 && !colidx) return fail(LGBC_EINVAL, "null colidx");
-    out += n[i];
-  }
-  // size-sorted groups of at most kGroupVertices vertices (one big graph alone)
-  std::vector<size_t> order(gs.size());
-  for (size_t i = 0; i < order.size(); ++i) order[i] = i;
-  std::stable_sort(order.begin(), order.end(),
-                   [&](size_t a, size_t b) { return gs[a].n > gs[b].n; });
-  const int64_t kGroupVertices = int64_t(1) << 21;
-  std::vector<ManyGraph> grp;
-  int64_t gv = 0;
-  for (size_t oi = 0; oi < order.size(); ++oi) {
-    const ManyGraph& m = gs[order[oi]];
-    if (!grp.empty() && gv + m.n > kGroupVertices) {
-      LGBC_TRY(many_group(grp, endpoints, bc_raw_out));
-      grp.clear();
-      gv = 0;
-    }
-    grp.push_back(m);
-    gv += m.n;
-  }
-  if (!grp.empty()) LGBC_TRY(many_group(grp, endpoints, bc_raw_out));
-  return LGBC_OK;
-}
-
-// ---------------------------------------------------------------------------
-// Learned source proposal (learned.cu, mlp.cu)
-// ---------------------------------------------------------------------------
-namespace {
-
-int ensure_learned(lgbc_graph* g) {
-  LearnedWorkspace& w = g->learned;
-  if (w.core) return LGBC_OK;
-  const size_t n = static_cast<size_t>(g->n);
-  const size_t tiles = static_cast<size_t>(proposal_tiles(g->n));
-  LGBC_TRY(dev_alloc(&w.core, n));
-  LGBC_TRY(dev_alloc(&w.flag, n));
-  LGBC_TRY(dev_alloc(&w.list, n));
-  LGBC_TRY(dev_alloc(&w.counters, 4));
-  LGBC_TRY(dev_alloc(&w.feat, n));
-  LGBC_TRY(dev_alloc(&w.y, n));
-  LGBC_TRY(dev_alloc(&w.fscr, tiles + 1));
-  LGBC_TRY(dev_alloc(&w.e, n));
-  LGBC_TRY(dev_alloc(&w.tsum, tiles));
-  LGBC_TRY(dev_alloc(&w.scal, 1));
-  LGBC_TRY(dev_alloc(&w.p, n));
-  LGBC_TRY(dev_alloc(&w.cdf, n));
-  LGBC_CUDA(cudaMemsetAsync(w.flag, 0, n, g->stream));
-  return LGBC_OK;
-}
-
-unsigned long long read_counter(lgbc_graph* g, int i, int* rc) {
-  unsigned long long v = 0;
-  cudaError_t e = cudaMemcpyAsync(&v, g->learned.counters + i, 8, cudaMemcpyDeviceToHost, g->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
-  *rc = e == cudaSuccess ? LGBC_OK : cuda_fail(e, "reading a device counter");
-  return v;
-}
-
-// Core numbers into learned.core: degrees without self-loops, then h-index
-// passes over the flagged vertices until none is lowered.  strict: a
-// self-loop is an error (core_number's ArgumentError).
-int compute_core(lgbc_graph* g, bool strict) {
-  LearnedWorkspace& w = g->learned;
-  const DevGraph dg = g->dev();
-  LGBC_CUDA(cudaMemsetAsync(w.counters, 0, 4 * 8, g->stream));
-  g->launches += core_degree(g->cfg, g->stream, dg, w.core, reinterpret_cast<int*>(w.counters));
-  LGBC_TRY(check_launch(g));
-  int rc = LGBC_OK;
-  const unsigned long long loops = read_counter(g, 0, &rc);
-  LGBC_TRY(rc);
-  if (strict && (loops & 0xffffffffull))
-    return fail(LGBC_EINVAL, "core_number: graph must not have self-loops");
-  const int32_t* list = nullptr;
-  int64_t nlist = g->n;
-  w.core_passes = 0;
-  while (nlist > 0) {
-    g->launches += core_pass(g->cfg, g->stream, dg, list, nlist, w.core, w.flag, w.counters + 1);
-    LGBC_CUDA(cudaMemsetAsync(w.counters + 2, 0, 8, g->stream));
-    g->launches += core_compact(g->cfg, g->stream, g->n, w.flag, w.list, w.counters + 2);
-    LGBC_TRY(check_launch(g));
-    nlist = static_cast<int64_t>(read_counter(g, 2, &rc));
-    LGBC_TRY(rc);
-    list = w.list;
-    // every pass with work lowers some value by at least one; the values
-    // start at the degrees, so more passes than stored entries means a fault
-    if (++w.core_passes > g->nnz + 2) return fail(LGBC_ETIMEOUT, "core iteration did not settle");
-  }
-  return LGBC_OK;
-}
-
-int compute_features(lgbc_graph* g) {
-  LGBC_TRY(ensure_learned(g));
-  LGBC_TRY(compute_core(g, false));
-  g->launches += features(g->cfg, g->stream, g->dev(), g->learned.core, g->learned.feat);
-  return check_launch(g);
-}
-
-// Per-source distance statistics over the multi-source BFS (no path counts):
-// vertices reached at levels >= 1, the sum and the maximum of their levels.
-int distance_stats(lgbc_graph* g, const int32_t* src, int64_t nsrc,
-                   std::vector<unsigned long long>* cnt, std::vector<unsigned long long>* dsum,
-                   std::vector<int>* dmax) {
-  cnt->assign(static_cast<size_t>(nsrc), 0ull);
-  dsum->assign(static_cast<size_t>(nsrc), 0ull);
-  dmax->assign(static_cast<size_t>(nsrc), 0);
-  if (nsrc == 0) return LGBC_OK;
-  LGBC_TRY(ensure_ms(g, false));
-  LGBC_TRY(ensure_src(g, nsrc));
-  unsigned long long* buf = nullptr;  // cnt | dsum | dmax (as int)
-  LGBC_TRY(dev_alloc(&buf, static_cast<size_t>(nsrc) * 3));
-  std::unique_ptr<unsigned long long, void (*)(unsigned long long*)> guard(
-      buf, [](unsigned long long* q) { cudaFree(q); });
-  LGBC_CUDA(cudaMemsetAsync(buf, 0, static_cast<size_t>(nsrc) * 24, g->stream));
-  LGBC_CUDA(cudaMemcpyAsync(g->d_src, src, static_cast<size_t>(nsrc) * 4, cudaMemcpyHostToDevice,
-                            g->stream));
-  int* dm = reinterpret_cast<int*>(buf + 2 * nsrc);
-  for (int64_t s0 = 0; s0 < nsrc; s0 += kMaxLanes) {
-    const int nl = static_cast<int>(std::min<int64_t>(kMaxLanes, nsrc - s0));
-    const LevelStats st{buf + s0, buf + nsrc + s0, dm + s0};
-    LGBC_TRY(run_ms_batch(g, g->d_src + s0, nl, kSigmaNone, nullptr, nullptr, 0, Seeds(), nullptr,
-                          &st));
-    g->stats.batches++;
-  }
-  LGBC_CUDA(cudaMemcpyAsync(cnt->data(), buf, static_cast<size_t>(nsrc) * 8, cudaMemcpyDeviceToHost,
-                            g->stream));
-  LGBC_CUDA(cudaMemcpyAsync(dsum->data(), buf + nsrc, static_cast<size_t>(nsrc) * 8,
-                            cudaMemcpyDeviceToHost, g->stream));
-  LGBC_CUDA(cudaMemcpyAsync(dmax->data(), dm, static_cast<size_t>(nsrc) * 4, cudaMemcpyDeviceToHost,
-                            g->stream));
-  LGBC_CUDA(cudaStreamSynchronize(g->stream));
-  return LGBC_OK;
-}
-
-int need_undirected(const lgbc_graph* g, const char* what) {
-  if (g->directed) return fail(LGBC_EINVAL, std::string(what) + " covers undirected graphs");
-  return LGBC_OK;
-}
-
-}  // namespace
-
-extern "C" {
-
-int lgbc_core_number(lgbc_graph* g, int32_t* core_out) {
-  LGBC_TRY(check_graph(g));
-  std::lock_guard<std::mutex> lock(g->mu);
-  LGBC_TRY(use_device(g));
-  if (!core_out && g->n > 0) return fail(LGBC_EINVAL, "null output");
-  reset_stats(g);
-  if (g->n == 0) return LGBC_OK;
-  LGBC_TRY(ensure_learned(g));
-  LGBC_TRY(compute_core(g, true));
-  LGBC_CUDA(cudaMemcpyAsync(core_out, g->learned.core, static_cast<size_t>(g->n) * 4,
-                            cudaMemcpyDeviceToHost, g->stream));
-  LGBC_CUDA(cudaStreamSynchronize(g->stream));
-  g->stats.levels = g->learned.core_passes;
-  finish_stats(g);
-  return LGBC_OK;
-}
-
-int lgbc_features(lgbc_graph* g, float* feat_out) {
-  LGBC_TRY(check_graph(g));
-  std::lock_guard<std::mutex> lock(g->mu);
-  LGBC_TRY(use_device(g));
-  LGBC_TRY(need_undirected(g, "lgbc_features"));
-  if (!feat_out && g->n > 0) return fail(LGBC_EINVAL, "null output");
-  reset_stats(g);
-  if (g->n == 0) return LGBC_OK;
-  LGBC_TRY(compute_features(g));
-  LGBC_CUDA(cudaMemcpyAsync(feat_out, g->learned.feat, static_cast<size_t>(g->n) * 16,
-                            cudaMemcpyDeviceToHost, g->stream));
-  LGBC_CUDA(cudaStreamSynchronize(g->stream));
-  g->stats.levels = g->learned.core_passes;
-  finish_stats(g);
-  return LGBC_OK;
-}
-
-int lgbc_distance_stats(lgbc_graph* g, const int32_t* src, int64_t nsrc, int64_t* reached_out,
-                        int64_t* dsum_out, int32_t* dmax_out) {
-  LGBC_TRY(check_graph(g));
-  std::lock_guard<std::mutex> lock(g->mu);
-  LGBC_TRY(use_device(g));
-  LGBC_TRY(check_sources(g, src, nsrc));
-  reset_stats(g);
-  std::vector<unsigned long long> cnt, dsum;
-  std::vector<int> dmax;
-  LGBC_TRY(distance_stats(g, src, nsrc, &cnt, &dsum, &dmax));
-  for (int64_t i = 0; i < nsrc; ++i) {
-    const size_t k = static_cast<size_t>(i);
-    if (reached_out) reached_out[i] = static_cast<int64_t>(cnt[k]) + 1;
-    if (dsum_out) dsum_out[i] = static_cast<int64_t>(dsum[k]);
-    if (dmax_out) dmax_out[i] = dmax[k];
-  }
-  finish_stats(g);
-  return LGBC_OK;
-}
-
-int lgbc_dependency_mass(lgbc_graph* g, const int32_t* src, int64_t nsrc, double* mass_out) {
-  LGBC_TRY(check_graph(g));
-  std::lock_guard<std::mutex> lock(g->mu);
-  LGBC_TRY(use_device(g));
-  LGBC_TRY(check_sources(g, src, nsrc));
-  if (nsrc > 0 && !mass_out) return fail(LGBC_EINVAL, "null output");
-  reset_stats(g);
-  std::vector<unsigned long long> cnt, dsum;
-  std::vector<int> dmax;
-  LGBC_TRY(distance_stats(g, src, nsrc, &cnt, &dsum, &dmax));
-  // sum over reached t != s of (d - 1)
-  for (int64_t i = 0; i < nsrc; ++i)
-    mass_out[i] = static_cast<double>(dsum[static_cast<size_t>(i)] - cnt[static_cast<size_t>(i)]);
-  finish_stats(g);
-  return LGBC_OK;
-}
-
-int lgbc_betweenness_weighted(lgbc_graph* g, const int32_t* src, const double* w, int64_t nsrc,
-                              double* bc_raw_out) {
-  LGBC_TRY(check_graph(g));
-  std::lock_guard<std::mutex> lock(g->mu);
-  LGBC_TRY(use_device(g));
-  if (!bc_raw_out && g->n > 0) return fail(LGBC_EINVAL, "null output");
-  LGBC_TRY(check_sources(g, src, nsrc));
-  if (nsrc > 0 && !w) return fail(LGBC_EINVAL, "null weights");
-  for (int64_t i = 0; i < nsrc; ++i)
-    if (!std::isfinite(w[i])) return fail(LGBC_EINVAL, "non-finite weight");
-  reset_stats(g);
-  if (g->n == 0) return LGBC_OK;
-  // degree-0 sources contribute nothing (betweenness.jl:58): drop them with
-  // their weights.  Repeats of a source are merged into one lane carrying the
-  // summed weight (sum_i w_i delta_{s_i} is unchanged; a sample drawn with
-  // replacement repeats its likeliest sources).
-  std::vector<std::pair<int32_t, double>> sw;
-  sw.reserve(static_cast<size_t>(nsrc));
-  for (int64_t i = 0; i < nsrc; ++i)
-    if (g->has_degree[static_cast<size_t>(src[i])]) sw.emplace_back(src[i], w[i]);
-  std::stable_sort(sw.begin(), sw.end(),
-                   [](const std::pair<int32_t, double>& a, const std::pair<int32_t, double>& b) {
-                     return a.first < b.first;
-                   });
-  std::vector<int32_t> act;
-  std::vector<double> aw;
-  act.reserve(sw.size());
-  aw.reserve(sw.size());
-  for (const auto& e : sw) {
-    if (!act.empty() && act.back() == e.first) {
-      aw.back() += e.second;
-    } else {
-      act.push_back(e.first);
-      aw.push_back(e.second);
-    }
-  }
-  LGBC_TRY(order_active(g, act, &aw));
-  const int64_t k_act = static_cast<int64_t>(act.size());
-  g->stats.active_sources = k_act;
-  g->h_active = act;
-  g->h_weights = aw;
-  LGBC_TRY(ensure_src(g, k_act));
-  double* d_w = nullptr;
-  LGBC_TRY(dev_alloc(&d_w, static_cast<size_t>(std::max<int64_t>(k_act, 1))));
-  std::unique_ptr<double, void (*)(double*)> guard(d_w, [](double* q) { cudaFree(q); });
-  if (k_act > 0) {
-    LGBC_CUDA(cudaMemcpyAsync(g->d_src, act.data(), static_cast<size_t>(k_act) * 4,
-                              cudaMemcpyHostToDevice, g->stream));
-    LGBC_CUDA(cudaMemcpyAsync(d_w, aw.data(), static_cast<size_t>(k_act) * 8, cudaMemcpyHostToDevice,
-                              g->stream));
-  }
-  if (!g->d_bc) LGBC_TRY(dev_alloc(&g->d_bc, static_cast<size_t>(g->n)));
-  LGBC_TRY(run_betweenness(g, k_act, 0, g->d_bc, d_w));
-  LGBC_CUDA(cudaMemcpyAsync(bc_raw_out, g->d_bc, static_cast<size_t>(g->n) * 8,
-                            cudaMemcpyDeviceToHost, g->stream));
-  LGBC_CUDA(cudaStreamSynchronize(g->stream));
-  finish_stats(g);
-  return LGBC_OK;
-}
-
-int lgbc_proposal_build(lgbc_graph* g, lgbc_mlp* m, double eps, double* p_out) {
-  LGBC_TRY(check_graph(g));
-  std::lock_guard<std::mutex> lock(g->mu);
-  LGBC_TRY(use_device(g));
-  LGBC_TRY(need_undirected(g, "the learned proposal"));
-  if (!(eps >= 0.0 && eps <= 1.0)) return fail(LGBC_EINVAL, "eps must be in [0, 1]");
-  MlpView mv;
-  LGBC_TRY(mlp_view(m, &mv));
-  if (mv.device != g->device) return fail(LGBC_EINVAL, "MLP and graph live on different devices");
-  reset_stats(g);
-  if (g->n == 0) return fail(LGBC_EINVAL, "empty graph");
-  g->learned.built = false;
-  LGBC_TRY(compute_features(g));
-  LearnedWorkspace& w = g->learned;
-  g->launches += mlp_forward(g->cfg, g->stream, w.feat, g->n, mv.P, mv.norm, w.y);
-  g->launches += proposal_build(g->stream, w.y, g->n, eps, w.fscr, w.e, w.tsum, w.scal, w.p, w.cdf);
-  LGBC_TRY(check_launch(g));
-  if (p_out)
-    LGBC_CUDA(cudaMemcpyAsync(p_out, w.p, static_cast<size_t>(g->n) * 8, cudaMemcpyDeviceToHost,
-                              g->stream));
-  LGBC_CUDA(cudaStreamSynchronize(g->stream));
-  w.built = true;
-  g->stats.levels = w.core_passes;
-  finish_stats(g);
-  return LGBC_OK;
-}
-
-int lgbc_proposal_sample(lgbc_graph* g, int64_t k, uint64_t seed, int scheme, int32_t* src_out,
-                         double* w_out) {
-  LGBC_TRY(check_graph(g));
-  std::lock_guard<std::mutex> lock(g->mu);
-  LGBC_TRY(use_device(g));
-  LearnedWorkspace& w = g->learned;
-  if (!w.built) return fail(LGBC_EINVAL, "no proposal built for this graph");
-  if (k < 0 || (k > 0 && (!src_out || !w_out))) return fail(LGBC_EINVAL, "bad sample count or null output");
-  if (scheme != LGBC_SAMPLE_IID && scheme != LGBC_SAMPLE_SYSTEMATIC)
-    return fail(LGBC_EINVAL, "unknown sampling scheme");
-  reset_stats(g);
-  if (k == 0) return LGBC_OK;
-  if (k > w.samp_cap) {
-    dev_free(w.samp);
-    dev_free(w.samp_w);
-    w.samp_cap = 0;
-    LGBC_TRY(dev_alloc(&w.samp, static_cast<size_t>(k)));
-    LGBC_TRY(dev_alloc(&w.samp_w, static_cast<size_t>(k)));
-    w.samp_cap = k;
-  }
-  g->launches += proposal_sample(g->stream, w.cdf, w.p, g->n, k, seed,
-                                 scheme == LGBC_SAMPLE_SYSTEMATIC, w.samp, w.samp_w);
-  LGBC_TRY(check_launch(g));
-  LGBC_CUDA(cudaMemcpyAsync(src_out, w.samp, static_cast<size_t>(k) * 4, cudaMemcpyDeviceToHost,
-                            g->stream));
-  LGBC_CUDA(cudaMemcpyAsync(w_out, w.samp_w, static_cast<size_t>(k) * 8, cudaMemcpyDeviceToHost,
-                            g->stream));
-  LGBC_CUDA(cudaStreamSynchronize(g->stream));
-  finish_stats(g);
-  return LGBC_OK;
-}
-
-}  // extern "C"
-
-// ---------------------------------------------------------------------------
-// Autotuner
-// ---------------------------------------------------------------------------
-namespace {
-
-// Identifies a graph shape and device for the tuning cache.
-std::string tune_signature(const lgbc_graph* g) {
-  cudaDeviceProp prop;
-  if (cudaGetDeviceProperties(&prop, g->device) != cudaSuccess) prop.multiProcessorCount = 0;
-  char buf[256];
-  std::snprintf(buf, sizeof buf, "n=%lld,nnz=%lld,dir=%d,sms=%d", static_cast<long long>(g->n),
-                static_cast<long long>(g->nnz), g->directed, prop.multiProcessorCount);
-  return buf;
-}
-
-bool tune_from_cache(const char* path, const std::string& sig, lgbc_tuning* out) {
-  if (!path) return false;
-  FILE* f = std::fopen(path, "r");
-  if (!f) return false;
-  char line[512];
-  bool found = false;
-  while (std::fgets(line, sizeof line, f)) {
-    char key[256];
-    lgbc_tuning t{};
-    if (std::sscanf(line, "%255s %lf %lf %d %d %d %d %d %d %d", key, &t.alpha, &t.beta,
-                    &t.hub_degree, &t.lanes, &t.dense_edges, &t.segment_degree, &t.source_order,
-                    &t.graph_loop, &t.stack_vertices) == 10 &&
-        sig == key && t.alpha > 0 && t.beta > 0 && t.lanes >= 1 && t.lanes <= kMaxLanes &&
-        t.hub_degree >= 1 && t.dense_edges >= 0 && t.segment_degree >= 0 &&
-        (t.source_order == 0 || t.source_order == 1) && (t.graph_loop == 0 || t.graph_loop == 1) &&
-        t.stack_vertices >= 0) {
-      *out = t;  // the last matching line wins
-      found = true;
-    }
-  }
-  std::fclose(f);
-  return found;
-}
-
-// Milliseconds of one Brandes pass over the k sources already in d_src with
-// tuning t (best of `reps`, after one unmeasured pass).
-int tune_measure(lgbc_graph* g, const lgbc_tuning& t, int64_t k, double* bc_dev, int reps,
-                 double* ms_out) {
-  g->tune = t;
-  LGBC_TRY(ensure_hubs(g));
-  double best = 1e300;
-  for (int r = 0; r <= reps; ++r) {
-    LGBC_CUDA(cudaEventRecord(g->ev_start, g->stream));
-    LGBC_TRY(run_betweenness(g, k, 0, bc_dev));
-    LGBC_CUDA(cudaEventRecord(g->ev_stop, g->stream));
-    LGBC_CUDA(cudaEventSynchronize(g->ev_stop));
-    float ms = 0.f;
-    LGBC_CUDA(cudaEventElapsedTime(&ms, g->ev_start, g->ev_stop));
-    if (r > 0) best = std::min(best, static_cast<double>(ms));
-  }
-  *ms_out = best;
-  return LGBC_OK;
-}
-
-}  // namespace
-
-extern "C" int lgbc_tune(lgbc_graph* g, const char* cache_path) {
-  LGBC_TRY(check_graph(g));
-  std::lock_guard<std::mutex> lock(g->mu);
-  LGBC_TRY(use_device(g));
-  reset_stats(g);
-  const std::string sig = tune_signature(g);
-  lgbc_tuning cached{};
-  if (tune_from_cache(cache_path, sig, &cached)) {
-    g->tune = cached;
-    return LGBC_OK;
-  }
-  // sample: 128 active sources spread evenly over the vertex ids
-  std::vector<int32_t> act;
-  for (int64_t v = 0; v < g->n; ++v)
-    if (g->has_degree[static_cast<size_t>(v)]) act.push_back(static_cast<int32_t>(v));
-  if (act.empty()) return LGBC_OK;  // nothing to traverse: keep the defaults
-  const int64_t k = std::min<int64_t>(128, static_cast<int64_t>(act.size()));
-  std::vector<int32_t> sample(static_cast<size_t>(k));
-  for (int64_t i = 0; i < k; ++i)
-    sample[static_cast<size_t>(i)] = act[static_cast<size_t>(i * static_cast<int64_t>(act.size()) / k)];
-  LGBC_TRY(ensure_src(g, k));
-  g->h_active = sample;
-  g->h_weights.clear();
-  LGBC_CUDA(cudaMemcpyAsync(g->d_src, sample.data(), static_cast<size_t>(k) * 4,
-                            cudaMemcpyHostToDevice, g->stream));
-  LGBC_CUDA(cudaStreamSynchronize(g->stream));
-  LGBC_TRY(ensure_ms(g, true));
-  if (!g->d_bc) LGBC_TRY(dev_alloc(&g->d_bc, static_cast<size_t>(g->n)));
-  // coordinate descent over the degree-bin cut, the batch width, the
-  // direction-switch thresholds and the two gather-strategy cuts
-  lgbc_tuning best = g->tune;
-  double best_ms = 0.0;
-  LGBC_TRY(tune_measure(g, best, k, g->d_bc, 2, &best_ms));
-  const int reps = 2;
-  for (int pass = 0; pass < 2; ++pass) {
-    auto try_field = [&](auto setter, const auto& values) -> int {
-      for (const auto& val : values) {
-        lgbc_tuning c = best;
-        setter(c, val);
-        if (std::memcmp(&c, &best, sizeof c) == 0) continue;
-        double ms = 0.0;
-        LGBC_TRY(tune_measure(g, c, k, g->d_bc, reps, &ms));
-        if (ms < best_ms * 0.98) {  // a change must win by 2 %
-          best = c;
-          best_ms = ms;
-        }
-      }
-      return LGBC_OK;
-    };
-    const int hubs[] = {64, 128, 256, 512, 1024, 4096, INT32_MAX};
-    const int lanes[] = {32, 48, 64};
-    const double alphas[] = {2.0, 4.0, 8.0, 14.0, 24.0, 48.0};
-    const double betas[] = {6.0, 12.0, 24.0, 48.0, 96.0};
-    const int dense[] = {4, 8, 16, 32};
-    const int segs[] = {0, 1 << 30};
-    LGBC_TRY(try_field([](lgbc_tuning& c, int v) { c.hub_degree = v; }, hubs));
-    LGBC_TRY(try_field([](lgbc_tuning& c, int v) { c.lanes = v; }, lanes));
-    LGBC_TRY(try_field([](lgbc_tuning& c, double v) { c.alpha = v; }, alphas));
-    LGBC_TRY(try_field([](lgbc_tuning& c, double v) { c.beta = v; }, betas));
-    LGBC_TRY(try_field([](lgbc_tuning& c, int v) { c.dense_edges = v; }, dense));
-    LGBC_TRY(try_field([](lgbc_tuning& c, int v) { c.segment_degree = v; }, segs));
-  }
-  g->tune = best;
-  LGBC_TRY(ensure_hubs(g));
-  if (cache_path) {
-    FILE* f = std::fopen(cache_path, "a");
-    if (!f) return fail(LGBC_EINVAL, std::string("cannot append to tuning cache ") + cache_path);
-    std::fprintf(f, "%s %.17g %.17g %d %d %d %d %d %d %d\n", sig.c_str(), best.alpha, best.beta,
-                 best.hub_degree, best.lanes, best.dense_edges, best.segment_degree,
-                 best.source_order, best.graph_loop, best.stack_vertices);
-    std::fclose(f);
-  }
-  finish_stats(g);
-  return LGBC_OK;
-}
-
-// ---------------------------------------------------------------------------
-// Stress centrality
-// ---------------------------------------------------------------------------
-extern "C" int lgbc_stress(lgbc_graph* g, const int32_t* src, int64_t nsrc, int64_t* stress_out) {
-  LGBC_TRY(check_graph(g));
-  std::lock_guard<std::mutex> lock(g->mu);
-  LGBC_TRY(use_device(g));
-  if (!stress_out && g->n > 0) return fail(LGBC_EINVAL, "null output");
-  reset_stats(g);
-  int64_t k_act = 0;
-  LGBC_TRY(prepare_sources(g, src, nsrc, &k_act));
-  g->stats.active_sources = k_act;
-  if (g->n == 0) return LGBC_OK;
-  unsigned long long* d_st = nullptr;
-  LGBC_TRY(dev_alloc(&d_st, static_cast<size_t>(g->n)));
-  std::unique_ptr<unsigned long long, void (*)(unsigned long long*)> guard(
-      d_st, [](unsigned long long* q) { cudaFree(q); });
-  LGBC_CUDA(cudaMemsetAsync(d_st, 0, static_cast<size_t>(g->n) * 8, g->stream));
-  if (k_act > 0) LGBC_TRY(ensure_ms(g, true));  // the path-count rows hold E
-  for (int64_t s0 = 0; s0 < k_act; s0 += kMaxLanes) {
-    const int nl = static_cast<int>(std::min<int64_t>(kMaxLanes, k_act - s0));
-    LGBC_TRY(run_ms_batch(g, g->d_src + s0, nl, kSigmaNone, nullptr, nullptr, 0, Seeds(), nullptr,
-                          nullptr, d_st));
-    g->stats.batches++;
-  }
-  LGBC_CUDA(cudaMemcpyAsync(stress_out, d_st, static_cast<size_t>(g->n) * 8, cudaMemcpyDeviceToHost,
-                            g->stream));
-  LGBC_CUDA(cudaStreamSynchronize(g->stream));
-  finish_stats(g);
-  return LGBC_OK;
-}
-
-// ---------------------------------------------------------------------------
-// BFS parents and reachability
-// ---------------------------------------------------------------------------
-extern "C" int lgbc_bfs_parents(lgbc_graph* g, int32_t s, int dir, int32_t* parents_out) {
-  LGBC_TRY(check_graph(g));
-  std::lock_guard<std::mutex> lock(g->mu);
-  LGBC_TRY(use_device(g));
-  if (dir != 0 && dir != 1) return fail(LGBC_EINVAL, "dir must be 0 (out) or 1 (in)");
-  if (!parents_out && g->n > 0) return fail(LGBC_EINVAL, "null output");
-  LGBC_TRY(check_sources(g, &s, 1));
-  reset_stats(g);
-  DevGraph dg = g->dev();
-  if (dir == 1) {  // follow in-edges: swap the two CSRs
-    std::swap(dg.rowptr, dg.in_rowptr);
-    std::swap(dg.colidx, dg.in_colidx);
-  }
-  LGBC_TRY(prepare_bfs(g, &s, 1));
-  LGBC_TRY(run_bfs(g, dg, 1));
-  int32_t* d_par = nullptr;
-  LGBC_TRY(dev_alloc(&d_par, static_cast<size_t>(g->n)));
-  std::unique_ptr<int32_t, void (*)(int32_t*)> guard(d_par, [](int32_t* q) { cudaFree(q); });
-  g->launches += bfs_parents(g->cfg, g->stream, dg, g->d_dist, d_par);
-  LGBC_TRY(check_launch(g));
-  LGBC_CUDA(cudaMemcpyAsync(parents_out, d_par, static_cast<size_t>(g->n) * 4,
-                            cudaMemcpyDeviceToHost, g->stream));
-  LGBC_CUDA(cudaStreamSynchronize(g->stream));
-  finish_stats(g);
-  return LGBC_OK;
-}
-
-extern "C" int lgbc_has_path(lgbc_graph* g, int32_t u, int32_t v, const int32_t* exclude,
-                             int64_t nexclude, int* result) {
-  LGBC_TRY(check_graph(g));
-  std::lock_guard<std::mutex> lock(g->mu);
-  LGBC_TRY(use_device(g));
-  if (!result) return fail(LGBC_EINVAL, "null output");
-  LGBC_TRY(check_sources(g, &u, 1));
-  LGBC_TRY(check_sources(g, &v, 1));
-  LGBC_TRY(check_sources(g, exclude, nexclude));
-  reset_stats(g);
-  for (int64_t i = 0; i < nexclude; ++i)
-    if (exclude[i] == u || exclude[i] == v) {
-      *result = 0;
-      return LGBC_OK;
-    }
-  if (u == v) {
-    *result = 1;
-    return LGBC_OK;
-  }
-  LGBC_TRY(prepare_bfs(g, &u, 1));
-  int32_t* d_ex = nullptr;
-  if (nexclude > 0) {
-    // excluded vertices count as visited from the start (a distance the BFS
-    // never writes), so the search neither claims nor expands them
-    LGBC_TRY(dev_alloc(&d_ex, static_cast<size_t>(nexclude)));
-    LGBC_CUDA(cudaMemcpyAsync(d_ex, exclude, static_cast<size_t>(nexclude) * 4,
-                              cudaMemcpyHostToDevice, g->stream));
-    g->launches += scatter_i32(g->cfg, g->stream, g->d_dist, d_ex, nexclude, -2);
-  }
-  std::unique_ptr<int32_t, void (*)(int32_t*)> guard(d_ex, [](int32_t* q) { if (q) cudaFree(q); });
-  LGBC_TRY(run_bfs(g, g->dev(), 1));
-  int32_t dv = kUnreached;
-  LGBC_CUDA(cudaMemcpyAsync(&dv, g->d_dist + v, 4, cudaMemcpyDeviceToHost, g->stream));
-  LGBC_CUDA(cudaStreamSynchronize(g->stream));
-  *result = dv != kUnreached ? 1 : 0;
-  finish_stats(g);
-  return LGBC_OK;
-}
-
-// ---------------------------------------------------------------------------
-// Graph ingest on the device (ingest.cu)
-// ---------------------------------------------------------------------------
-namespace {
-
-// Sort `count` keys (owned: keys / alt swap), keep the first copy of each, and
-// emit the CSR rows into colidx (allocated here) and rowptr.  With `sorted_out`
-// the kept keys are also returned compacted.
-int build_rows(lgbc_graph* g, unsigned long long*& keys, unsigned long long*& alt, int64_t count,
-               int B, int32_t** colidx, int64_t* rowptr_dev, int64_t* nnz,
-               unsigned long long** sorted_out) {
-  cudaStream_t s = g->stream;
-  const int64_t cells = radix_scratch_words(count);
-  const int64_t nsums = std::max<int64_t>(std::max(scan_tiles(cells), scan_tiles(count)),
-                                          scan_tiles(g->n)) + 1;
-  uint32_t* hist = nullptr;
-  int64_t* off = nullptr;
-  int64_t* sums = nullptr;
-  uint8_t* keep = nullptr;
-  int64_t* pos = nullptr;
-  unsigned int* deg = nullptr;
-  int64_t* d_nkept = nullptr;
-  auto cleanup = [&]() {
-    cudaFree(hist); cudaFree(off); cudaFree(sums); cudaFree(keep); cudaFree(pos); cudaFree(deg);
-    cudaFree(d_nkept);
-  };
-  int rc = LGBC_OK;
-  if ((rc = dev_alloc(&hist, static_cast<size_t>(cells))) || (rc = dev_alloc(&off, static_cast<size_t>(cells))) ||
-      (rc = dev_alloc(&sums, static_cast<size_t>(nsums))) || (rc = dev_alloc(&keep, static_cast<size_t>(count))) ||
-      (rc = dev_alloc(&pos, static_cast<size_t>(count))) || (rc = dev_alloc(&deg, static_cast<size_t>(g->n))) ||
-      (rc = dev_alloc(&d_nkept, 1))) {
-    cleanup();
-    return rc;
-  }
-  g->launches += radix_sort(s, keys, alt, count, 2 * B, hist, off, sums);
-  g->launches += ingest_unique(g->cfg, s, keys, count, keep, pos, sums, d_nkept);
-  int64_t nk = 0;
-  cudaError_t e = cudaMemcpyAsync(&nk, d_nkept, 8, cudaMemcpyDeviceToHost, s);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  if (e != cudaSuccess) {
-    cleanup();
-    return cuda_fail(e, "ingest: unique arcs");
-  }
-  if (count == 0) nk = 0;
-  *nnz = nk;
-  if ((rc = dev_alloc(colidx, static_cast<size_t>(std::max<int64_t>(nk, 1))))) {
-    cleanup();
-    return rc;
-  }
-  cudaMemsetAsync(deg, 0, static_cast<size_t>(g->n) * 4, s);
-  g->launches += ingest_emit(g->cfg, s, keys, count, keep, pos, B, *colidx, deg);
-  g->launches += ingest_rowptr(s, deg, g->n, sums, rowptr_dev);
-  if (g->n == 0) cudaMemsetAsync(rowptr_dev, 0, 8, s);
-  if (sorted_out) {
-    *sorted_out = alt;  // reuse the spare buffer for the compacted keys
-    alt = nullptr;
-    g->launches += ingest_compact(g->cfg, s, keys, count, keep, pos, *sorted_out);
-  }
-  e = cudaStreamSynchronize(s);
-  cleanup();
-  if (e != cudaSuccess) return cuda_fail(e, "ingest: rows");
-  return check_launch(g);
-}
-
-int create_from_edges_impl(lgbc_graph* g, int64_t n, int64_t m, const int32_t* src,
-                           const int32_t* dst, int directed) {
-  LGBC_TRY(init_handle(g, n, directed));
-  cudaStream_t s = g->stream;
-  const int B = ingest_bits(n);
-  const int64_t count = directed ? m : 2 * m;
-  int32_t* d_edges = nullptr;
-  unsigned long long* keys = nullptr;
-  unsigned long long* alt = nullptr;
-  int* d_bad = nullptr;
-  auto cleanup = [&]() { cudaFree(d_edges); cudaFree(keys); cudaFree(alt); cudaFree(d_bad); };
-  int rc = LGBC_OK;
-  if ((rc = dev_alloc(&d_edges, static_cast<size_t>(2 * std::max<int64_t>(m, 1)))) ||
-      (rc = dev_alloc(&keys, static_cast<size_t>(std::max<int64_t>(count, 1)))) ||
-      (rc = dev_alloc(&alt, static_cast<size_t>(std::max<int64_t>(count, 1)))) ||
-      (rc = dev_alloc(&d_bad, 1))) {
-    cleanup();
-    return rc;
-  }
-  cudaMemsetAsync(d_bad, 0, 4, s);
-  if (m > 0) {
-    LGBC_CUDA(cudaMemcpyAsync(d_edges, src, static_cast<size_t>(m) * 4, cudaMemcpyHostToDevice, s));
-    LGBC_CUDA(cudaMemcpyAsync(d_edges + m, dst, static_cast<size_t>(m) * 4, cudaMemcpyHostToDevice, s));
-  }
-  g->launches += ingest_make_keys(g->cfg, s, d_edges, d_edges + m, m, n, B, directed, keys, d_bad);
-  int bad = 0;
-  LGBC_CUDA(cudaMemcpyAsync(&bad, d_bad, 4, cudaMemcpyDeviceToHost, s));
-  LGBC_CUDA(cudaStreamSynchronize(s));
-  if (bad) {
-    cleanup();
-    return fail(LGBC_EINVAL, "edge endpoint outside [0, n)");
-  }
-  cudaFree(d_edges);
-  d_edges = nullptr;
-  if ((rc = dev_alloc(&g->d_rowptr, static_cast<size_t>(n + 1)))) {
-    cleanup();
-    return rc;
-  }
-  unsigned long long* sorted = nullptr;
-  int64_t nnz = 0;
-  rc = build_rows(g, keys, alt, count, B, &g->d_colidx, g->d_rowptr, &nnz, directed ? &sorted : nullptr);
-  if (rc != LGBC_OK) {
-    cudaFree(sorted);
-    cleanup();
-    return rc;
-  }
-  g->nnz = nnz;
-  std::vector<int64_t> rp(static_cast<size_t>(n + 1)), irp;
-  if (directed) {
-    // in-CSR: the kept arcs with their ends swapped, sorted again
-    cudaFree(keys);
-    keys = nullptr;
-    unsigned long long* ikeys = nullptr;
-    if ((rc = dev_alloc(&ikeys, static_cast<size_t>(std::max<int64_t>(nnz, 1))))) {
-      cudaFree(sorted);
-      cleanup();
-      return rc;
-    }
-    g->launches += ingest_swap_keys(g->cfg, s, sorted, nnz, B, ikeys);
-    unsigned long long* ialt = sorted;
-    if ((rc = dev_alloc(&g->d_in_rowptr, static_cast<size_t>(n + 1)))) {
-      cudaFree(ikeys);
-      cudaFree(ialt);
-      cleanup();
-      return rc;
-    }
-    int64_t innz = 0;
-    rc = build_rows(g, ikeys, ialt, nnz, B, &g->d_in_colidx, g->d_in_rowptr, &innz, nullptr);
-    cudaFree(ikeys);
-    cudaFree(ialt);
-    if (rc != LGBC_OK) {
-      cleanup();
-      return rc;
-    }
-    irp.resize(static_cast<size_t>(n + 1));
-    LGBC_CUDA(cudaMemcpy(irp.data(), g->d_in_rowptr, irp.size() * 8, cudaMemcpyDeviceToHost));
-  } else {
-    g->d_in_rowptr = g->d_rowptr;
-    g->d_in_colidx = g->d_colidx;
-  }
-  cleanup();
-  LGBC_CUDA(cudaMemcpy(rp.data(), g->d_rowptr, rp.size() * 8, cudaMemcpyDeviceToHost));
-  return finish_handle(g, rp.data(), directed ? irp.data() : rp.data());
-}
-
-}  // namespace
-
-extern "C" int lgbc_graph_create_from_edges(lgbc_graph** out, int64_t n, int64_t m,
-                                            const int32_t* src, const int32_t* dst, int directed) {
-  if (!out) return fail(LGBC_EINVAL, "null output handle pointer");
-  *out = nullptr;
-  if (n < 0 || m < 0) return fail(LGBC_EINVAL, "negative vertex or edge count");
-  if (n >= INT32_MAX) return fail(LGBC_EINVAL, "vertex ids must fit in int32");
-  if (m > 0 && (!src || !dst)) return fail(LGBC_EINVAL, "null edge array");
-  if (m > (int64_t{1} << 31) - 1) return fail(LGBC_EINVAL, "at most 2^31 - 1 edges per call");
-  int ndev = 0;
-  cudaError_t e = cudaGetDeviceCount(&ndev);
-  if (e != cudaSuccess || ndev == 0) {
-    cudaGetLastError();
-    return fail(LGBC_ECUDA, std::string("no CUDA device available: ") +
-                                (e != cudaSuccess ? cudaGetErrorString(e) : "0 devices"));
-  }
-  lgbc_graph* g = new (std::nothrow) lgbc_graph();
-  if (!g) return fail(LGBC_ENOMEM, "host allocation failed");
-  const int rc = create_from_edges_impl(g, n, m, src, dst, directed);
-  if (rc != LGBC_OK) {
-    const std::string msg = g_last_error;
-    lgbc_graph_destroy(g);
-    g_last_error = msg;
-    return rc;
-  }
-  *out = g;
-  return LGBC_OK;
-}
-
-extern "C" int lgbc_graph_csr(const lgbc_graph* g, int64_t* rowptr, int32_t* colidx,
-                              int64_t* in_rowptr, int32_t* in_colidx) {
-  LGBC_TRY(check_graph(g));
-  lgbc_graph* gm = const_cast<lgbc_graph*>(g);
-  std::lock_guard<std::mutex> lock(gm->mu);
-  LGBC_TRY(use_device(gm));
-  LGBC_CUDA(cudaStreamSynchronize(g->stream));
-  if (rowptr)
-    LGBC_CUDA(cudaMemcpy(rowptr, g->d_rowptr, static_cast<size_t>(g->n + 1) * 8, cudaMemcpyDeviceToHost));
-  if (colidx && g->nnz > 0)
-    LGBC_CUDA(cudaMemcpy(colidx, g->d_colidx, static_cast<size_t>(g->nnz) * 4, cudaMemcpyDeviceToHost));
-  if (in_rowptr)
-    LGBC_CUDA(cudaMemcpy(in_rowptr, g->d_in_rowptr, static_cast<size_t>(g->n + 1) * 8,
-                         cudaMemcpyDeviceToHost));
-  if (in_colidx && g->nnz > 0)
-    LGBC_CUDA(cudaMemcpy(in_colidx, g->d_in_colidx, static_cast<size_t>(g->nnz) * 4,
-                         cudaMemcpyDeviceToHost));
-  return LGBC_OK;
-}
