@@ -41,6 +41,8 @@ def test_ingest_matches_host_storage(directed):
 @pytest.mark.parametrize("directed", [False, True])
 def test_ingest_edge_cases(directed):
     _check(5, np.zeros(0, np.int64), np.zeros(0, np.int64), directed)  # no edges
+    g0 = lgbc.graph_from_edges(0, [], [], directed=directed)             # no vertices
+    assert g0.nv() == 0 and len(g0.csr()[1]) == 0
     _check(1, [0], [0], directed)                                       # one self-loop
     _check(7, [6, 6, 0], [0, 0, 6], directed)                           # repeats both ways
     with pytest.raises((lgbc.ArgumentError, lgbc.BoundsError)):
