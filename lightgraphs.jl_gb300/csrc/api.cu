@@ -462,7 +462,7 @@ int run_ms_batch(lgbc_graph* g, const int32_t* lane_src, int nl, int sigma_kind,
     if (seeds.seg_mark) g->launches += ms_premark(g->cfg, g->stream, b, seeds.seg_off, seeds.seg_mark,
                                                   seeds.nseg);
     if (seeds.v)
-      g->launches += ms_init_seeds(g->cfg, g->stream, dg, b, seeds.v, seeds.lane, seeds.count,
+      g->launches += ms_init_seeds(g->cfg, g->stream, dg, b, seeds.v, seeds.mask, seeds.count,
                                    sigma_kind, g->sigma_limit, dist, dist_ld);
     else
       g->launches += ms_init(g->stream, dg, b, nl, sigma_kind, g->sigma_limit, dist, dist_ld);
@@ -736,7 +736,8 @@ int run_stacked(lgbc_graph* g, int64_t copies, double* bc_dev, const std::vector
   const int64_t k = static_cast<int64_t>(act.size());
   const int64_t per = L * copies;
   const int64_t nbu = (k + per - 1) / per;
-  std::vector<int32_t> sv, sl;
+  std::vector<int32_t> sv;
+  std::vector<uint64_t> sm;
   std::vector<int64_t> bstart(static_cast<size_t>(nbu + 1), 0), voff(static_cast<size_t>(copies + 1));
   std::vector<uint64_t> marks(static_cast<size_t>(nbu * copies));
   std::vector<int64_t> filled(static_cast<size_t>(nbu), 0);  // ordinary batches per union batch
@@ -748,9 +749,16 @@ int run_stacked(lgbc_graph* g, int64_t copies, double* bc_dev, const std::vector
       if ((u * copies + r) * L < k) filled[static_cast<size_t>(u)]++;
       uint64_t seeded = 0;
       const int64_t i0 = (u * copies + r) * L;
+      const size_t first = sv.size();  // this copy's seeds: a repeated source is one seed
       for (int l = 0; l < L && i0 + l < k; ++l) {
-        sv.push_back(static_cast<int32_t>(r * n + act[static_cast<size_t>(i0 + l)]));
-        sl.push_back(l);
+        const int32_t v = static_cast<int32_t>(r * n + act[static_cast<size_t>(i0 + l)]);
+        size_t j = first;
+        while (j < sv.size() && sv[j] != v) ++j;
+        if (j == sv.size()) {
+          sv.push_back(v);
+          sm.push_back(0ull);
+        }
+        sm[j] |= 1ull << l;
         seeded |= 1ull << l;
         if (w) wrows[static_cast<size_t>((u * copies + r) * 64 + l)] = (*w)[static_cast<size_t>(i0 + l)];
       }
@@ -759,9 +767,9 @@ int run_stacked(lgbc_graph* g, int64_t copies, double* bc_dev, const std::vector
     }
     bstart[static_cast<size_t>(u + 1)] = static_cast<int64_t>(sv.size());
   }
-  // one device buffer: weight rows | voff | marks | seed vertices | seed lanes
-  const size_t bytes = wrows.size() * 8 + voff.size() * 8 + marks.size() * 8 + sv.size() * 4 +
-                       sl.size() * 4 + 16;
+  // one device buffer: weight rows | voff | marks | seed masks | seed vertices
+  const size_t bytes = wrows.size() * 8 + voff.size() * 8 + marks.size() * 8 + sm.size() * 8 +
+                       sv.size() * 4 + 16;
   unsigned char* buf = nullptr;
   LGBC_TRY(dev_alloc(&buf, bytes));
   std::unique_ptr<unsigned char, cudaError_t (*)(void*)> guard(buf, cudaFree);
@@ -771,12 +779,12 @@ int run_stacked(lgbc_graph* g, int64_t copies, double* bc_dev, const std::vector
                               st->stream));
   int64_t* d_voff = reinterpret_cast<int64_t*>(buf + wrows.size() * 8);
   uint64_t* d_marks = reinterpret_cast<uint64_t*>(d_voff + voff.size());
-  int32_t* d_sv = reinterpret_cast<int32_t*>(d_marks + marks.size());
-  int32_t* d_sl = d_sv + sv.size();
+  uint64_t* d_sm = d_marks + marks.size();
+  int32_t* d_sv = reinterpret_cast<int32_t*>(d_sm + sm.size());
   LGBC_CUDA(cudaMemcpyAsync(d_voff, voff.data(), voff.size() * 8, cudaMemcpyHostToDevice, st->stream));
   LGBC_CUDA(cudaMemcpyAsync(d_marks, marks.data(), marks.size() * 8, cudaMemcpyHostToDevice, st->stream));
+  LGBC_CUDA(cudaMemcpyAsync(d_sm, sm.data(), sm.size() * 8, cudaMemcpyHostToDevice, st->stream));
   LGBC_CUDA(cudaMemcpyAsync(d_sv, sv.data(), sv.size() * 4, cudaMemcpyHostToDevice, st->stream));
-  LGBC_CUDA(cudaMemcpyAsync(d_sl, sl.data(), sl.size() * 4, cudaMemcpyHostToDevice, st->stream));
   if (!st->d_bc) LGBC_TRY(dev_alloc(&st->d_bc, static_cast<size_t>(st->n)));
   st->launches += fill_f64(st->cfg, st->stream, st->d_bc, st->n, 0.0);
   LGBC_TRY(ensure_ms(st, true));
@@ -785,7 +793,7 @@ int run_stacked(lgbc_graph* g, int64_t copies, double* bc_dev, const std::vector
   for (int64_t u = 0; u < nbu; ++u) {
     Seeds sd;
     sd.v = d_sv + bstart[static_cast<size_t>(u)];
-    sd.lane = d_sl + bstart[static_cast<size_t>(u)];
+    sd.mask = d_sm + bstart[static_cast<size_t>(u)];
     sd.count = bstart[static_cast<size_t>(u + 1)] - bstart[static_cast<size_t>(u)];
     sd.seg_off = d_voff;
     sd.seg_mark = d_marks + static_cast<size_t>(u * copies);

@@ -203,10 +203,12 @@ struct LoopGraph {
 }  // namespace lgbc::api
 
 namespace lgbc::api {
-// Explicit (vertex, lane) seeds on the device, for unions of graphs.
+// Explicit (vertex, lane mask) seeds on the device, for unions of graphs;
+// the vertices are distinct (a vertex that starts several lanes has them all
+// in its mask).
 struct Seeds {
   const int32_t* v = nullptr;
-  const int32_t* lane = nullptr;
+  const uint64_t* mask = nullptr;
   int64_t count = 0;
   // optional premark of seedless lanes per component (unions of graphs)
   const int64_t* seg_off = nullptr;

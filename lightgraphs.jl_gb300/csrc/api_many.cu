@@ -26,7 +26,8 @@ struct ManyGraph {
 int order_many(lgbc_graph* g, const std::vector<ManyGraph>& grp, const std::vector<int64_t>& voff,
                std::vector<std::vector<int32_t>>& act) {
   const int nl = kLandmarks;
-  std::vector<int32_t> sv, sl;
+  std::vector<int32_t> sv;
+  std::vector<uint64_t> sm;
   for (size_t k = 0; k < grp.size(); ++k) {
     std::vector<std::pair<int64_t, int32_t>> deg;
     for (int64_t v = 0; v < grp[k].n; ++v) {
@@ -37,23 +38,25 @@ int order_many(lgbc_graph* g, const std::vector<ManyGraph>& grp, const std::vect
     std::partial_sort(deg.begin(), deg.begin() + static_cast<std::ptrdiff_t>(top), deg.end());
     for (size_t j = 0; j < top; ++j) {
       sv.push_back(static_cast<int32_t>(voff[k] + deg[j].second));
-      sl.push_back(static_cast<int32_t>(j));
+      sm.push_back(1ull << j);
     }
   }
   if (sv.empty()) return LGBC_OK;
   const int64_t N = g->n;
   LGBC_TRY(ensure_ms(g, false));
-  int32_t* d_dist = nullptr;  // nl x N distances | seeds | lanes
-  LGBC_TRY(dev_alloc(&d_dist, static_cast<size_t>(nl) * static_cast<size_t>(N) + 2 * sv.size()));
+  int32_t* d_dist = nullptr;  // nl x N distances | seed vertices
+  LGBC_TRY(dev_alloc(&d_dist, static_cast<size_t>(nl) * static_cast<size_t>(N) + sv.size()));
   std::unique_ptr<int32_t, cudaError_t (*)(void*)> guard(d_dist, cudaFree);
+  uint64_t* d_sm = nullptr;
+  LGBC_TRY(dev_alloc(&d_sm, sm.size()));
+  std::unique_ptr<uint64_t, cudaError_t (*)(void*)> guard2(d_sm, cudaFree);
   int32_t* d_sv = d_dist + static_cast<int64_t>(nl) * N;
-  int32_t* d_sl = d_sv + sv.size();
   LGBC_CUDA(cudaMemcpyAsync(d_sv, sv.data(), sv.size() * 4, cudaMemcpyHostToDevice, g->stream));
-  LGBC_CUDA(cudaMemcpyAsync(d_sl, sl.data(), sl.size() * 4, cudaMemcpyHostToDevice, g->stream));
+  LGBC_CUDA(cudaMemcpyAsync(d_sm, sm.data(), sm.size() * 8, cudaMemcpyHostToDevice, g->stream));
   g->launches += fill_i32(g->cfg, g->stream, d_dist, static_cast<int64_t>(nl) * N, kUnreached);
   Seeds sd;
   sd.v = d_sv;
-  sd.lane = d_sl;
+  sd.mask = d_sm;
   sd.count = static_cast<int64_t>(sv.size());
   LGBC_TRY(run_ms_batch(g, nullptr, nl, kSigmaNone, nullptr, d_dist, N, sd));
   std::vector<int32_t> dist(static_cast<size_t>(nl) * static_cast<size_t>(N));
@@ -107,7 +110,8 @@ int many_group(const std::vector<ManyGraph>& grp, int endpoints, double* bc_raw_
 
   // every graph's active sources (degree > 0), and the endpoint terms
   std::vector<std::vector<int32_t>> act(grp.size());
-  std::vector<int32_t> sv, sl, act_src;
+  std::vector<int32_t> sv, act_src;
+  std::vector<uint64_t> sm;
   std::vector<double> seg_add(grp.size()), src_add;
   int64_t maxa = 0;
   for (size_t k = 0; k < grp.size(); ++k) {
@@ -133,7 +137,7 @@ int many_group(const std::vector<ManyGraph>& grp, int endpoints, double* bc_raw_
         const int64_t i = b * kMaxLanes + l;
         if (i < static_cast<int64_t>(act[k].size())) {
           sv.push_back(static_cast<int32_t>(voff[k] + act[k][static_cast<size_t>(i)]));
-          sl.push_back(l);
+          sm.push_back(1ull << l);
           seeded |= 1ull << l;
         }
       }
@@ -152,14 +156,14 @@ int many_group(const std::vector<ManyGraph>& grp, int endpoints, double* bc_raw_
     LGBC_CUDA(cudaMemcpyAsync(d_marks, marks.data(), marks.size() * 8, cudaMemcpyHostToDevice,
                               g->stream));
   int32_t* d_sv = nullptr;
-  int32_t* d_sl = nullptr;
+  uint64_t* d_sm = nullptr;
   LGBC_TRY(dev_alloc(&d_sv, sv.size()));
   std::unique_ptr<int32_t, cudaError_t (*)(void*)> g1(d_sv, cudaFree);
-  LGBC_TRY(dev_alloc(&d_sl, sl.size()));
-  std::unique_ptr<int32_t, cudaError_t (*)(void*)> g2(d_sl, cudaFree);
+  LGBC_TRY(dev_alloc(&d_sm, sm.size()));
+  std::unique_ptr<uint64_t, cudaError_t (*)(void*)> g2(d_sm, cudaFree);
   if (!sv.empty()) {
     LGBC_CUDA(cudaMemcpyAsync(d_sv, sv.data(), sv.size() * 4, cudaMemcpyHostToDevice, g->stream));
-    LGBC_CUDA(cudaMemcpyAsync(d_sl, sl.data(), sl.size() * 4, cudaMemcpyHostToDevice, g->stream));
+    LGBC_CUDA(cudaMemcpyAsync(d_sm, sm.data(), sm.size() * 8, cudaMemcpyHostToDevice, g->stream));
   }
   if (!g->d_bc) LGBC_TRY(dev_alloc(&g->d_bc, static_cast<size_t>(N)));
   g->launches += fill_f64(g->cfg, g->stream, g->d_bc, N, 0.0);
@@ -167,7 +171,7 @@ int many_group(const std::vector<ManyGraph>& grp, int endpoints, double* bc_raw_
   for (int64_t b = 0; b < nb; ++b) {
     Seeds sd;
     sd.v = d_sv + bstart[static_cast<size_t>(b)];
-    sd.lane = d_sl + bstart[static_cast<size_t>(b)];
+    sd.mask = d_sm + bstart[static_cast<size_t>(b)];
     sd.count = bstart[static_cast<size_t>(b + 1)] - bstart[static_cast<size_t>(b)];
     if (sd.count == 0) continue;
     sd.seg_off = d_voff;

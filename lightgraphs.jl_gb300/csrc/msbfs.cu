@@ -1476,27 +1476,30 @@ __global__ void __launch_bounds__(256) k_ms_level_stats(MsBuffers b, unsigned lo
 }
 
 // Batch initialisation with explicit seeds: seed i puts vertex seed_v[i] at
-// level 0 of lane seed_lane[i].  Used for disjoint unions of graphs, where a
+// level 0 of the lanes in seed_mask[i].  Used for disjoint unions of graphs, where a
 // lane may hold one source in every component: BFS trees of different
 // components never meet, so each component sees a single-source traversal.
-// Seed vertices must be distinct.  The host zeroes the control block first.
+// Seed vertices must be distinct (a vertex that starts several lanes is one
+// seed with several mask bits).  The host zeroes the control block first.
 template <int SK>
 __global__ void k_ms_init_seeds(DevGraph g, MsBuffers b, const int32_t* seed_v,
-                                const int32_t* seed_lane, long long nseeds, int32_t* dist,
+                                const uint64_t* seed_mask, long long nseeds, int32_t* dist,
                                 int64_t ld) {
   using T = typename Sig<SK>::T;
   unsigned long long mf = 0;
   for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < nseeds;
        i += static_cast<long long>(gridDim.x) * blockDim.x) {
     const int32_t v = seed_v[i];
-    const int l = seed_lane[i];
-    const uint64_t m = 1ull << l;
+    const uint64_t m = seed_mask[i];
     b.mb[0][v] = m;
     b.visit[v] |= m;
     b.qv[i] = v;
     b.qm[i] = m;
-    if (SK != kSigmaNone) reinterpret_cast<T*>(b.sigma)[static_cast<int64_t>(v) * 64 + l] = T(1);
-    if (dist) dist[static_cast<int64_t>(l) * ld + v] = 0;
+    for (uint64_t r = m; r; r &= r - 1) {
+      const int l = __ffsll(static_cast<long long>(r)) - 1;
+      if (SK != kSigmaNone) reinterpret_cast<T*>(b.sigma)[static_cast<int64_t>(v) * 64 + l] = T(1);
+      if (dist) dist[static_cast<int64_t>(l) * ld + v] = 0;
+    }
     mf += static_cast<unsigned long long>(g.rowptr[v + 1] - g.rowptr[v]);
   }
   mf = warp_sum_u64(mf);
@@ -1557,21 +1560,21 @@ int ms_init(cudaStream_t s, const DevGraph& g, const MsBuffers& b, int nlanes, i
 }
 
 int ms_init_seeds(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
-                  const int32_t* seed_v, const int32_t* seed_lane, int64_t nseeds, int sigma_kind,
+                  const int32_t* seed_v, const uint64_t* seed_mask, int64_t nseeds, int sigma_kind,
                   unsigned long long sigma_limit, int32_t* dist, int64_t dist_ld) {
   cudaMemsetAsync(b.ctl, 0, sizeof(BatchCtl), s);
   const int grid = static_cast<int>(std::min<int64_t>((nseeds + 255) / 256, c.grid));
   switch (sigma_kind) {
     case kSigmaU64:
-      k_ms_init_seeds<kSigmaU64><<<grid, 256, 0, s>>>(g, b, seed_v, seed_lane, nseeds, dist, dist_ld);
+      k_ms_init_seeds<kSigmaU64><<<grid, 256, 0, s>>>(g, b, seed_v, seed_mask, nseeds, dist, dist_ld);
       k_ms_init_seeds_ctl<<<1, 1, 0, s>>>(b, nseeds, b.cap, sigma_limit);
       break;
     case kSigmaF64:
-      k_ms_init_seeds<kSigmaF64><<<grid, 256, 0, s>>>(g, b, seed_v, seed_lane, nseeds, dist, dist_ld);
+      k_ms_init_seeds<kSigmaF64><<<grid, 256, 0, s>>>(g, b, seed_v, seed_mask, nseeds, dist, dist_ld);
       k_ms_init_seeds_ctl<<<1, 1, 0, s>>>(b, nseeds, b.cap, ~0ull);
       break;
     default:
-      k_ms_init_seeds<kSigmaNone><<<grid, 256, 0, s>>>(g, b, seed_v, seed_lane, nseeds, dist, dist_ld);
+      k_ms_init_seeds<kSigmaNone><<<grid, 256, 0, s>>>(g, b, seed_v, seed_mask, nseeds, dist, dist_ld);
       k_ms_init_seeds_ctl<<<1, 1, 0, s>>>(b, nseeds, b.cap, ~0ull);
       break;
   }

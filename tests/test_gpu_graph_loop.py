@@ -140,3 +140,19 @@ def test_weighted_batches_in_every_mode(directed):
         kw = dict(directed=True, in_rowptr=irp, in_colidx=ici)
     _, want = oracle.dependency(rp, ci, src, w, **kw)
     np.testing.assert_allclose(base, want, rtol=1e-9, atol=1e-9)
+
+
+def test_stacked_batches_with_repeated_sources():
+    # a source repeated inside one copy's batch becomes one seed with several lanes
+    g = gen.erdos_renyi_nm(600, 1600, seed=13)
+    rng = np.random.default_rng(6)
+    src = rng.choice(np.arange(1, g.nv() + 1), 300, replace=True)
+    src[:20] = src[0]
+    h = g.device_handle()
+    for lanes in (7, 64):
+        h.set_tuning(lanes=lanes, stack_vertices=1 << 21)
+        b = lgbc.betweenness_centrality(g, src)
+        rp, ci = g.csr()
+        want = oracle.betweenness_centrality(rp, ci, (src - 1).astype(np.int32))
+        np.testing.assert_allclose(b, want, rtol=1e-9, atol=1e-12)
+    h.set_tuning(lanes=64)
