@@ -47,37 +47,48 @@ int ensure_src(lgbc_graph* g, int64_t count) {
   return LGBC_OK;
 }
 
-int ensure_ms(lgbc_graph* g, bool need_sigma) {
+int ensure_ms(lgbc_graph* g, bool need_sigma, int words) {
   MsWorkspace& w = g->ms;
   const size_t n = static_cast<size_t>(g->n);
+  const size_t mask_words = n * kMaxWords;
   if (!w.visit) {
-    LGBC_TRY(dev_alloc(&w.visit, n));
-    LGBC_TRY(dev_alloc(&w.mb0, n));
-    LGBC_TRY(dev_alloc(&w.mb1, n));
+    LGBC_TRY(dev_alloc(&w.visit, mask_words));
+    LGBC_TRY(dev_alloc(&w.mb0, mask_words));
+    LGBC_TRY(dev_alloc(&w.mb1, mask_words));
     LGBC_TRY(dev_alloc(&w.lvl_off, n + 3));
     LGBC_TRY(dev_alloc(&w.ctl, 1));
-    LGBC_CUDA(cudaMemsetAsync(w.visit, 0, n * 8, g->stream));
-    LGBC_CUDA(cudaMemsetAsync(w.mb0, 0, n * 8, g->stream));
-    LGBC_CUDA(cudaMemsetAsync(w.mb1, 0, n * 8, g->stream));
+    LGBC_CUDA(cudaMemsetAsync(w.visit, 0, mask_words * 8, g->stream));
+    LGBC_CUDA(cudaMemsetAsync(w.mb0, 0, mask_words * 8, g->stream));
+    LGBC_CUDA(cudaMemsetAsync(w.mb1, 0, mask_words * 8, g->stream));
   }
   if (!w.qv) {
     const unsigned long long cap = 4ull * n + 1024;
     LGBC_TRY(dev_alloc(&w.qv, cap));
-    LGBC_TRY(dev_alloc(&w.qm, cap));
+    LGBC_TRY(dev_alloc(&w.qm, cap * kMaxWords));
     w.cap = cap;
   }
-  if (need_sigma && !w.have_sigma) {
+  if (words > 1 && !w.claim) {
+    LGBC_TRY(dev_alloc(&w.claim, n + 1));
+    LGBC_CUDA(cudaMemsetAsync(w.claim, 0, (n + 1) * sizeof(unsigned), g->stream));
+  }
+  if (need_sigma && w.sigma_words < words) {
+    LGBC_CUDA(cudaStreamSynchronize(g->stream));
+    if (w.sigma) cudaFree(w.sigma);
+    if (w.psi) cudaFree(w.psi);
+    w.sigma = w.psi = nullptr;
+    w.sigma_words = 0;
+    const size_t row = static_cast<size_t>(64) * static_cast<size_t>(words);
     unsigned long long* s = nullptr;
     unsigned long long* p = nullptr;
-    LGBC_TRY(dev_alloc(&s, n * kMaxLanes));
-    int rc = dev_alloc(&p, n * kMaxLanes);
+    LGBC_TRY(dev_alloc(&s, n * row));
+    int rc = dev_alloc(&p, n * row);
     if (rc != LGBC_OK) {
       cudaFree(s);
       return rc;
     }
     w.sigma = s;
     w.psi = p;
-    w.have_sigma = true;
+    w.sigma_words = words;
   }
   return LGBC_OK;
 }
@@ -85,14 +96,15 @@ int ensure_ms(lgbc_graph* g, bool need_sigma) {
 int grow_ms_lists(lgbc_graph* g) {
   MsWorkspace& w = g->ms;
   const unsigned long long n = static_cast<unsigned long long>(g->n);
-  const unsigned long long max_cap = 65ull * n + 1024;  // 64 lanes x n levels + level 0
+  // every lane puts a vertex on at most one level: lanes x n entries + level 0
+  const unsigned long long max_cap = (kWideLanes + 1ull) * n + 1024;
   unsigned long long cap = std::min(max_cap, w.cap * 2);
   if (cap <= w.cap) return fail(LGBC_ENOMEM, "level lists cannot grow further");
   LGBC_CUDA(cudaStreamSynchronize(g->stream));
   dev_free(w.qv);
   dev_free(w.qm);
   LGBC_TRY(dev_alloc(&w.qv, cap));
-  LGBC_TRY(dev_alloc(&w.qm, cap));
+  LGBC_TRY(dev_alloc(&w.qm, cap * kMaxWords));
   w.cap = cap;
   return LGBC_OK;
 }
@@ -173,11 +185,12 @@ int build_hubs(lgbc_graph* g, const int64_t* rowptr, const int64_t* in_rowptr, i
     g->hubs.in_items = g->hubs.out_items;
     g->hubs.n_in = g->hubs.n_out;
   }
-  LGBC_TRY(dev_alloc(&g->hubs.acc, static_cast<size_t>(nslots) * kMaxLanes));
-  LGBC_TRY(dev_alloc(&g->hubs.mask, static_cast<size_t>(nslots)));
+  // accumulators for the widest batch: 64 * kMaxWords lanes, kMaxWords mask words
+  LGBC_TRY(dev_alloc(&g->hubs.acc, static_cast<size_t>(nslots) * kWideLanes));
+  LGBC_TRY(dev_alloc(&g->hubs.mask, static_cast<size_t>(nslots) * kMaxWords));
   LGBC_TRY(dev_alloc(&g->hubs.cnt, static_cast<size_t>(nslots)));
-  LGBC_CUDA(cudaMemset(g->hubs.acc, 0, static_cast<size_t>(nslots) * kMaxLanes * 8));
-  LGBC_CUDA(cudaMemset(g->hubs.mask, 0, static_cast<size_t>(nslots) * 8));
+  LGBC_CUDA(cudaMemset(g->hubs.acc, 0, static_cast<size_t>(nslots) * kWideLanes * 8));
+  LGBC_CUDA(cudaMemset(g->hubs.mask, 0, static_cast<size_t>(nslots) * kMaxWords * 8));
   LGBC_CUDA(cudaMemset(g->hubs.cnt, 0, static_cast<size_t>(nslots) * 4));
   return LGBC_OK;
 }
@@ -242,6 +255,8 @@ MsBuffers ms_buffers(lgbc_graph* g, const int32_t* lane_src, const double* lane_
   b.cap = w.cap;
   b.lane_w = lane_w;
   b.lane_w_n = 0;
+  b.claim = w.claim;
+  b.words = 1;
   return b;
 }
 
@@ -424,7 +439,7 @@ int get_loop(lgbc_graph* g, const LoopKey& k, LoopGraph** out) {
   return LGBC_OK;
 }
 
-LoopKey loop_key(lgbc_graph* g, int backward, int sigma_kind, unsigned long long act,
+LoopKey loop_key(lgbc_graph* g, int backward, int sigma_kind, const LaneSet& act,
                  const int32_t* dist, int64_t ld, const double* bc, const MsBuffers& b,
                  const HubData& hd) {
   LoopKey k;
@@ -455,9 +470,17 @@ int run_ms_batch(lgbc_graph* g, const int32_t* lane_src, int nl, int sigma_kind,
   const DevGraph dg = g->dev();
   LGBC_TRY(ensure_hubs(g));
   const HubData hd = hub_data(g);
-  const uint64_t act = nl >= 64 ? ~0ull : ((1ull << nl) - 1ull);
+  // more than 64 lanes: a two-word batch (plain Brandes batches only)
+  const int words = nl > kMaxLanes ? 2 : 1;
+  if (nl < 1 || nl > kWideLanes)
+    return fail(LGBC_EINVAL, "internal: a multi-source batch holds 1 to 128 lanes");
+  if (words > 1 && (dist || seeds.v || stats || stress || sigma_kind == kSigmaNone ||
+                    g->ms.sigma_words < words || !g->ms.claim))
+    return fail(LGBC_EINVAL, "internal: a two-word batch is a plain Brandes batch");
+  const LaneSet act = lane_set(nl, words);
   for (;;) {
     MsBuffers b = ms_buffers(g, lane_src, lane_w);
+    b.words = words;
     b.lane_w_n = seeds.lane_w_n;
     if (seeds.seg_mark) g->launches += ms_premark(g->cfg, g->stream, b, seeds.seg_off, seeds.seg_mark,
                                                   seeds.nseg);
@@ -596,8 +619,8 @@ int run_betweenness(lgbc_graph* g, int64_t k_act, int endpoints, double* bc_dev,
     if (endpoints) g->launches += add_endpoints(g->cfg, g->stream, bc_dev, g->n, g->d_src, k_act);
     return check_launch(g);
   }
-  if (k_act > 0) LGBC_TRY(ensure_ms(g, true));
-  const int lanes = std::max(1, std::min<int>(kMaxLanes, g->tune.lanes));
+  const int lanes = std::max(1, std::min<int>(kWideLanes, g->tune.lanes));
+  if (k_act > 0) LGBC_TRY(ensure_ms(g, true, lanes > kMaxLanes ? 2 : 1));
   for (int64_t s0 = 0; s0 < k_act; s0 += lanes) {
     const int nl = static_cast<int>(std::min<int64_t>(lanes, k_act - s0));
     const double* lw = d_w ? d_w + s0 : nullptr;
@@ -1229,12 +1252,12 @@ int lgbc_get_tuning(const lgbc_graph* g, lgbc_tuning* out) {
 int lgbc_set_tuning(lgbc_graph* g, const lgbc_tuning* t) {
   LGBC_TRY(check_graph(g));
   if (!t) return fail(LGBC_EINVAL, "null tuning");
-  if (!(t->alpha > 0) || !(t->beta > 0) || t->lanes < 1 || t->lanes > kMaxLanes ||
+  if (!(t->alpha > 0) || !(t->beta > 0) || t->lanes < 1 || t->lanes > kWideLanes ||
       t->hub_degree < 1 || t->dense_edges < 0 || t->segment_degree < 0 ||
       (t->source_order != 0 && t->source_order != 1) || (t->graph_loop != 0 && t->graph_loop != 1) ||
       t->stack_vertices < 0)
     return fail(LGBC_EINVAL,
-                "tuning out of range (alpha, beta > 0; 1 <= lanes <= 64; hub_degree >= 1; dense_edges >= 0)");
+                "tuning out of range (alpha, beta > 0; 1 <= lanes <= 128; hub_degree >= 1; dense_edges >= 0)");
   std::lock_guard<std::mutex> lock(g->mu);
   g->tune = *t;
   return LGBC_OK;

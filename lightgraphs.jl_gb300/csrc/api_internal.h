@@ -66,7 +66,8 @@ void dev_free(T*& p) {
   p = nullptr;
 }
 
-// Multi-source workspace (msbfs.cu), sized for one batch of 64 lanes.
+// Multi-source workspace (msbfs.cu): lane sets sized for two words per
+// vertex / list entry; path-count and psi rows for `sigma_words` words.
 struct MsWorkspace {
   uint64_t* visit = nullptr;
   uint64_t* mb0 = nullptr;
@@ -77,8 +78,9 @@ struct MsWorkspace {
   uint64_t* qm = nullptr;
   unsigned long long* lvl_off = nullptr;
   BatchCtl* ctl = nullptr;
+  unsigned* claim = nullptr;    // two-word batches only
   unsigned long long cap = 0;
-  bool have_sigma = false;
+  int sigma_words = 0;          // 0: no path-count rows yet
 
   void release() {
     dev_free(visit);
@@ -91,8 +93,9 @@ struct MsWorkspace {
     dev_free(qm);
     dev_free(lvl_off);
     dev_free(ctl);
+    dev_free(claim);
     cap = 0;
-    have_sigma = false;
+    sigma_words = 0;
   }
 };
 
@@ -176,7 +179,7 @@ struct LearnedWorkspace {
 struct LoopKey {
   int backward;                 // 0 forward sweep, 1 backward (dependency) sweep
   int sigma_kind;
-  unsigned long long act;
+  LaneSet act;
   const int32_t* dist;
   int64_t dist_ld;
   const double* bc;
@@ -275,7 +278,9 @@ int check_graph(const lgbc_graph* g);
 int use_device(lgbc_graph* g);
 int check_sources(const lgbc_graph* g, const int32_t* src, int64_t nsrc);
 int ensure_src(lgbc_graph* g, int64_t count);
-int ensure_ms(lgbc_graph* g, bool need_sigma);
+// Multi-source workspace; with need_sigma, path-count / psi rows for batches
+// of up to 64 * words lanes.
+int ensure_ms(lgbc_graph* g, bool need_sigma, int words = 1);
 int ensure_bfs(lgbc_graph* g);
 int ensure_dist(lgbc_graph* g, int64_t count);
 int ensure_hubs(lgbc_graph* g);

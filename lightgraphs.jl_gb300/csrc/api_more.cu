@@ -32,7 +32,7 @@ bool tune_from_cache(const char* path, const std::string& sig, lgbc_tuning* out)
     if (std::sscanf(line, "%255s %lf %lf %d %d %d %d %d %d %d", key, &t.alpha, &t.beta,
                     &t.hub_degree, &t.lanes, &t.dense_edges, &t.segment_degree, &t.source_order,
                     &t.graph_loop, &t.stack_vertices) == 10 &&
-        sig == key && t.alpha > 0 && t.beta > 0 && t.lanes >= 1 && t.lanes <= kMaxLanes &&
+        sig == key && t.alpha > 0 && t.beta > 0 && t.lanes >= 1 && t.lanes <= kWideLanes &&
         t.hub_degree >= 1 && t.dense_edges >= 0 && t.segment_degree >= 0 &&
         (t.source_order == 0 || t.source_order == 1) && (t.graph_loop == 0 || t.graph_loop == 1) &&
         t.stack_vertices >= 0) {
@@ -116,7 +116,7 @@ extern "C" int lgbc_tune(lgbc_graph* g, const char* cache_path) {
       return LGBC_OK;
     };
     const int hubs[] = {64, 128, 256, 512, 1024, 4096, INT32_MAX};
-    const int lanes[] = {32, 48, 64};
+    const int lanes[] = {32, 48, 64, 128};
     const double alphas[] = {2.0, 4.0, 8.0, 14.0, 24.0, 48.0};
     const double betas[] = {6.0, 12.0, 24.0, 48.0, 96.0};
     const int dense[] = {4, 8, 16, 32};

@@ -7,7 +7,9 @@
 namespace lgbc {
 
 constexpr int kWarp = 32;
-constexpr int kMaxLanes = 64;            // sources per multi-source batch
+constexpr int kMaxLanes = 64;            // sources per one-word multi-source batch
+constexpr int kMaxWords = 2;             // 64-bit lane words per vertex in a wide batch
+constexpr int kWideLanes = 64 * kMaxWords;  // sources per wide (two-word) batch
 constexpr int32_t kUnreached = INT32_MAX;
 constexpr unsigned kFull = 0xffffffffu;
 

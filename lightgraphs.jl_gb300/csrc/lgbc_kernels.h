@@ -31,22 +31,42 @@ struct LaunchCfg {
 };
 
 // ---- multi-source (bit-lane) BFS and Brandes sweeps: msbfs.cu ----------
-// Per-batch device buffers.  Lane l of vertex v lives at [v * 64 + l].
+// Per-batch device buffers.  A batch has 64 * words lanes (words = 1 or 2);
+// every lane set is `words` consecutive uint64 (lane l in word l / 64, bit
+// l % 64), so the mask of vertex v is at [v * words], and lane l of v's
+// path-count / psi row lives at [v * 64 * words + l].  The buffers are sized
+// for two words; a one-word batch uses their first half.
 struct MsBuffers {
-  uint64_t* visit;     // n: lanes that have reached v
-  uint64_t* mb[2];     // n each: dense level masks, F_L lives in mb[L & 1]
-  void* sigma;         // n * 64: uint64 or double path counts
-  void* psi;           // n * 64: df32 or double, (1 + delta) / sigma
+  uint64_t* visit;     // n lane sets: lanes that have reached v
+  uint64_t* mb[2];     // n lane sets each: dense level masks, F_L lives in mb[L & 1]
+  void* sigma;         // n rows: uint64 or double path counts
+  void* psi;           // n rows: df32 or double, (1 + delta) / sigma
   int32_t* qv;         // cap: concatenated level lists (vertex)
-  uint64_t* qm;        // cap: lanes of that vertex at that level
+  uint64_t* qm;        // cap lane sets: lanes of that vertex at that level
   unsigned long long* lvl_off;  // n + 3: start of each level's list
   BatchCtl* ctl;       // control block
   const int32_t* lane_src;      // sources of the batch (device)
   unsigned long long cap;       // entries in qv / qm
-  const double* lane_w;         // 64 lane weights (weighted accumulation) or nullptr
+  const double* lane_w;         // 64 * words lane weights (weighted accumulation) or nullptr
   int64_t lane_w_n;             // > 0: a union of copies of an n-vertex graph, one row of 64
-                                // weights per copy (vertex v uses row v / lane_w_n)
+                                // weights per copy (vertex v uses row v / lane_w_n; one word)
+  unsigned* claim;              // n, two-word batches: top-down first-discovery flags, kept zero
+  int words;                    // 64-bit lane words per vertex: 1 or 2
 };
+
+// The active lanes of a batch (word 1 unused in a one-word batch).
+struct LaneSet {
+  uint64_t w[kMaxWords];
+};
+// Lanes [0, nl) of a batch with `words` words.
+inline LaneSet lane_set(int nl, int words) {
+  LaneSet a{};
+  for (int j = 0; j < words; ++j) {
+    const int k = nl - 64 * j;
+    a.w[j] = k >= 64 ? ~0ull : (k <= 0 ? 0ull : ((1ull << k) - 1ull));
+  }
+  return a;
+}
 
 // Vertices with more than hub_degree neighbours ("hubs") are not expanded by
 // one warp: their edge lists are cut into kHubChunk-edge work items spread over
@@ -65,8 +85,8 @@ struct HubData {
   long long n_out;
   const HubItem* in_items;       // items over in-edges (path-count pulls, bottom-up)
   long long n_in;
-  unsigned long long* acc;       // slots x 64 partial sums (uint64 or FP64 bits), kept zero
-  unsigned long long* mask;      // slots: OR of discovering lanes, kept zero
+  unsigned long long* acc;       // slots x 64 * words partial sums (uint64 or FP64 bits), kept zero
+  unsigned long long* mask;      // slots x words: OR of discovering lanes, kept zero
   unsigned int* cnt;             // slots: finished items, kept zero
   int hub_degree;                // degree above which a vertex is a hub (INT32_MAX: none)
   int dense_edges;               // chunks with more contributing edges use the transposed gather
@@ -86,10 +106,13 @@ int ms_init_seeds(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const M
 // [seg_off[k], seg_off[k+1])): the lanes with no source in that component.
 int ms_premark(const LaunchCfg& c, cudaStream_t s, const MsBuffers& b, const int64_t* seg_off,
                const uint64_t* seg_mark, int64_t nseg);
+// Top-down / bottom-up level.  Distances (dist) only with one word.
 int ms_topdown(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
-               const HubData& hd, uint64_t act, int sigma_kind, int32_t* dist, int64_t dist_ld);
+               const HubData& hd, const LaneSet& act, int sigma_kind, int32_t* dist,
+               int64_t dist_ld);
 int ms_bottomup(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
-                const HubData& hd, uint64_t act, int sigma_kind, int32_t* dist, int64_t dist_ld);
+                const HubData& hd, const LaneSet& act, int sigma_kind, int32_t* dist,
+                int64_t dist_ld);
 int ms_advance(cudaStream_t s, const DevGraph& g, const MsBuffers& b);
 // Set ctl->level = maxlevel for the backward sweep (on the device).
 int ms_begin_backward(cudaStream_t s, const MsBuffers& b);

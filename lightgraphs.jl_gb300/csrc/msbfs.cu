@@ -49,6 +49,85 @@ __device__ __forceinline__ uint64_t* mb_at(const MsBuffers& b, int level) {
   return (level & 1) ? b.mb[1] : b.mb[0];
 }
 
+// ---------------------------------------------------------------------------
+// Lane sets of a batch of 64 * W sources: W words per vertex, loaded and
+// stored as one 8 * W-byte access.  Thread t of a warp owns the lanes
+// 32 k + t, k < 2 W ("its lanes"); bit k of my_bits() and element k of the
+// per-thread accumulator arrays below refer to lane 32 k + t.
+// ---------------------------------------------------------------------------
+template <int W> struct alignas(8 * W) Lanes {
+  uint64_t w[W];
+};
+
+template <int W> __device__ __forceinline__ Lanes<W> lz() {
+  Lanes<W> r;
+#pragma unroll
+  for (int j = 0; j < W; ++j) r.w[j] = 0ull;
+  return r;
+}
+template <int W> __device__ __forceinline__ bool lany(const Lanes<W>& a) {
+  uint64_t x = 0;
+#pragma unroll
+  for (int j = 0; j < W; ++j) x |= a.w[j];
+  return x != 0ull;
+}
+template <int W> __device__ __forceinline__ Lanes<W> land(const Lanes<W>& a, const Lanes<W>& b) {
+  Lanes<W> r;
+#pragma unroll
+  for (int j = 0; j < W; ++j) r.w[j] = a.w[j] & b.w[j];
+  return r;
+}
+template <int W> __device__ __forceinline__ Lanes<W> lor(const Lanes<W>& a, const Lanes<W>& b) {
+  Lanes<W> r;
+#pragma unroll
+  for (int j = 0; j < W; ++j) r.w[j] = a.w[j] | b.w[j];
+  return r;
+}
+// a & ~b
+template <int W> __device__ __forceinline__ Lanes<W> lminus(const Lanes<W>& a, const Lanes<W>& b) {
+  Lanes<W> r;
+#pragma unroll
+  for (int j = 0; j < W; ++j) r.w[j] = a.w[j] & ~b.w[j];
+  return r;
+}
+template <int W> __device__ __forceinline__ bool leq(const Lanes<W>& a, const Lanes<W>& b) {
+  bool e = true;
+#pragma unroll
+  for (int j = 0; j < W; ++j) e = e && a.w[j] == b.w[j];
+  return e;
+}
+template <int W> __device__ __forceinline__ Lanes<W> lshfl(const Lanes<W>& a, int src) {
+  Lanes<W> r;
+#pragma unroll
+  for (int j = 0; j < W; ++j) r.w[j] = shfl_u64(a.w[j], src);
+  return r;
+}
+template <int W> __device__ __forceinline__ Lanes<W> lwarp_or(const Lanes<W>& a) {
+  Lanes<W> r;
+#pragma unroll
+  for (int j = 0; j < W; ++j) r.w[j] = warp_or_u64(a.w[j]);
+  return r;
+}
+// The 32-bit half k (lanes 32 k .. 32 k + 31) of a lane set.
+template <int W> __device__ __forceinline__ uint32_t lhalf(const Lanes<W>& a, int k) {
+  return static_cast<uint32_t>(a.w[k >> 1] >> (32 * (k & 1)));
+}
+template <int W> __host__ __device__ __forceinline__ Lanes<W> lane_cast(const LaneSet& a) {
+  Lanes<W> r;
+#pragma unroll
+  for (int j = 0; j < W; ++j) r.w[j] = a.w[j];
+  return r;
+}
+template <int W> __device__ __forceinline__ Lanes<W>* lanes_of(uint64_t* p) {
+  return reinterpret_cast<Lanes<W>*>(p);
+}
+template <int W> __device__ __forceinline__ const Lanes<W>* lanes_of(const uint64_t* p) {
+  return reinterpret_cast<const Lanes<W>*>(p);
+}
+template <int W> __device__ __forceinline__ Lanes<W>* mbw(const MsBuffers& b, int level) {
+  return lanes_of<W>(mb_at(b, level));
+}
+
 template <int SK> struct Sig;
 template <> struct Sig<kSigmaNone> {
   using T = unsigned long long;
@@ -83,36 +162,48 @@ __device__ __forceinline__ unsigned my_bits(uint64_t m) {
          (static_cast<unsigned>((m >> (32 + ln)) & 1ull) << 1);
 }
 
+// Bit k = lane 32 k + t of a lane set, k < 2 W.
+template <int W> __device__ __forceinline__ unsigned my_bits(const Lanes<W>& m) {
+  const int ln = lane_id();
+  unsigned r = 0;
+#pragma unroll
+  for (int k = 0; k < 2 * W; ++k) r |= ((lhalf(m, k) >> ln) & 1u) << k;
+  return r;
+}
+
 __device__ __forceinline__ unsigned long long max_u64(unsigned long long a, unsigned long long b) {
   return a > b ? a : b;
 }
 
-// Store the path counts of lanes (t, t + 32) of w that are set in `mask`.
+// Store the path counts of this thread's lanes of w that are set in `mask`.
 // Lanes outside `mask` may be read concurrently by other warps (w sits at
 // another level for them), so they are never written.  Tracks the largest
 // stored count (for the per-level overflow bound).
-template <int SK>
-__device__ __forceinline__ void store_sigma(void* sigma, int32_t w, uint64_t mask,
-                                            typename Sig<SK>::T a0, typename Sig<SK>::T a1,
+template <int SK, int W>
+__device__ __forceinline__ void store_sigma(void* sigma, int32_t w, const Lanes<W>& mask,
+                                            const typename Sig<SK>::T (&a)[2 * W],
                                             unsigned long long& smax) {
   using T = typename Sig<SK>::T;
   const int ln = lane_id();
   const unsigned my = my_bits(mask);
-  T* row = reinterpret_cast<T*>(sigma) + static_cast<int64_t>(w) * 64;
-  if (my & 1u) row[ln] = a0;
-  if (my & 2u) row[32 + ln] = a1;
-  if (SK == kSigmaU64) {
-    if (my & 1u) smax = max_u64(smax, static_cast<unsigned long long>(a0));
-    if (my & 2u) smax = max_u64(smax, static_cast<unsigned long long>(a1));
+  T* row = reinterpret_cast<T*>(sigma) + static_cast<int64_t>(w) * (64 * W);
+#pragma unroll
+  for (int k = 0; k < 2 * W; ++k) {
+    if (my & (1u << k)) {
+      row[32 * k + ln] = a[k];
+      if (SK == kSigmaU64) smax = max_u64(smax, static_cast<unsigned long long>(a[k]));
+    }
   }
 }
 
-__device__ __forceinline__ void store_dist(int32_t* dist, int64_t ld, int32_t w, uint64_t mask,
+template <int W>
+__device__ __forceinline__ void store_dist(int32_t* dist, int64_t ld, int32_t w, const Lanes<W>& mask,
                                            int32_t level) {
   const int ln = lane_id();
   const unsigned my = my_bits(mask);
-  if (my & 1u) dist[static_cast<int64_t>(ln) * ld + w] = level;
-  if (my & 2u) dist[static_cast<int64_t>(32 + ln) * ld + w] = level;
+#pragma unroll
+  for (int k = 0; k < 2 * W; ++k)
+    if (my & (1u << k)) dist[static_cast<int64_t>(32 * k + ln) * ld + w] = level;
 }
 
 // Compensated double-float accumulator: hi carries the running sum, lo the
@@ -125,11 +216,6 @@ __device__ __forceinline__ void acc_add(df32& acc, float xh, float xl) {
 }
 __device__ __forceinline__ df32 acc_done(df32 acc) { return fast_two_sum(acc.hi, acc.lo); }
 
-// Row element types of the two gathers.
-template <int SK> struct Rows;
-template <> struct Rows<kSigmaU64> { using T = unsigned long long; };
-template <> struct Rows<kSigmaF64> { using T = double; };
-
 template <class T, class A> __device__ __forceinline__ void acc_row(A& acc, T x);
 template <> __device__ __forceinline__ void acc_row(unsigned long long& acc, unsigned long long x) { acc += x; }
 template <> __device__ __forceinline__ void acc_row(double& acc, double x) { acc += x; }
@@ -140,77 +226,93 @@ template <> __device__ __forceinline__ unsigned long long zero_row() { return 0u
 template <> __device__ __forceinline__ double zero_row() { return 0.0; }
 template <> __device__ __forceinline__ float2 zero_row() { return make_float2(0.f, 0.f); }
 
+template <class A> __device__ __forceinline__ A zero_acc();
+template <> __device__ __forceinline__ unsigned long long zero_acc() { return 0ull; }
+template <> __device__ __forceinline__ double zero_acc() { return 0.0; }
+template <> __device__ __forceinline__ df32 zero_acc() { return df32{0.f, 0.f}; }
+
+template <class A, int K> __device__ __forceinline__ void zero_accs(A (&a)[K]) {
+#pragma unroll
+  for (int k = 0; k < K; ++k) a[k] = zero_acc<A>();
+}
+
 // Per-warp staging of one chunk's contributing edges (compacted).
-struct ChunkStage {
-  uint64_t f[kWarp];
+template <int W> struct ChunkStage {
+  Lanes<W> f[kWarp];
   int32_t v[kWarp];
   int32_t j[kWarp];  // owner segment (seg_gather)
 };
 constexpr int kWarpsPerBlock = 8;  // every gather kernel runs 256-thread blocks
 
-__device__ __forceinline__ ChunkStage& my_stage() {
-  __shared__ ChunkStage stage[kWarpsPerBlock];
+template <int W> __device__ __forceinline__ ChunkStage<W>& my_stage() {
+  __shared__ ChunkStage<W> stage[kWarpsPerBlock];
   return stage[threadIdx.x >> 5];
 }
 
+// Rows gathered per step of a staged walk: 4 with one word, 2 with two (eight
+// row loads in flight per thread either way).
+template <int W> constexpr int kRowsInFlight = 4 / W;
+
 // Chunk gather.  Each of the 32 threads holds one edge (neighbour id `nb`,
-// lane mask `f` of the lanes that edge contributes to).  Adds, for this
-// thread's lanes t and t + 32, rows[nb_j * 64 + lane] over every edge j whose
-// mask has that lane, into (a0, a1).
+// lane set `f` of the lanes that edge contributes to).  Adds, for this
+// thread's lanes 32 k + t, rows[nb_j * 64 W + 32 k + t] over every edge j whose
+// set has that lane, into acc[k].
 //  * at most `dense` contributing edges: the edges are compacted into shared
 //    memory and the warp walks them, each edge's row read by coalesced loads;
 //  * more: the (edge, lane) bit matrix is transposed so each thread walks only
 //    the edges that carry its own lanes.
-template <class T, class A>
-__device__ __forceinline__ void gather_chunk(int32_t nb, uint64_t f, const T* __restrict__ rows,
-                                             int dense, A& a0, A& a1) {
+template <class T, class A, int W>
+__device__ __forceinline__ void gather_chunk(int32_t nb, const Lanes<W>& f, const T* __restrict__ rows,
+                                             int dense, A (&acc)[2 * W]) {
+  constexpr int RS = 64 * W;
+  constexpr int G = kRowsInFlight<W>;
   const int ln = lane_id();
-  const unsigned bal = __ballot_sync(kFull, f != 0);
+  const unsigned bal = __ballot_sync(kFull, lany(f));
   if (bal == 0) return;
   const T* r0 = rows + ln;
-  const T* r1 = rows + 32 + ln;
   const int S = __popc(bal);
   if (S <= dense) {
-    ChunkStage& st = my_stage();
-    if (f) {
+    ChunkStage<W>& st = my_stage<W>();
+    if (lany(f)) {
       const int r = __popc(bal & ((1u << ln) - 1u));
       st.v[r] = nb;
       st.f[r] = f;
     }
     __syncwarp();
-    for (int r = 0; r < S; r += 4) {
-      T x0[4], x1[4];
-      unsigned my[4];
+    for (int r = 0; r < S; r += G) {
+      T x[G][2 * W];
+      unsigned my[G];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
+      for (int q = 0; q < G; ++q) {
         const bool ok = r + q < S;
-        const uint64_t fj = ok ? st.f[r + q] : 0ull;
-        const int64_t off = static_cast<int64_t>(ok ? st.v[r + q] : 0) * 64;
+        const Lanes<W> fj = ok ? st.f[r + q] : lz<W>();
+        const int64_t off = static_cast<int64_t>(ok ? st.v[r + q] : 0) * RS;
         my[q] = my_bits(fj);
-        x0[q] = zero_row<T>();
-        x1[q] = zero_row<T>();
-        if (my[q] & 1u) x0[q] = r0[off];
-        if (my[q] & 2u) x1[q] = r1[off];
+#pragma unroll
+        for (int k = 0; k < 2 * W; ++k) {
+          x[q][k] = zero_row<T>();
+          if (my[q] & (1u << k)) x[q][k] = r0[off + 32 * k];
+        }
       }
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        if (my[q] & 1u) acc_row<T, A>(a0, x0[q]);
-        if (my[q] & 2u) acc_row<T, A>(a1, x1[q]);
-      }
+      for (int q = 0; q < G; ++q)
+#pragma unroll
+        for (int k = 0; k < 2 * W; ++k)
+          if (my[q] & (1u << k)) acc_row<T, A>(acc[k], x[q][k]);
     }
     __syncwarp();
     return;
   }
-  // transposed path: thread t gets the edges that carry lane t / lane t + 32
-  uint32_t E[2] = {warp_transpose32(static_cast<uint32_t>(f)),
-                   warp_transpose32(static_cast<uint32_t>(f >> 32))};
+  // transposed path: thread t gets the edges that carry its lane 32 k + t
+  uint32_t E[2 * W];
 #pragma unroll
-  for (int h = 0; h < 2; ++h) {
-    const T* rb = h ? r1 : r0;
-    A& acc = h ? a1 : a0;
-    uint32_t m = E[h];
+  for (int k = 0; k < 2 * W; ++k) E[k] = warp_transpose32(lhalf(f, k));
+#pragma unroll
+  for (int k = 0; k < 2 * W; ++k) {
+    const T* rb = r0 + 32 * k;
+    uint32_t m = E[k];
     const int cnt = static_cast<int>(__reduce_max_sync(kFull, static_cast<unsigned>(__popc(m))));
-    for (int k = 0; k < cnt; k += 4) {
+    for (int c = 0; c < cnt; c += 4) {
       int32_t vj[4];
       bool ok[4];
 #pragma unroll
@@ -224,143 +326,133 @@ __device__ __forceinline__ void gather_chunk(int32_t nb, uint64_t f, const T* __
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         x[q] = zero_row<T>();
-        if (ok[q]) x[q] = rb[static_cast<int64_t>(vj[q]) * 64];
+        if (ok[q]) x[q] = rb[static_cast<int64_t>(vj[q]) * RS];
       }
 #pragma unroll
       for (int q = 0; q < 4; ++q)
-        if (ok[q]) acc_row<T, A>(acc, x[q]);
+        if (ok[q]) acc_row<T, A>(acc[k], x[q]);
     }
   }
 }
 
 // Path-count gather over in-edges [e0, e1) of one vertex: for every
 // in-neighbour v, f = front[v] & want marks the lanes whose predecessor it is;
-// their rows are added into (a0, a1).  Returns the OR of all f (the lanes
-// that discover the vertex).  With SK == kSigmaNone only the OR is formed,
+// their rows are added into a.  Returns the union of all f (the lanes that
+// discover the vertex).  With SK == kSigmaNone only the union is formed,
 // and the scan stops once every wanted lane is found.
-template <int SK>
-__device__ __forceinline__ uint64_t pull_range(const int32_t* __restrict__ ci, int64_t e0,
-                                               int64_t e1, uint64_t want,
-                                               const uint64_t* __restrict__ front,
+template <int SK, int W>
+__device__ __forceinline__ Lanes<W> pull_range(const int32_t* __restrict__ ci, int64_t e0, int64_t e1,
+                                               const Lanes<W>& want,
+                                               const Lanes<W>* __restrict__ front,
                                                const void* __restrict__ sigma, int dense,
-                                               typename Sig<SK>::T& a0, typename Sig<SK>::T& a1) {
+                                               typename Sig<SK>::T (&a)[2 * W]) {
   const int ln = lane_id();
-  uint64_t found = 0;
+  Lanes<W> found = lz<W>();
   if (SK == kSigmaNone) {
     for (int64_t e = e0; e < e1; e += kWarp) {
       const int64_t idx = e + ln;
-      if (idx < e1) found |= front[ci[idx]] & want;
-      if (warp_or_u64(found) == want) break;
+      if (idx < e1) found = lor(found, land(front[ci[idx]], want));
+      if (leq(lwarp_or(found), want)) break;
     }
-    return warp_or_u64(found);
+    return lwarp_or(found);
   }
   // software-pipelined: the next chunk's neighbour ids and masks are loaded
   // before the current chunk's rows are gathered
   using T = typename Sig<SK>::T;
   int32_t v = 0;
-  uint64_t f = 0;
+  Lanes<W> f = lz<W>();
   if (e0 + ln < e1) {
     v = ci[e0 + ln];
-    f = front[v] & want;
+    f = land(front[v], want);
   }
   for (int64_t e = e0; e < e1; e += kWarp) {
     const int64_t nidx = e + kWarp + ln;
     int32_t vn = 0;
-    uint64_t fn = 0;
+    Lanes<W> fn = lz<W>();
     if (nidx < e1) {
       vn = ci[nidx];
-      fn = front[vn] & want;
+      fn = land(front[vn], want);
     }
-    found |= f;
-    gather_chunk<T, T>(v, f, reinterpret_cast<const T*>(sigma), dense, a0, a1);
+    found = lor(found, f);
+    gather_chunk<T, T, W>(v, f, reinterpret_cast<const T*>(sigma), dense, a);
     v = vn;
     f = fn;
   }
-  return warp_or_u64(found);
+  return lwarp_or(found);
 }
 
 // Dependency gather over out-edges [e0, e1) of v at level L: for every
 // out-neighbour w, g = succ[w] & F marks the lanes for which w is a DAG
 // successor; their psi = (1 + delta[w]) / sigma[w] are summed.
 // (Software-pipelined like pull_range: the next chunk's ids and masks are in
-// flight while the current chunk's rows are gathered.)
-__device__ __forceinline__ void psi_range_df(const int32_t* __restrict__ ci, int64_t e0, int64_t e1,
-                                             uint64_t F, const uint64_t* __restrict__ succ,
-                                             const void* __restrict__ psi, int dense, df32& acc0,
-                                             df32& acc1) {
+// flight while the current chunk's rows are gathered.)  T / A: float2 / df32
+// (df32 psi, normalised at the end) or double / double.
+template <class T, class A, int W>
+__device__ __forceinline__ void psi_range(const int32_t* __restrict__ ci, int64_t e0, int64_t e1,
+                                          const Lanes<W>& F, const Lanes<W>* __restrict__ succ,
+                                          const void* __restrict__ psi, int dense,
+                                          A (&acc)[2 * W]) {
   const int ln = lane_id();
   int32_t w = 0;
-  uint64_t gm = 0;
+  Lanes<W> gm = lz<W>();
   if (e0 + ln < e1) {
     w = ci[e0 + ln];
-    gm = succ[w] & F;
+    gm = land(succ[w], F);
   }
   for (int64_t e = e0; e < e1; e += kWarp) {
     const int64_t nidx = e + kWarp + ln;
     int32_t wn = 0;
-    uint64_t gn = 0;
+    Lanes<W> gn = lz<W>();
     if (nidx < e1) {
       wn = ci[nidx];
-      gn = succ[wn] & F;
+      gn = land(succ[wn], F);
     }
-    gather_chunk<float2, df32>(w, gm, reinterpret_cast<const float2*>(psi), dense, acc0, acc1);
+    gather_chunk<T, A, W>(w, gm, reinterpret_cast<const T*>(psi), dense, acc);
     w = wn;
     gm = gn;
   }
-  acc0 = acc_done(acc0);
-  acc1 = acc_done(acc1);
 }
 
+template <int W>
+__device__ __forceinline__ void psi_range_df(const int32_t* __restrict__ ci, int64_t e0, int64_t e1,
+                                             const Lanes<W>& F, const Lanes<W>* __restrict__ succ,
+                                             const void* __restrict__ psi, int dense,
+                                             df32 (&acc)[2 * W]) {
+  psi_range<float2, df32, W>(ci, e0, e1, F, succ, psi, dense, acc);
+#pragma unroll
+  for (int k = 0; k < 2 * W; ++k) acc[k] = acc_done(acc[k]);
+}
+
+template <int W>
 __device__ __forceinline__ void psi_range_f64(const int32_t* __restrict__ ci, int64_t e0, int64_t e1,
-                                              uint64_t F, const uint64_t* __restrict__ succ,
+                                              const Lanes<W>& F, const Lanes<W>* __restrict__ succ,
                                               const void* __restrict__ psi, int dense,
-                                              double& acc0, double& acc1) {
-  const int ln = lane_id();
-  int32_t w = 0;
-  uint64_t gm = 0;
-  if (e0 + ln < e1) {
-    w = ci[e0 + ln];
-    gm = succ[w] & F;
-  }
-  for (int64_t e = e0; e < e1; e += kWarp) {
-    const int64_t nidx = e + kWarp + ln;
-    int32_t wn = 0;
-    uint64_t gn = 0;
-    if (nidx < e1) {
-      wn = ci[nidx];
-      gn = succ[wn] & F;
-    }
-    gather_chunk<double, double>(w, gm, reinterpret_cast<const double*>(psi), dense, acc0, acc1);
-    w = wn;
-    gm = gn;
-  }
+                                              double (&acc)[2 * W]) {
+  psi_range<double, double, W>(ci, e0, e1, F, succ, psi, dense, acc);
 }
 
 __device__ __forceinline__ int64_t shfl_i64(int64_t x, int src) {
   return static_cast<int64_t>(shfl_u64(static_cast<uint64_t>(x), src));
 }
 
-template <class A> __device__ __forceinline__ A zero_acc();
-template <> __device__ __forceinline__ unsigned long long zero_acc() { return 0ull; }
-template <> __device__ __forceinline__ double zero_acc() { return 0.0; }
-template <> __device__ __forceinline__ df32 zero_acc() { return df32{0.f, 0.f}; }
-
 // Segmented gather for low-degree graphs: lane j of the warp holds one
 // vertex ("segment"): `valid`, its edge range [e0, e0 + deg) in `ci`, and a
-// lane mask `mask`.  The warp streams the concatenation of the valid
+// lane set `mask`.  The warp streams the concatenation of the valid
 // segments' edges 32 at a time, so a vertex with a handful of edges does not
 // occupy a whole warp pass; for an edge to neighbour x of segment j, the
-// lanes f = gate[x] & mask_j contribute rows[x * 64 + lane].  Contributing
-// edges are compacted into shared memory with their segment, read four at a
-// time into per-thread accumulators for lanes t and t + 32; when the segment
-// changes, flush(j, nm_j, acc_lo, acc_hi) runs (warp-uniformly) with nm_j the
-// OR of segment j's f.  With VISIT_ALL every valid segment is flushed once,
+// lanes f = gate[x] & mask_j contribute rows[x * 64 W + lane].  Contributing
+// edges are compacted into shared memory with their segment, read a few at a
+// time into per-thread accumulators acc[k] (lane 32 k + t); when the segment
+// changes, flush(j, nm_j, acc) runs (warp-uniformly) with nm_j the union of
+// segment j's f.  With VISIT_ALL every valid segment is flushed once,
 // contributions or not.
-template <class T, class A, bool VISIT_ALL, class Flush>
-__device__ __forceinline__ void seg_gather(bool valid, int64_t e0, int deg, uint64_t mask,
+template <class T, class A, bool VISIT_ALL, int W, class Flush>
+__device__ __forceinline__ void seg_gather(bool valid, int64_t e0, int deg, const Lanes<W>& mask,
                                            const int32_t* __restrict__ ci,
-                                           const uint64_t* __restrict__ gate,
+                                           const Lanes<W>* __restrict__ gate,
                                            const T* __restrict__ rows, Flush&& flush) {
+  constexpr int RS = 64 * W;
+  constexpr int G = kRowsInFlight<W>;
   const int ln = lane_id();
   const int d = valid ? deg : 0;
   int incl = d;
@@ -373,12 +465,12 @@ __device__ __forceinline__ void seg_gather(bool valid, int64_t e0, int deg, uint
   const int off = incl - d;
   const unsigned vmask = __ballot_sync(kFull, valid);
   const T* r0 = rows + ln;
-  const T* r1 = rows + 32 + ln;
-  ChunkStage& st = my_stage();
+  ChunkStage<W>& st = my_stage<W>();
   int cur = -1;
   unsigned done = 0;
-  uint64_t nm = 0;
-  A a0 = zero_acc<A>(), a1 = zero_acc<A>();
+  Lanes<W> nm = lz<W>();
+  A acc[2 * W];
+  zero_accs(acc);
   for (int c = 0; c < total; c += kWarp) {
     const int gi = c + ln;
     int pos = 0;
@@ -391,15 +483,15 @@ __device__ __forceinline__ void seg_gather(bool valid, int64_t e0, int deg, uint
     const int j = ok ? pos : 0;
     const int64_t ej = shfl_i64(e0, j);
     const int oj = __shfl_sync(kFull, off, j);
-    const uint64_t mj = shfl_u64(mask, j);
+    const Lanes<W> mj = lshfl(mask, j);
     int32_t x = 0;
-    uint64_t f = 0;
+    Lanes<W> f = lz<W>();
     if (ok) {
       x = ci[ej + (gi - oj)];
-      f = gate[x] & mj;
+      f = land(gate[x], mj);
     }
-    const unsigned bal = __ballot_sync(kFull, f != 0);
-    if (f) {
+    const unsigned bal = __ballot_sync(kFull, lany(f));
+    if (lany(f)) {
       const int r = __popc(bal & ((1u << ln) - 1u));
       st.v[r] = x;
       st.f[r] = f;
@@ -407,45 +499,46 @@ __device__ __forceinline__ void seg_gather(bool valid, int64_t e0, int deg, uint
     }
     __syncwarp();
     const int S = __popc(bal);
-    for (int r = 0; r < S; r += 4) {
-      T x0[4], x1[4];
-      unsigned my[4];
-      uint64_t fq[4];
-      int jq[4];
+    for (int r = 0; r < S; r += G) {
+      T xr[G][2 * W];
+      unsigned my[G];
+      Lanes<W> fq[G];
+      int jq[G];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
+      for (int q = 0; q < G; ++q) {
         const bool okq = r + q < S;
-        fq[q] = okq ? st.f[r + q] : 0ull;
+        fq[q] = okq ? st.f[r + q] : lz<W>();
         jq[q] = okq ? st.j[r + q] : -1;
-        const int64_t o = static_cast<int64_t>(okq ? st.v[r + q] : 0) * 64;
+        const int64_t o = static_cast<int64_t>(okq ? st.v[r + q] : 0) * RS;
         my[q] = my_bits(fq[q]);
-        x0[q] = zero_row<T>();
-        x1[q] = zero_row<T>();
-        if (my[q] & 1u) x0[q] = r0[o];
-        if (my[q] & 2u) x1[q] = r1[o];
+#pragma unroll
+        for (int k = 0; k < 2 * W; ++k) {
+          xr[q][k] = zero_row<T>();
+          if (my[q] & (1u << k)) xr[q][k] = r0[o + 32 * k];
+        }
       }
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
+      for (int q = 0; q < G; ++q) {
         if (jq[q] < 0) continue;
         if (jq[q] != cur) {
           if (cur >= 0) {
-            flush(cur, nm, a0, a1);
+            flush(cur, nm, acc);
             done |= 1u << cur;
           }
           cur = jq[q];
-          nm = 0;
-          a0 = zero_acc<A>();
-          a1 = zero_acc<A>();
+          nm = lz<W>();
+          zero_accs(acc);
         }
-        nm |= fq[q];
-        if (my[q] & 1u) acc_row<T, A>(a0, x0[q]);
-        if (my[q] & 2u) acc_row<T, A>(a1, x1[q]);
+        nm = lor(nm, fq[q]);
+#pragma unroll
+        for (int k = 0; k < 2 * W; ++k)
+          if (my[q] & (1u << k)) acc_row<T, A>(acc[k], xr[q][k]);
       }
     }
     __syncwarp();
   }
   if (cur >= 0) {
-    flush(cur, nm, a0, a1);
+    flush(cur, nm, acc);
     done |= 1u << cur;
   }
   if (VISIT_ALL) {
@@ -453,7 +546,8 @@ __device__ __forceinline__ void seg_gather(bool valid, int64_t e0, int deg, uint
     while (rem) {
       const int j = __ffs(rem) - 1;
       rem &= rem - 1;
-      flush(j, 0ull, zero_acc<A>(), zero_acc<A>());
+      zero_accs(acc);
+      flush(j, lz<W>(), acc);
     }
   }
 }
@@ -477,64 +571,75 @@ __device__ __forceinline__ double finish_lane_f64(const double* srow, double* pr
   return d;
 }
 
-// Finalise the dependencies of lanes `mine` (bit 0 = lane t, bit 1 = lane
-// t + 32) of v from the psi sums; returns the lanes' delta sum.
+// Finalise the dependencies of this thread's lanes `mine` (bit k = lane
+// 32 k + t) of v from the psi sums; returns the lanes' delta sum.
+template <int W>
 __device__ __forceinline__ df32 finish_df(void* psi, const void* sigma, int32_t v, unsigned mine,
-                                          df32 acc0, df32 acc1) {
+                                          const df32 (&acc)[2 * W]) {
   const int ln = lane_id();
   df32 contrib{0.f, 0.f};
   if (!mine) return contrib;
   const unsigned long long* srow =
-      reinterpret_cast<const unsigned long long*>(sigma) + static_cast<int64_t>(v) * 64;
-  float2* prow = reinterpret_cast<float2*>(psi) + static_cast<int64_t>(v) * 64;
-  if (mine & 1u) contrib = finish_lane_df(srow, prow, ln, acc0);
-  if (mine & 2u) contrib = df_add(contrib, finish_lane_df(srow, prow, 32 + ln, acc1));
+      reinterpret_cast<const unsigned long long*>(sigma) + static_cast<int64_t>(v) * (64 * W);
+  float2* prow = reinterpret_cast<float2*>(psi) + static_cast<int64_t>(v) * (64 * W);
+  if (mine & 1u) contrib = finish_lane_df(srow, prow, ln, acc[0]);
+#pragma unroll
+  for (int k = 1; k < 2 * W; ++k)
+    if (mine & (1u << k)) contrib = df_add(contrib, finish_lane_df(srow, prow, 32 * k + ln, acc[k]));
   return contrib;
 }
 
+template <int W>
 __device__ __forceinline__ double finish_f64(void* psi, const void* sigma, int32_t v, unsigned mine,
-                                             double acc0, double acc1) {
+                                             const double (&acc)[2 * W]) {
   const int ln = lane_id();
   double contrib = 0.0;
   if (!mine) return contrib;
-  const double* srow = reinterpret_cast<const double*>(sigma) + static_cast<int64_t>(v) * 64;
-  double* prow = reinterpret_cast<double*>(psi) + static_cast<int64_t>(v) * 64;
-  if (mine & 1u) contrib += finish_lane_f64(srow, prow, ln, acc0);
-  if (mine & 2u) contrib += finish_lane_f64(srow, prow, 32 + ln, acc1);
+  const double* srow = reinterpret_cast<const double*>(sigma) + static_cast<int64_t>(v) * (64 * W);
+  double* prow = reinterpret_cast<double*>(psi) + static_cast<int64_t>(v) * (64 * W);
+#pragma unroll
+  for (int k = 0; k < 2 * W; ++k)
+    if (mine & (1u << k)) contrib += finish_lane_f64(srow, prow, 32 * k + ln, acc[k]);
   return contrib;
 }
 
-// The lane weights of vertex v (its copy's row in a stacked union).
-__device__ __forceinline__ const double* weights_of(const MsBuffers& b, int32_t v) {
-  return b.lane_w_n > 0 ? b.lane_w + (static_cast<int64_t>(v) / b.lane_w_n) * 64 : b.lane_w;
+// The lane weights of vertex v (its copy's row in a stacked union; stacked
+// unions are one-word batches).
+template <int W> __device__ __forceinline__ const double* weights_of(const MsBuffers& b, int32_t v) {
+  return b.lane_w_n > 0 ? b.lane_w + (static_cast<int64_t>(v) / b.lane_w_n) * (64 * W) : b.lane_w;
 }
 
 // Weighted finalisation (importance-sampled estimators): the same psi
 // updates, returning sum over the lanes of w[lane] * delta in FP64.
+template <int W>
 __device__ __forceinline__ double finish_df_w(void* psi, const void* sigma, int32_t v,
-                                              unsigned mine, df32 acc0, df32 acc1,
+                                              unsigned mine, const df32 (&acc)[2 * W],
                                               const double* __restrict__ lw) {
   const int ln = lane_id();
   double contrib = 0.0;
   if (!mine) return contrib;
   const unsigned long long* srow =
-      reinterpret_cast<const unsigned long long*>(sigma) + static_cast<int64_t>(v) * 64;
-  float2* prow = reinterpret_cast<float2*>(psi) + static_cast<int64_t>(v) * 64;
-  if (mine & 1u) contrib = lw[ln] * df_to_double(finish_lane_df(srow, prow, ln, acc0));
-  if (mine & 2u) contrib += lw[32 + ln] * df_to_double(finish_lane_df(srow, prow, 32 + ln, acc1));
+      reinterpret_cast<const unsigned long long*>(sigma) + static_cast<int64_t>(v) * (64 * W);
+  float2* prow = reinterpret_cast<float2*>(psi) + static_cast<int64_t>(v) * (64 * W);
+#pragma unroll
+  for (int k = 0; k < 2 * W; ++k)
+    if (mine & (1u << k))
+      contrib += lw[32 * k + ln] * df_to_double(finish_lane_df(srow, prow, 32 * k + ln, acc[k]));
   return contrib;
 }
 
+template <int W>
 __device__ __forceinline__ double finish_f64_w(void* psi, const void* sigma, int32_t v,
-                                               unsigned mine, double acc0, double acc1,
+                                               unsigned mine, const double (&acc)[2 * W],
                                                const double* __restrict__ lw) {
   const int ln = lane_id();
   double contrib = 0.0;
   if (!mine) return contrib;
-  const double* srow = reinterpret_cast<const double*>(sigma) + static_cast<int64_t>(v) * 64;
-  double* prow = reinterpret_cast<double*>(psi) + static_cast<int64_t>(v) * 64;
-  if (mine & 1u) contrib = lw[ln] * finish_lane_f64(srow, prow, ln, acc0);
-  if (mine & 2u) contrib += lw[32 + ln] * finish_lane_f64(srow, prow, 32 + ln, acc1);
+  const double* srow = reinterpret_cast<const double*>(sigma) + static_cast<int64_t>(v) * (64 * W);
+  double* prow = reinterpret_cast<double*>(psi) + static_cast<int64_t>(v) * (64 * W);
+#pragma unroll
+  for (int k = 0; k < 2 * W; ++k)
+    if (mine & (1u << k)) contrib += lw[32 * k + ln] * finish_lane_f64(srow, prow, 32 * k + ln, acc[k]);
   return contrib;
 }
 
@@ -559,31 +664,35 @@ __device__ __forceinline__ bool hub_last(unsigned int* cnt, int nitems) {
 // Batch initialisation: level 0 = the sources (one lane each; a repeated
 // source gets several lanes in one list entry).
 // ---------------------------------------------------------------------------
-template <int SK>
-__global__ void k_ms_init(DevGraph g, MsBuffers b, int nl, unsigned long long cap,
+template <int SK, int W>
+__global__ void k_ms_init(DevGraph g, MsBuffers b, int nl, Lanes<W> act, unsigned long long cap,
                           unsigned long long sigma_limit, int32_t* dist, int64_t ld) {
   if (blockIdx.x != 0 || threadIdx.x != 0) return;
   using T = typename Sig<SK>::T;
-  const uint64_t act = nl >= 64 ? ~0ull : ((1ull << nl) - 1ull);
-  uint64_t* front = b.mb[0];
+  Lanes<W>* front = lanes_of<W>(b.mb[0]);
+  Lanes<W>* qm = lanes_of<W>(b.qm);
+  Lanes<W>* visit = lanes_of<W>(b.visit);
   unsigned long long tail = 0, mf = 0, mu = 0;
   for (int l = 0; l < nl; ++l) {
     const int32_t s = b.lane_src[l];
-    const uint64_t old = front[s];
-    front[s] = old | (1ull << l);
-    if (old == 0) {
+    Lanes<W> m = front[s];
+    const bool fresh = !lany(m);
+    m.w[l >> 6] |= 1ull << (l & 63);
+    front[s] = m;
+    if (fresh) {
       b.qv[tail++] = s;
       mf += static_cast<unsigned long long>(g.rowptr[s + 1] - g.rowptr[s]);
     }
-    if (SK != kSigmaNone) reinterpret_cast<T*>(b.sigma)[static_cast<int64_t>(s) * 64 + l] = T(1);
+    if (SK != kSigmaNone)
+      reinterpret_cast<T*>(b.sigma)[static_cast<int64_t>(s) * (64 * W) + l] = T(1);
     if (dist) dist[static_cast<int64_t>(l) * ld + s] = 0;
   }
   for (unsigned long long i = 0; i < tail; ++i) {
     const int32_t s = b.qv[i];
-    const uint64_t m = front[s];
-    b.qm[i] = m;
-    b.visit[s] = m;
-    if (m == act) mu += static_cast<unsigned long long>(g.in_rowptr[s + 1] - g.in_rowptr[s]);
+    const Lanes<W> m = front[s];
+    qm[i] = m;
+    visit[s] = m;
+    if (leq(m, act)) mu += static_cast<unsigned long long>(g.in_rowptr[s + 1] - g.in_rowptr[s]);
   }
   BatchCtl* c = b.ctl;
   c->lo = 0;
@@ -611,10 +720,14 @@ __global__ void k_ms_init(DevGraph g, MsBuffers b, int nl, unsigned long long ca
 // ---------------------------------------------------------------------------
 // Top-down, phase 1: expand Q_L over out-edges; the first lane set on a new
 // vertex appends it to Q_{L+1}.  next[w] collects the discovering lanes.
+// With two words the words are ORed separately, so the first discoverer is
+// decided by a per-vertex claim flag instead (cleared by the settle phase).
 // ---------------------------------------------------------------------------
+template <int W>
 __device__ __forceinline__ void discover_range(const int32_t* __restrict__ ci, int64_t e0, int64_t e1,
-                                               uint64_t F, const uint64_t* __restrict__ visit,
-                                               uint64_t* next, int32_t* qv, BatchCtl* c) {
+                                               const Lanes<W>& F, const Lanes<W>* __restrict__ visit,
+                                               Lanes<W>* next, unsigned* claim, int32_t* qv,
+                                               BatchCtl* c) {
   const int ln = lane_id();
   for (int64_t e = e0; e < e1; e += kWarp) {
     const int64_t idx = e + ln;
@@ -622,10 +735,17 @@ __device__ __forceinline__ void discover_range(const int32_t* __restrict__ ci, i
     int32_t w = 0;
     if (idx < e1) {
       w = ci[idx];
-      const uint64_t m = F & ~visit[w];
-      if (m) {
-        const unsigned long long old = atomicOr(reinterpret_cast<unsigned long long*>(next + w), m);
-        app = (old == 0);
+      const Lanes<W> m = lminus(F, visit[w]);
+      if (lany(m)) {
+        unsigned long long* nw = reinterpret_cast<unsigned long long*>(next[w].w);
+        if (W == 1) {
+          app = atomicOr(nw, m.w[0]) == 0ull;
+        } else {
+#pragma unroll
+          for (int j = 0; j < W; ++j)
+            if (m.w[j]) atomicOr(nw + j, m.w[j]);
+          app = atomicExch(claim + w, 1u) == 0u;
+        }
       }
     }
     const unsigned long long slot = warp_append(app, &c->tail);
@@ -633,62 +753,71 @@ __device__ __forceinline__ void discover_range(const int32_t* __restrict__ ci, i
   }
 }
 
+template <int W>
 __global__ void __launch_bounds__(256) k_ms_td_discover(DevGraph g, MsBuffers b, HubData hd) {
   BatchCtl* c = b.ctl;
   const unsigned long long lo = c->lo, hi = c->hi;
   const int L = c->level;
-  uint64_t* next = mb_at(b, L + 1);
+  Lanes<W>* next = mbw<W>(b, L + 1);
+  const Lanes<W>* qm = lanes_of<W>(b.qm);
+  const Lanes<W>* visit = lanes_of<W>(b.visit);
   for (unsigned long long i = lo + gwarp(); i < hi; i += nwarps()) {
     const int32_t v = b.qv[i];
     const int64_t e0 = g.rowptr[v], e1 = g.rowptr[v + 1];
     if (e1 - e0 > hd.hub_degree) continue;  // k_ms_hub_discover
-    discover_range(g.colidx, e0, e1, b.qm[i], b.visit, next, b.qv, c);
+    discover_range<W>(g.colidx, e0, e1, qm[i], visit, next, b.claim, b.qv, c);
   }
 }
 
+template <int W>
 __global__ void __launch_bounds__(256) k_ms_hub_discover(DevGraph g, MsBuffers b, HubData hd) {
   BatchCtl* c = b.ctl;
   const int L = c->level;
-  const uint64_t* front = mb_at(b, L);
-  uint64_t* next = mb_at(b, L + 1);
+  const Lanes<W>* front = mbw<W>(b, L);
+  Lanes<W>* next = mbw<W>(b, L + 1);
+  const Lanes<W>* visit = lanes_of<W>(b.visit);
   for (long long it = gwarp(); it < hd.n_out; it += nwarps()) {
     const HubItem I = hd.out_items[it];
-    const uint64_t F = front[I.v];
-    if (!F) continue;
-    discover_range(g.colidx, I.lo, I.hi, F, b.visit, next, b.qv, c);
+    const Lanes<W> F = front[I.v];
+    if (!lany(F)) continue;
+    discover_range<W>(g.colidx, I.lo, I.hi, F, visit, next, b.claim, b.qv, c);
   }
 }
 
 // Top-down, phase 2: for every vertex appended in phase 1, record its lane
-// mask, mark it visited and pull its path counts from its predecessors
+// set, mark it visited and pull its path counts from its predecessors
 // (hubs: k_ms_hub_pull).
-template <int SK, bool DIST>
-__global__ void __launch_bounds__(256) k_ms_td_settle(DevGraph g, MsBuffers b, HubData hd,
-                                                      uint64_t act, int32_t* dist, int64_t ld) {
+template <int SK, bool DIST, int W>
+__global__ void __launch_bounds__(256, 4) k_ms_td_settle(DevGraph g, MsBuffers b, HubData hd,
+                                                      Lanes<W> act, int32_t* dist, int64_t ld) {
   using T = typename Sig<SK>::T;
   BatchCtl* c = b.ctl;
   const unsigned long long lo = c->hi, hi = c->tail;
   const int L = c->level;
-  const uint64_t* __restrict__ front = mb_at(b, L);
-  const uint64_t* __restrict__ next = mb_at(b, L + 1);
+  const Lanes<W>* __restrict__ front = mbw<W>(b, L);
+  const Lanes<W>* __restrict__ next = mbw<W>(b, L + 1);
+  Lanes<W>* qm = lanes_of<W>(b.qm);
+  Lanes<W>* visit = lanes_of<W>(b.visit);
   const int ln = lane_id();
   unsigned long long mf = 0, mu = 0, smax = 0;
   for (unsigned long long i = lo + gwarp(); i < hi; i += nwarps()) {
     const int32_t w = b.qv[i];
-    const uint64_t mask = next[w];
+    const Lanes<W> mask = next[w];
     const int64_t e0 = g.in_rowptr[w], e1 = g.in_rowptr[w + 1];
     if (ln == 0) {
-      const uint64_t nv = b.visit[w] | mask;
-      b.qm[i] = mask;
-      b.visit[w] = nv;
+      const Lanes<W> nv = lor(visit[w], mask);
+      qm[i] = mask;
+      visit[w] = nv;
+      if (W > 1) b.claim[w] = 0u;
       mf += static_cast<unsigned long long>(g.rowptr[w + 1] - g.rowptr[w]);
-      if (nv == act) mu += static_cast<unsigned long long>(e1 - e0);
+      if (leq(nv, act)) mu += static_cast<unsigned long long>(e1 - e0);
     }
     if (DIST) store_dist(dist, ld, w, mask, L + 1);
     if (SK != kSigmaNone && e1 - e0 <= hd.hub_degree) {
-      T a0 = T(0), a1 = T(0);
-      pull_range<SK>(g.in_colidx, e0, e1, mask, front, b.sigma, hd.dense_edges, a0, a1);
-      store_sigma<SK>(b.sigma, w, mask, a0, a1, smax);
+      T a[2 * W];
+      zero_accs(a);
+      pull_range<SK, W>(g.in_colidx, e0, e1, mask, front, b.sigma, hd.dense_edges, a);
+      store_sigma<SK, W>(b.sigma, w, mask, a, smax);
     }
   }
   if (SK == kSigmaU64) {
@@ -707,52 +836,55 @@ __global__ void __launch_bounds__(256) k_ms_td_settle(DevGraph g, MsBuffers b, H
 // vertices, so its discoveries are appended with one atomic.  Hubs are left
 // to k_ms_hub_pull.
 // ---------------------------------------------------------------------------
-template <int SK, bool DIST>
-__global__ void __launch_bounds__(256) k_ms_bu(DevGraph g, MsBuffers b, HubData hd, uint64_t act,
+template <int SK, bool DIST, int W>
+__global__ void __launch_bounds__(256, W == 1 ? 4 : 3) k_ms_bu(DevGraph g, MsBuffers b, HubData hd, Lanes<W> act,
                                                int32_t* dist, int64_t ld) {
   using T = typename Sig<SK>::T;
   BatchCtl* c = b.ctl;
   const int L = c->level;
-  const uint64_t* __restrict__ front = mb_at(b, L);
-  uint64_t* next = mb_at(b, L + 1);
+  const Lanes<W>* __restrict__ front = mbw<W>(b, L);
+  Lanes<W>* next = mbw<W>(b, L + 1);
+  Lanes<W>* qm = lanes_of<W>(b.qm);
+  Lanes<W>* visit = lanes_of<W>(b.visit);
   const int64_t n = g.n;
   const int ln = lane_id();
   unsigned long long mf = 0, mu = 0, smax = 0;
   for (int64_t base = gwarp() * kWarp; base < n; base += nwarps() * kWarp) {
     const int64_t wme = base + ln;
-    uint64_t vis = 0;
+    Lanes<W> vis = lz<W>();
     bool cand = false;
     if (wme < n) {
-      vis = b.visit[wme];
+      vis = visit[wme];
       const int64_t d = g.in_rowptr[wme + 1] - g.in_rowptr[wme];
-      cand = (vis != act) && d > 0 && d <= hd.hub_degree;
+      cand = !leq(vis, act) && d > 0 && d <= hd.hub_degree;
     }
     unsigned cb = __ballot_sync(kFull, cand);
-    uint64_t my_nm = 0;
+    Lanes<W> my_nm = lz<W>();
     while (cb) {
       const int j = __ffs(cb) - 1;
       cb &= cb - 1;
       const int32_t w = static_cast<int32_t>(base + j);
-      const uint64_t want = act & ~shfl_u64(vis, j);
-      T a0 = T(0), a1 = T(0);
-      const uint64_t nm = pull_range<SK>(g.in_colidx, g.in_rowptr[w], g.in_rowptr[w + 1], want,
-                                         front, b.sigma, hd.dense_edges, a0, a1);
-      if (nm) {
-        if (SK != kSigmaNone) store_sigma<SK>(b.sigma, w, nm, a0, a1, smax);
+      const Lanes<W> want = lminus(act, lshfl(vis, j));
+      T a[2 * W];
+      zero_accs(a);
+      const Lanes<W> nm = pull_range<SK, W>(g.in_colidx, g.in_rowptr[w], g.in_rowptr[w + 1], want,
+                                            front, b.sigma, hd.dense_edges, a);
+      if (lany(nm)) {
+        if (SK != kSigmaNone) store_sigma<SK, W>(b.sigma, w, nm, a, smax);
         if (DIST) store_dist(dist, ld, w, nm, L + 1);
       }
       if (ln == j) my_nm = nm;
     }
-    const bool app = my_nm != 0;
+    const bool app = lany(my_nm);
     const unsigned long long slot = warp_append(app, &c->tail);
     if (app) {
       b.qv[slot] = static_cast<int32_t>(wme);
-      b.qm[slot] = my_nm;
+      qm[slot] = my_nm;
       next[wme] = my_nm;
-      const uint64_t nv = vis | my_nm;
-      b.visit[wme] = nv;
+      const Lanes<W> nv = lor(vis, my_nm);
+      visit[wme] = nv;
       mf += static_cast<unsigned long long>(g.rowptr[wme + 1] - g.rowptr[wme]);
-      if (nv == act) mu += static_cast<unsigned long long>(g.in_rowptr[wme + 1] - g.in_rowptr[wme]);
+      if (leq(nv, act)) mu += static_cast<unsigned long long>(g.in_rowptr[wme + 1] - g.in_rowptr[wme]);
     }
   }
   if (SK == kSigmaU64) {
@@ -772,62 +904,75 @@ __global__ void __launch_bounds__(256) k_ms_bu(DevGraph g, MsBuffers b, HubData 
 // bottom-up phase (BU == true: the hub is not finished, want = unvisited
 // lanes).  Partial sums go to the hub's slot; its last item stores sigma and,
 // bottom-up, appends the hub to the next level.
-template <int SK, bool DIST, bool BU>
-__global__ void __launch_bounds__(256) k_ms_hub_pull(DevGraph g, MsBuffers b, HubData hd,
-                                                     uint64_t act, int32_t* dist, int64_t ld) {
+template <int SK, bool DIST, bool BU, int W>
+__global__ void __launch_bounds__(256, 4) k_ms_hub_pull(DevGraph g, MsBuffers b, HubData hd,
+                                                     Lanes<W> act, int32_t* dist, int64_t ld) {
   using T = typename Sig<SK>::T;
   BatchCtl* c = b.ctl;
   const int L = c->level;
-  const uint64_t* __restrict__ front = mb_at(b, L);
-  uint64_t* next = mb_at(b, L + 1);
+  const Lanes<W>* __restrict__ front = mbw<W>(b, L);
+  Lanes<W>* next = mbw<W>(b, L + 1);
+  Lanes<W>* qm = lanes_of<W>(b.qm);
+  Lanes<W>* visit = lanes_of<W>(b.visit);
   const int ln = lane_id();
   unsigned long long mf = 0, mu = 0, smax = 0;
   for (long long it = gwarp(); it < hd.n_in; it += nwarps()) {
     const HubItem I = hd.in_items[it];
     const int32_t h = I.v;
-    uint64_t vis = 0, want;
+    Lanes<W> vis = lz<W>(), want;
     if (BU) {
-      vis = b.visit[h];
-      if (vis == act) continue;
-      want = act & ~vis;
+      vis = visit[h];
+      if (leq(vis, act)) continue;
+      want = lminus(act, vis);
     } else {
       want = next[h];
-      if (!want) continue;
+      if (!lany(want)) continue;
     }
-    T a0 = T(0), a1 = T(0);
-    const uint64_t found =
-        pull_range<SK>(g.in_colidx, I.lo, I.hi, want, front, b.sigma, hd.dense_edges, a0, a1);
-    unsigned long long* acc = hd.acc + static_cast<int64_t>(I.slot) * 64;
+    T a[2 * W];
+    zero_accs(a);
+    const Lanes<W> found =
+        pull_range<SK, W>(g.in_colidx, I.lo, I.hi, want, front, b.sigma, hd.dense_edges, a);
+    unsigned long long* acc = hd.acc + static_cast<int64_t>(I.slot) * (64 * W);
+    unsigned long long* hmask = hd.mask + static_cast<int64_t>(I.slot) * W;
     if (SK != kSigmaNone) {
-      if (a0 != T(0)) hub_add(acc + ln, a0);
-      if (a1 != T(0)) hub_add(acc + 32 + ln, a1);
+#pragma unroll
+      for (int k = 0; k < 2 * W; ++k)
+        if (a[k] != T(0)) hub_add(acc + 32 * k + ln, a[k]);
     }
-    if (BU && ln == 0 && found) atomicOr(hd.mask + I.slot, found);
+    if (BU && ln == 0) {
+#pragma unroll
+      for (int j = 0; j < W; ++j)
+        if (found.w[j]) atomicOr(hmask + j, found.w[j]);
+    }
     if (!hub_last(hd.cnt + I.slot, I.nitems)) continue;
-    uint64_t nm = want;
+    Lanes<W> nm = want;
     if (BU) {
-      unsigned long long x = 0;
-      if (ln == 0) x = atomicExch(hd.mask + I.slot, 0ull);
-      nm = shfl_u64(x, 0);
+#pragma unroll
+      for (int j = 0; j < W; ++j) {
+        unsigned long long x = 0;
+        if (ln == 0) x = atomicExch(hmask + j, 0ull);
+        nm.w[j] = shfl_u64(x, 0);
+      }
     }
-    T s0 = T(0), s1 = T(0);
-    if (SK != kSigmaNone) {
-      s0 = from_bits<T>(atomicExch(acc + ln, 0ull));
-      s1 = from_bits<T>(atomicExch(acc + 32 + ln, 0ull));
+    T s[2 * W];
+#pragma unroll
+    for (int k = 0; k < 2 * W; ++k) {
+      s[k] = T(0);
+      if (SK != kSigmaNone) s[k] = from_bits<T>(atomicExch(acc + 32 * k + ln, 0ull));
     }
     if (ln == 0) hd.cnt[I.slot] = 0u;
-    if (nm) {
-      if (SK != kSigmaNone) store_sigma<SK>(b.sigma, h, nm, s0, s1, smax);
+    if (lany(nm)) {
+      if (SK != kSigmaNone) store_sigma<SK, W>(b.sigma, h, nm, s, smax);
       if (DIST) store_dist(dist, ld, h, nm, L + 1);
       if (BU && ln == 0) {
         const unsigned long long slot = atomicAdd(&c->tail, 1ull);
         b.qv[slot] = h;
-        b.qm[slot] = nm;
+        qm[slot] = nm;
         next[h] = nm;
-        const uint64_t nv = vis | nm;
-        b.visit[h] = nv;
+        const Lanes<W> nv = lor(vis, nm);
+        visit[h] = nv;
         mf += static_cast<unsigned long long>(g.rowptr[h + 1] - g.rowptr[h]);
-        if (nv == act) mu += static_cast<unsigned long long>(g.in_rowptr[h + 1] - g.in_rowptr[h]);
+        if (leq(nv, act)) mu += static_cast<unsigned long long>(g.in_rowptr[h + 1] - g.in_rowptr[h]);
       }
     }
   }
@@ -843,14 +988,15 @@ __global__ void __launch_bounds__(256) k_ms_hub_pull(DevGraph g, MsBuffers b, Hu
 
 // After a level: clear the old frontier's dense masks (kept when the forward
 // sweep just ended, because the backward sweep starts from them).
+template <int W>
 __global__ void k_ms_clear_front(MsBuffers b) {
   BatchCtl* c = b.ctl;
   if (c->tail == c->hi) return;
   const unsigned long long lo = c->lo, hi = c->hi;
-  uint64_t* front = mb_at(b, c->level);
+  Lanes<W>* front = mbw<W>(b, c->level);
   for (unsigned long long i = lo + blockIdx.x * blockDim.x + threadIdx.x; i < hi;
        i += static_cast<unsigned long long>(gridDim.x) * blockDim.x)
-    front[b.qv[i]] = 0;
+    front[b.qv[i]] = lz<W>();
 }
 
 __device__ __forceinline__ void advance_step(const MsBuffers& b, int64_t n);
@@ -932,15 +1078,16 @@ __device__ __forceinline__ void advance_step(const MsBuffers& b, int64_t n) {
 __global__ void k_ms_begin_backward(MsBuffers b) { b.ctl->level = b.ctl->maxlevel; }
 
 // Backward step at level L, part 1: mb[L & 1] still holds F_{L+2}; clear it.
+template <int W>
 __global__ void k_ms_back_clear(MsBuffers b) {
   BatchCtl* c = b.ctl;
   const int L = c->level;
   if (L + 2 > c->maxlevel) return;
   const unsigned long long lo = b.lvl_off[L + 2], hi = b.lvl_off[L + 3];
-  uint64_t* other = mb_at(b, L);
+  Lanes<W>* other = mbw<W>(b, L);
   for (unsigned long long i = lo + blockIdx.x * blockDim.x + threadIdx.x; i < hi;
        i += static_cast<unsigned long long>(gridDim.x) * blockDim.x)
-    other[b.qv[i]] = 0;
+    other[b.qv[i]] = lz<W>();
 }
 
 // Backward step at level L, part 2 (pull): for every (v, lane) at level L,
@@ -951,42 +1098,46 @@ __global__ void k_ms_back_clear(MsBuffers b) {
 // psi is the reference's `coeff` (betweenness.jl:96) stored once per vertex.
 // Writes F_L into mb[L & 1] for every v (hubs included) before
 // k_ms_hub_delta finishes the hubs.
-template <int SK>
-__global__ void __launch_bounds__(256) k_ms_delta(DevGraph g, MsBuffers b, HubData hd, double* bc) {
+template <int SK, int W>
+__global__ void __launch_bounds__(256, W == 1 ? 5 : 4) k_ms_delta(DevGraph g, MsBuffers b, HubData hd, double* bc) {
   BatchCtl* c = b.ctl;
   const int L = c->level;
   const unsigned long long lo = b.lvl_off[L], hi = b.lvl_off[L + 1];
-  const uint64_t* __restrict__ succ = mb_at(b, L + 1);
-  uint64_t* other = mb_at(b, L);
+  const Lanes<W>* __restrict__ succ = mbw<W>(b, L + 1);
+  Lanes<W>* other = mbw<W>(b, L);
+  const Lanes<W>* qm = lanes_of<W>(b.qm);
+  Lanes<W>* visit = lanes_of<W>(b.visit);
   const int ln = lane_id();
   for (unsigned long long i = lo + gwarp(); i < hi; i += nwarps()) {
     const int32_t v = b.qv[i];
-    const uint64_t F = b.qm[i];
+    const Lanes<W> F = qm[i];
     if (ln == 0) {
       other[v] = F;
-      b.visit[v] = 0;
+      visit[v] = lz<W>();
     }
     if (L == 0) continue;
     const int64_t e0 = g.rowptr[v], e1 = g.rowptr[v + 1];
     if (e1 - e0 > hd.hub_degree) continue;  // k_ms_hub_delta
     const unsigned mine = my_bits(F);
     if (SK == kSigmaU64) {
-      df32 acc0{0.f, 0.f}, acc1{0.f, 0.f};
-      psi_range_df(g.colidx, e0, e1, F, succ, b.psi, hd.dense_edges, acc0, acc1);
+      df32 acc[2 * W];
+      zero_accs(acc);
+      psi_range_df<W>(g.colidx, e0, e1, F, succ, b.psi, hd.dense_edges, acc);
       if (b.lane_w) {
         const double contrib =
-            warp_sum_f64(finish_df_w(b.psi, b.sigma, v, mine, acc0, acc1, weights_of(b, v)));
+            warp_sum_f64(finish_df_w<W>(b.psi, b.sigma, v, mine, acc, weights_of<W>(b, v)));
         if (ln == 0) bc[v] += contrib;
       } else {
-        df32 contrib = finish_df(b.psi, b.sigma, v, mine, acc0, acc1);
+        df32 contrib = finish_df<W>(b.psi, b.sigma, v, mine, acc);
         contrib = warp_sum_df(contrib);
         if (ln == 0) bc[v] += df_to_double(contrib);
       }
     } else {
-      double acc0 = 0.0, acc1 = 0.0;
-      psi_range_f64(g.colidx, e0, e1, F, succ, b.psi, hd.dense_edges, acc0, acc1);
-      double contrib = b.lane_w ? finish_f64_w(b.psi, b.sigma, v, mine, acc0, acc1, weights_of(b, v))
-                                : finish_f64(b.psi, b.sigma, v, mine, acc0, acc1);
+      double acc[2 * W];
+      zero_accs(acc);
+      psi_range_f64<W>(g.colidx, e0, e1, F, succ, b.psi, hd.dense_edges, acc);
+      double contrib = b.lane_w ? finish_f64_w<W>(b.psi, b.sigma, v, mine, acc, weights_of<W>(b, v))
+                                : finish_f64<W>(b.psi, b.sigma, v, mine, acc);
       contrib = warp_sum_f64(contrib);
       if (ln == 0) bc[v] += contrib;
     }
@@ -995,50 +1146,57 @@ __global__ void __launch_bounds__(256) k_ms_delta(DevGraph g, MsBuffers b, HubDa
 
 // Hub dependencies at level L over out-edge items; partial psi sums are
 // combined in FP64 atomics, the hub's last item finalises delta / psi / bc.
-template <int SK>
-__global__ void __launch_bounds__(256) k_ms_hub_delta(DevGraph g, MsBuffers b, HubData hd, double* bc) {
+template <int SK, int W>
+__global__ void __launch_bounds__(256, W == 1 ? 5 : 4) k_ms_hub_delta(DevGraph g, MsBuffers b,
+                                                                     HubData hd, double* bc) {
   BatchCtl* c = b.ctl;
   const int L = c->level;
   if (L == 0) return;
-  const uint64_t* __restrict__ succ = mb_at(b, L + 1);
-  const uint64_t* __restrict__ cur = mb_at(b, L);
+  const Lanes<W>* __restrict__ succ = mbw<W>(b, L + 1);
+  const Lanes<W>* __restrict__ cur = mbw<W>(b, L);
   const int ln = lane_id();
   for (long long it = gwarp(); it < hd.n_out; it += nwarps()) {
     const HubItem I = hd.out_items[it];
     const int32_t h = I.v;
-    const uint64_t F = cur[h];
-    if (!F) continue;
-    unsigned long long* acc = hd.acc + static_cast<int64_t>(I.slot) * 64;
-    double part0, part1;
+    const Lanes<W> F = cur[h];
+    if (!lany(F)) continue;
+    unsigned long long* acc = hd.acc + static_cast<int64_t>(I.slot) * (64 * W);
+    double part[2 * W];
     if (SK == kSigmaU64) {
-      df32 a0{0.f, 0.f}, a1{0.f, 0.f};
-      psi_range_df(g.colidx, I.lo, I.hi, F, succ, b.psi, hd.dense_edges, a0, a1);
-      part0 = df_to_double(a0);
-      part1 = df_to_double(a1);
+      df32 a[2 * W];
+      zero_accs(a);
+      psi_range_df<W>(g.colidx, I.lo, I.hi, F, succ, b.psi, hd.dense_edges, a);
+#pragma unroll
+      for (int k = 0; k < 2 * W; ++k) part[k] = df_to_double(a[k]);
     } else {
-      part0 = part1 = 0.0;
-      psi_range_f64(g.colidx, I.lo, I.hi, F, succ, b.psi, hd.dense_edges, part0, part1);
+      zero_accs(part);
+      psi_range_f64<W>(g.colidx, I.lo, I.hi, F, succ, b.psi, hd.dense_edges, part);
     }
-    if (part0 != 0.0) hub_add(acc + ln, part0);
-    if (part1 != 0.0) hub_add(acc + 32 + ln, part1);
+#pragma unroll
+    for (int k = 0; k < 2 * W; ++k)
+      if (part[k] != 0.0) hub_add(acc + 32 * k + ln, part[k]);
     if (!hub_last(hd.cnt + I.slot, I.nitems)) continue;
-    const double s0 = from_bits<double>(atomicExch(acc + ln, 0ull));
-    const double s1 = from_bits<double>(atomicExch(acc + 32 + ln, 0ull));
+    double s[2 * W];
+#pragma unroll
+    for (int k = 0; k < 2 * W; ++k) s[k] = from_bits<double>(atomicExch(acc + 32 * k + ln, 0ull));
     if (ln == 0) hd.cnt[I.slot] = 0u;
     const unsigned mine = my_bits(F);
     if (SK == kSigmaU64) {
+      df32 d[2 * W];
+#pragma unroll
+      for (int k = 0; k < 2 * W; ++k) d[k] = df_from_double(s[k]);
       if (b.lane_w) {
-        const double contrib = warp_sum_f64(finish_df_w(
-            b.psi, b.sigma, h, mine, df_from_double(s0), df_from_double(s1), weights_of(b, h)));
+        const double contrib =
+            warp_sum_f64(finish_df_w<W>(b.psi, b.sigma, h, mine, d, weights_of<W>(b, h)));
         if (ln == 0) bc[h] += contrib;
       } else {
-        df32 contrib = finish_df(b.psi, b.sigma, h, mine, df_from_double(s0), df_from_double(s1));
+        df32 contrib = finish_df<W>(b.psi, b.sigma, h, mine, d);
         contrib = warp_sum_df(contrib);
         if (ln == 0) bc[h] += df_to_double(contrib);
       }
     } else {
-      double contrib = b.lane_w ? finish_f64_w(b.psi, b.sigma, h, mine, s0, s1, weights_of(b, h))
-                                : finish_f64(b.psi, b.sigma, h, mine, s0, s1);
+      double contrib = b.lane_w ? finish_f64_w<W>(b.psi, b.sigma, h, mine, s, weights_of<W>(b, h))
+                                : finish_f64<W>(b.psi, b.sigma, h, mine, s);
       contrib = warp_sum_f64(contrib);
       if (ln == 0) bc[h] += contrib;
     }
@@ -1051,15 +1209,17 @@ __global__ void __launch_bounds__(256) k_ms_hub_delta(DevGraph g, MsBuffers b, H
 // giving each vertex a whole warp pass.  Same results as k_ms_td_settle,
 // k_ms_bu and k_ms_delta.
 // ---------------------------------------------------------------------------
-template <int SK>
-__global__ void __launch_bounds__(256) k_ms_td_settle_seg(DevGraph g, MsBuffers b, HubData hd,
-                                                          uint64_t act) {
+template <int SK, int W>
+__global__ void __launch_bounds__(256, W == 1 ? 3 : 2) k_ms_td_settle_seg(DevGraph g, MsBuffers b, HubData hd,
+                                                          Lanes<W> act) {
   using T = typename Sig<SK>::T;
   BatchCtl* c = b.ctl;
   const unsigned long long lo = c->hi, hi = c->tail;
   const int L = c->level;
-  const uint64_t* __restrict__ front = mb_at(b, L);
-  const uint64_t* __restrict__ next = mb_at(b, L + 1);
+  const Lanes<W>* __restrict__ front = mbw<W>(b, L);
+  const Lanes<W>* __restrict__ next = mbw<W>(b, L + 1);
+  Lanes<W>* qm = lanes_of<W>(b.qm);
+  Lanes<W>* visit = lanes_of<W>(b.visit);
   const int ln = lane_id();
   unsigned long long mf = 0, mu = 0, smax = 0;
   for (unsigned long long base = lo + static_cast<unsigned long long>(gwarp()) * kWarp; base < hi;
@@ -1067,25 +1227,26 @@ __global__ void __launch_bounds__(256) k_ms_td_settle_seg(DevGraph g, MsBuffers 
     const unsigned long long i = base + ln;
     const bool ve = i < hi;
     int32_t w = 0;
-    uint64_t mask = 0;
+    Lanes<W> mask = lz<W>();
     int64_t e0 = 0, deg = 0;
     if (ve) {
       w = b.qv[i];
       mask = next[w];
       e0 = g.in_rowptr[w];
       deg = g.in_rowptr[w + 1] - e0;
-      const uint64_t nv = b.visit[w] | mask;
-      b.qm[i] = mask;
-      b.visit[w] = nv;
+      const Lanes<W> nv = lor(visit[w], mask);
+      qm[i] = mask;
+      visit[w] = nv;
+      if (W > 1) b.claim[w] = 0u;
       mf += static_cast<unsigned long long>(g.rowptr[w + 1] - g.rowptr[w]);
-      if (nv == act) mu += static_cast<unsigned long long>(deg);
+      if (leq(nv, act)) mu += static_cast<unsigned long long>(deg);
     }
     const bool mine = ve && deg <= hd.hub_degree;  // hubs: k_ms_hub_pull
-    seg_gather<T, T, false>(mine, e0, static_cast<int>(mine ? deg : 0), mask, g.in_colidx, front,
-                            reinterpret_cast<const T*>(b.sigma),
-                            [&](int j, uint64_t nm, T a0, T a1) {
-                              store_sigma<SK>(b.sigma, __shfl_sync(kFull, w, j), nm, a0, a1, smax);
-                            });
+    seg_gather<T, T, false, W>(mine, e0, static_cast<int>(mine ? deg : 0), mask, g.in_colidx, front,
+                               reinterpret_cast<const T*>(b.sigma),
+                               [&](int j, const Lanes<W>& nm, const T (&a)[2 * W]) {
+                                 store_sigma<SK, W>(b.sigma, __shfl_sync(kFull, w, j), nm, a, smax);
+                               });
   }
   if (SK == kSigmaU64) {
     smax = warp_max_u64(smax);
@@ -1099,46 +1260,48 @@ __global__ void __launch_bounds__(256) k_ms_td_settle_seg(DevGraph g, MsBuffers 
   }
 }
 
-template <int SK>
-__global__ void __launch_bounds__(256) k_ms_bu_seg(DevGraph g, MsBuffers b, HubData hd, uint64_t act) {
+template <int SK, int W>
+__global__ void __launch_bounds__(256, W == 1 ? 3 : 2) k_ms_bu_seg(DevGraph g, MsBuffers b, HubData hd, Lanes<W> act) {
   using T = typename Sig<SK>::T;
   BatchCtl* c = b.ctl;
   const int L = c->level;
-  const uint64_t* __restrict__ front = mb_at(b, L);
-  uint64_t* next = mb_at(b, L + 1);
+  const Lanes<W>* __restrict__ front = mbw<W>(b, L);
+  Lanes<W>* next = mbw<W>(b, L + 1);
+  Lanes<W>* qm = lanes_of<W>(b.qm);
+  Lanes<W>* visit = lanes_of<W>(b.visit);
   const int64_t n = g.n;
   const int ln = lane_id();
   unsigned long long mf = 0, mu = 0, smax = 0;
   for (int64_t base = gwarp() * kWarp; base < n; base += nwarps() * kWarp) {
     const int64_t wme = base + ln;
-    uint64_t vis = 0;
+    Lanes<W> vis = lz<W>();
     int64_t e0 = 0, deg = 0;
     bool cand = false;
     if (wme < n) {
-      vis = b.visit[wme];
+      vis = visit[wme];
       e0 = g.in_rowptr[wme];
       deg = g.in_rowptr[wme + 1] - e0;
-      cand = (vis != act) && deg > 0 && deg <= hd.hub_degree;
+      cand = !leq(vis, act) && deg > 0 && deg <= hd.hub_degree;
     }
-    uint64_t my_nm = 0;
-    seg_gather<T, T, false>(cand, e0, static_cast<int>(cand ? deg : 0), act & ~vis, g.in_colidx,
-                            front, reinterpret_cast<const T*>(b.sigma),
-                            [&](int j, uint64_t nm, T a0, T a1) {
-                              if (nm)
-                                store_sigma<SK>(b.sigma, static_cast<int32_t>(base + j), nm, a0, a1,
-                                                smax);
-                              if (ln == j) my_nm = nm;
-                            });
-    const bool app = my_nm != 0;
+    Lanes<W> my_nm = lz<W>();
+    seg_gather<T, T, false, W>(cand, e0, static_cast<int>(cand ? deg : 0), lminus(act, vis),
+                               g.in_colidx, front, reinterpret_cast<const T*>(b.sigma),
+                               [&](int j, const Lanes<W>& nm, const T (&a)[2 * W]) {
+                                 if (lany(nm))
+                                   store_sigma<SK, W>(b.sigma, static_cast<int32_t>(base + j), nm,
+                                                      a, smax);
+                                 if (ln == j) my_nm = nm;
+                               });
+    const bool app = lany(my_nm);
     const unsigned long long slot = warp_append(app, &c->tail);
     if (app) {
       b.qv[slot] = static_cast<int32_t>(wme);
-      b.qm[slot] = my_nm;
+      qm[slot] = my_nm;
       next[wme] = my_nm;
-      const uint64_t nv = vis | my_nm;
-      b.visit[wme] = nv;
+      const Lanes<W> nv = lor(vis, my_nm);
+      visit[wme] = nv;
       mf += static_cast<unsigned long long>(g.rowptr[wme + 1] - g.rowptr[wme]);
-      if (nv == act) mu += static_cast<unsigned long long>(deg);
+      if (leq(nv, act)) mu += static_cast<unsigned long long>(deg);
     }
   }
   if (SK == kSigmaU64) {
@@ -1153,26 +1316,28 @@ __global__ void __launch_bounds__(256) k_ms_bu_seg(DevGraph g, MsBuffers b, HubD
   }
 }
 
-template <int SK>
-__global__ void __launch_bounds__(256) k_ms_delta_seg(DevGraph g, MsBuffers b, HubData hd, double* bc) {
+template <int SK, int W>
+__global__ void __launch_bounds__(256, W == 1 ? 3 : 2) k_ms_delta_seg(DevGraph g, MsBuffers b, HubData hd, double* bc) {
   BatchCtl* c = b.ctl;
   const int L = c->level;
   const unsigned long long lo = b.lvl_off[L], hi = b.lvl_off[L + 1];
-  const uint64_t* __restrict__ succ = mb_at(b, L + 1);
-  uint64_t* other = mb_at(b, L);
+  const Lanes<W>* __restrict__ succ = mbw<W>(b, L + 1);
+  Lanes<W>* other = mbw<W>(b, L);
+  const Lanes<W>* qm = lanes_of<W>(b.qm);
+  Lanes<W>* visit = lanes_of<W>(b.visit);
   const int ln = lane_id();
   for (unsigned long long base = lo + static_cast<unsigned long long>(gwarp()) * kWarp; base < hi;
        base += static_cast<unsigned long long>(nwarps()) * kWarp) {
     const unsigned long long i = base + ln;
     const bool ve = i < hi;
     int32_t v = 0;
-    uint64_t F = 0;
+    Lanes<W> F = lz<W>();
     int64_t e0 = 0, deg = 0;
     if (ve) {
       v = b.qv[i];
-      F = b.qm[i];
+      F = qm[i];
       other[v] = F;
-      b.visit[v] = 0;
+      visit[v] = lz<W>();
       e0 = g.rowptr[v];
       deg = g.rowptr[v + 1] - e0;
     }
@@ -1180,26 +1345,28 @@ __global__ void __launch_bounds__(256) k_ms_delta_seg(DevGraph g, MsBuffers b, H
     const bool mine = ve && deg <= hd.hub_degree;  // hubs: k_ms_hub_delta
     const int dg = static_cast<int>(mine ? deg : 0);
     if (SK == kSigmaU64) {
-      seg_gather<float2, df32, true>(mine, e0, dg, F, g.colidx, succ,
-                                     reinterpret_cast<const float2*>(b.psi),
-                                     [&](int j, uint64_t, df32 a0, df32 a1) {
-                                       const int32_t vj = __shfl_sync(kFull, v, j);
-                                       df32 contrib = finish_df(b.psi, b.sigma, vj,
-                                                                my_bits(shfl_u64(F, j)),
-                                                                acc_done(a0), acc_done(a1));
-                                       contrib = warp_sum_df(contrib);
-                                       if (ln == 0 && contrib.hi != 0.f) bc[vj] += df_to_double(contrib);
-                                     });
+      seg_gather<float2, df32, true, W>(mine, e0, dg, F, g.colidx, succ,
+                                        reinterpret_cast<const float2*>(b.psi),
+                                        [&](int j, const Lanes<W>&, const df32 (&a)[2 * W]) {
+                                          const int32_t vj = __shfl_sync(kFull, v, j);
+                                          df32 d[2 * W];
+#pragma unroll
+                                          for (int k = 0; k < 2 * W; ++k) d[k] = acc_done(a[k]);
+                                          df32 contrib = finish_df<W>(b.psi, b.sigma, vj,
+                                                                      my_bits(lshfl(F, j)), d);
+                                          contrib = warp_sum_df(contrib);
+                                          if (ln == 0 && contrib.hi != 0.f) bc[vj] += df_to_double(contrib);
+                                        });
     } else {
-      seg_gather<double, double, true>(mine, e0, dg, F, g.colidx, succ,
-                                       reinterpret_cast<const double*>(b.psi),
-                                       [&](int j, uint64_t, double a0, double a1) {
-                                         const int32_t vj = __shfl_sync(kFull, v, j);
-                                         double contrib = finish_f64(b.psi, b.sigma, vj,
-                                                                     my_bits(shfl_u64(F, j)), a0, a1);
-                                         contrib = warp_sum_f64(contrib);
-                                         if (ln == 0 && contrib != 0.0) bc[vj] += contrib;
-                                       });
+      seg_gather<double, double, true, W>(mine, e0, dg, F, g.colidx, succ,
+                                          reinterpret_cast<const double*>(b.psi),
+                                          [&](int j, const Lanes<W>&, const double (&a)[2 * W]) {
+                                            const int32_t vj = __shfl_sync(kFull, v, j);
+                                            double contrib = finish_f64<W>(b.psi, b.sigma, vj,
+                                                                           my_bits(lshfl(F, j)), a);
+                                            contrib = warp_sum_f64(contrib);
+                                            if (ln == 0 && contrib != 0.0) bc[vj] += contrib;
+                                          });
     }
   }
 }
@@ -1271,7 +1438,7 @@ __global__ void __launch_bounds__(256) k_st_delta(DevGraph g, MsBuffers b, HubDa
     if (L == 0) continue;
     const int64_t e0 = g.rowptr[v], e1 = g.rowptr[v + 1];
     if (e1 - e0 > hd.hub_degree) continue;
-    unsigned long long a0 = 0, a1 = 0;
+    unsigned long long a[2] = {0ull, 0ull};
     for (int64_t e = e0; e < e1; e += kWarp) {
       const int64_t idx = e + ln;
       int32_t w = 0;
@@ -1280,12 +1447,12 @@ __global__ void __launch_bounds__(256) k_st_delta(DevGraph g, MsBuffers b, HubDa
         w = g.colidx[idx];
         gm = succ[w] & F;
       }
-      gather_chunk<unsigned long long, unsigned long long>(w, gm, E, hd.dense_edges, a0, a1);
+      gather_chunk<unsigned long long, unsigned long long, 1>(w, Lanes<1>{{gm}}, E, hd.dense_edges, a);
     }
     const unsigned mine = my_bits(F);
     unsigned long long* row = E + static_cast<int64_t>(v) * 64;
-    if (mine & 1u) row[ln] = a0 + 1ull;
-    if (mine & 2u) row[32 + ln] = a1 + 1ull;
+    if (mine & 1u) row[ln] = a[0] + 1ull;
+    if (mine & 2u) row[32 + ln] = a[1] + 1ull;
   }
 }
 
@@ -1303,7 +1470,7 @@ __global__ void __launch_bounds__(256) k_st_hub_delta(DevGraph g, MsBuffers b, H
     const uint64_t F = cur[h];
     if (!F) continue;
     unsigned long long* acc = hd.acc + static_cast<int64_t>(I.slot) * 64;
-    unsigned long long a0 = 0, a1 = 0;
+    unsigned long long a[2] = {0ull, 0ull};
     for (int64_t e = I.lo; e < I.hi; e += kWarp) {
       const int64_t idx = e + ln;
       int32_t w = 0;
@@ -1312,10 +1479,10 @@ __global__ void __launch_bounds__(256) k_st_hub_delta(DevGraph g, MsBuffers b, H
         w = g.colidx[idx];
         gm = succ[w] & F;
       }
-      gather_chunk<unsigned long long, unsigned long long>(w, gm, E, hd.dense_edges, a0, a1);
+      gather_chunk<unsigned long long, unsigned long long, 1>(w, Lanes<1>{{gm}}, E, hd.dense_edges, a);
     }
-    if (a0) atomicAdd(acc + ln, a0);
-    if (a1) atomicAdd(acc + 32 + ln, a1);
+    if (a[0]) atomicAdd(acc + ln, a[0]);
+    if (a[1]) atomicAdd(acc + 32 + ln, a[1]);
     if (!hub_last(hd.cnt + I.slot, I.nitems)) continue;
     const unsigned long long s0 = atomicExch(acc + ln, 0ull);
     const unsigned long long s1 = atomicExch(acc + 32 + ln, 0ull);
@@ -1379,14 +1546,18 @@ __global__ void k_ms_back_advance(MsBuffers b) { b.ctl->level -= 1; }
 
 // End of a Brandes batch: the backward sweep cleared visit for every listed
 // vertex; clear the dense masks of levels 0 and 1 that remain.
+template <int W>
 __global__ void k_ms_cleanup(MsBuffers b) {
   const unsigned long long lo = b.lvl_off[0], hi = b.lvl_off[2];
+  Lanes<W>* m0 = lanes_of<W>(b.mb[0]);
+  Lanes<W>* m1 = lanes_of<W>(b.mb[1]);
+  Lanes<W>* visit = lanes_of<W>(b.visit);
   for (unsigned long long i = lo + blockIdx.x * blockDim.x + threadIdx.x; i < hi;
        i += static_cast<unsigned long long>(gridDim.x) * blockDim.x) {
     const int32_t v = b.qv[i];
-    b.mb[0][v] = 0;
-    b.mb[1][v] = 0;
-    b.visit[v] = 0;
+    m0[v] = lz<W>();
+    m1[v] = lz<W>();
+    visit[v] = lz<W>();
   }
 }
 
@@ -1545,15 +1716,32 @@ __global__ void k_ms_init_seeds_ctl(MsBuffers b, long long nseeds, unsigned long
 
 int ms_init(cudaStream_t s, const DevGraph& g, const MsBuffers& b, int nlanes, int sigma_kind,
             unsigned long long sigma_limit, int32_t* dist, int64_t dist_ld) {
+  const LaneSet act = lane_set(nlanes, b.words);
+  if (b.words == 2) {
+    const Lanes<2> a = lane_cast<2>(act);
+    switch (sigma_kind) {
+      case kSigmaU64:
+        k_ms_init<kSigmaU64, 2><<<1, 32, 0, s>>>(g, b, nlanes, a, b.cap, sigma_limit, nullptr, 0);
+        break;
+      case kSigmaF64:
+        k_ms_init<kSigmaF64, 2><<<1, 32, 0, s>>>(g, b, nlanes, a, b.cap, ~0ull, nullptr, 0);
+        break;
+      default:
+        k_ms_init<kSigmaNone, 2><<<1, 32, 0, s>>>(g, b, nlanes, a, b.cap, ~0ull, nullptr, 0);
+        break;
+    }
+    return 1;
+  }
+  const Lanes<1> a = lane_cast<1>(act);
   switch (sigma_kind) {
     case kSigmaU64:
-      k_ms_init<kSigmaU64><<<1, 32, 0, s>>>(g, b, nlanes, b.cap, sigma_limit, dist, dist_ld);
+      k_ms_init<kSigmaU64, 1><<<1, 32, 0, s>>>(g, b, nlanes, a, b.cap, sigma_limit, dist, dist_ld);
       break;
     case kSigmaF64:
-      k_ms_init<kSigmaF64><<<1, 32, 0, s>>>(g, b, nlanes, b.cap, ~0ull, dist, dist_ld);
+      k_ms_init<kSigmaF64, 1><<<1, 32, 0, s>>>(g, b, nlanes, a, b.cap, ~0ull, dist, dist_ld);
       break;
     default:
-      k_ms_init<kSigmaNone><<<1, 32, 0, s>>>(g, b, nlanes, b.cap, ~0ull, dist, dist_ld);
+      k_ms_init<kSigmaNone, 1><<<1, 32, 0, s>>>(g, b, nlanes, a, b.cap, ~0ull, dist, dist_ld);
       break;
   }
   return 1;
@@ -1587,80 +1775,149 @@ int ms_premark(const LaunchCfg& c, cudaStream_t s, const MsBuffers& b, const int
   return 1;
 }
 
-int ms_topdown(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
-               const HubData& hd, uint64_t act, int sigma_kind, int32_t* dist, int64_t dist_ld) {
+namespace {
+
+template <int W>
+int topdown_w(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
+              const HubData& hd, const Lanes<W>& act, int sigma_kind, int32_t* dist,
+              int64_t dist_ld) {
   int launches = 0;
-  k_ms_td_discover<<<c.grid, c.block, 0, s>>>(g, b, hd);
+  k_ms_td_discover<W><<<c.grid, c.block, 0, s>>>(g, b, hd);
   ++launches;
   if (hd.n_out > 0) {
-    k_ms_hub_discover<<<c.grid, c.block, 0, s>>>(g, b, hd);
+    k_ms_hub_discover<W><<<c.grid, c.block, 0, s>>>(g, b, hd);
     ++launches;
   }
   if (sigma_kind == kSigmaNone) {
-    if (dist)
-      k_ms_td_settle<kSigmaNone, true><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
-    else
-      k_ms_td_settle<kSigmaNone, false><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
+    if constexpr (W == 1) {
+      if (dist)
+        k_ms_td_settle<kSigmaNone, true, 1><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
+      else
+        k_ms_td_settle<kSigmaNone, false, 1><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
+    } else {
+      k_ms_td_settle<kSigmaNone, false, W><<<c.grid, c.block, 0, s>>>(g, b, hd, act, nullptr, 0);
+    }
   } else if (sigma_kind == kSigmaU64) {
     if (hd.segmented)
-      k_ms_td_settle_seg<kSigmaU64><<<c.grid, c.block, 0, s>>>(g, b, hd, act);
+      k_ms_td_settle_seg<kSigmaU64, W><<<c.grid, c.block, 0, s>>>(g, b, hd, act);
     else
-      k_ms_td_settle<kSigmaU64, false><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
+      k_ms_td_settle<kSigmaU64, false, W><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
     if (hd.n_in > 0) {
-      k_ms_hub_pull<kSigmaU64, false, false><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
+      k_ms_hub_pull<kSigmaU64, false, false, W><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist,
+                                                                          dist_ld);
       ++launches;
     }
   } else {
     if (hd.segmented)
-      k_ms_td_settle_seg<kSigmaF64><<<c.grid, c.block, 0, s>>>(g, b, hd, act);
+      k_ms_td_settle_seg<kSigmaF64, W><<<c.grid, c.block, 0, s>>>(g, b, hd, act);
     else
-      k_ms_td_settle<kSigmaF64, false><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
+      k_ms_td_settle<kSigmaF64, false, W><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
     if (hd.n_in > 0) {
-      k_ms_hub_pull<kSigmaF64, false, false><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
+      k_ms_hub_pull<kSigmaF64, false, false, W><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist,
+                                                                          dist_ld);
       ++launches;
     }
   }
   ++launches;
-  k_ms_clear_front<<<c.grid, c.block, 0, s>>>(b);
+  k_ms_clear_front<W><<<c.grid, c.block, 0, s>>>(b);
   return launches + 1;
 }
 
-int ms_bottomup(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
-                const HubData& hd, uint64_t act, int sigma_kind, int32_t* dist, int64_t dist_ld) {
+template <int W>
+int bottomup_w(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
+               const HubData& hd, const Lanes<W>& act, int sigma_kind, int32_t* dist,
+               int64_t dist_ld) {
   int launches = 1;
   if (sigma_kind == kSigmaNone) {
-    if (dist)
-      k_ms_bu<kSigmaNone, true><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
-    else
-      k_ms_bu<kSigmaNone, false><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
-    if (hd.n_in > 0) {
+    if constexpr (W == 1) {
       if (dist)
-        k_ms_hub_pull<kSigmaNone, true, true><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
+        k_ms_bu<kSigmaNone, true, 1><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
       else
-        k_ms_hub_pull<kSigmaNone, false, true><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
-      ++launches;
+        k_ms_bu<kSigmaNone, false, 1><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
+      if (hd.n_in > 0) {
+        if (dist)
+          k_ms_hub_pull<kSigmaNone, true, true, 1><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist,
+                                                                             dist_ld);
+        else
+          k_ms_hub_pull<kSigmaNone, false, true, 1><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist,
+                                                                              dist_ld);
+        ++launches;
+      }
+    } else {
+      k_ms_bu<kSigmaNone, false, W><<<c.grid, c.block, 0, s>>>(g, b, hd, act, nullptr, 0);
+      if (hd.n_in > 0) {
+        k_ms_hub_pull<kSigmaNone, false, true, W><<<c.grid, c.block, 0, s>>>(g, b, hd, act, nullptr, 0);
+        ++launches;
+      }
     }
   } else if (sigma_kind == kSigmaU64) {
     if (hd.segmented)
-      k_ms_bu_seg<kSigmaU64><<<c.grid, c.block, 0, s>>>(g, b, hd, act);
+      k_ms_bu_seg<kSigmaU64, W><<<c.grid, c.block, 0, s>>>(g, b, hd, act);
     else
-      k_ms_bu<kSigmaU64, false><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
+      k_ms_bu<kSigmaU64, false, W><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
     if (hd.n_in > 0) {
-      k_ms_hub_pull<kSigmaU64, false, true><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
+      k_ms_hub_pull<kSigmaU64, false, true, W><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist,
+                                                                         dist_ld);
       ++launches;
     }
   } else {
     if (hd.segmented)
-      k_ms_bu_seg<kSigmaF64><<<c.grid, c.block, 0, s>>>(g, b, hd, act);
+      k_ms_bu_seg<kSigmaF64, W><<<c.grid, c.block, 0, s>>>(g, b, hd, act);
     else
-      k_ms_bu<kSigmaF64, false><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
+      k_ms_bu<kSigmaF64, false, W><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
     if (hd.n_in > 0) {
-      k_ms_hub_pull<kSigmaF64, false, true><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
+      k_ms_hub_pull<kSigmaF64, false, true, W><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist,
+                                                                         dist_ld);
       ++launches;
     }
   }
-  k_ms_clear_front<<<c.grid, c.block, 0, s>>>(b);
+  k_ms_clear_front<W><<<c.grid, c.block, 0, s>>>(b);
   return launches + 1;
+}
+
+template <int W>
+int backward_body_w(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
+                    const HubData& hd, int sigma_kind, double* bc) {
+  int launches = 2;
+  k_ms_back_clear<W><<<c.grid, c.block, 0, s>>>(b);
+  // the segmented variant has no weighted finalisation
+  const bool seg = hd.segmented && !b.lane_w;
+  if (sigma_kind == kSigmaF64) {
+    if (seg)
+      k_ms_delta_seg<kSigmaF64, W><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
+    else
+      k_ms_delta<kSigmaF64, W><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
+    if (hd.n_out > 0) {
+      k_ms_hub_delta<kSigmaF64, W><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
+      ++launches;
+    }
+  } else {
+    if (seg)
+      k_ms_delta_seg<kSigmaU64, W><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
+    else
+      k_ms_delta<kSigmaU64, W><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
+    if (hd.n_out > 0) {
+      k_ms_hub_delta<kSigmaU64, W><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
+      ++launches;
+    }
+  }
+  return launches;
+}
+
+}  // namespace
+
+int ms_topdown(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
+               const HubData& hd, const LaneSet& act, int sigma_kind, int32_t* dist,
+               int64_t dist_ld) {
+  if (b.words == 2) return topdown_w<2>(c, s, g, b, hd, lane_cast<2>(act), sigma_kind, dist, dist_ld);
+  return topdown_w<1>(c, s, g, b, hd, lane_cast<1>(act), sigma_kind, dist, dist_ld);
+}
+
+int ms_bottomup(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
+                const HubData& hd, const LaneSet& act, int sigma_kind, int32_t* dist,
+                int64_t dist_ld) {
+  if (b.words == 2) return bottomup_w<2>(c, s, g, b, hd, lane_cast<2>(act), sigma_kind, dist, dist_ld);
+  return bottomup_w<1>(c, s, g, b, hd, lane_cast<1>(act), sigma_kind, dist, dist_ld);
 }
 
 int ms_advance(cudaStream_t s, const DevGraph& g, const MsBuffers& b) {
@@ -1682,30 +1939,8 @@ int ms_backward_level(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, con
 
 int ms_backward_body(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
                      const HubData& hd, int sigma_kind, double* bc) {
-  int launches = 2;
-  k_ms_back_clear<<<c.grid, c.block, 0, s>>>(b);
-  // the segmented variant has no weighted finalisation
-  const bool seg = hd.segmented && !b.lane_w;
-  if (sigma_kind == kSigmaF64) {
-    if (seg)
-      k_ms_delta_seg<kSigmaF64><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
-    else
-      k_ms_delta<kSigmaF64><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
-    if (hd.n_out > 0) {
-      k_ms_hub_delta<kSigmaF64><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
-      ++launches;
-    }
-  } else {
-    if (seg)
-      k_ms_delta_seg<kSigmaU64><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
-    else
-      k_ms_delta<kSigmaU64><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
-    if (hd.n_out > 0) {
-      k_ms_hub_delta<kSigmaU64><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
-      ++launches;
-    }
-  }
-  return launches;
+  if (b.words == 2) return backward_body_w<2>(c, s, g, b, hd, sigma_kind, bc);
+  return backward_body_w<1>(c, s, g, b, hd, sigma_kind, bc);
 }
 
 int loop_arm(cudaStream_t s, const MsBuffers& b, const LoopParams& lp) {
@@ -1731,7 +1966,7 @@ int loop_back_advance(cudaStream_t s, const MsBuffers& b, const LoopParams& lp) 
 int st_backward_level(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
                       const HubData& hd, unsigned long long* stress) {
   int launches = 4;
-  k_ms_back_clear<<<c.grid, c.block, 0, s>>>(b);
+  k_ms_back_clear<1><<<c.grid, c.block, 0, s>>>(b);
   k_st_delta<<<c.grid, c.block, 0, s>>>(g, b, hd);
   if (hd.n_out > 0) {
     k_st_hub_delta<<<c.grid, c.block, 0, s>>>(g, b, hd);
@@ -1747,7 +1982,10 @@ int st_backward_level(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, con
 }
 
 int ms_cleanup(const LaunchCfg& c, cudaStream_t s, const MsBuffers& b) {
-  k_ms_cleanup<<<c.grid, c.block, 0, s>>>(b);
+  if (b.words == 2)
+    k_ms_cleanup<2><<<c.grid, c.block, 0, s>>>(b);
+  else
+    k_ms_cleanup<1><<<c.grid, c.block, 0, s>>>(b);
   return 1;
 }
 
@@ -1762,10 +2000,11 @@ int ms_cleanup_all(const LaunchCfg& c, cudaStream_t s, const MsBuffers& b) {
 }
 
 int ms_reset_all(cudaStream_t s, const DevGraph& g, const MsBuffers& b) {
-  const size_t bytes = static_cast<size_t>(g.n) * sizeof(uint64_t);
+  const size_t bytes = static_cast<size_t>(g.n) * sizeof(uint64_t) * kMaxWords;
   cudaMemsetAsync(b.visit, 0, bytes, s);
   cudaMemsetAsync(b.mb[0], 0, bytes, s);
   cudaMemsetAsync(b.mb[1], 0, bytes, s);
+  if (b.claim) cudaMemsetAsync(b.claim, 0, static_cast<size_t>(g.n) * sizeof(unsigned), s);
   return 0;
 }
 

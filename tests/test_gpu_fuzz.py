@@ -26,7 +26,7 @@ def _graph(rng):
 
 
 def _tuning(rng):
-    return dict(lanes=int(rng.choice([1, 7, 32, 48, 64])),
+    return dict(lanes=int(rng.choice([1, 7, 32, 48, 64, 65, 128])),
                 hub_degree=int(rng.choice([2, 16, 256, 2**31 - 1])),
                 dense_edges=int(rng.choice([0, 4, 32])),
                 alpha=float(rng.choice([1.0, 14.0, 1e9])),

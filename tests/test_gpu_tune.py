@@ -18,7 +18,7 @@ def test_tune_keeps_results_and_uses_cache(tmp_path, directed):
     cache = tmp_path / "tune.txt"
     chosen = h.tune(cache)
     assert chosen["hub_degree"] in (64, 128, 256, 512, 1024, 4096, 2**31 - 1)
-    assert chosen["lanes"] in (32, 48, 64)
+    assert chosen["lanes"] in (32, 48, 64, 128)
     assert chosen["alpha"] in (2.0, 4.0, 8.0, 14.0, 24.0, 48.0)
     assert chosen["beta"] in (6.0, 12.0, 24.0, 48.0, 96.0)
     after = lgbc.betweenness_centrality(g, src)
@@ -65,7 +65,7 @@ def test_tuning_validation():
     g = gen.rmat(8, 4, seed=2)
     h = g.device_handle()
     for bad in (dict(source_order=2), dict(graph_loop=-1), dict(stack_vertices=-5),
-                dict(lanes=0), dict(lanes=65), dict(alpha=0.0), dict(hub_degree=0)):
+                dict(lanes=0), dict(lanes=129), dict(alpha=0.0), dict(hub_degree=0)):
         with pytest.raises(lgbc.ArgumentError):
             h.set_tuning(**bad)
     h.set_tuning(lanes=7, source_order=0, graph_loop=0, stack_vertices=0)
