@@ -146,12 +146,12 @@ def peak_hbm() -> tuple[float, str]:
         return 6800.0, "fallback"
 
 
-def bc_algorithmic_bytes(n: int, nnz: int, k_act: int) -> int:
-    """Brandes bytes for k_act sources in batches of 64 lanes: per batch the
-    CSR is streamed forward and backward and bc read-modified once
+def bc_algorithmic_bytes(n: int, nnz: int, k_act: int, lanes: int = LANES) -> int:
+    """Brandes bytes for k_act sources in batches of `lanes` sources: per batch
+    the CSR is streamed forward and backward and bc read-modified once
     (8 nnz + 32 n + 16 bytes); per source the lane state (write d 4 B + sigma
     8 B, read d 4 B + sigma 8 B, write delta 8 B) is 32 n bytes."""
-    return math.ceil(k_act / LANES) * (8 * nnz + 32 * n + 16) + 32 * n * k_act
+    return math.ceil(k_act / lanes) * (8 * nnz + 32 * n + 16) + 32 * n * k_act
 
 
 def gd_algorithmic_bytes(n: int, nnz: int, q: int) -> int:
@@ -440,7 +440,7 @@ def run_ours(args, dist: Dist):
     # ---- roofline --------------------------------------------------------------------
     peak, peak_kind = peak_hbm()
     t_step = t_dev / args.steps
-    abytes = bc_algorithmic_bytes(n, nnz, k_act)
+    abytes = bc_algorithmic_bytes(n, nnz, k_act, max(1, min(128, int(tuning["lanes"]))))
     achieved = abytes / t_step / 1e9
     # the committed capture is of the default workload (R-MAT 20, k = 4096) only
     traffic = (traffic_per_step() if args.workload == "c2" and args.scale == 20

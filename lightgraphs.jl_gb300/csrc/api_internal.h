@@ -253,7 +253,7 @@ struct lgbc_graph {
   size_t max_smem = 0;
   unsigned long long sigma_limit = ~0ull;  // (2^64 - 1) / (max in-degree + 1)
   lgbc_stats stats{};
-  lgbc_tuning tune{14.0, 24.0, 256, 64, 32, 0, 1, 1, 1 << 21, 0};
+  lgbc_tuning tune{14.0, 24.0, 256, 128, 32, 0, 1, 1, 1 << 21, 0};
   lgbc_graph* stack = nullptr;        // R copies of this graph (stacked batches)
   int64_t stack_copies = 0;
   std::vector<int32_t> h_active;      // the last call's ordered active sources

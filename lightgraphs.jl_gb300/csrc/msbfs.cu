@@ -837,7 +837,7 @@ __global__ void __launch_bounds__(256, 4) k_ms_td_settle(DevGraph g, MsBuffers b
 // to k_ms_hub_pull.
 // ---------------------------------------------------------------------------
 template <int SK, bool DIST, int W>
-__global__ void __launch_bounds__(256, W == 1 ? 4 : 3) k_ms_bu(DevGraph g, MsBuffers b, HubData hd, Lanes<W> act,
+__global__ void __launch_bounds__(256, 4) k_ms_bu(DevGraph g, MsBuffers b, HubData hd, Lanes<W> act,
                                                int32_t* dist, int64_t ld) {
   using T = typename Sig<SK>::T;
   BatchCtl* c = b.ctl;

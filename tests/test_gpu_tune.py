@@ -47,7 +47,7 @@ def test_source_order_keeps_results(directed):
     rng = np.random.default_rng(3)
     src = rng.choice(np.arange(1, g.nv() + 1), 700, replace=False)
     h = g.device_handle()
-    h.set_tuning(source_order=0)
+    h.set_tuning(source_order=0, lanes=64)
     a = lgbc.betweenness_centrality(g, src, endpoints=True)
     s0 = lgbc.stress_centrality(g, src)
     w = rng.uniform(0.5, 2.0, len(src))
