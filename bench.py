@@ -343,7 +343,7 @@ def run_ours(args, dist: Dist):
         t0 = time.perf_counter()
         dg.tune()
         tune_s = time.perf_counter() - t0
-    tuning = {k: getattr(dg.tuning(), k) for k, _ in _lib.LgbcTuning._fields_ if k != "reserved"}
+    tuning = {k: getattr(dg.tuning(), k) for k, _ in _lib.LgbcTuning._fields_}
     log(f"[rank {dist.rank}] tuning {tuning}" + (f" (autotuned in {tune_s:.2f} s)" if tune_s else ""))
     bc_dev = ctypes.c_void_p()
     _lib.check(lib.lgbc_device_alloc(ctypes.byref(bc_dev), 8 * n))

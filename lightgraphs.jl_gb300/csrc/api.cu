@@ -130,10 +130,18 @@ int ensure_dist(lgbc_graph* g, int64_t count) {
   return LGBC_OK;
 }
 
-// Cut every edge list longer than H into kHubChunk-edge items.
-void make_items(const int64_t* rowptr, int64_t n, int H, const std::vector<int32_t>& slot_of,
-                std::vector<HubItem>& items) {
+// Cut every edge list longer than H into kHubChunk-edge work items.  With
+// block > 0 the items are ordered by the column block (neighbour id / block)
+// of their middle edge instead of by hub: the grid works through the item
+// list roughly in order, so the items in flight at any time gather the rows
+// of a limited range of vertices, which stay in L2 while several hubs read
+// them, and a hub's items are spread out (fewer concurrent atomics on one
+// accumulator row).  Any order gives the same results.
+void make_items(const int64_t* rowptr, const int32_t* colidx, int64_t n, int H, int64_t block,
+                const std::vector<int32_t>& slot_of, std::vector<HubItem>& items) {
   items.clear();
+  std::vector<int64_t> key;
+  const bool ordered = block > 0 && block < n && colidx != nullptr;
   for (int64_t v = 0; v < n; ++v) {
     const int64_t e0 = rowptr[v], e1 = rowptr[v + 1];
     if (e1 - e0 <= H) continue;
@@ -147,8 +155,18 @@ void make_items(const int64_t* rowptr, int64_t n, int H, const std::vector<int32
       it.nitems = nit;
       it.pad = 0;
       items.push_back(it);
+      if (ordered) key.push_back(colidx[lo + (it.hi - lo) / 2] / block);
     }
   }
+  if (!ordered) return;
+  std::vector<int64_t> order(items.size());
+  for (size_t i = 0; i < order.size(); ++i) order[i] = static_cast<int64_t>(i);
+  std::stable_sort(order.begin(), order.end(), [&](int64_t x, int64_t y) {
+    return key[static_cast<size_t>(x)] < key[static_cast<size_t>(y)];
+  });
+  std::vector<HubItem> sorted(items.size());
+  for (size_t i = 0; i < order.size(); ++i) sorted[i] = items[static_cast<size_t>(order[i])];
+  items.swap(sorted);
 }
 
 int upload_items(const std::vector<HubItem>& items, HubItem** out) {
@@ -159,8 +177,11 @@ int upload_items(const std::vector<HubItem>& items, HubItem** out) {
   return LGBC_OK;
 }
 
-// Build the hub work items from host copies of rowptr / in_rowptr.
-int build_hubs(lgbc_graph* g, const int64_t* rowptr, const int64_t* in_rowptr, int H) {
+// Build the hub work items from host copies of rowptr / in_rowptr; colidx /
+// in_colidx are host copies or null (then copied from the device when the
+// items are cut into column blocks).
+int build_hubs(lgbc_graph* g, const int64_t* rowptr, const int32_t* colidx, const int64_t* in_rowptr,
+               const int32_t* in_colidx, int H, int block) {
   g->hubs.release();
   const int64_t n = g->n;
   std::vector<int32_t> slot_of(static_cast<size_t>(n), -1);
@@ -172,13 +193,28 @@ int build_hubs(lgbc_graph* g, const int64_t* rowptr, const int64_t* in_rowptr, i
   }
   g->hubs.nslots = nslots;
   g->hubs.built_for = H;
+  g->hubs.built_block = block;
   if (nslots == 0) return LGBC_OK;
+  std::vector<int32_t> ci, ici;
+  if (block > 0 && block < n && g->nnz > 0) {
+    if (!colidx) {
+      LGBC_CUDA(cudaStreamSynchronize(g->stream));
+      ci.resize(static_cast<size_t>(g->nnz));
+      LGBC_CUDA(cudaMemcpy(ci.data(), g->d_colidx, ci.size() * 4, cudaMemcpyDeviceToHost));
+      colidx = ci.data();
+    }
+    if (g->directed && !in_colidx) {
+      ici.resize(static_cast<size_t>(g->nnz));
+      LGBC_CUDA(cudaMemcpy(ici.data(), g->d_in_colidx, ici.size() * 4, cudaMemcpyDeviceToHost));
+      in_colidx = ici.data();
+    }
+  }
   std::vector<HubItem> items;
-  make_items(rowptr, n, H, slot_of, items);
+  make_items(rowptr, colidx, n, H, block, slot_of, items);
   g->hubs.n_out = static_cast<int64_t>(items.size());
   LGBC_TRY(upload_items(items, &g->hubs.out_items));
   if (g->directed) {
-    make_items(in_rowptr, n, H, slot_of, items);
+    make_items(in_rowptr, in_colidx, n, H, block, slot_of, items);
     g->hubs.n_in = static_cast<int64_t>(items.size());
     LGBC_TRY(upload_items(items, &g->hubs.in_items));
   } else {
@@ -195,9 +231,10 @@ int build_hubs(lgbc_graph* g, const int64_t* rowptr, const int64_t* in_rowptr, i
   return LGBC_OK;
 }
 
-// Rebuild the hub table after hub_degree changed (rowptr copied back).
+// Rebuild the hub table after hub_degree or hub_block changed (rowptr copied back).
 int ensure_hubs(lgbc_graph* g) {
-  if (g->hubs.built_for == g->tune.hub_degree) return LGBC_OK;
+  if (g->hubs.built_for == g->tune.hub_degree && g->hubs.built_block == g->tune.hub_block)
+    return LGBC_OK;
   LGBC_CUDA(cudaStreamSynchronize(g->stream));
   std::vector<int64_t> rp(static_cast<size_t>(g->n + 1)), irp;
   LGBC_CUDA(cudaMemcpy(rp.data(), g->d_rowptr, rp.size() * 8, cudaMemcpyDeviceToHost));
@@ -207,7 +244,7 @@ int ensure_hubs(lgbc_graph* g) {
     LGBC_CUDA(cudaMemcpy(irp.data(), g->d_in_rowptr, irp.size() * 8, cudaMemcpyDeviceToHost));
     in_rp = irp.data();
   }
-  return build_hubs(g, rp.data(), in_rp, g->tune.hub_degree);
+  return build_hubs(g, rp.data(), nullptr, in_rp, nullptr, g->tune.hub_degree, g->tune.hub_block);
 }
 
 HubData hub_data(const lgbc_graph* g) {
@@ -906,7 +943,8 @@ int init_handle(lgbc_graph* g, int64_t n, int directed) {
 
 // Host-side bookkeeping from the row pointers: degree filter, path-count
 // bound, landmarks and the hub table.
-int finish_handle(lgbc_graph* g, const int64_t* rowptr, const int64_t* in_rowptr);
+int finish_handle(lgbc_graph* g, const int64_t* rowptr, const int64_t* in_rowptr,
+                  const int32_t* colidx, const int32_t* in_colidx);
 
 int create_impl(lgbc_graph* g, int64_t n, int64_t nnz, const int64_t* rowptr, const int32_t* colidx,
                 const int64_t* in_rowptr, const int32_t* in_colidx, int directed) {
@@ -947,10 +985,11 @@ int create_impl(lgbc_graph* g, int64_t n, int64_t nnz, const int64_t* rowptr, co
   LGBC_TRY(check_launch(g));
   if (bad & 1) return fail(LGBC_EINVAL, "rowptr must be non-decreasing");
   if (bad & 2) return fail(LGBC_EINVAL, "column index out of range");
-  return finish_handle(g, rowptr, directed ? in_rowptr : rowptr);
+  return finish_handle(g, rowptr, directed ? in_rowptr : rowptr, colidx, directed ? in_colidx : colidx);
 }
 
-int finish_handle(lgbc_graph* g, const int64_t* rowptr, const int64_t* in_rowptr) {
+int finish_handle(lgbc_graph* g, const int64_t* rowptr, const int64_t* in_rowptr,
+                  const int32_t* colidx, const int32_t* in_colidx) {
   const int64_t n = g->n;
   const int directed = g->directed;
   // degree(g, v) > 0: in+out for digraphs (src/core.jl:66-67), kept on the host
@@ -983,7 +1022,8 @@ int finish_handle(lgbc_graph* g, const int64_t* rowptr, const int64_t* in_rowptr
     std::sort(top.begin(), top.end());
     for (const auto& t : top) g->landmarks.push_back(t.second);
   }
-  return build_hubs(g, rowptr, directed ? in_rowptr : rowptr, g->tune.hub_degree);
+  return build_hubs(g, rowptr, colidx, directed ? in_rowptr : rowptr, directed ? in_colidx : colidx,
+                    g->tune.hub_degree, g->tune.hub_block);
 }
 
 }  // namespace lgbc::api
@@ -1255,9 +1295,10 @@ int lgbc_set_tuning(lgbc_graph* g, const lgbc_tuning* t) {
   if (!(t->alpha > 0) || !(t->beta > 0) || t->lanes < 1 || t->lanes > kWideLanes ||
       t->hub_degree < 1 || t->dense_edges < 0 || t->segment_degree < 0 ||
       (t->source_order != 0 && t->source_order != 1) || (t->graph_loop != 0 && t->graph_loop != 1) ||
-      t->stack_vertices < 0)
+      t->stack_vertices < 0 || t->hub_block < 0)
     return fail(LGBC_EINVAL,
-                "tuning out of range (alpha, beta > 0; 1 <= lanes <= 128; hub_degree >= 1; dense_edges >= 0)");
+                "tuning out of range (alpha, beta > 0; 1 <= lanes <= 128; hub_degree >= 1; "
+                "dense_edges, segment_degree, stack_vertices, hub_block >= 0)");
   std::lock_guard<std::mutex> lock(g->mu);
   g->tune = *t;
   return LGBC_OK;

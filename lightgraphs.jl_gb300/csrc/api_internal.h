@@ -110,6 +110,7 @@ struct HubTable {
   unsigned int* cnt = nullptr;
   int64_t nslots = 0;
   int built_for = -1;            // hub_degree the table was built with
+  int built_block = -1;          // and hub_block
   void release() {
     if (in_items && in_items != out_items) cudaFree(in_items);
     dev_free(out_items);
@@ -119,6 +120,7 @@ struct HubTable {
     dev_free(cnt);
     n_out = n_in = nslots = 0;
     built_for = -1;
+    built_block = -1;
   }
 };
 
@@ -253,7 +255,7 @@ struct lgbc_graph {
   size_t max_smem = 0;
   unsigned long long sigma_limit = ~0ull;  // (2^64 - 1) / (max in-degree + 1)
   lgbc_stats stats{};
-  lgbc_tuning tune{14.0, 24.0, 256, 128, 32, 0, 1, 1, 1 << 21, 0};
+  lgbc_tuning tune{14.0, 24.0, 256, 128, 32, 0, 1, 1, 1 << 21, 1};
   lgbc_graph* stack = nullptr;        // R copies of this graph (stacked batches)
   int64_t stack_copies = 0;
   std::vector<int32_t> h_active;      // the last call's ordered active sources
@@ -307,7 +309,10 @@ int prepare_sources(lgbc_graph* g, const int32_t* src, int64_t nsrc, int64_t* k_
 void reset_stats(lgbc_graph* g);
 void finish_stats(lgbc_graph* g);
 int init_handle(lgbc_graph* g, int64_t n, int directed);
-int finish_handle(lgbc_graph* g, const int64_t* rowptr, const int64_t* in_rowptr);
+// Host rowptr copies are required; colidx copies may be null (copied back
+// from the device when the hub items need them).
+int finish_handle(lgbc_graph* g, const int64_t* rowptr, const int64_t* in_rowptr,
+                  const int32_t* colidx = nullptr, const int32_t* in_colidx = nullptr);
 int run_bfs(lgbc_graph* g, const DevGraph& dg, int64_t nsrc);
 int prepare_bfs(lgbc_graph* g, const int32_t* src, int64_t nsrc);
 

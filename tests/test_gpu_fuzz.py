@@ -34,7 +34,8 @@ def _tuning(rng):
                 source_order=int(rng.integers(0, 2)),
                 graph_loop=int(rng.integers(0, 2)),
                 stack_vertices=int(rng.choice([0, 1 << 21])),
-                segment_degree=int(rng.choice([0, 1 << 30])))
+                segment_degree=int(rng.choice([0, 1 << 30])),
+                hub_block=int(rng.choice([0, 50, 32768])))
 
 
 @pytest.mark.parametrize("seed", range(24))
