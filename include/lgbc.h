@@ -175,11 +175,12 @@ int lgbc_graph_stats(const lgbc_graph *g, lgbc_stats *out);
  *                 disjoint union of R copies of the graph, each copy holding
  *                 its own batch of sources, with R * n <= stack_vertices
  *                 (used when R >= 4; 0 = never).  Default 2^21.
- *   hub_block     > 0: hub work items run in the order of the column block
- *                 (neighbour id / hub_block) of their middle edge, so that
- *                 the items in flight gather rows of a limited range of
- *                 vertices (1: ordered by the middle neighbour id itself);
- *                 0: items run hub by hub.  Default 1. */
+ *   hub_order     order of the hub work items: 0 hub by hub; 1 by the
+ *                 neighbour id of each item's middle edge; 2 by the relative
+ *                 position of each item in its hub's row (follows 1 on rows
+ *                 sorted by neighbour id, without reading them on the host).
+ *                 1 and 2 interleave the hubs so that the items in flight
+ *                 gather rows of a limited range of vertices.  Default 2. */
 typedef struct lgbc_tuning {
   double alpha;
   double beta;
@@ -190,7 +191,7 @@ typedef struct lgbc_tuning {
   int32_t source_order;
   int32_t graph_loop;
   int32_t stack_vertices;
-  int32_t hub_block;
+  int32_t hub_order;
 } lgbc_tuning;
 int lgbc_get_tuning(const lgbc_graph *g, lgbc_tuning *out);
 int lgbc_set_tuning(lgbc_graph *g, const lgbc_tuning *t);
@@ -200,11 +201,11 @@ int lgbc_set_tuning(lgbc_graph *g, const lgbc_tuning *t);
  * descent (two passes; a change must win by 2 %), the degree-bin cut
  * (hub_degree), the source-batch width (lanes), the direction-switch
  * thresholds (alpha, beta), the gather cuts (dense_edges, segment_degree) and
- * the hub column block (hub_block); the result stays set on the handle (read
+ * the hub item order (hub_order); the result stays set on the handle (read
  * it with lgbc_get_tuning).  Every setting gives the same results; only the
  * speed differs.  cache_path (may be NULL) is a text file of "signature alpha
  * beta hub_degree lanes dense_edges segment_degree source_order graph_loop
- * stack_vertices hub_block" lines, keyed by n, nnz, directedness and the device's SM
+ * stack_vertices hub_order" lines, keyed by n, nnz, directedness and the device's SM
  * count: a matching line is applied without measuring, and a new result is
  * appended. */
 int lgbc_tune(lgbc_graph *g, const char *cache_path);

@@ -130,18 +130,22 @@ int ensure_dist(lgbc_graph* g, int64_t count) {
   return LGBC_OK;
 }
 
-// Cut every edge list longer than H into kHubChunk-edge work items.  With
-// block > 0 the items are ordered by the column block (neighbour id / block)
-// of their middle edge instead of by hub: the grid works through the item
-// list roughly in order, so the items in flight at any time gather the rows
-// of a limited range of vertices, which stay in L2 while several hubs read
-// them, and a hub's items are spread out (fewer concurrent atomics on one
-// accumulator row).  Any order gives the same results.
-void make_items(const int64_t* rowptr, const int32_t* colidx, int64_t n, int H, int64_t block,
+// Cut every edge list longer than H into kHubChunk-edge work items, in the
+// order `order` selects: 0 hub by hub; 1 by the neighbour id of each item's
+// middle edge (colidx must be given); 2 by the relative position of each
+// item's middle in its hub's row (on rows sorted by neighbour id this follows
+// order 1 without reading colidx).  Orders 1 and 2 interleave the hubs: the
+// grid works through the item list roughly in order, so the items in flight
+// at one time gather rows of a limited range of vertices (reused from L2 by
+// the hubs that share them) and a hub's items are spread out (fewer
+// simultaneous atomics on one accumulator row).  Any order gives the same
+// results.
+void make_items(const int64_t* rowptr, const int32_t* colidx, int64_t n, int H, int order,
                 const std::vector<int32_t>& slot_of, std::vector<HubItem>& items) {
+  constexpr int64_t kBuckets = int64_t(1) << 16;
   items.clear();
   std::vector<int64_t> key;
-  const bool ordered = block > 0 && block < n && colidx != nullptr;
+  const bool ordered = order == 2 || (order == 1 && colidx != nullptr && n > 0);
   for (int64_t v = 0; v < n; ++v) {
     const int64_t e0 = rowptr[v], e1 = rowptr[v + 1];
     if (e1 - e0 <= H) continue;
@@ -155,17 +159,19 @@ void make_items(const int64_t* rowptr, const int32_t* colidx, int64_t n, int H, 
       it.nitems = nit;
       it.pad = 0;
       items.push_back(it);
-      if (ordered) key.push_back(colidx[lo + (it.hi - lo) / 2] / block);
+      if (!ordered) continue;
+      const int64_t mid2 = (lo - e0) + it.hi - e0;  // twice the middle's offset in the row
+      key.push_back(order == 1 ? static_cast<int64_t>(colidx[lo + (it.hi - lo) / 2]) * kBuckets / n
+                               : mid2 * kBuckets / (2 * (e1 - e0)));
     }
   }
   if (!ordered) return;
-  std::vector<int64_t> order(items.size());
-  for (size_t i = 0; i < order.size(); ++i) order[i] = static_cast<int64_t>(i);
-  std::stable_sort(order.begin(), order.end(), [&](int64_t x, int64_t y) {
-    return key[static_cast<size_t>(x)] < key[static_cast<size_t>(y)];
-  });
+  // stable counting sort on the bucket
+  std::vector<int64_t> start(static_cast<size_t>(kBuckets + 1), 0);
+  for (int64_t k : key) start[static_cast<size_t>(k + 1)]++;
+  for (int64_t b = 0; b < kBuckets; ++b) start[static_cast<size_t>(b + 1)] += start[static_cast<size_t>(b)];
   std::vector<HubItem> sorted(items.size());
-  for (size_t i = 0; i < order.size(); ++i) sorted[i] = items[static_cast<size_t>(order[i])];
+  for (size_t i = 0; i < items.size(); ++i) sorted[static_cast<size_t>(start[static_cast<size_t>(key[i])]++)] = items[i];
   items.swap(sorted);
 }
 
@@ -178,10 +184,10 @@ int upload_items(const std::vector<HubItem>& items, HubItem** out) {
 }
 
 // Build the hub work items from host copies of rowptr / in_rowptr; colidx /
-// in_colidx are host copies or null (then copied from the device when the
-// items are cut into column blocks).
+// in_colidx are host copies or null (then copied from the device when item
+// order 1 needs them).
 int build_hubs(lgbc_graph* g, const int64_t* rowptr, const int32_t* colidx, const int64_t* in_rowptr,
-               const int32_t* in_colidx, int H, int block) {
+               const int32_t* in_colidx, int H, int order) {
   g->hubs.release();
   const int64_t n = g->n;
   std::vector<int32_t> slot_of(static_cast<size_t>(n), -1);
@@ -193,10 +199,10 @@ int build_hubs(lgbc_graph* g, const int64_t* rowptr, const int32_t* colidx, cons
   }
   g->hubs.nslots = nslots;
   g->hubs.built_for = H;
-  g->hubs.built_block = block;
+  g->hubs.built_order = order;
   if (nslots == 0) return LGBC_OK;
   std::vector<int32_t> ci, ici;
-  if (block > 0 && block < n && g->nnz > 0) {
+  if (order == 1 && g->nnz > 0) {
     if (!colidx) {
       LGBC_CUDA(cudaStreamSynchronize(g->stream));
       ci.resize(static_cast<size_t>(g->nnz));
@@ -210,11 +216,11 @@ int build_hubs(lgbc_graph* g, const int64_t* rowptr, const int32_t* colidx, cons
     }
   }
   std::vector<HubItem> items;
-  make_items(rowptr, colidx, n, H, block, slot_of, items);
+  make_items(rowptr, colidx, n, H, order, slot_of, items);
   g->hubs.n_out = static_cast<int64_t>(items.size());
   LGBC_TRY(upload_items(items, &g->hubs.out_items));
   if (g->directed) {
-    make_items(in_rowptr, in_colidx, n, H, block, slot_of, items);
+    make_items(in_rowptr, in_colidx, n, H, order, slot_of, items);
     g->hubs.n_in = static_cast<int64_t>(items.size());
     LGBC_TRY(upload_items(items, &g->hubs.in_items));
   } else {
@@ -231,9 +237,9 @@ int build_hubs(lgbc_graph* g, const int64_t* rowptr, const int32_t* colidx, cons
   return LGBC_OK;
 }
 
-// Rebuild the hub table after hub_degree or hub_block changed (rowptr copied back).
+// Rebuild the hub table after hub_degree or hub_order changed (rowptr copied back).
 int ensure_hubs(lgbc_graph* g) {
-  if (g->hubs.built_for == g->tune.hub_degree && g->hubs.built_block == g->tune.hub_block)
+  if (g->hubs.built_for == g->tune.hub_degree && g->hubs.built_order == g->tune.hub_order)
     return LGBC_OK;
   LGBC_CUDA(cudaStreamSynchronize(g->stream));
   std::vector<int64_t> rp(static_cast<size_t>(g->n + 1)), irp;
@@ -244,7 +250,7 @@ int ensure_hubs(lgbc_graph* g) {
     LGBC_CUDA(cudaMemcpy(irp.data(), g->d_in_rowptr, irp.size() * 8, cudaMemcpyDeviceToHost));
     in_rp = irp.data();
   }
-  return build_hubs(g, rp.data(), nullptr, in_rp, nullptr, g->tune.hub_degree, g->tune.hub_block);
+  return build_hubs(g, rp.data(), nullptr, in_rp, nullptr, g->tune.hub_degree, g->tune.hub_order);
 }
 
 HubData hub_data(const lgbc_graph* g) {
@@ -745,44 +751,62 @@ int order_active(lgbc_graph* g, std::vector<int32_t>& act, std::vector<double>* 
 // (one lane each, as in lgbc_betweenness_many), lanes without a source in a
 // copy are premarked there, and the copies' raw vectors are summed at the end.
 // Each union batch does the work of `copies` batches with the launches of one.
+// A handle for the disjoint union of `copies` copies of g, built on the
+// device from g's CSR (valid by construction, so not validated again).
+int create_replicated(lgbc_graph* g, int64_t copies, lgbc_graph** out) {
+  *out = nullptr;
+  lgbc_graph* st = new (std::nothrow) lgbc_graph();
+  if (!st) return fail(LGBC_ENOMEM, "host allocation failed");
+  auto build = [&]() -> int {
+    const int64_t n = g->n, nnz = g->nnz, N = copies * n, NNZ = copies * nnz;
+    LGBC_TRY(init_handle(st, N, g->directed));
+    st->nnz = NNZ;
+    LGBC_CUDA(cudaStreamSynchronize(g->stream));  // g's CSR is complete
+    LGBC_TRY(dev_alloc(&st->d_rowptr, static_cast<size_t>(N + 1)));
+    LGBC_TRY(dev_alloc(&st->d_colidx, static_cast<size_t>(std::max<int64_t>(NNZ, 1))));
+    st->launches += replicate_csr(st->cfg, st->stream, g->d_rowptr, g->d_colidx, n, nnz, copies,
+                                  st->d_rowptr, st->d_colidx);
+    std::vector<int64_t> rp(static_cast<size_t>(N + 1)), irp;
+    if (g->directed) {
+      LGBC_TRY(dev_alloc(&st->d_in_rowptr, static_cast<size_t>(N + 1)));
+      LGBC_TRY(dev_alloc(&st->d_in_colidx, static_cast<size_t>(std::max<int64_t>(NNZ, 1))));
+      st->launches += replicate_csr(st->cfg, st->stream, g->d_in_rowptr, g->d_in_colidx, n, nnz,
+                                    copies, st->d_in_rowptr, st->d_in_colidx);
+      irp.resize(rp.size());
+      LGBC_CUDA(cudaMemcpyAsync(irp.data(), st->d_in_rowptr, irp.size() * 8, cudaMemcpyDeviceToHost,
+                                st->stream));
+    } else {
+      st->d_in_rowptr = st->d_rowptr;
+      st->d_in_colidx = st->d_colidx;
+    }
+    LGBC_CUDA(cudaMemcpyAsync(rp.data(), st->d_rowptr, rp.size() * 8, cudaMemcpyDeviceToHost,
+                              st->stream));
+    LGBC_CUDA(cudaStreamSynchronize(st->stream));
+    LGBC_TRY(check_launch(st));
+    return finish_handle(st, rp.data(), g->directed ? irp.data() : rp.data());
+  };
+  const int rc = build();
+  if (rc != LGBC_OK) {
+    const std::string msg = g_last_error;
+    lgbc_graph_destroy(st);
+    g_last_error = msg;
+    return rc;
+  }
+  *out = st;
+  return LGBC_OK;
+}
+
 int run_stacked(lgbc_graph* g, int64_t copies, double* bc_dev, const std::vector<double>* w) {
-  const int64_t n = g->n, nnz = g->nnz;
+  const int64_t n = g->n;
   const int L = std::max(1, std::min<int>(kMaxLanes, g->tune.lanes));
   if (!g->stack || g->stack_copies != copies) {
     if (g->stack) lgbc_graph_destroy(g->stack);
     g->stack = nullptr;
     g->stack_copies = 0;
-    // replicate the CSR(s) on the host: copy r holds vertices [r n, (r + 1) n)
-    std::vector<int64_t> rp(static_cast<size_t>(n + 1)), irp;
-    std::vector<int32_t> ci(static_cast<size_t>(nnz)), ici;
-    LGBC_CUDA(cudaMemcpy(rp.data(), g->d_rowptr, rp.size() * 8, cudaMemcpyDeviceToHost));
-    if (nnz) LGBC_CUDA(cudaMemcpy(ci.data(), g->d_colidx, ci.size() * 4, cudaMemcpyDeviceToHost));
-    if (g->directed) {
-      irp.resize(rp.size());
-      ici.resize(ci.size());
-      LGBC_CUDA(cudaMemcpy(irp.data(), g->d_in_rowptr, irp.size() * 8, cudaMemcpyDeviceToHost));
-      if (nnz)
-        LGBC_CUDA(cudaMemcpy(ici.data(), g->d_in_colidx, ici.size() * 4, cudaMemcpyDeviceToHost));
-    }
-    auto replicate = [&](const std::vector<int64_t>& r0, const std::vector<int32_t>& c0,
-                         std::vector<int64_t>& r1, std::vector<int32_t>& c1) {
-      r1.resize(static_cast<size_t>(copies * n + 1));
-      c1.resize(static_cast<size_t>(copies * nnz));
-      for (int64_t r = 0; r < copies; ++r) {
-        for (int64_t v = 0; v < n; ++v) r1[static_cast<size_t>(r * n + v)] = r * nnz + r0[static_cast<size_t>(v)];
-        for (int64_t e = 0; e < nnz; ++e)
-          c1[static_cast<size_t>(r * nnz + e)] = static_cast<int32_t>(r * n + c0[static_cast<size_t>(e)]);
-      }
-      r1[static_cast<size_t>(copies * n)] = copies * nnz;
-    };
-    std::vector<int64_t> srp, sirp;
-    std::vector<int32_t> sci, sici;
-    replicate(rp, ci, srp, sci);
-    if (g->directed) replicate(irp, ici, sirp, sici);
+    // the union's CSR(s) are replicated on the device: copy r holds vertices [r n, (r + 1) n)
+    if (copies * n >= INT32_MAX) return fail(LGBC_EINVAL, "stacked union exceeds int32 vertex ids");
     lgbc_graph* st = nullptr;
-    LGBC_TRY(lgbc_graph_create(&st, copies * n, copies * nnz, srp.data(), sci.data(),
-                               g->directed ? sirp.data() : nullptr,
-                               g->directed ? sici.data() : nullptr, g->directed));
+    LGBC_TRY(create_replicated(g, copies, &st));
     g->stack = st;
     g->stack_copies = copies;
   }
@@ -992,38 +1016,33 @@ int finish_handle(lgbc_graph* g, const int64_t* rowptr, const int64_t* in_rowptr
                   const int32_t* colidx, const int32_t* in_colidx) {
   const int64_t n = g->n;
   const int directed = g->directed;
-  // degree(g, v) > 0: in+out for digraphs (src/core.jl:66-67), kept on the host
+  // degree(g, v) > 0: in+out for digraphs (src/core.jl:66-67), kept on the
+  // host; and, in the same pass, the kLandmarks highest-degree vertices (ties:
+  // smaller id) for source ordering
   g->has_degree.assign(static_cast<size_t>(n), 0);
   int64_t max_in = 0;
+  std::vector<std::pair<int64_t, int32_t>> top;  // max-heap of (-degree, id)
   for (int64_t v = 0; v < n; ++v) {
     const int64_t dout = rowptr[v + 1] - rowptr[v];
     const int64_t din = directed ? in_rowptr[v + 1] - in_rowptr[v] : dout;
     const int64_t d = directed ? dout + din : dout;
     g->has_degree[static_cast<size_t>(v)] = d > 0 ? 1 : 0;
     max_in = std::max(max_in, din);
+    if (d == 0) continue;
+    if (top.size() < static_cast<size_t>(kLandmarks)) {
+      top.emplace_back(-d, static_cast<int32_t>(v));
+      std::push_heap(top.begin(), top.end());
+    } else if (-d < top.front().first) {  // a larger degree (equal: the smaller id stays)
+      std::pop_heap(top.begin(), top.end());
+      top.back() = std::make_pair(-d, static_cast<int32_t>(v));
+      std::push_heap(top.begin(), top.end());
+    }
   }
   g->sigma_limit = ~0ull / static_cast<unsigned long long>(max_in + 1);
-  {
-    // the kLandmarks highest-degree vertices (ties: smaller id), for source ordering
-    std::vector<std::pair<int64_t, int32_t>> top;
-    for (int64_t v = 0; v < n; ++v) {
-      const int64_t d = (rowptr[v + 1] - rowptr[v]) + (directed ? in_rowptr[v + 1] - in_rowptr[v] : 0);
-      if (d == 0) continue;
-      const std::pair<int64_t, int32_t> item(-d, static_cast<int32_t>(v));
-      if (top.size() < static_cast<size_t>(kLandmarks)) {
-        top.push_back(item);
-        std::push_heap(top.begin(), top.end());
-      } else if (item < top.front()) {
-        std::pop_heap(top.begin(), top.end());
-        top.back() = item;
-        std::push_heap(top.begin(), top.end());
-      }
-    }
-    std::sort(top.begin(), top.end());
-    for (const auto& t : top) g->landmarks.push_back(t.second);
-  }
+  std::sort(top.begin(), top.end());
+  for (const auto& t : top) g->landmarks.push_back(t.second);
   return build_hubs(g, rowptr, colidx, directed ? in_rowptr : rowptr, directed ? in_colidx : colidx,
-                    g->tune.hub_degree, g->tune.hub_block);
+                    g->tune.hub_degree, g->tune.hub_order);
 }
 
 }  // namespace lgbc::api
@@ -1295,10 +1314,10 @@ int lgbc_set_tuning(lgbc_graph* g, const lgbc_tuning* t) {
   if (!(t->alpha > 0) || !(t->beta > 0) || t->lanes < 1 || t->lanes > kWideLanes ||
       t->hub_degree < 1 || t->dense_edges < 0 || t->segment_degree < 0 ||
       (t->source_order != 0 && t->source_order != 1) || (t->graph_loop != 0 && t->graph_loop != 1) ||
-      t->stack_vertices < 0 || t->hub_block < 0)
+      t->stack_vertices < 0 || t->hub_order < 0 || t->hub_order > 2)
     return fail(LGBC_EINVAL,
                 "tuning out of range (alpha, beta > 0; 1 <= lanes <= 128; hub_degree >= 1; "
-                "dense_edges, segment_degree, stack_vertices, hub_block >= 0)");
+                "dense_edges, segment_degree, stack_vertices >= 0; hub_order 0..2)");
   std::lock_guard<std::mutex> lock(g->mu);
   g->tune = *t;
   return LGBC_OK;

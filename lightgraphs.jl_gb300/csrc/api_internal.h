@@ -110,7 +110,7 @@ struct HubTable {
   unsigned int* cnt = nullptr;
   int64_t nslots = 0;
   int built_for = -1;            // hub_degree the table was built with
-  int built_block = -1;          // and hub_block
+  int built_order = -1;          // and hub_order
   void release() {
     if (in_items && in_items != out_items) cudaFree(in_items);
     dev_free(out_items);
@@ -120,7 +120,7 @@ struct HubTable {
     dev_free(cnt);
     n_out = n_in = nslots = 0;
     built_for = -1;
-    built_block = -1;
+    built_order = -1;
   }
 };
 
@@ -255,7 +255,7 @@ struct lgbc_graph {
   size_t max_smem = 0;
   unsigned long long sigma_limit = ~0ull;  // (2^64 - 1) / (max in-degree + 1)
   lgbc_stats stats{};
-  lgbc_tuning tune{14.0, 24.0, 256, 128, 32, 0, 1, 1, 1 << 21, 1};
+  lgbc_tuning tune{14.0, 24.0, 256, 128, 32, 0, 1, 1, 1 << 21, 2};
   lgbc_graph* stack = nullptr;        // R copies of this graph (stacked batches)
   int64_t stack_copies = 0;
   std::vector<int32_t> h_active;      // the last call's ordered active sources

@@ -31,11 +31,11 @@ bool tune_from_cache(const char* path, const std::string& sig, lgbc_tuning* out)
     lgbc_tuning t{};
     if (std::sscanf(line, "%255s %lf %lf %d %d %d %d %d %d %d %d", key, &t.alpha, &t.beta,
                     &t.hub_degree, &t.lanes, &t.dense_edges, &t.segment_degree, &t.source_order,
-                    &t.graph_loop, &t.stack_vertices, &t.hub_block) == 11 &&
+                    &t.graph_loop, &t.stack_vertices, &t.hub_order) == 11 &&
         sig == key && t.alpha > 0 && t.beta > 0 && t.lanes >= 1 && t.lanes <= kWideLanes &&
         t.hub_degree >= 1 && t.dense_edges >= 0 && t.segment_degree >= 0 &&
         (t.source_order == 0 || t.source_order == 1) && (t.graph_loop == 0 || t.graph_loop == 1) &&
-        t.stack_vertices >= 0 && t.hub_block >= 0) {
+        t.stack_vertices >= 0 && t.hub_order >= 0 && t.hub_order <= 2) {
       *out = t;  // the last matching line wins
       found = true;
     }
@@ -121,14 +121,14 @@ extern "C" int lgbc_tune(lgbc_graph* g, const char* cache_path) {
     const double betas[] = {6.0, 12.0, 24.0, 48.0, 96.0};
     const int dense[] = {4, 8, 16, 32};
     const int segs[] = {0, 1 << 30};
-    const int blocks[] = {0, 1, 4096};
+    const int orders[] = {0, 1, 2};
     LGBC_TRY(try_field([](lgbc_tuning& c, int v) { c.hub_degree = v; }, hubs));
     LGBC_TRY(try_field([](lgbc_tuning& c, int v) { c.lanes = v; }, lanes));
     LGBC_TRY(try_field([](lgbc_tuning& c, double v) { c.alpha = v; }, alphas));
     LGBC_TRY(try_field([](lgbc_tuning& c, double v) { c.beta = v; }, betas));
     LGBC_TRY(try_field([](lgbc_tuning& c, int v) { c.dense_edges = v; }, dense));
     LGBC_TRY(try_field([](lgbc_tuning& c, int v) { c.segment_degree = v; }, segs));
-    LGBC_TRY(try_field([](lgbc_tuning& c, int v) { c.hub_block = v; }, blocks));
+    LGBC_TRY(try_field([](lgbc_tuning& c, int v) { c.hub_order = v; }, orders));
   }
   g->tune = best;
   LGBC_TRY(ensure_hubs(g));
@@ -137,7 +137,7 @@ extern "C" int lgbc_tune(lgbc_graph* g, const char* cache_path) {
     if (!f) return fail(LGBC_EINVAL, std::string("cannot append to tuning cache ") + cache_path);
     std::fprintf(f, "%s %.17g %.17g %d %d %d %d %d %d %d %d\n", sig.c_str(), best.alpha, best.beta,
                  best.hub_degree, best.lanes, best.dense_edges, best.segment_degree,
-                 best.source_order, best.graph_loop, best.stack_vertices, best.hub_block);
+                 best.source_order, best.graph_loop, best.stack_vertices, best.hub_order);
     std::fclose(f);
   }
   finish_stats(g);

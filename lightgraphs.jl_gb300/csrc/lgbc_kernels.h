@@ -192,6 +192,10 @@ void set_last_error(const char* msg);
 int validate_csr(const LaunchCfg& c, cudaStream_t s, const int64_t* rowptr, const int32_t* colidx,
                  int64_t n, int64_t nnz, int* bad);
 int fill_i32(const LaunchCfg& c, cudaStream_t s, int32_t* p, int64_t count, int32_t value);
+// The CSR of a disjoint union of `copies` copies of an n-vertex graph (copy
+// r = vertices [r n, (r + 1) n)): rp1[copies n + 1], c1[copies nnz]; n > 0.
+int replicate_csr(const LaunchCfg& c, cudaStream_t s, const int64_t* rp0, const int32_t* c0,
+                  int64_t n, int64_t nnz, int64_t copies, int64_t* rp1, int32_t* c1);
 // out[v] = sum over r < copies of stacked[r * n + v] (a fixed order).
 int sum_copies(const LaunchCfg& c, cudaStream_t s, const double* stacked, int64_t n, int64_t copies,
                double* out);

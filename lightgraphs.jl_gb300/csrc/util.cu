@@ -110,7 +110,38 @@ __global__ void k_sum_copies(const double* stacked, int64_t n, int64_t copies, d
     out[v] = acc;
   }
 }
+// Disjoint union of `copies` copies of a CSR: copy r holds vertices
+// [r n, (r + 1) n) and entries [r nnz, (r + 1) nnz).  rp1 has copies n + 1
+// entries (index copies n reads rp0[0] = 0, giving copies nnz).
+__global__ void k_replicate_rows(const int64_t* rp0, int64_t n, int64_t nnz, int64_t copies,
+                                 int64_t* rp1) {
+  const int64_t total = copies * n + 1;
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < total;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int64_t r = i / n;
+    rp1[i] = r * nnz + rp0[i - r * n];
+  }
+}
+
+__global__ void k_replicate_cols(const int32_t* c0, int64_t nnz, int64_t n, int64_t copies,
+                                 int32_t* c1) {
+  const int64_t total = copies * nnz;
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < total;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int64_t r = i / nnz;
+    c1[i] = static_cast<int32_t>(r * n + c0[i - r * nnz]);
+  }
+}
 }  // namespace
+
+int replicate_csr(const LaunchCfg& c, cudaStream_t s, const int64_t* rp0, const int32_t* c0,
+                  int64_t n, int64_t nnz, int64_t copies, int64_t* rp1, int32_t* c1) {
+  if (n <= 0 || copies <= 0) return 0;
+  k_replicate_rows<<<c.grid, c.block, 0, s>>>(rp0, n, nnz, copies, rp1);
+  if (nnz <= 0) return 1;
+  k_replicate_cols<<<c.grid, c.block, 0, s>>>(c0, nnz, n, copies, c1);
+  return 2;
+}
 
 int sum_copies(const LaunchCfg& c, cudaStream_t s, const double* stacked, int64_t n, int64_t copies,
                double* out) {

@@ -35,7 +35,7 @@ def _tuning(rng):
                 graph_loop=int(rng.integers(0, 2)),
                 stack_vertices=int(rng.choice([0, 1 << 21])),
                 segment_degree=int(rng.choice([0, 1 << 30])),
-                hub_block=int(rng.choice([0, 50, 32768])))
+                hub_order=int(rng.integers(0, 3)))
 
 
 @pytest.mark.parametrize("seed", range(24))
