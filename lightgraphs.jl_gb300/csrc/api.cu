@@ -517,9 +517,15 @@ int run_ms_batch(lgbc_graph* g, const int32_t* lane_src, int nl, int sigma_kind,
   const int words = nl > kMaxLanes ? 2 : 1;
   if (nl < 1 || nl > kWideLanes)
     return fail(LGBC_EINVAL, "internal: a multi-source batch holds 1 to 128 lanes");
-  if (words > 1 && (dist || seeds.v || stats || stress || sigma_kind == kSigmaNone ||
+  if (words > 1 && (dist || stats || stress || sigma_kind == kSigmaNone ||
                     g->ms.sigma_words < words || !g->ms.claim))
-    return fail(LGBC_EINVAL, "internal: a two-word batch is a plain Brandes batch");
+    return fail(LGBC_EINVAL, "internal: a two-word batch is a Brandes batch");
+  // two-word lane sets are read as single 16-byte accesses
+  auto misaligned = [&](const void* p) {
+    return words > 1 && (reinterpret_cast<uintptr_t>(p) & 15u) != 0;
+  };
+  if (misaligned(seeds.mask) || misaligned(seeds.seg_mark))
+    return fail(LGBC_EINVAL, "internal: seed lane sets must start on a 16-byte boundary");
   const LaneSet act = lane_set(nl, words);
   for (;;) {
     MsBuffers b = ms_buffers(g, lane_src, lane_w);
@@ -580,7 +586,7 @@ int run_ms_batch(lgbc_graph* g, const int32_t* lane_src, int nl, int sigma_kind,
       LGBC_CUDA(cudaGraphLaunch(bg->exec, g->stream));
       g->launches += 2 + static_cast<int64_t>(maxl + 1) * bg->body_kernels;
       if (seeds.seg_mark)  // premarked vertices were never listed: clear visit outright
-        LGBC_CUDA(cudaMemsetAsync(b.visit, 0, static_cast<size_t>(g->n) * 8, g->stream));
+        LGBC_CUDA(cudaMemsetAsync(b.visit, 0, static_cast<size_t>(g->n) * 8 * words, g->stream));
       return check_launch(g);
     }
     bool bu = false;
@@ -640,7 +646,7 @@ int run_ms_batch(lgbc_graph* g, const int32_t* lane_src, int nl, int sigma_kind,
       g->launches += ms_backward_level(g->cfg, g->stream, dg, b, hd, sigma_kind, bc);
     g->launches += ms_cleanup(g->cfg, g->stream, b);
     if (seeds.seg_mark)  // premarked vertices were never listed: clear visit outright
-      LGBC_CUDA(cudaMemsetAsync(b.visit, 0, static_cast<size_t>(g->n) * 8, g->stream));
+      LGBC_CUDA(cudaMemsetAsync(b.visit, 0, static_cast<size_t>(g->n) * 8 * words, g->stream));
     return check_launch(g);
   }
 }
@@ -653,7 +659,7 @@ int run_stacked(lgbc_graph* g, int64_t copies, double* bc_dev, const std::vector
 int run_betweenness(lgbc_graph* g, int64_t k_act, int endpoints, double* bc_dev,
                     const double* d_w) {
   g->launches += fill_f64(g->cfg, g->stream, bc_dev, g->n, 0.0);
-  const int lanes0 = std::max(1, std::min<int>(kMaxLanes, g->tune.lanes));
+  const int lanes0 = std::max(1, std::min<int>(kWideLanes, g->tune.lanes));
   const int64_t batches = (k_act + lanes0 - 1) / lanes0;
   const int64_t copies = g->n > 0 ? std::min<int64_t>(g->tune.stack_vertices / g->n, batches) : 0;
   const bool host_w = d_w && static_cast<int64_t>(g->h_weights.size()) == k_act;
@@ -798,7 +804,9 @@ int create_replicated(lgbc_graph* g, int64_t copies, lgbc_graph** out) {
 
 int run_stacked(lgbc_graph* g, int64_t copies, double* bc_dev, const std::vector<double>* w) {
   const int64_t n = g->n;
-  const int L = std::max(1, std::min<int>(kMaxLanes, g->tune.lanes));
+  const int L = std::max(1, std::min<int>(kWideLanes, g->tune.lanes));
+  const int W = L > kMaxLanes ? 2 : 1;  // lane words per vertex of the union batches
+  const int64_t row = 64 * W;            // weights per copy row
   if (!g->stack || g->stack_copies != copies) {
     if (g->stack) lgbc_graph_destroy(g->stack);
     g->stack = nullptr;
@@ -823,15 +831,17 @@ int run_stacked(lgbc_graph* g, int64_t copies, double* bc_dev, const std::vector
   std::vector<int32_t> sv;
   std::vector<uint64_t> sm;
   std::vector<int64_t> bstart(static_cast<size_t>(nbu + 1), 0), voff(static_cast<size_t>(copies + 1));
-  std::vector<uint64_t> marks(static_cast<size_t>(nbu * copies));
+  // W words per seed mask and per copy mark
+  std::vector<uint64_t> marks(static_cast<size_t>(nbu * copies * W));
   std::vector<int64_t> filled(static_cast<size_t>(nbu), 0);  // ordinary batches per union batch
-  // lane weights: row u * copies + r holds copy r's 64 lanes of union batch u
-  std::vector<double> wrows(w ? static_cast<size_t>(nbu * copies * 64) : 0, 0.0);
+  // lane weights: row u * copies + r holds copy r's 64 W lanes of union batch u
+  std::vector<double> wrows(w ? static_cast<size_t>(nbu * copies * row) : 0, 0.0);
+  const LaneSet all = lane_set(L, W);
   for (int64_t r = 0; r <= copies; ++r) voff[static_cast<size_t>(r)] = r * n;
   for (int64_t u = 0; u < nbu; ++u) {
     for (int64_t r = 0; r < copies; ++r) {
       if ((u * copies + r) * L < k) filled[static_cast<size_t>(u)]++;
-      uint64_t seeded = 0;
+      LaneSet seeded{};
       const int64_t i0 = (u * copies + r) * L;
       const size_t first = sv.size();  // this copy's seeds: a repeated source is one seed
       for (int l = 0; l < L && i0 + l < k; ++l) {
@@ -840,20 +850,26 @@ int run_stacked(lgbc_graph* g, int64_t copies, double* bc_dev, const std::vector
         while (j < sv.size() && sv[j] != v) ++j;
         if (j == sv.size()) {
           sv.push_back(v);
-          sm.push_back(0ull);
+          for (int q = 0; q < W; ++q) sm.push_back(0ull);
         }
-        sm[j] |= 1ull << l;
-        seeded |= 1ull << l;
-        if (w) wrows[static_cast<size_t>((u * copies + r) * 64 + l)] = (*w)[static_cast<size_t>(i0 + l)];
+        sm[j * W + static_cast<size_t>(l >> 6)] |= 1ull << (l & 63);
+        seeded.w[l >> 6] |= 1ull << (l & 63);
+        if (w) wrows[static_cast<size_t>((u * copies + r) * row + l)] = (*w)[static_cast<size_t>(i0 + l)];
       }
-      const uint64_t all = L >= 64 ? ~0ull : ((1ull << L) - 1ull);
-      marks[static_cast<size_t>(u * copies + r)] = all & ~seeded;
+      for (int q = 0; q < W; ++q)
+        marks[static_cast<size_t>((u * copies + r) * W + q)] = all.w[q] & ~seeded.w[q];
     }
     bstart[static_cast<size_t>(u + 1)] = static_cast<int64_t>(sv.size());
   }
-  // one device buffer: weight rows | voff | marks | seed masks | seed vertices
-  const size_t bytes = wrows.size() * 8 + voff.size() * 8 + marks.size() * 8 + sm.size() * 8 +
-                       sv.size() * 4 + 16;
+  // one device buffer: weight rows | voff | marks | seed masks | seed vertices,
+  // each part starting on a 16-byte boundary (two-word lane sets are read as
+  // one 16-byte access)
+  auto up16 = [](size_t x) { return (x + 15) & ~static_cast<size_t>(15); };
+  const size_t o_voff = up16(wrows.size() * 8);
+  const size_t o_marks = up16(o_voff + voff.size() * 8);
+  const size_t o_sm = up16(o_marks + marks.size() * 8);
+  const size_t o_sv = up16(o_sm + sm.size() * 8);
+  const size_t bytes = o_sv + sv.size() * 4 + 16;
   unsigned char* buf = nullptr;
   LGBC_TRY(dev_alloc(&buf, bytes));
   std::unique_ptr<unsigned char, cudaError_t (*)(void*)> guard(buf, cudaFree);
@@ -861,32 +877,32 @@ int run_stacked(lgbc_graph* g, int64_t copies, double* bc_dev, const std::vector
   if (!wrows.empty())
     LGBC_CUDA(cudaMemcpyAsync(d_wrows, wrows.data(), wrows.size() * 8, cudaMemcpyHostToDevice,
                               st->stream));
-  int64_t* d_voff = reinterpret_cast<int64_t*>(buf + wrows.size() * 8);
-  uint64_t* d_marks = reinterpret_cast<uint64_t*>(d_voff + voff.size());
-  uint64_t* d_sm = d_marks + marks.size();
-  int32_t* d_sv = reinterpret_cast<int32_t*>(d_sm + sm.size());
+  int64_t* d_voff = reinterpret_cast<int64_t*>(buf + o_voff);
+  uint64_t* d_marks = reinterpret_cast<uint64_t*>(buf + o_marks);
+  uint64_t* d_sm = reinterpret_cast<uint64_t*>(buf + o_sm);
+  int32_t* d_sv = reinterpret_cast<int32_t*>(buf + o_sv);
   LGBC_CUDA(cudaMemcpyAsync(d_voff, voff.data(), voff.size() * 8, cudaMemcpyHostToDevice, st->stream));
   LGBC_CUDA(cudaMemcpyAsync(d_marks, marks.data(), marks.size() * 8, cudaMemcpyHostToDevice, st->stream));
   LGBC_CUDA(cudaMemcpyAsync(d_sm, sm.data(), sm.size() * 8, cudaMemcpyHostToDevice, st->stream));
   LGBC_CUDA(cudaMemcpyAsync(d_sv, sv.data(), sv.size() * 4, cudaMemcpyHostToDevice, st->stream));
   if (!st->d_bc) LGBC_TRY(dev_alloc(&st->d_bc, static_cast<size_t>(st->n)));
   st->launches += fill_f64(st->cfg, st->stream, st->d_bc, st->n, 0.0);
-  LGBC_TRY(ensure_ms(st, true));
+  LGBC_TRY(ensure_ms(st, true, W));
   // the caller's stream waits for nothing of ours: order the two streams
   LGBC_CUDA(cudaStreamSynchronize(g->stream));
   for (int64_t u = 0; u < nbu; ++u) {
     Seeds sd;
     sd.v = d_sv + bstart[static_cast<size_t>(u)];
-    sd.mask = d_sm + bstart[static_cast<size_t>(u)];
+    sd.mask = d_sm + bstart[static_cast<size_t>(u)] * W;
     sd.count = bstart[static_cast<size_t>(u + 1)] - bstart[static_cast<size_t>(u)];
     sd.seg_off = d_voff;
-    sd.seg_mark = d_marks + static_cast<size_t>(u * copies);
+    sd.seg_mark = d_marks + static_cast<size_t>(u * copies * W);
     sd.nseg = copies;
     const double* lw = nullptr;
     if (w) {
-      lw = d_wrows + u * copies * 64;
+      lw = d_wrows + u * copies * row;
       sd.lane_w_n = n;
-      sd.lane_w_count = copies * 64;
+      sd.lane_w_count = copies * row;
     }
     int rc = run_ms_batch(st, nullptr, L, kSigmaU64, st->d_bc, nullptr, 0, sd, lw);
     if (rc == 1) {

@@ -213,14 +213,14 @@ namespace lgbc::api {
 // in its mask).
 struct Seeds {
   const int32_t* v = nullptr;
-  const uint64_t* mask = nullptr;
+  const uint64_t* mask = nullptr;   // one lane set per seed (1 or 2 words: the batch's)
   int64_t count = 0;
   // optional premark of seedless lanes per component (unions of graphs)
   const int64_t* seg_off = nullptr;
-  const uint64_t* seg_mark = nullptr;
+  const uint64_t* seg_mark = nullptr;  // one lane set per component
   int64_t nseg = 0;
-  // stacked unions with lane weights: one row of 64 weights per copy of an
-  // lane_w_n-vertex graph, lane_w_count weights in all
+  // stacked unions with lane weights: one row of 64 * words weights per copy
+  // of an lane_w_n-vertex graph, lane_w_count weights in all
   int64_t lane_w_n = 0;
   int64_t lane_w_count = 0;
 };

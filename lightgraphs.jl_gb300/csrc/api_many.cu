@@ -124,24 +124,30 @@ int many_group(const std::vector<ManyGraph>& grp, int endpoints, double* bc_raw_
     seg_add[k] = static_cast<double>(act[k].size());
     maxa = std::max<int64_t>(maxa, static_cast<int64_t>(act[k].size()));
   }
-  if (g->tune.source_order == 1 && maxa > kMaxLanes)
+  // L lanes per batch (the handle's default batch width), W lane words
+  const int L = std::max(1, std::min<int>(kWideLanes, g->tune.lanes));
+  const int W = L > kMaxLanes ? 2 : 1;
+  if (g->tune.source_order == 1 && maxa > L)
     LGBC_TRY(order_many(g, grp, voff, act));
-  // batch b, lane l holds the (64 b + l)-th ordered source of every graph
-  const int64_t nb = (maxa + kMaxLanes - 1) / kMaxLanes;
+  // batch b, lane l holds the (L b + l)-th ordered source of every graph;
+  // W mask words per seed and per (batch, graph) mark
+  const int64_t nb = (maxa + L - 1) / L;
+  const LaneSet all = lane_set(L, W);
   std::vector<int64_t> bstart(static_cast<size_t>(nb + 1), 0);
-  std::vector<uint64_t> marks(static_cast<size_t>(nb) * grp.size());
+  std::vector<uint64_t> marks(static_cast<size_t>(nb) * grp.size() * W);
   for (int64_t b = 0; b < nb; ++b) {
     for (size_t k = 0; k < grp.size(); ++k) {
-      uint64_t seeded = 0;
-      for (int l = 0; l < kMaxLanes; ++l) {
-        const int64_t i = b * kMaxLanes + l;
+      LaneSet seeded{};
+      for (int l = 0; l < L; ++l) {
+        const int64_t i = b * L + l;
         if (i < static_cast<int64_t>(act[k].size())) {
           sv.push_back(static_cast<int32_t>(voff[k] + act[k][static_cast<size_t>(i)]));
-          sm.push_back(1ull << l);
-          seeded |= 1ull << l;
+          for (int q = 0; q < W; ++q) sm.push_back(q == (l >> 6) ? 1ull << (l & 63) : 0ull);
+          seeded.w[l >> 6] |= 1ull << (l & 63);
         }
       }
-      marks[static_cast<size_t>(b) * grp.size() + k] = ~seeded;
+      for (int q = 0; q < W; ++q)
+        marks[(static_cast<size_t>(b) * grp.size() + k) * W + q] = all.w[q] & ~seeded.w[q];
     }
     bstart[static_cast<size_t>(b + 1)] = static_cast<int64_t>(sv.size());
   }
@@ -167,18 +173,18 @@ int many_group(const std::vector<ManyGraph>& grp, int endpoints, double* bc_raw_
   }
   if (!g->d_bc) LGBC_TRY(dev_alloc(&g->d_bc, static_cast<size_t>(N)));
   g->launches += fill_f64(g->cfg, g->stream, g->d_bc, N, 0.0);
-  if (!sv.empty()) LGBC_TRY(ensure_ms(g, true));
+  if (!sv.empty()) LGBC_TRY(ensure_ms(g, true, W));
   for (int64_t b = 0; b < nb; ++b) {
     Seeds sd;
     sd.v = d_sv + bstart[static_cast<size_t>(b)];
-    sd.mask = d_sm + bstart[static_cast<size_t>(b)];
+    sd.mask = d_sm + bstart[static_cast<size_t>(b)] * W;
     sd.count = bstart[static_cast<size_t>(b + 1)] - bstart[static_cast<size_t>(b)];
     if (sd.count == 0) continue;
     sd.seg_off = d_voff;
-    sd.seg_mark = d_marks + static_cast<size_t>(b) * grp.size();
+    sd.seg_mark = d_marks + static_cast<size_t>(b) * grp.size() * W;
     sd.nseg = static_cast<int64_t>(grp.size());
-    int rc = run_ms_batch(g, nullptr, kMaxLanes, kSigmaU64, g->d_bc, nullptr, 0, sd);
-    if (rc == 1) rc = run_ms_batch(g, nullptr, kMaxLanes, kSigmaF64, g->d_bc, nullptr, 0, sd);
+    int rc = run_ms_batch(g, nullptr, L, kSigmaU64, g->d_bc, nullptr, 0, sd);
+    if (rc == 1) rc = run_ms_batch(g, nullptr, L, kSigmaF64, g->d_bc, nullptr, 0, sd);
     if (rc != LGBC_OK) return rc;
   }
   if (endpoints && !act_src.empty()) {

@@ -97,13 +97,15 @@ struct HubData {
 // level may hold without the next level risking 64-bit overflow.
 int ms_init(cudaStream_t s, const DevGraph& g, const MsBuffers& b, int nlanes, int sigma_kind,
             unsigned long long sigma_limit, int32_t* dist, int64_t dist_ld);
-// Level 0 from explicit (vertex, lane mask) seeds (distinct vertices); for
-// disjoint unions of graphs, where one lane holds a source in every component.
+// Level 0 from explicit (vertex, lane set) seeds (distinct vertices; b.words
+// mask words per seed); for disjoint unions of graphs, where one lane holds a
+// source in every component.  Distances (dist) only with one word.
 int ms_init_seeds(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
                   const int32_t* seed_v, const uint64_t* seed_mask, int64_t nseeds, int sigma_kind,
                   unsigned long long sigma_limit, int32_t* dist, int64_t dist_ld);
-// visit[v] = seg_mark[k] for every vertex of segment k (vertices
-// [seg_off[k], seg_off[k+1])): the lanes with no source in that component.
+// visit[v] = seg_mark[k] (b.words words) for every vertex of segment k
+// (vertices [seg_off[k], seg_off[k+1])): the lanes with no source in that
+// component.
 int ms_premark(const LaunchCfg& c, cudaStream_t s, const MsBuffers& b, const int64_t* seg_off,
                const uint64_t* seg_mark, int64_t nseg);
 // Top-down / bottom-up level.  Distances (dist) only with one word.

@@ -1647,29 +1647,38 @@ __global__ void __launch_bounds__(256) k_ms_level_stats(MsBuffers b, unsigned lo
 }
 
 // Batch initialisation with explicit seeds: seed i puts vertex seed_v[i] at
-// level 0 of the lanes in seed_mask[i].  Used for disjoint unions of graphs, where a
-// lane may hold one source in every component: BFS trees of different
-// components never meet, so each component sees a single-source traversal.
-// Seed vertices must be distinct (a vertex that starts several lanes is one
-// seed with several mask bits).  The host zeroes the control block first.
-template <int SK>
+// level 0 of the lanes in its lane set (W words at seed_mask[i * W]).  Used
+// for disjoint unions of graphs, where a lane may hold one source in every
+// component: BFS trees of different components never meet, so each component
+// sees a single-source traversal.  Seed vertices must be distinct (a vertex
+// that starts several lanes is one seed with several bits).  The host zeroes
+// the control block first.
+template <int SK, int W>
 __global__ void k_ms_init_seeds(DevGraph g, MsBuffers b, const int32_t* seed_v,
                                 const uint64_t* seed_mask, long long nseeds, int32_t* dist,
                                 int64_t ld) {
   using T = typename Sig<SK>::T;
+  const Lanes<W>* masks = lanes_of<W>(seed_mask);
+  Lanes<W>* front = lanes_of<W>(b.mb[0]);
+  Lanes<W>* visit = lanes_of<W>(b.visit);
+  Lanes<W>* qm = lanes_of<W>(b.qm);
   unsigned long long mf = 0;
   for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < nseeds;
        i += static_cast<long long>(gridDim.x) * blockDim.x) {
     const int32_t v = seed_v[i];
-    const uint64_t m = seed_mask[i];
-    b.mb[0][v] = m;
-    b.visit[v] |= m;
+    const Lanes<W> m = masks[i];
+    front[v] = m;
+    visit[v] = lor(visit[v], m);
     b.qv[i] = v;
-    b.qm[i] = m;
-    for (uint64_t r = m; r; r &= r - 1) {
-      const int l = __ffsll(static_cast<long long>(r)) - 1;
-      if (SK != kSigmaNone) reinterpret_cast<T*>(b.sigma)[static_cast<int64_t>(v) * 64 + l] = T(1);
-      if (dist) dist[static_cast<int64_t>(l) * ld + v] = 0;
+    qm[i] = m;
+#pragma unroll
+    for (int j = 0; j < W; ++j) {
+      for (uint64_t r = m.w[j]; r; r &= r - 1) {
+        const int l = 64 * j + __ffsll(static_cast<long long>(r)) - 1;
+        if (SK != kSigmaNone)
+          reinterpret_cast<T*>(b.sigma)[static_cast<int64_t>(v) * (64 * W) + l] = T(1);
+        if (dist) dist[static_cast<int64_t>(l) * ld + v] = 0;
+      }
     }
     mf += static_cast<unsigned long long>(g.rowptr[v + 1] - g.rowptr[v]);
   }
@@ -1679,11 +1688,15 @@ __global__ void k_ms_init_seeds(DevGraph g, MsBuffers b, const int32_t* seed_v,
 
 // Union batches: lanes that hold no source in a component can never reach
 // its vertices; marking them visited there keeps bottom-up levels from
-// rescanning those vertices.  Block k covers component k.
-__global__ void k_ms_premark(uint64_t* visit, const int64_t* seg_off, const uint64_t* seg_mark,
+// rescanning those vertices.  Block k covers component k; seg_mark holds W
+// words per component.
+template <int W>
+__global__ void k_ms_premark(uint64_t* visit_words, const int64_t* seg_off, const uint64_t* seg_mark,
                              int64_t nseg) {
+  Lanes<W>* visit = lanes_of<W>(visit_words);
+  const Lanes<W>* marks = lanes_of<W>(seg_mark);
   for (int64_t k = blockIdx.x; k < nseg; k += gridDim.x) {
-    const uint64_t m = seg_mark[k];
+    const Lanes<W> m = marks[k];
     for (int64_t v = seg_off[k] + threadIdx.x; v < seg_off[k + 1]; v += blockDim.x) visit[v] = m;
   }
 }
@@ -1747,31 +1760,48 @@ int ms_init(cudaStream_t s, const DevGraph& g, const MsBuffers& b, int nlanes, i
   return 1;
 }
 
+namespace {
+
+template <int W>
+void init_seeds_w(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
+                  const int32_t* seed_v, const uint64_t* seed_mask, int64_t nseeds, int sigma_kind,
+                  unsigned long long sigma_limit, int32_t* dist, int64_t dist_ld) {
+  const int grid = static_cast<int>(std::min<int64_t>((nseeds + 255) / 256, c.grid));
+  switch (sigma_kind) {
+    case kSigmaU64:
+      k_ms_init_seeds<kSigmaU64, W><<<grid, 256, 0, s>>>(g, b, seed_v, seed_mask, nseeds, dist, dist_ld);
+      k_ms_init_seeds_ctl<<<1, 1, 0, s>>>(b, nseeds, b.cap, sigma_limit);
+      break;
+    case kSigmaF64:
+      k_ms_init_seeds<kSigmaF64, W><<<grid, 256, 0, s>>>(g, b, seed_v, seed_mask, nseeds, dist, dist_ld);
+      k_ms_init_seeds_ctl<<<1, 1, 0, s>>>(b, nseeds, b.cap, ~0ull);
+      break;
+    default:
+      k_ms_init_seeds<kSigmaNone, W><<<grid, 256, 0, s>>>(g, b, seed_v, seed_mask, nseeds, dist, dist_ld);
+      k_ms_init_seeds_ctl<<<1, 1, 0, s>>>(b, nseeds, b.cap, ~0ull);
+      break;
+  }
+}
+
+}  // namespace
+
 int ms_init_seeds(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
                   const int32_t* seed_v, const uint64_t* seed_mask, int64_t nseeds, int sigma_kind,
                   unsigned long long sigma_limit, int32_t* dist, int64_t dist_ld) {
   cudaMemsetAsync(b.ctl, 0, sizeof(BatchCtl), s);
-  const int grid = static_cast<int>(std::min<int64_t>((nseeds + 255) / 256, c.grid));
-  switch (sigma_kind) {
-    case kSigmaU64:
-      k_ms_init_seeds<kSigmaU64><<<grid, 256, 0, s>>>(g, b, seed_v, seed_mask, nseeds, dist, dist_ld);
-      k_ms_init_seeds_ctl<<<1, 1, 0, s>>>(b, nseeds, b.cap, sigma_limit);
-      break;
-    case kSigmaF64:
-      k_ms_init_seeds<kSigmaF64><<<grid, 256, 0, s>>>(g, b, seed_v, seed_mask, nseeds, dist, dist_ld);
-      k_ms_init_seeds_ctl<<<1, 1, 0, s>>>(b, nseeds, b.cap, ~0ull);
-      break;
-    default:
-      k_ms_init_seeds<kSigmaNone><<<grid, 256, 0, s>>>(g, b, seed_v, seed_mask, nseeds, dist, dist_ld);
-      k_ms_init_seeds_ctl<<<1, 1, 0, s>>>(b, nseeds, b.cap, ~0ull);
-      break;
-  }
+  if (b.words == 2)
+    init_seeds_w<2>(c, s, g, b, seed_v, seed_mask, nseeds, sigma_kind, sigma_limit, nullptr, 0);
+  else
+    init_seeds_w<1>(c, s, g, b, seed_v, seed_mask, nseeds, sigma_kind, sigma_limit, dist, dist_ld);
   return 2;
 }
 
 int ms_premark(const LaunchCfg& c, cudaStream_t s, const MsBuffers& b, const int64_t* seg_off,
                const uint64_t* seg_mark, int64_t nseg) {
-  k_ms_premark<<<c.grid, c.block, 0, s>>>(b.visit, seg_off, seg_mark, nseg);
+  if (b.words == 2)
+    k_ms_premark<2><<<c.grid, c.block, 0, s>>>(b.visit, seg_off, seg_mark, nseg);
+  else
+    k_ms_premark<1><<<c.grid, c.block, 0, s>>>(b.visit, seg_off, seg_mark, nseg);
   return 1;
 }
 

@@ -1,8 +1,8 @@
 """Batches of 65-128 sources, which keep two 64-bit lane words per vertex:
 every kernel family (top-down / bottom-up, hub items, both gather strategies,
 segmented warps, host- and device-driven level loops, FP64 replay, weighted
-accumulation) against the oracle, and the entry points that stay at 64 lanes
-with such a tuning set."""
+accumulation, stacked unions and unions of graphs) against the oracle, and
+the entry points that stay at 64 lanes with such a tuning set."""
 import numpy as np
 import pytest
 
@@ -106,7 +106,7 @@ def test_weighted_two_words(name):
 
 
 def test_other_entry_points_with_wide_tuning():
-    # stress, distances and many-graph unions run at most 64 lanes whatever the tuning
+    # stress and distance batches run at most 64 lanes whatever the tuning
     g = GRAPHS["rmat10"]()
     g.device_handle().set_tuning(lanes=128)
     rp, ci, _ = csr_args(g)
@@ -124,3 +124,31 @@ def test_tuning_limits():
     with pytest.raises(Exception):
         h.set_tuning(lanes=129)
     assert h.tuning().lanes == 128
+
+
+@pytest.mark.parametrize("directed", [False, True])
+def test_stacked_unions_two_words(directed):
+    # a small graph runs as a stacked union of copies, each holding a 128-lane
+    # batch; repeated sources inside one copy share a seed
+    g = G.erdos_renyi_nm(1500, 6000, seed=21, directed=directed)
+    h = g.device_handle()
+    h.set_tuning(lanes=128, stack_vertices=1 << 21)
+    rng = np.random.default_rng(8)
+    src = rng.choice(g.nv(), 700, replace=True).astype(np.int32)
+    rp, ci, kw = csr_args(g)
+    for ep in (False, True):
+        z = lgbc.betweenness_centrality(g, list(src + 1), normalize=False, endpoints=ep)
+        assert_bc_close(z, oracle_bc(g, src, normalize=False, endpoints=ep))
+    w = rng.uniform(0.1, 5.0, size=len(src))
+    got = betweenness_raw_weighted(g, src, w)
+    _, want = oracle.dependency(rp, ci, src, w, **kw)
+    np.testing.assert_allclose(got, want, rtol=1e-9, atol=1e-9 * max(1.0, np.abs(want).max()))
+
+
+def test_many_graphs_two_words():
+    # unions of graphs run 128 lanes per batch by default
+    gs = [G.barabasi_albert(int(n), 3, seed=50 + i) for i, n in enumerate([90, 300, 1200, 700, 130])]
+    gs.append(G.erdos_renyi_nm(400, 900, seed=5))
+    outs = lgbc.betweenness_centrality_many(gs, normalize=False)
+    for g, z in zip(gs, outs):
+        assert_bc_close(z, oracle_bc(g, normalize=False))
