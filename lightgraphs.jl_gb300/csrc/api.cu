@@ -143,33 +143,45 @@ int ensure_dist(lgbc_graph* g, int64_t count) {
 void make_items(const int64_t* rowptr, const int32_t* colidx, int64_t n, int H, int order,
                 const std::vector<int32_t>& slot_of, std::vector<HubItem>& items) {
   constexpr int64_t kBuckets = int64_t(1) << 16;
+  const bool ordered = order == 2 || (order == 1 && colidx != nullptr && n > 0);
+  // items (and their order keys) per contiguous part of the vertex range,
+  // concatenated in vertex order
+  std::vector<std::vector<HubItem>> pit(8);
+  std::vector<std::vector<int64_t>> pkey(8);
+  const int parts = parallel_parts(n, [&](int p, int64_t vb, int64_t ve) {
+    std::vector<HubItem>& out = pit[static_cast<size_t>(p)];
+    std::vector<int64_t>& key = pkey[static_cast<size_t>(p)];
+    for (int64_t v = vb; v < ve; ++v) {
+      const int64_t e0 = rowptr[v], e1 = rowptr[v + 1];
+      if (e1 - e0 <= H) continue;
+      const int32_t nit = static_cast<int32_t>((e1 - e0 + kHubChunk - 1) / kHubChunk);
+      for (int64_t lo = e0; lo < e1; lo += kHubChunk) {
+        HubItem it;
+        it.lo = lo;
+        it.hi = std::min<int64_t>(lo + kHubChunk, e1);
+        it.v = static_cast<int32_t>(v);
+        it.slot = slot_of[static_cast<size_t>(v)];
+        it.nitems = nit;
+        it.pad = 0;
+        out.push_back(it);
+        if (!ordered) continue;
+        const int64_t mid2 = (lo - e0) + it.hi - e0;  // twice the middle's offset in the row
+        key.push_back(order == 1 ? static_cast<int64_t>(colidx[lo + (it.hi - lo) / 2]) * kBuckets / n
+                                 : mid2 * kBuckets / (2 * (e1 - e0)));
+      }
+    }
+  });
   items.clear();
   std::vector<int64_t> key;
-  const bool ordered = order == 2 || (order == 1 && colidx != nullptr && n > 0);
-  for (int64_t v = 0; v < n; ++v) {
-    const int64_t e0 = rowptr[v], e1 = rowptr[v + 1];
-    if (e1 - e0 <= H) continue;
-    const int32_t nit = static_cast<int32_t>((e1 - e0 + kHubChunk - 1) / kHubChunk);
-    for (int64_t lo = e0; lo < e1; lo += kHubChunk) {
-      HubItem it;
-      it.lo = lo;
-      it.hi = std::min<int64_t>(lo + kHubChunk, e1);
-      it.v = static_cast<int32_t>(v);
-      it.slot = slot_of[static_cast<size_t>(v)];
-      it.nitems = nit;
-      it.pad = 0;
-      items.push_back(it);
-      if (!ordered) continue;
-      const int64_t mid2 = (lo - e0) + it.hi - e0;  // twice the middle's offset in the row
-      key.push_back(order == 1 ? static_cast<int64_t>(colidx[lo + (it.hi - lo) / 2]) * kBuckets / n
-                               : mid2 * kBuckets / (2 * (e1 - e0)));
-    }
+  for (int p = 0; p < parts; ++p) {
+    items.insert(items.end(), pit[static_cast<size_t>(p)].begin(), pit[static_cast<size_t>(p)].end());
+    key.insert(key.end(), pkey[static_cast<size_t>(p)].begin(), pkey[static_cast<size_t>(p)].end());
   }
   if (!ordered) return;
   // stable counting sort on the bucket
   std::vector<int64_t> start(static_cast<size_t>(kBuckets + 1), 0);
   for (int64_t k : key) start[static_cast<size_t>(k + 1)]++;
-  for (int64_t b = 0; b < kBuckets; ++b) start[static_cast<size_t>(b + 1)] += start[static_cast<size_t>(b)];
+  for (int64_t bk = 0; bk < kBuckets; ++bk) start[static_cast<size_t>(bk + 1)] += start[static_cast<size_t>(bk)];
   std::vector<HubItem> sorted(items.size());
   for (size_t i = 0; i < items.size(); ++i) sorted[static_cast<size_t>(start[static_cast<size_t>(key[i])]++)] = items[i];
   items.swap(sorted);
@@ -191,12 +203,23 @@ int build_hubs(lgbc_graph* g, const int64_t* rowptr, const int32_t* colidx, cons
   g->hubs.release();
   const int64_t n = g->n;
   std::vector<int32_t> slot_of(static_cast<size_t>(n), -1);
-  int64_t nslots = 0;
-  for (int64_t v = 0; v < n; ++v) {
-    const int64_t dout = rowptr[v + 1] - rowptr[v];
-    const int64_t din = in_rowptr[v + 1] - in_rowptr[v];
-    if (dout > H || din > H) slot_of[static_cast<size_t>(v)] = static_cast<int32_t>(nslots++);
-  }
+  auto is_hub = [&](int64_t v) {
+    return rowptr[v + 1] - rowptr[v] > H || in_rowptr[v + 1] - in_rowptr[v] > H;
+  };
+  // slots in vertex order: count per part, then number
+  std::vector<int64_t> first(9, 0);
+  const int parts = parallel_parts(n, [&](int p, int64_t vb, int64_t ve) {
+    int64_t c = 0;
+    for (int64_t v = vb; v < ve; ++v) c += is_hub(v) ? 1 : 0;
+    first[static_cast<size_t>(p + 1)] = c;
+  });
+  for (int p = 0; p < parts; ++p) first[static_cast<size_t>(p + 1)] += first[static_cast<size_t>(p)];
+  const int64_t nslots = first[static_cast<size_t>(parts)];
+  parallel_parts(n, [&](int p, int64_t vb, int64_t ve) {
+    int64_t next = first[static_cast<size_t>(p)];
+    for (int64_t v = vb; v < ve; ++v)
+      if (is_hub(v)) slot_of[static_cast<size_t>(v)] = static_cast<int32_t>(next++);
+  });
   g->hubs.nslots = nslots;
   g->hubs.built_for = H;
   g->hubs.built_order = order;
@@ -985,6 +1008,7 @@ int init_handle(lgbc_graph* g, int64_t n, int directed) {
 // bound, landmarks and the hub table.
 int finish_handle(lgbc_graph* g, const int64_t* rowptr, const int64_t* in_rowptr,
                   const int32_t* colidx, const int32_t* in_colidx);
+void degree_pass(lgbc_graph* g, const int64_t* rowptr, const int64_t* in_rowptr);
 
 int create_impl(lgbc_graph* g, int64_t n, int64_t nnz, const int64_t* rowptr, const int32_t* colidx,
                 const int64_t* in_rowptr, const int32_t* in_colidx, int directed) {
@@ -1019,44 +1043,67 @@ int create_impl(lgbc_graph* g, int64_t n, int64_t nnz, const int64_t* rowptr, co
     g->launches += validate_csr(g->cfg, g->stream, g->d_in_rowptr, g->d_in_colidx, n, nnz, d_bad);
   int bad = 0;
   cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, g->stream);
+  // the degree pass (differences of row pointers only) overlaps the upload;
+  // the hub items walk row ranges and wait for the validation
+  degree_pass(g, rowptr, directed ? in_rowptr : rowptr);
   cudaError_t e = cudaStreamSynchronize(g->stream);
   cudaFree(d_bad);
   if (e != cudaSuccess) return cuda_fail(e, "graph upload");
   LGBC_TRY(check_launch(g));
   if (bad & 1) return fail(LGBC_EINVAL, "rowptr must be non-decreasing");
   if (bad & 2) return fail(LGBC_EINVAL, "column index out of range");
-  return finish_handle(g, rowptr, directed ? in_rowptr : rowptr, colidx, directed ? in_colidx : colidx);
+  return build_hubs(g, rowptr, colidx, directed ? in_rowptr : rowptr, directed ? in_colidx : colidx,
+                    g->tune.hub_degree, g->tune.hub_order);
+}
+
+// degree(g, v) > 0 (in+out for digraphs, src/core.jl:66-67), kept on the
+// host; the path-count bound; and the kLandmarks highest-degree vertices (ties:
+// smaller id) for source ordering.  Reads the row pointers only.
+void degree_pass(lgbc_graph* g, const int64_t* rowptr, const int64_t* in_rowptr) {
+  const int64_t n = g->n;
+  const int directed = g->directed;
+  g->has_degree.assign(static_cast<size_t>(n), 0);
+  uint8_t* has = g->has_degree.data();
+  std::vector<int64_t> max_in(8, 0);
+  std::vector<std::vector<std::pair<int64_t, int32_t>>> tops(8);  // max-heaps of (-degree, id)
+  const int parts = parallel_parts(n, [&](int p, int64_t vb, int64_t ve) {
+    int64_t mi = 0;
+    auto& top = tops[static_cast<size_t>(p)];
+    for (int64_t v = vb; v < ve; ++v) {
+      const int64_t dout = rowptr[v + 1] - rowptr[v];
+      const int64_t din = directed ? in_rowptr[v + 1] - in_rowptr[v] : dout;
+      const int64_t d = directed ? dout + din : dout;
+      has[v] = d > 0 ? 1 : 0;
+      mi = std::max(mi, din);
+      if (d <= 0) continue;
+      if (top.size() < static_cast<size_t>(kLandmarks)) {
+        top.emplace_back(-d, static_cast<int32_t>(v));
+        std::push_heap(top.begin(), top.end());
+      } else if (-d < top.front().first) {  // a larger degree (equal: the smaller id stays)
+        std::pop_heap(top.begin(), top.end());
+        top.back() = std::make_pair(-d, static_cast<int32_t>(v));
+        std::push_heap(top.begin(), top.end());
+      }
+    }
+    max_in[static_cast<size_t>(p)] = mi;
+  });
+  int64_t mi = 0;
+  std::vector<std::pair<int64_t, int32_t>> all;
+  for (int p = 0; p < parts; ++p) {
+    mi = std::max(mi, max_in[static_cast<size_t>(p)]);
+    all.insert(all.end(), tops[static_cast<size_t>(p)].begin(), tops[static_cast<size_t>(p)].end());
+  }
+  g->sigma_limit = ~0ull / static_cast<unsigned long long>(mi + 1);
+  std::sort(all.begin(), all.end());
+  g->landmarks.clear();
+  for (size_t i = 0; i < all.size() && i < static_cast<size_t>(kLandmarks); ++i)
+    g->landmarks.push_back(all[i].second);
 }
 
 int finish_handle(lgbc_graph* g, const int64_t* rowptr, const int64_t* in_rowptr,
                   const int32_t* colidx, const int32_t* in_colidx) {
-  const int64_t n = g->n;
+  degree_pass(g, rowptr, in_rowptr);
   const int directed = g->directed;
-  // degree(g, v) > 0: in+out for digraphs (src/core.jl:66-67), kept on the
-  // host; and, in the same pass, the kLandmarks highest-degree vertices (ties:
-  // smaller id) for source ordering
-  g->has_degree.assign(static_cast<size_t>(n), 0);
-  int64_t max_in = 0;
-  std::vector<std::pair<int64_t, int32_t>> top;  // max-heap of (-degree, id)
-  for (int64_t v = 0; v < n; ++v) {
-    const int64_t dout = rowptr[v + 1] - rowptr[v];
-    const int64_t din = directed ? in_rowptr[v + 1] - in_rowptr[v] : dout;
-    const int64_t d = directed ? dout + din : dout;
-    g->has_degree[static_cast<size_t>(v)] = d > 0 ? 1 : 0;
-    max_in = std::max(max_in, din);
-    if (d == 0) continue;
-    if (top.size() < static_cast<size_t>(kLandmarks)) {
-      top.emplace_back(-d, static_cast<int32_t>(v));
-      std::push_heap(top.begin(), top.end());
-    } else if (-d < top.front().first) {  // a larger degree (equal: the smaller id stays)
-      std::pop_heap(top.begin(), top.end());
-      top.back() = std::make_pair(-d, static_cast<int32_t>(v));
-      std::push_heap(top.begin(), top.end());
-    }
-  }
-  g->sigma_limit = ~0ull / static_cast<unsigned long long>(max_in + 1);
-  std::sort(top.begin(), top.end());
-  for (const auto& t : top) g->landmarks.push_back(t.second);
   return build_hubs(g, rowptr, colidx, directed ? in_rowptr : rowptr, directed ? in_colidx : colidx,
                     g->tune.hub_degree, g->tune.hub_order);
 }

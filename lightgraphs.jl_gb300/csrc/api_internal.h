@@ -12,6 +12,7 @@
 #include <mutex>
 #include <new>
 #include <string>
+#include <thread>
 #include <utility>
 #include <vector>
 
@@ -64,6 +65,21 @@ template <class T>
 void dev_free(T*& p) {
   if (p) cudaFree(p);
   p = nullptr;
+}
+
+// Host passes over the vertices of a large graph run on several threads:
+// f(part, begin, end) for `parts` contiguous chunks of [0, n), part 0 on the
+// calling thread.  Returns the number of parts (1 below 2^16 elements).
+template <class F>
+int parallel_parts(int64_t n, F&& f) {
+  const unsigned hw = std::thread::hardware_concurrency();
+  const int parts = n < (int64_t(1) << 16) ? 1 : static_cast<int>(std::max(1u, std::min(8u, hw)));
+  std::vector<std::thread> pool;
+  for (int p = 1; p < parts; ++p)
+    pool.emplace_back([&, p] { f(p, n * p / parts, n * (p + 1) / parts); });
+  f(0, int64_t(0), n / parts);
+  for (auto& t : pool) t.join();
+  return parts;
 }
 
 // Multi-source workspace (msbfs.cu): lane sets sized for two words per
