@@ -134,7 +134,7 @@ int lgbc_timer_stop(lgbc_graph *g, double *elapsed_ms, int64_t *kernel_launches)
 /* Statistics of the last betweenness / gdistances call on this handle. */
 typedef struct lgbc_stats {
   int64_t kernel_launches;   /* kernels the call launched */
-  int64_t batches;           /* source batches (<= 64 sources each) */
+  int64_t batches;           /* source batches (<= 128 sources each) */
   int64_t levels;            /* BFS levels summed over batches */
   int64_t active_sources;    /* sources with degree > 0 */
   int64_t wide_batches;      /* batches replayed in FP64 because a path count exceeded 2^64 */

@@ -536,7 +536,7 @@ int run_ms_batch(lgbc_graph* g, const int32_t* lane_src, int nl, int sigma_kind,
   const DevGraph dg = g->dev();
   LGBC_TRY(ensure_hubs(g));
   const HubData hd = hub_data(g);
-  // more than 64 lanes: a two-word batch (plain Brandes batches only)
+  // more than 64 lanes: a two-word batch (Brandes batches only)
   const int words = nl > kMaxLanes ? 2 : 1;
   if (nl < 1 || nl > kWideLanes)
     return fail(LGBC_EINVAL, "internal: a multi-source batch holds 1 to 128 lanes");

@@ -1,7 +1,7 @@
 // msbfs.cu -- multi-source (bit-lane) BFS with path counting and the
 // reverse-level dependency sweep of Brandes' algorithm.
 //
-// Replaces, for up to 64 sources at once, the per-source loop body of
+// Replaces, for up to 128 sources at once, the per-source loop body of
 // betweenness_centrality (src/centrality/betweenness.jl:57-67):
 //   forward  = dijkstra_shortest_paths(g, s; allpaths=true, trackvertices=true)
 //              with unit weights (src/shortestpaths/dijkstra.jl:59-141): the
@@ -15,20 +15,21 @@
 // below 2^64 here; the reference's Float64 sums are exact below 2^53) and the
 // dependencies up to summation order.
 //
-// Layout in HBM (per batch of <= 64 sources, "lanes"):
-//   visit[v]          uint64  lanes that reached v
-//   mb[L & 1][v]      uint64  lanes for which v is at level L (dense)
-//   sigma[v*64 + l]   uint64 path count (or FP64 in the overflow replay)
-//   psi[v*64 + l]     df32 (1 + delta) / sigma (or FP64)
-//   qv/qm             concatenated per-level lists of (vertex, lane mask)
-// A warp owns one vertex; thread t owns lanes t and t + 32.  Edges are read
-// 32 at a time; when several of them carry lanes, the warp transposes the
-// 32 x 64 bit matrix (edge, lane) so that each thread walks only the edges
-// on which its own lanes are set, four row loads in flight at a time (each
-// useful lane-op costs one 8-byte load and one add, no broadcast).  Chunks
-// with one or two such edges take a per-edge path instead.  Hubs (more than
-// hub_degree neighbours) are cut into kHubChunk-edge items processed by the
-// whole grid (k_ms_hub_*).
+// Layout in HBM (per batch of <= 64 W sources, "lanes"; W = 1 or 2 64-bit
+// words per lane set, a template parameter of every Brandes kernel):
+//   visit[v]          W x uint64  lanes that reached v
+//   mb[L & 1][v]      W x uint64  lanes for which v is at level L (dense)
+//   sigma[v*64W + l]  uint64 path count (or FP64 in the overflow replay)
+//   psi[v*64W + l]    df32 (1 + delta) / sigma (or FP64)
+//   qv/qm             concatenated per-level lists of (vertex, lane set)
+// A warp owns one vertex; thread t owns lanes 32 k + t (k < 2 W).  Edges are
+// read 32 at a time; the edges that carry lanes are compacted in shared
+// memory and walked edge by edge, each neighbour row read with coalesced
+// loads.  Above the dense_edges tuning cut the warp instead transposes the
+// 32 x 64W bit matrix (edge, lane) so that each thread walks only the edges
+// on which its own lanes are set.  Hubs (more than hub_degree neighbours) are
+// cut into kHubChunk-edge items processed by the whole grid (k_ms_hub_*).
+// Stress, distance and level-statistics batches are one-word.
 #include <algorithm>
 
 #include "lgbc_kernels.h"
@@ -155,7 +156,7 @@ template <> __device__ __forceinline__ double from_bits(unsigned long long x) {
   return __longlong_as_double(static_cast<long long>(x));
 }
 
-// Bits (t, t + 32) of a lane mask, as bit 0 / bit 1.
+// Bits (t, t + 32) of a one-word lane mask, as bit 0 / bit 1 (stress kernels).
 __device__ __forceinline__ unsigned my_bits(uint64_t m) {
   const int ln = lane_id();
   return static_cast<unsigned>((m >> ln) & 1ull) |
