@@ -209,9 +209,12 @@ __device__ __forceinline__ void store_dist(int32_t* dist, int64_t ld, int32_t w,
 
 // Compensated double-float accumulator: hi carries the running sum, lo the
 // exact rounding errors of the hi additions plus the addends' own lo parts;
-// normalised once at the end (acc_done).  7 FP32 additions per term.
+// normalised once at the end (acc_done).  The summed psi values are positive
+// and so is the running sum, so the larger of the two hi operands is known
+// by a max / min and Dekker's Fast2Sum gives the exact error of the hi
+// addition (the same pair as Knuth's TwoSum) in 5 operations instead of 6.
 __device__ __forceinline__ void acc_add(df32& acc, float xh, float xl) {
-  const df32 t = two_sum(acc.hi, xh);
+  const df32 t = fast_two_sum(fmaxf(acc.hi, xh), fminf(acc.hi, xh));
   acc.hi = t.hi;
   acc.lo = __fadd_rn(acc.lo, __fadd_rn(t.lo, xl));
 }
