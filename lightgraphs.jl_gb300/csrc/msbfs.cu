@@ -853,22 +853,25 @@ __global__ void __launch_bounds__(256, 4) k_ms_bu(DevGraph g, MsBuffers b, HubDa
   const int64_t n = g.n;
   const int ln = lane_id();
   unsigned long long mf = 0, mu = 0, smax = 0;
+  // the lanes each of the warp's 32 vertices discovers, kept in shared memory
+  // rather than in registers across the candidate loop
+  __shared__ Lanes<W> found_of[kWarpsPerBlock][kWarp];
+  Lanes<W>* my_found = found_of[threadIdx.x >> 5];
   for (int64_t base = gwarp() * kWarp; base < n; base += nwarps() * kWarp) {
     const int64_t wme = base + ln;
-    Lanes<W> vis = lz<W>();
     bool cand = false;
+    my_found[ln] = lz<W>();
     if (wme < n) {
-      vis = visit[wme];
       const int64_t d = g.in_rowptr[wme + 1] - g.in_rowptr[wme];
-      cand = !leq(vis, act) && d > 0 && d <= hd.hub_degree;
+      cand = !leq(visit[wme], act) && d > 0 && d <= hd.hub_degree;
     }
     unsigned cb = __ballot_sync(kFull, cand);
-    Lanes<W> my_nm = lz<W>();
+    __syncwarp();
     while (cb) {
       const int j = __ffs(cb) - 1;
       cb &= cb - 1;
       const int32_t w = static_cast<int32_t>(base + j);
-      const Lanes<W> want = lminus(act, lshfl(vis, j));
+      const Lanes<W> want = lminus(act, visit[w]);
       T a[2 * W];
       zero_accs(a);
       const Lanes<W> nm = pull_range<SK, W>(g.in_colidx, g.in_rowptr[w], g.in_rowptr[w + 1], want,
@@ -877,15 +880,17 @@ __global__ void __launch_bounds__(256, 4) k_ms_bu(DevGraph g, MsBuffers b, HubDa
         if (SK != kSigmaNone) store_sigma<SK, W>(b.sigma, w, nm, a, smax);
         if (DIST) store_dist(dist, ld, w, nm, L + 1);
       }
-      if (ln == j) my_nm = nm;
+      if (ln == j) my_found[j] = nm;
     }
+    __syncwarp();
+    const Lanes<W> my_nm = my_found[ln];
     const bool app = lany(my_nm);
     const unsigned long long slot = warp_append(app, &c->tail);
     if (app) {
       b.qv[slot] = static_cast<int32_t>(wme);
       qm[slot] = my_nm;
       next[wme] = my_nm;
-      const Lanes<W> nv = lor(vis, my_nm);
+      const Lanes<W> nv = lor(visit[wme], my_nm);
       visit[wme] = nv;
       mf += static_cast<unsigned long long>(g.rowptr[wme + 1] - g.rowptr[wme]);
       if (leq(nv, act)) mu += static_cast<unsigned long long>(g.in_rowptr[wme + 1] - g.in_rowptr[wme]);
