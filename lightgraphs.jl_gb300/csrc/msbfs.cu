@@ -666,45 +666,63 @@ __device__ __forceinline__ bool hub_last(unsigned int* cnt, int nitems) {
 
 // ---------------------------------------------------------------------------
 // Batch initialisation: level 0 = the sources (one lane each; a repeated
-// source gets several lanes in one list entry).
+// source gets several lanes in one list entry).  One block, thread l = lane
+// l: the lanes OR themselves into their source's lane set, and the first lane
+// of each distinct source appends it, in lane order (its position is the
+// number of first lanes before it).
 // ---------------------------------------------------------------------------
 template <int SK, int W>
-__global__ void k_ms_init(DevGraph g, MsBuffers b, int nl, Lanes<W> act, unsigned long long cap,
-                          unsigned long long sigma_limit, int32_t* dist, int64_t ld) {
-  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+__global__ void __launch_bounds__(kWideLanes) k_ms_init(DevGraph g, MsBuffers b, int nl, Lanes<W> act,
+                                                        unsigned long long cap,
+                                                        unsigned long long sigma_limit,
+                                                        int32_t* dist, int64_t ld) {
   using T = typename Sig<SK>::T;
+  __shared__ int32_t src[kWideLanes];
+  __shared__ unsigned firsts[kWideLanes / kWarp];
+  __shared__ unsigned long long sums[2];  // out-degrees of the sources, in-degrees of finished ones
   Lanes<W>* front = lanes_of<W>(b.mb[0]);
   Lanes<W>* qm = lanes_of<W>(b.qm);
   Lanes<W>* visit = lanes_of<W>(b.visit);
-  unsigned long long tail = 0, mf = 0, mu = 0;
-  for (int l = 0; l < nl; ++l) {
-    const int32_t s = b.lane_src[l];
-    Lanes<W> m = front[s];
-    const bool fresh = !lany(m);
-    m.w[l >> 6] |= 1ull << (l & 63);
-    front[s] = m;
-    if (fresh) {
-      b.qv[tail++] = s;
-      mf += static_cast<unsigned long long>(g.rowptr[s + 1] - g.rowptr[s]);
-    }
-    if (SK != kSigmaNone)
-      reinterpret_cast<T*>(b.sigma)[static_cast<int64_t>(s) * (64 * W) + l] = T(1);
+  const int l = static_cast<int>(threadIdx.x);
+  const bool live = l < nl;
+  const int32_t s = live ? b.lane_src[l] : -1;
+  src[l] = s;
+  if (l < 2) sums[l] = 0ull;
+  __syncthreads();
+  if (live) {
+    atomicOr(reinterpret_cast<unsigned long long*>(&front[s].w[l >> 6]), 1ull << (l & 63));
+    if (SK != kSigmaNone) reinterpret_cast<T*>(b.sigma)[static_cast<int64_t>(s) * (64 * W) + l] = T(1);
     if (dist) dist[static_cast<int64_t>(l) * ld + s] = 0;
   }
-  for (unsigned long long i = 0; i < tail; ++i) {
-    const int32_t s = b.qv[i];
-    const Lanes<W> m = front[s];
-    qm[i] = m;
-    visit[s] = m;
-    if (leq(m, act)) mu += static_cast<unsigned long long>(g.in_rowptr[s + 1] - g.in_rowptr[s]);
+  bool first = live;
+  for (int j = 0; j < l && first; ++j) first = src[j] != s;
+  const unsigned bal = __ballot_sync(kFull, first);
+  if (lane_id() == 0) firsts[l >> 5] = static_cast<unsigned>(__popc(bal));
+  __syncthreads();  // also completes every lane's OR before the lane sets are read
+  unsigned pos = static_cast<unsigned>(__popc(bal & ((1u << lane_id()) - 1u)));
+  unsigned total = 0;
+  for (int wi = 0; wi < kWideLanes / kWarp; ++wi) {
+    if (wi < (l >> 5)) pos += firsts[wi];
+    total += firsts[wi];
   }
+  if (first) {
+    const Lanes<W> m = front[s];
+    b.qv[pos] = s;
+    qm[pos] = m;
+    visit[s] = m;
+    atomicAdd(&sums[0], static_cast<unsigned long long>(g.rowptr[s + 1] - g.rowptr[s]));
+    if (leq(m, act))
+      atomicAdd(&sums[1], static_cast<unsigned long long>(g.in_rowptr[s + 1] - g.in_rowptr[s]));
+  }
+  __syncthreads();
+  if (l != 0) return;
   BatchCtl* c = b.ctl;
   c->lo = 0;
-  c->hi = tail;
-  c->tail = tail;
+  c->hi = total;
+  c->tail = total;
   c->mf = 0;
-  c->mf_cur = mf;
-  c->mu_done = mu;
+  c->mf_cur = sums[0];
+  c->mu_done = sums[1];
   c->cap = cap;
   c->level = 0;
   c->maxlevel = 0;
@@ -718,7 +736,7 @@ __global__ void k_ms_init(DevGraph g, MsBuffers b, int nl, Lanes<W> act, unsigne
   c->bu_levels = 0;
   c->runaway = 0;
   b.lvl_off[0] = 0;
-  b.lvl_off[1] = tail;
+  b.lvl_off[1] = total;
 }
 
 // ---------------------------------------------------------------------------
@@ -1743,13 +1761,13 @@ int ms_init(cudaStream_t s, const DevGraph& g, const MsBuffers& b, int nlanes, i
     const Lanes<2> a = lane_cast<2>(act);
     switch (sigma_kind) {
       case kSigmaU64:
-        k_ms_init<kSigmaU64, 2><<<1, 32, 0, s>>>(g, b, nlanes, a, b.cap, sigma_limit, nullptr, 0);
+        k_ms_init<kSigmaU64, 2><<<1, kWideLanes, 0, s>>>(g, b, nlanes, a, b.cap, sigma_limit, nullptr, 0);
         break;
       case kSigmaF64:
-        k_ms_init<kSigmaF64, 2><<<1, 32, 0, s>>>(g, b, nlanes, a, b.cap, ~0ull, nullptr, 0);
+        k_ms_init<kSigmaF64, 2><<<1, kWideLanes, 0, s>>>(g, b, nlanes, a, b.cap, ~0ull, nullptr, 0);
         break;
       default:
-        k_ms_init<kSigmaNone, 2><<<1, 32, 0, s>>>(g, b, nlanes, a, b.cap, ~0ull, nullptr, 0);
+        k_ms_init<kSigmaNone, 2><<<1, kWideLanes, 0, s>>>(g, b, nlanes, a, b.cap, ~0ull, nullptr, 0);
         break;
     }
     return 1;
@@ -1757,13 +1775,13 @@ int ms_init(cudaStream_t s, const DevGraph& g, const MsBuffers& b, int nlanes, i
   const Lanes<1> a = lane_cast<1>(act);
   switch (sigma_kind) {
     case kSigmaU64:
-      k_ms_init<kSigmaU64, 1><<<1, 32, 0, s>>>(g, b, nlanes, a, b.cap, sigma_limit, dist, dist_ld);
+      k_ms_init<kSigmaU64, 1><<<1, kWideLanes, 0, s>>>(g, b, nlanes, a, b.cap, sigma_limit, dist, dist_ld);
       break;
     case kSigmaF64:
-      k_ms_init<kSigmaF64, 1><<<1, 32, 0, s>>>(g, b, nlanes, a, b.cap, ~0ull, dist, dist_ld);
+      k_ms_init<kSigmaF64, 1><<<1, kWideLanes, 0, s>>>(g, b, nlanes, a, b.cap, ~0ull, dist, dist_ld);
       break;
     default:
-      k_ms_init<kSigmaNone, 1><<<1, 32, 0, s>>>(g, b, nlanes, a, b.cap, ~0ull, dist, dist_ld);
+      k_ms_init<kSigmaNone, 1><<<1, kWideLanes, 0, s>>>(g, b, nlanes, a, b.cap, ~0ull, dist, dist_ld);
       break;
   }
   return 1;
