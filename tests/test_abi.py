@@ -60,3 +60,34 @@ def test_no_cpu_fallback_without_gpu():
     with pytest.raises(lgbc.LGBCError) as ei:
         lgbc.betweenness_centrality(g)
     assert "CUDA" in str(ei.value) or "device" in str(ei.value)
+
+
+def _struct_fields(header_text, name):
+    """(type, field) pairs of `typedef struct name { ... } name;` in a header."""
+    text = re.sub(r"/\*.*?\*/", "", header_text, flags=re.S)
+    m = re.search(r"typedef\s+struct\s+" + name + r"\s*\{(.*?)\}\s*" + name + ";", text, flags=re.S)
+    assert m, name
+    return [tuple(f.split()) for f in (x.strip() for x in m.group(1).split(";")) if f]
+
+
+def test_tuning_struct_matches_header():
+    # the Python mirror of lgbc_tuning must have the header's fields, in order,
+    # with the same C types, so that lgbc_get_tuning / lgbc_set_tuning agree
+    text = open(os.path.join(ROOT, "include", "lgbc.h")).read()
+    fields = _struct_fields(text, "lgbc_tuning")
+    ctypes_of = {"double": ctypes.c_double, "int32_t": ctypes.c_int32}
+    assert [f for _, f in fields] == [n for n, _ in _lib.LgbcTuning._fields_]
+    assert [ctypes_of[t] for t, _ in fields] == [c for _, c in _lib.LgbcTuning._fields_]
+    assert "hub_order" in dict(_lib.LgbcTuning._fields_)
+
+
+def test_bench_bytes_model():
+    # the roofline numerator of the default workload (R-MAT 20, 2,549 active
+    # sources): 20 batches of 128 (or 40 of 64) CSR passes + 32 n bytes per source
+    import sys
+    sys.path.insert(0, ROOT)
+    import bench
+    n, nnz, k = 1 << 20, 31401246, 2549
+    assert bench.bc_algorithmic_bytes(n, nnz, k, 128) == 20 * (8 * nnz + 32 * n + 16) + 32 * n * k
+    assert bench.bc_algorithmic_bytes(n, nnz, k, 128) == 91225535488
+    assert bench.bc_algorithmic_bytes(n, nnz, k, 64) == 40 * (8 * nnz + 32 * n + 16) + 32 * n * k
