@@ -323,6 +323,10 @@ MsBuffers ms_buffers(lgbc_graph* g, const int32_t* lane_src, const double* lane_
   b.lane_w_n = 0;
   b.claim = w.claim;
   b.words = 1;
+  // lanes die at reachability boundaries in digraphs (every vertex a source
+  // cannot reach); on undirected graphs with one giant component the filter
+  // costs more than it skips
+  b.lane_filter = g->directed ? 1 : 0;
   return b;
 }
 

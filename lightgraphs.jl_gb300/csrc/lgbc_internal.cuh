@@ -47,6 +47,10 @@ struct BatchCtl {
   unsigned long long td_levels;   // levels expanded top-down / bottom-up by a
   unsigned long long bu_levels;   //   device-driven level loop
   int runaway;                    // a device-driven loop reached its level cap
+  // lanes present in the current frontier Q_L (a superset is allowed): a lane
+  // outside it discovers nothing at level L + 1, so bottom-up scans skip it
+  unsigned long long front_union[kMaxWords];
+  unsigned long long next_union[kMaxWords];  // lanes of Q_{L+1}, accumulated after its appends
 };
 
 // ---------------------------------------------------------------------------

@@ -52,6 +52,7 @@ struct MsBuffers {
                                 // weights per copy (vertex v uses row v / lane_w_n; one word)
   unsigned* claim;              // n, two-word batches: top-down first-discovery flags, kept zero
   int words;                    // 64-bit lane words per vertex: 1 or 2
+  int lane_filter;              // 1: bottom-up levels skip lanes absent from the frontier
 };
 
 // The active lanes of a batch (word 1 unused in a one-word batch).

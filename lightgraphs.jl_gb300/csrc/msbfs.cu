@@ -128,6 +128,13 @@ template <int W> __device__ __forceinline__ const Lanes<W>* lanes_of(const uint6
 template <int W> __device__ __forceinline__ Lanes<W>* mbw(const MsBuffers& b, int level) {
   return lanes_of<W>(mb_at(b, level));
 }
+// The lanes present in the current frontier (BatchCtl::front_union).
+template <int W> __device__ __forceinline__ Lanes<W> frontier_lanes(const BatchCtl* c) {
+  Lanes<W> r;
+#pragma unroll
+  for (int j = 0; j < W; ++j) r.w[j] = c->front_union[j];
+  return r;
+}
 
 template <int SK> struct Sig;
 template <> struct Sig<kSigmaNone> {
@@ -735,6 +742,10 @@ __global__ void __launch_bounds__(kWideLanes) k_ms_init(DevGraph g, MsBuffers b,
   c->td_levels = 0;
   c->bu_levels = 0;
   c->runaway = 0;
+  for (int j = 0; j < kMaxWords; ++j) {
+    c->front_union[j] = j < W ? act.w[j < W ? j : 0] : 0ull;
+    c->next_union[j] = 0ull;
+  }
   b.lvl_off[0] = 0;
   b.lvl_off[1] = total;
 }
@@ -858,7 +869,7 @@ __global__ void __launch_bounds__(256, 4) k_ms_td_settle(DevGraph g, MsBuffers b
 // vertices, so its discoveries are appended with one atomic.  Hubs are left
 // to k_ms_hub_pull.
 // ---------------------------------------------------------------------------
-template <int SK, bool DIST, int W>
+template <int SK, bool DIST, int W, bool LF>
 __global__ void __launch_bounds__(256, 4) k_ms_bu(DevGraph g, MsBuffers b, HubData hd, Lanes<W> act,
                                                int32_t* dist, int64_t ld) {
   using T = typename Sig<SK>::T;
@@ -872,16 +883,23 @@ __global__ void __launch_bounds__(256, 4) k_ms_bu(DevGraph g, MsBuffers b, HubDa
   const int ln = lane_id();
   unsigned long long mf = 0, mu = 0, smax = 0;
   // the lanes each of the warp's 32 vertices discovers, kept in shared memory
-  // rather than in registers across the candidate loop
+  // rather than in registers across the candidate loop; with LF the lanes of
+  // the frontier are read once per block and bound the wanted lanes
   __shared__ Lanes<W> found_of[kWarpsPerBlock][kWarp];
+  __shared__ Lanes<W> live;
   Lanes<W>* my_found = found_of[threadIdx.x >> 5];
+  if (LF) {
+    if (threadIdx.x == 0) live = frontier_lanes<W>(c);
+    __syncthreads();
+  }
   for (int64_t base = gwarp() * kWarp; base < n; base += nwarps() * kWarp) {
     const int64_t wme = base + ln;
     bool cand = false;
     my_found[ln] = lz<W>();
     if (wme < n) {
       const int64_t d = g.in_rowptr[wme + 1] - g.in_rowptr[wme];
-      cand = !leq(visit[wme], act) && d > 0 && d <= hd.hub_degree;
+      cand = (LF ? lany(land(lminus(act, visit[wme]), live)) : !leq(visit[wme], act)) && d > 0 &&
+             d <= hd.hub_degree;
     }
     unsigned cb = __ballot_sync(kFull, cand);
     __syncwarp();
@@ -889,7 +907,7 @@ __global__ void __launch_bounds__(256, 4) k_ms_bu(DevGraph g, MsBuffers b, HubDa
       const int j = __ffs(cb) - 1;
       cb &= cb - 1;
       const int32_t w = static_cast<int32_t>(base + j);
-      const Lanes<W> want = lminus(act, visit[w]);
+      const Lanes<W> want = LF ? land(lminus(act, visit[w]), live) : lminus(act, visit[w]);
       T a[2 * W];
       zero_accs(a);
       const Lanes<W> nm = pull_range<SK, W>(g.in_colidx, g.in_rowptr[w], g.in_rowptr[w + 1], want,
@@ -931,7 +949,7 @@ __global__ void __launch_bounds__(256, 4) k_ms_bu(DevGraph g, MsBuffers b, HubDa
 // bottom-up phase (BU == true: the hub is not finished, want = unvisited
 // lanes).  Partial sums go to the hub's slot; its last item stores sigma and,
 // bottom-up, appends the hub to the next level.
-template <int SK, bool DIST, bool BU, int W>
+template <int SK, bool DIST, bool BU, int W, bool LF>
 __global__ void __launch_bounds__(256, 4) k_ms_hub_pull(DevGraph g, MsBuffers b, HubData hd,
                                                      Lanes<W> act, int32_t* dist, int64_t ld) {
   using T = typename Sig<SK>::T;
@@ -948,9 +966,12 @@ __global__ void __launch_bounds__(256, 4) k_ms_hub_pull(DevGraph g, MsBuffers b,
     const int32_t h = I.v;
     Lanes<W> vis = lz<W>(), want;
     if (BU) {
+      // every item of a hub reads the same visit[h] and frontier lanes, so
+      // all of them skip it or none does (the last-item count stays whole)
       vis = visit[h];
-      if (leq(vis, act)) continue;
       want = lminus(act, vis);
+      if (LF) want = land(want, frontier_lanes<W>(c));
+      if (!lany(want)) continue;
     } else {
       want = next[h];
       if (!lany(want)) continue;
@@ -1015,15 +1036,37 @@ __global__ void __launch_bounds__(256, 4) k_ms_hub_pull(DevGraph g, MsBuffers b,
 
 // After a level: clear the old frontier's dense masks (kept when the forward
 // sweep just ended, because the backward sweep starts from them).
-template <int W>
+// Also ORs the lane sets of the new level Q_{L+1} = list[hi, tail) into
+// ctl->next_union (per block in shared memory, then only bits not yet set).
+template <int W, bool LF>
 __global__ void k_ms_clear_front(MsBuffers b) {
+  __shared__ unsigned long long blk[W];
   BatchCtl* c = b.ctl;
-  if (c->tail == c->hi) return;
-  const unsigned long long lo = c->lo, hi = c->hi;
+  if (c->tail == c->hi) return;  // uniform: the sweep ended
+  const unsigned long long lo = c->lo, hi = c->hi, tail = c->tail;
   Lanes<W>* front = mbw<W>(b, c->level);
-  for (unsigned long long i = lo + blockIdx.x * blockDim.x + threadIdx.x; i < hi;
-       i += static_cast<unsigned long long>(gridDim.x) * blockDim.x)
+  const unsigned long long stride = static_cast<unsigned long long>(gridDim.x) * blockDim.x;
+  for (unsigned long long i = lo + blockIdx.x * blockDim.x + threadIdx.x; i < hi; i += stride)
     front[b.qv[i]] = lz<W>();
+  if (!LF) return;
+  if (threadIdx.x < W) blk[threadIdx.x] = 0ull;
+  __syncthreads();
+  const Lanes<W>* qm = lanes_of<W>(b.qm);
+  Lanes<W> u = lz<W>();
+  for (unsigned long long i = hi + blockIdx.x * blockDim.x + threadIdx.x; i < tail; i += stride)
+    u = lor(u, qm[i]);
+  u = lwarp_or(u);
+  if (lane_id() == 0) {
+#pragma unroll
+    for (int j = 0; j < W; ++j)
+      if (u.w[j]) atomicOr(&blk[j], u.w[j]);
+  }
+  __syncthreads();
+  if (threadIdx.x < W) {
+    const unsigned long long mine = blk[threadIdx.x];
+    const unsigned long long have = *reinterpret_cast<volatile unsigned long long*>(&c->next_union[threadIdx.x]);
+    if (mine & ~have) atomicOr(&c->next_union[threadIdx.x], mine);
+  }
 }
 
 __device__ __forceinline__ void advance_step(const MsBuffers& b, int64_t n);
@@ -1099,6 +1142,10 @@ __device__ __forceinline__ void advance_step(const MsBuffers& b, int64_t n) {
   c->level = L + 1;
   c->mf_cur = c->mf;
   c->mf = 0;
+  for (int j = 0; j < kMaxWords; ++j) {
+    c->front_union[j] = c->next_union[j];
+    c->next_union[j] = 0ull;
+  }
   if (c->cap - c->tail < static_cast<unsigned long long>(n)) c->overflow_list = 1;
 }
 
@@ -1287,10 +1334,11 @@ __global__ void __launch_bounds__(256, W == 1 ? 3 : 2) k_ms_td_settle_seg(DevGra
   }
 }
 
-template <int SK, int W>
+template <int SK, int W, bool LF>
 __global__ void __launch_bounds__(256, W == 1 ? 3 : 2) k_ms_bu_seg(DevGraph g, MsBuffers b, HubData hd, Lanes<W> act) {
   using T = typename Sig<SK>::T;
   BatchCtl* c = b.ctl;
+  const Lanes<W> fl = LF ? frontier_lanes<W>(c) : act;
   const int L = c->level;
   const Lanes<W>* __restrict__ front = mbw<W>(b, L);
   Lanes<W>* next = mbw<W>(b, L + 1);
@@ -1308,10 +1356,10 @@ __global__ void __launch_bounds__(256, W == 1 ? 3 : 2) k_ms_bu_seg(DevGraph g, M
       vis = visit[wme];
       e0 = g.in_rowptr[wme];
       deg = g.in_rowptr[wme + 1] - e0;
-      cand = !leq(vis, act) && deg > 0 && deg <= hd.hub_degree;
+      cand = lany(land(lminus(act, vis), fl)) && deg > 0 && deg <= hd.hub_degree;
     }
     Lanes<W> my_nm = lz<W>();
-    seg_gather<T, T, false, W>(cand, e0, static_cast<int>(cand ? deg : 0), lminus(act, vis),
+    seg_gather<T, T, false, W>(cand, e0, static_cast<int>(cand ? deg : 0), land(lminus(act, vis), fl),
                                g.in_colidx, front, reinterpret_cast<const T*>(b.sigma),
                                [&](int j, const Lanes<W>& nm, const T (&a)[2 * W]) {
                                  if (lany(nm))
@@ -1748,6 +1796,10 @@ __global__ void k_ms_init_seeds_ctl(MsBuffers b, long long nseeds, unsigned long
   c->td_levels = 0;
   c->bu_levels = 0;
   c->runaway = 0;
+  for (int j = 0; j < kMaxWords; ++j) {
+    c->front_union[j] = ~0ull;  // every lane may be seeded
+    c->next_union[j] = 0ull;
+  }
   b.lvl_off[0] = 0;
   b.lvl_off[1] = static_cast<unsigned long long>(nseeds);
 }
@@ -1834,7 +1886,7 @@ int ms_premark(const LaunchCfg& c, cudaStream_t s, const MsBuffers& b, const int
 
 namespace {
 
-template <int W>
+template <int W, bool LF>
 int topdown_w(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
               const HubData& hd, const Lanes<W>& act, int sigma_kind, int32_t* dist,
               int64_t dist_ld) {
@@ -1860,8 +1912,8 @@ int topdown_w(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuf
     else
       k_ms_td_settle<kSigmaU64, false, W><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
     if (hd.n_in > 0) {
-      k_ms_hub_pull<kSigmaU64, false, false, W><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist,
-                                                                          dist_ld);
+      k_ms_hub_pull<kSigmaU64, false, false, W, false><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist,
+                                                                                 dist_ld);
       ++launches;
     }
   } else {
@@ -1870,17 +1922,17 @@ int topdown_w(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuf
     else
       k_ms_td_settle<kSigmaF64, false, W><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
     if (hd.n_in > 0) {
-      k_ms_hub_pull<kSigmaF64, false, false, W><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist,
-                                                                          dist_ld);
+      k_ms_hub_pull<kSigmaF64, false, false, W, false><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist,
+                                                                                 dist_ld);
       ++launches;
     }
   }
   ++launches;
-  k_ms_clear_front<W><<<c.grid, c.block, 0, s>>>(b);
+  k_ms_clear_front<W, LF><<<c.grid, c.block, 0, s>>>(b);
   return launches + 1;
 }
 
-template <int W>
+template <int W, bool LF>
 int bottomup_w(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
                const HubData& hd, const Lanes<W>& act, int sigma_kind, int32_t* dist,
                int64_t dist_ld) {
@@ -1888,47 +1940,48 @@ int bottomup_w(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBu
   if (sigma_kind == kSigmaNone) {
     if constexpr (W == 1) {
       if (dist)
-        k_ms_bu<kSigmaNone, true, 1><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
+        k_ms_bu<kSigmaNone, true, 1, LF><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
       else
-        k_ms_bu<kSigmaNone, false, 1><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
+        k_ms_bu<kSigmaNone, false, 1, LF><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
       if (hd.n_in > 0) {
         if (dist)
-          k_ms_hub_pull<kSigmaNone, true, true, 1><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist,
-                                                                             dist_ld);
+          k_ms_hub_pull<kSigmaNone, true, true, 1, LF><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist,
+                                                                                 dist_ld);
         else
-          k_ms_hub_pull<kSigmaNone, false, true, 1><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist,
-                                                                              dist_ld);
+          k_ms_hub_pull<kSigmaNone, false, true, 1, LF><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist,
+                                                                                  dist_ld);
         ++launches;
       }
     } else {
-      k_ms_bu<kSigmaNone, false, W><<<c.grid, c.block, 0, s>>>(g, b, hd, act, nullptr, 0);
+      k_ms_bu<kSigmaNone, false, W, LF><<<c.grid, c.block, 0, s>>>(g, b, hd, act, nullptr, 0);
       if (hd.n_in > 0) {
-        k_ms_hub_pull<kSigmaNone, false, true, W><<<c.grid, c.block, 0, s>>>(g, b, hd, act, nullptr, 0);
+        k_ms_hub_pull<kSigmaNone, false, true, W, LF><<<c.grid, c.block, 0, s>>>(g, b, hd, act, nullptr,
+                                                                                0);
         ++launches;
       }
     }
   } else if (sigma_kind == kSigmaU64) {
     if (hd.segmented)
-      k_ms_bu_seg<kSigmaU64, W><<<c.grid, c.block, 0, s>>>(g, b, hd, act);
+      k_ms_bu_seg<kSigmaU64, W, LF><<<c.grid, c.block, 0, s>>>(g, b, hd, act);
     else
-      k_ms_bu<kSigmaU64, false, W><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
+      k_ms_bu<kSigmaU64, false, W, LF><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
     if (hd.n_in > 0) {
-      k_ms_hub_pull<kSigmaU64, false, true, W><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist,
-                                                                         dist_ld);
+      k_ms_hub_pull<kSigmaU64, false, true, W, LF><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist,
+                                                                             dist_ld);
       ++launches;
     }
   } else {
     if (hd.segmented)
-      k_ms_bu_seg<kSigmaF64, W><<<c.grid, c.block, 0, s>>>(g, b, hd, act);
+      k_ms_bu_seg<kSigmaF64, W, LF><<<c.grid, c.block, 0, s>>>(g, b, hd, act);
     else
-      k_ms_bu<kSigmaF64, false, W><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
+      k_ms_bu<kSigmaF64, false, W, LF><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
     if (hd.n_in > 0) {
-      k_ms_hub_pull<kSigmaF64, false, true, W><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist,
-                                                                         dist_ld);
+      k_ms_hub_pull<kSigmaF64, false, true, W, LF><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist,
+                                                                             dist_ld);
       ++launches;
     }
   }
-  k_ms_clear_front<W><<<c.grid, c.block, 0, s>>>(b);
+  k_ms_clear_front<W, LF><<<c.grid, c.block, 0, s>>>(b);
   return launches + 1;
 }
 
@@ -1966,15 +2019,25 @@ int backward_body_w(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const
 int ms_topdown(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
                const HubData& hd, const LaneSet& act, int sigma_kind, int32_t* dist,
                int64_t dist_ld) {
-  if (b.words == 2) return topdown_w<2>(c, s, g, b, hd, lane_cast<2>(act), sigma_kind, dist, dist_ld);
-  return topdown_w<1>(c, s, g, b, hd, lane_cast<1>(act), sigma_kind, dist, dist_ld);
+  if (b.words == 2)
+    return b.lane_filter
+               ? topdown_w<2, true>(c, s, g, b, hd, lane_cast<2>(act), sigma_kind, dist, dist_ld)
+               : topdown_w<2, false>(c, s, g, b, hd, lane_cast<2>(act), sigma_kind, dist, dist_ld);
+  return b.lane_filter
+             ? topdown_w<1, true>(c, s, g, b, hd, lane_cast<1>(act), sigma_kind, dist, dist_ld)
+             : topdown_w<1, false>(c, s, g, b, hd, lane_cast<1>(act), sigma_kind, dist, dist_ld);
 }
 
 int ms_bottomup(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
                 const HubData& hd, const LaneSet& act, int sigma_kind, int32_t* dist,
                 int64_t dist_ld) {
-  if (b.words == 2) return bottomup_w<2>(c, s, g, b, hd, lane_cast<2>(act), sigma_kind, dist, dist_ld);
-  return bottomup_w<1>(c, s, g, b, hd, lane_cast<1>(act), sigma_kind, dist, dist_ld);
+  if (b.words == 2)
+    return b.lane_filter
+               ? bottomup_w<2, true>(c, s, g, b, hd, lane_cast<2>(act), sigma_kind, dist, dist_ld)
+               : bottomup_w<2, false>(c, s, g, b, hd, lane_cast<2>(act), sigma_kind, dist, dist_ld);
+  return b.lane_filter
+             ? bottomup_w<1, true>(c, s, g, b, hd, lane_cast<1>(act), sigma_kind, dist, dist_ld)
+             : bottomup_w<1, false>(c, s, g, b, hd, lane_cast<1>(act), sigma_kind, dist, dist_ld);
 }
 
 int ms_advance(cudaStream_t s, const DevGraph& g, const MsBuffers& b) {
