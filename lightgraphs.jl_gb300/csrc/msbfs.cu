@@ -743,7 +743,7 @@ __global__ void __launch_bounds__(kWideLanes) k_ms_init(DevGraph g, MsBuffers b,
   c->bu_levels = 0;
   c->runaway = 0;
   for (int j = 0; j < kMaxWords; ++j) {
-    c->front_union[j] = j < W ? act.w[j < W ? j : 0] : 0ull;
+    c->front_union[j] = j < W ? act.w[j % W] : 0ull;
     c->next_union[j] = 0ull;
   }
   b.lvl_off[0] = 0;
@@ -1036,8 +1036,9 @@ __global__ void __launch_bounds__(256, 4) k_ms_hub_pull(DevGraph g, MsBuffers b,
 
 // After a level: clear the old frontier's dense masks (kept when the forward
 // sweep just ended, because the backward sweep starts from them).
-// Also ORs the lane sets of the new level Q_{L+1} = list[hi, tail) into
-// ctl->next_union (per block in shared memory, then only bits not yet set).
+// With LF (digraphs) it also ORs the lane sets of the new level Q_{L+1} =
+// list[hi, tail) into ctl->next_union (per block in shared memory, then only
+// the bits not yet set), the frontier lanes of the next bottom-up level.
 template <int W, bool LF>
 __global__ void k_ms_clear_front(MsBuffers b) {
   __shared__ unsigned long long blk[W];
