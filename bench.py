@@ -181,6 +181,15 @@ WORKLOADS = {
 }
 
 
+def dep_dtype(tuning: dict) -> str:
+    """The arithmetic of the timed path: exact uint64 path counts (FP64 after
+    an overflow) and FP64 dependency sums, or double-float ones when the
+    dependency_df32 tuning field is set."""
+    if int(tuning.get("dependency_df32", 0)):
+        return "u64 path counts, df32 dependencies (opt-in, narrower than f64)"
+    return "u64 path counts, f64 dependencies"
+
+
 def parse_tuning(spec: str | None) -> dict:
     """"key=value,..." -> lgbc_tuning overrides (numbers)."""
     out = {}
@@ -461,7 +470,7 @@ def run_ours(args, dist: Dist):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "u64 path counts, df32/f64 dependencies", "data": "synthetic",
+            "dtype": dep_dtype(tuning), "data": "synthetic",
             "config": {"workload": wname, "description": WORKLOADS[args.workload],
                        "n": n, "m": m, "nnz": nnz, "directed": directed, "sources": len(src),
                        "active_sources": k_act, "lanes": tuning["lanes"], "tuning": tuning,
@@ -513,7 +522,7 @@ def run_ours_many(args, dist: Dist):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "u64 path counts, df32/f64 dependencies", "data": "synthetic",
+            "dtype": "u64 path counts, f64 dependencies", "data": "synthetic",
             "config": {"workload": f"ba_many_{len(graphs)}_exact_bc", "description": WORKLOADS["c3"],
                        "graphs": len(graphs), "graphs_per_s": len(graphs) / t},
             "e2e": {"value": value, "unit": UNIT,

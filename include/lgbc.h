@@ -181,7 +181,17 @@ int lgbc_graph_stats(const lgbc_graph *g, lgbc_stats *out);
  *                 position of each item in its hub's row (follows 1 on rows
  *                 sorted by neighbour id, without reading them on the host).
  *                 1 and 2 interleave the hubs so that the items in flight
- *                 gather rows of a limited range of vertices.  Default 2. */
+ *                 gather rows of a limited range of vertices.  Default 2.
+ *   dependency_df32  0: the dependency sums psi = (1 + delta) / sigma and
+ *                 delta = sigma * sum(psi) are FP64, as the reference's
+ *                 Float64 `coeff` and `delta` (src/centrality/betweenness.jl:
+ *                 81-107) -- the default.  1: they are double-float (two
+ *                 FP32 values, a 48-bit significand) -- faster on this GPU,
+ *                 whose FP64 rate is a small fraction of its FP32 rate, and
+ *                 still within 1e-9 of the FP64 result on the tested graphs,
+ *                 but narrower than the reference's type.  Path counts are
+ *                 exact uint64 integers either way (FP64 after an overflow).
+ *                 Not changed by lgbc_tune. */
 typedef struct lgbc_tuning {
   double alpha;
   double beta;
@@ -193,6 +203,7 @@ typedef struct lgbc_tuning {
   int32_t graph_loop;
   int32_t stack_vertices;
   int32_t hub_order;
+  int32_t dependency_df32;
 } lgbc_tuning;
 int lgbc_get_tuning(const lgbc_graph *g, lgbc_tuning *out);
 int lgbc_set_tuning(lgbc_graph *g, const lgbc_tuning *t);

@@ -594,7 +594,7 @@ int run_ms_batch(lgbc_graph* g, const int32_t* lane_src, int nl, int sigma_kind,
       g->launches += 1 + lv + static_cast<int64_t>(c.td_levels) * lg->td_kernels +
                      static_cast<int64_t>(c.bu_levels) * lg->bu_kernels;
       if (c.runaway) return fail(LGBC_ETIMEOUT, "forward sweep exceeded n + 1 levels");
-      if (c.overflow_sigma && sigma_kind == kSigmaU64) {
+      if (c.overflow_sigma && u64_counts(sigma_kind)) {
         g->launches += ms_reset_all(g->stream, dg, b);
         return 1;
       }
@@ -635,7 +635,7 @@ int run_ms_batch(lgbc_graph* g, const int32_t* lane_src, int nl, int sigma_kind,
       // longer than n + 1 levels can only mean a fault
       if (levels > g->n + 1) return fail(LGBC_ETIMEOUT, "forward sweep exceeded n + 1 levels");
       const BatchCtl& c = *g->h_ctl;
-      if (c.overflow_sigma && sigma_kind == kSigmaU64) break;
+      if (c.overflow_sigma && u64_counts(sigma_kind)) break;
       if (c.done) break;
       if (c.overflow_list) {
         regrow = true;
@@ -649,7 +649,7 @@ int run_ms_batch(lgbc_graph* g, const int32_t* lane_src, int nl, int sigma_kind,
       g->launches += ms_reset_all(g->stream, dg, ms_buffers(g, lane_src));
       continue;
     }
-    if (g->h_ctl->overflow_sigma && sigma_kind == kSigmaU64) {
+    if (g->h_ctl->overflow_sigma && u64_counts(sigma_kind)) {
       g->launches += ms_reset_all(g->stream, dg, b);
       return 1;
     }
@@ -700,7 +700,7 @@ int run_betweenness(lgbc_graph* g, int64_t k_act, int endpoints, double* bc_dev,
   for (int64_t s0 = 0; s0 < k_act; s0 += lanes) {
     const int nl = static_cast<int>(std::min<int64_t>(lanes, k_act - s0));
     const double* lw = d_w ? d_w + s0 : nullptr;
-    int rc = run_ms_batch(g, g->d_src + s0, nl, kSigmaU64, bc_dev, nullptr, 0, Seeds(), lw);
+    int rc = run_ms_batch(g, g->d_src + s0, nl, dep_kind(g), bc_dev, nullptr, 0, Seeds(), lw);
     if (rc == 1) {
       g->stats.wide_batches++;
       rc = run_ms_batch(g, g->d_src + s0, nl, kSigmaF64, bc_dev, nullptr, 0, Seeds(), lw);
@@ -931,7 +931,7 @@ int run_stacked(lgbc_graph* g, int64_t copies, double* bc_dev, const std::vector
       sd.lane_w_n = n;
       sd.lane_w_count = copies * row;
     }
-    int rc = run_ms_batch(st, nullptr, L, kSigmaU64, st->d_bc, nullptr, 0, sd, lw);
+    int rc = run_ms_batch(st, nullptr, L, dep_kind(st), st->d_bc, nullptr, 0, sd, lw);
     if (rc == 1) {
       g->stats.wide_batches++;
       rc = run_ms_batch(st, nullptr, L, kSigmaF64, st->d_bc, nullptr, 0, sd, lw);
@@ -1056,6 +1056,7 @@ int create_impl(lgbc_graph* g, int64_t n, int64_t nnz, const int64_t* rowptr, co
   LGBC_TRY(check_launch(g));
   if (bad & 1) return fail(LGBC_EINVAL, "rowptr must be non-decreasing");
   if (bad & 2) return fail(LGBC_EINVAL, "column index out of range");
+  if (bad & 4) return fail(LGBC_EINVAL, "rowptr must run from 0 to nnz");
   return build_hubs(g, rowptr, colidx, directed ? in_rowptr : rowptr, directed ? in_colidx : colidx,
                     g->tune.hub_degree, g->tune.hub_order);
 }
@@ -1381,10 +1382,12 @@ int lgbc_set_tuning(lgbc_graph* g, const lgbc_tuning* t) {
   if (!(t->alpha > 0) || !(t->beta > 0) || t->lanes < 1 || t->lanes > kWideLanes ||
       t->hub_degree < 1 || t->dense_edges < 0 || t->segment_degree < 0 ||
       (t->source_order != 0 && t->source_order != 1) || (t->graph_loop != 0 && t->graph_loop != 1) ||
-      t->stack_vertices < 0 || t->hub_order < 0 || t->hub_order > 2)
+      t->stack_vertices < 0 || t->hub_order < 0 || t->hub_order > 2 ||
+      (t->dependency_df32 != 0 && t->dependency_df32 != 1))
     return fail(LGBC_EINVAL,
                 "tuning out of range (alpha, beta > 0; 1 <= lanes <= 128; hub_degree >= 1; "
-                "dense_edges, segment_degree, stack_vertices >= 0; hub_order 0..2)");
+                "dense_edges, segment_degree, stack_vertices >= 0; hub_order 0..2; "
+                "dependency_df32 0 or 1)");
   std::lock_guard<std::mutex> lock(g->mu);
   g->tune = *t;
   return LGBC_OK;

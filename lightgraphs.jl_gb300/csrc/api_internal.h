@@ -271,7 +271,7 @@ struct lgbc_graph {
   size_t max_smem = 0;
   unsigned long long sigma_limit = ~0ull;  // (2^64 - 1) / (max in-degree + 1)
   lgbc_stats stats{};
-  lgbc_tuning tune{14.0, 24.0, 256, 128, 32, 0, 1, 1, 1 << 21, 2};
+  lgbc_tuning tune{14.0, 24.0, 256, 128, 32, 0, 1, 1, 1 << 21, 2, 0};
   lgbc_graph* stack = nullptr;        // R copies of this graph (stacked batches)
   int64_t stack_copies = 0;
   std::vector<int32_t> h_active;      // the last call's ordered active sources
@@ -315,6 +315,12 @@ int run_ms_batch(lgbc_graph* g, const int32_t* lane_src, int nl, int sigma_kind,
                  int32_t* dist, int64_t dist_ld, const Seeds& seeds = Seeds(),
                  const double* lane_w = nullptr, const LevelStats* stats = nullptr,
                  unsigned long long* stress = nullptr);
+// The path-count / dependency kind of a Brandes batch on this handle: exact
+// uint64 path counts with FP64 dependencies (default) or, with the
+// dependency_df32 tuning field, double-float dependencies.
+inline int dep_kind(const lgbc_graph* g) {
+  return g->tune.dependency_df32 ? kSigmaU64 : kSigmaU64F64;
+}
 // Brandes over the active sources already on the device (g->d_src[0, k)),
 // accumulating into bc_dev (zeroed here); with d_w, source i's dependencies
 // are scaled by d_w[i].

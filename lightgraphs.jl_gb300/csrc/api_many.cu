@@ -183,7 +183,7 @@ int many_group(const std::vector<ManyGraph>& grp, int endpoints, double* bc_raw_
     sd.seg_off = d_voff;
     sd.seg_mark = d_marks + static_cast<size_t>(b) * grp.size() * W;
     sd.nseg = static_cast<int64_t>(grp.size());
-    int rc = run_ms_batch(g, nullptr, L, kSigmaU64, g->d_bc, nullptr, 0, sd);
+    int rc = run_ms_batch(g, nullptr, L, dep_kind(g), g->d_bc, nullptr, 0, sd);
     if (rc == 1) rc = run_ms_batch(g, nullptr, L, kSigmaF64, g->d_bc, nullptr, 0, sd);
     if (rc != LGBC_OK) return rc;
   }

@@ -74,6 +74,7 @@ extern "C" int lgbc_tune(lgbc_graph* g, const char* cache_path) {
   const std::string sig = tune_signature(g);
   lgbc_tuning cached{};
   if (tune_from_cache(cache_path, sig, &cached)) {
+    cached.dependency_df32 = g->tune.dependency_df32;  // a precision choice, not tuned
     g->tune = cached;
     return LGBC_OK;
   }

@@ -16,10 +16,16 @@ namespace lgbc {
 
 // Path-count representation of a multi-source batch.
 enum SigmaKind : int {
-  kSigmaNone = 0,  // distances only (gdistances_batch)
-  kSigmaU64 = 1,   // exact uint64 path counts, df dependency sums
-  kSigmaF64 = 2,   // FP64 path counts and dependencies (replay after overflow)
+  kSigmaNone = 0,    // distances only (gdistances_batch)
+  kSigmaU64 = 1,     // exact uint64 path counts, double-float (df32) dependency sums (opt-in)
+  kSigmaF64 = 2,     // FP64 path counts and dependencies (replay after overflow)
+  kSigmaU64F64 = 3,  // exact uint64 path counts, FP64 dependencies (the default)
 };
+// The forward sweep only sees the path counts: both uint64 kinds run the same
+// forward kernels.
+constexpr int fwd_kind(int sk) { return sk == kSigmaU64F64 ? kSigmaU64 : sk; }
+// Path counts kept as exact uint64 (an overflow replays the batch in FP64).
+constexpr bool u64_counts(int sk) { return sk == kSigmaU64 || sk == kSigmaU64F64; }
 
 // Landmark vertices (highest degree) whose BFS distances order the sources.
 constexpr int kLandmarks = 16;
@@ -191,7 +197,8 @@ int bfs_configure(size_t max_dyn_smem);
 void set_last_error(const char* msg);
 
 // ---- small utilities: util.cu ----------------------------------------------
-// ORs into *bad: 1 = rowptr decreases somewhere, 2 = a column index is not in [0, n).
+// ORs into *bad: 1 = rowptr decreases somewhere, 2 = a column index is not in
+// [0, n), 4 = rowptr[0] != 0 or rowptr[n] != nnz.
 int validate_csr(const LaunchCfg& c, cudaStream_t s, const int64_t* rowptr, const int32_t* colidx,
                  int64_t n, int64_t nnz, int* bad);
 int fill_i32(const LaunchCfg& c, cudaStream_t s, int32_t* p, int64_t count, int32_t value);

@@ -33,6 +33,7 @@
 #include <algorithm>
 
 #include "lgbc_kernels.h"
+#include "xf64.cuh"
 
 namespace lgbc {
 namespace {
@@ -149,6 +150,15 @@ template <> struct Sig<kSigmaF64> {
   using T = double;
   using Pair = double2;
 };
+template <> struct Sig<kSigmaU64F64> {
+  using T = unsigned long long;
+  using Pair = ulonglong2;
+};
+
+// A path count as an FP64 value (uint64 counts round to nearest, as the
+// reference's Float64 counts do above 2^53).
+__device__ __forceinline__ double sigma_f64(unsigned long long x) { return __ull2double_rn(x); }
+__device__ __forceinline__ double sigma_f64(double x) { return x; }
 
 __device__ __forceinline__ void hub_add(unsigned long long* p, unsigned long long x) {
   atomicAdd(p, x);
@@ -229,6 +239,10 @@ __device__ __forceinline__ df32 acc_done(df32 acc) { return fast_two_sum(acc.hi,
 
 template <class T, class A> __device__ __forceinline__ void acc_row(A& acc, T x);
 template <> __device__ __forceinline__ void acc_row(unsigned long long& acc, unsigned long long x) { acc += x; }
+// FP64 dependencies: psi rows hold binary64 bits, summed in the extended format.
+template <> __device__ __forceinline__ void acc_row(xf64& acc, unsigned long long x) {
+  acc = xf_add_bits(acc, x);
+}
 template <> __device__ __forceinline__ void acc_row(double& acc, double x) { acc += x; }
 template <> __device__ __forceinline__ void acc_row(df32& acc, float2 x) { acc_add(acc, x.x, x.y); }
 
@@ -241,6 +255,7 @@ template <class A> __device__ __forceinline__ A zero_acc();
 template <> __device__ __forceinline__ unsigned long long zero_acc() { return 0ull; }
 template <> __device__ __forceinline__ double zero_acc() { return 0.0; }
 template <> __device__ __forceinline__ df32 zero_acc() { return df32{0.f, 0.f}; }
+template <> __device__ __forceinline__ xf64 zero_acc() { return xf_zero(); }
 
 template <class A, int K> __device__ __forceinline__ void zero_accs(A (&a)[K]) {
 #pragma unroll
@@ -442,6 +457,14 @@ __device__ __forceinline__ void psi_range_f64(const int32_t* __restrict__ ci, in
   psi_range<double, double, W>(ci, e0, e1, F, succ, psi, dense, acc);
 }
 
+template <int W>
+__device__ __forceinline__ void psi_range_x(const int32_t* __restrict__ ci, int64_t e0, int64_t e1,
+                                            const Lanes<W>& F, const Lanes<W>* __restrict__ succ,
+                                            const void* __restrict__ psi, int dense,
+                                            xf64 (&acc)[2 * W]) {
+  psi_range<unsigned long long, xf64, W>(ci, e0, e1, F, succ, psi, dense, acc);
+}
+
 __device__ __forceinline__ int64_t shfl_i64(int64_t x, int src) {
   return static_cast<int64_t>(shfl_u64(static_cast<uint64_t>(x), src));
 }
@@ -574,9 +597,11 @@ __device__ __forceinline__ df32 finish_lane_df(const unsigned long long* srow, f
   return d;
 }
 
-__device__ __forceinline__ double finish_lane_f64(const double* srow, double* prow, int l,
-                                                  double acc) {
-  const double sv = srow[l];
+// FP64 dependencies: delta = sigma * acc and psi = (1 + delta) / sigma in
+// double, sigma read as uint64 (kSigmaU64F64) or double (kSigmaF64) counts.
+template <class ST>
+__device__ __forceinline__ double finish_lane_f64(const ST* srow, double* prow, int l, double acc) {
+  const double sv = sigma_f64(srow[l]);
   const double d = sv * acc;
   prow[l] = (1.0 + d) / sv;
   return d;
@@ -600,18 +625,67 @@ __device__ __forceinline__ df32 finish_df(void* psi, const void* sigma, int32_t 
   return contrib;
 }
 
-template <int W>
+template <int SK, int W>
 __device__ __forceinline__ double finish_f64(void* psi, const void* sigma, int32_t v, unsigned mine,
                                              const double (&acc)[2 * W]) {
+  using ST = typename Sig<SK>::T;
   const int ln = lane_id();
   double contrib = 0.0;
   if (!mine) return contrib;
-  const double* srow = reinterpret_cast<const double*>(sigma) + static_cast<int64_t>(v) * (64 * W);
+  const ST* srow = reinterpret_cast<const ST*>(sigma) + static_cast<int64_t>(v) * (64 * W);
   double* prow = reinterpret_cast<double*>(psi) + static_cast<int64_t>(v) * (64 * W);
 #pragma unroll
   for (int k = 0; k < 2 * W; ++k)
     if (mine & (1u << k)) contrib += finish_lane_f64(srow, prow, 32 * k + ln, acc[k]);
   return contrib;
+}
+
+// FP64 dependencies from an extended psi sum (kSigmaU64F64): with acc =
+// sum of the successors' psi = delta / sigma, psi = 1 / sigma + acc (the
+// reference's coeff, (1 + delta) / sigma) is stored as binary64 and
+// delta = sigma * acc is returned; the path count stays an exact integer.
+__device__ __forceinline__ xf64 finish_lane_x(const unsigned long long* srow,
+                                              unsigned long long* prow, int l, xf64 acc) {
+  const unsigned long long sv = srow[l];
+  prow[l] = xf_to_bits(xf_add(acc, xf_recip_u64(sv)));
+  return xf_mul_u64(acc, sv);
+}
+
+// Finalise this thread's lanes `mine` of v; returns the sum of their deltas
+// (lw: per-lane weights, or null).
+template <int W>
+__device__ __forceinline__ xf64 finish_x(void* psi, const void* sigma, int32_t v, unsigned mine,
+                                         const xf64 (&acc)[2 * W], const double* __restrict__ lw) {
+  const int ln = lane_id();
+  xf64 contrib = xf_zero();
+  if (!mine) return contrib;
+  const unsigned long long* srow =
+      reinterpret_cast<const unsigned long long*>(sigma) + static_cast<int64_t>(v) * (64 * W);
+  unsigned long long* prow = reinterpret_cast<unsigned long long*>(psi) + static_cast<int64_t>(v) * (64 * W);
+#pragma unroll
+  for (int k = 0; k < 2 * W; ++k)
+    if (mine & (1u << k)) {
+      xf64 d = finish_lane_x(srow, prow, 32 * k + ln, acc[k]);
+      if (lw) d = xf_mul(d, xf_from_bits(__double_as_longlong(lw[32 * k + ln])));
+      contrib = xf_add(contrib, d);
+    }
+  return contrib;
+}
+
+__device__ __forceinline__ xf64 warp_sum_x(xf64 a) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const xf64 b{__shfl_xor_sync(kFull, a.m, o), __shfl_xor_sync(kFull, a.e, o)};
+    a = xf_add(a, b);
+  }
+  return a;
+}
+
+// bc[v] += x, rounded once (lane 0 of the warp that owns v at this level).
+__device__ __forceinline__ void bc_add_x(double* bc, int32_t v, xf64 x) {
+  if (x.m == 0) return;
+  unsigned long long* p = reinterpret_cast<unsigned long long*>(bc) + v;
+  *p = xf_to_bits(xf_add_bits(x, *p));
 }
 
 // The lane weights of vertex v (its copy's row in a stacked union; stacked
@@ -639,14 +713,15 @@ __device__ __forceinline__ double finish_df_w(void* psi, const void* sigma, int3
   return contrib;
 }
 
-template <int W>
+template <int SK, int W>
 __device__ __forceinline__ double finish_f64_w(void* psi, const void* sigma, int32_t v,
                                                unsigned mine, const double (&acc)[2 * W],
                                                const double* __restrict__ lw) {
+  using ST = typename Sig<SK>::T;
   const int ln = lane_id();
   double contrib = 0.0;
   if (!mine) return contrib;
-  const double* srow = reinterpret_cast<const double*>(sigma) + static_cast<int64_t>(v) * (64 * W);
+  const ST* srow = reinterpret_cast<const ST*>(sigma) + static_cast<int64_t>(v) * (64 * W);
   double* prow = reinterpret_cast<double*>(psi) + static_cast<int64_t>(v) * (64 * W);
 #pragma unroll
   for (int k = 0; k < 2 * W; ++k)
@@ -1092,7 +1167,7 @@ __global__ void k_loop_advance(MsBuffers b, LoopParams lp) {
   BatchCtl* c = b.ctl;
   if (c->mode) c->bu_levels += 1; else c->td_levels += 1;
   advance_step(b, lp.n);
-  bool stop = c->done || c->overflow_list || (lp.sigma_kind == kSigmaU64 && c->overflow_sigma);
+  bool stop = c->done || c->overflow_list || (u64_counts(lp.sigma_kind) && c->overflow_sigma);
   if (!stop && c->level >= lp.max_levels) {
     c->runaway = 1;
     stop = true;
@@ -1207,12 +1282,19 @@ __global__ void __launch_bounds__(256, W == 1 ? 5 : 4) k_ms_delta(DevGraph g, Ms
         contrib = warp_sum_df(contrib);
         if (ln == 0) bc[v] += df_to_double(contrib);
       }
+    } else if (SK == kSigmaU64F64) {
+      xf64 acc[2 * W];
+      zero_accs(acc);
+      psi_range_x<W>(g.colidx, e0, e1, F, succ, b.psi, hd.dense_edges, acc);
+      const xf64 contrib = warp_sum_x(
+          finish_x<W>(b.psi, b.sigma, v, mine, acc, b.lane_w ? weights_of<W>(b, v) : nullptr));
+      if (ln == 0) bc_add_x(bc, v, contrib);
     } else {
       double acc[2 * W];
       zero_accs(acc);
       psi_range_f64<W>(g.colidx, e0, e1, F, succ, b.psi, hd.dense_edges, acc);
-      double contrib = b.lane_w ? finish_f64_w<W>(b.psi, b.sigma, v, mine, acc, weights_of<W>(b, v))
-                                : finish_f64<W>(b.psi, b.sigma, v, mine, acc);
+      double contrib = b.lane_w ? finish_f64_w<SK, W>(b.psi, b.sigma, v, mine, acc, weights_of<W>(b, v))
+                                : finish_f64<SK, W>(b.psi, b.sigma, v, mine, acc);
       contrib = warp_sum_f64(contrib);
       if (ln == 0) bc[v] += contrib;
     }
@@ -1243,6 +1325,12 @@ __global__ void __launch_bounds__(256, W == 1 ? 5 : 4) k_ms_hub_delta(DevGraph g
       psi_range_df<W>(g.colidx, I.lo, I.hi, F, succ, b.psi, hd.dense_edges, a);
 #pragma unroll
       for (int k = 0; k < 2 * W; ++k) part[k] = df_to_double(a[k]);
+    } else if (SK == kSigmaU64F64) {
+      xf64 a[2 * W];
+      zero_accs(a);
+      psi_range_x<W>(g.colidx, I.lo, I.hi, F, succ, b.psi, hd.dense_edges, a);
+#pragma unroll
+      for (int k = 0; k < 2 * W; ++k) part[k] = __longlong_as_double(static_cast<long long>(xf_to_bits(a[k])));
     } else {
       zero_accs(part);
       psi_range_f64<W>(g.colidx, I.lo, I.hi, F, succ, b.psi, hd.dense_edges, part);
@@ -1269,9 +1357,16 @@ __global__ void __launch_bounds__(256, W == 1 ? 5 : 4) k_ms_hub_delta(DevGraph g
         contrib = warp_sum_df(contrib);
         if (ln == 0) bc[h] += df_to_double(contrib);
       }
+    } else if (SK == kSigmaU64F64) {
+      xf64 d[2 * W];
+#pragma unroll
+      for (int k = 0; k < 2 * W; ++k) d[k] = xf_from_bits(static_cast<unsigned long long>(__double_as_longlong(s[k])));
+      const xf64 contrib = warp_sum_x(
+          finish_x<W>(b.psi, b.sigma, h, mine, d, b.lane_w ? weights_of<W>(b, h) : nullptr));
+      if (ln == 0) bc_add_x(bc, h, contrib);
     } else {
-      double contrib = b.lane_w ? finish_f64_w<W>(b.psi, b.sigma, h, mine, s, weights_of<W>(b, h))
-                                : finish_f64<W>(b.psi, b.sigma, h, mine, s);
+      double contrib = b.lane_w ? finish_f64_w<SK, W>(b.psi, b.sigma, h, mine, s, weights_of<W>(b, h))
+                                : finish_f64<SK, W>(b.psi, b.sigma, h, mine, s);
       contrib = warp_sum_f64(contrib);
       if (ln == 0) bc[h] += contrib;
     }
@@ -1433,12 +1528,21 @@ __global__ void __launch_bounds__(256, W == 1 ? 3 : 2) k_ms_delta_seg(DevGraph g
                                           contrib = warp_sum_df(contrib);
                                           if (ln == 0 && contrib.hi != 0.f) bc[vj] += df_to_double(contrib);
                                         });
+    } else if (SK == kSigmaU64F64) {
+      seg_gather<unsigned long long, xf64, true, W>(
+          mine, e0, dg, F, g.colidx, succ, reinterpret_cast<const unsigned long long*>(b.psi),
+          [&](int j, const Lanes<W>&, const xf64 (&a)[2 * W]) {
+            const int32_t vj = __shfl_sync(kFull, v, j);
+            const xf64 contrib =
+                warp_sum_x(finish_x<W>(b.psi, b.sigma, vj, my_bits(lshfl(F, j)), a, nullptr));
+            if (ln == 0) bc_add_x(bc, vj, contrib);
+          });
     } else {
       seg_gather<double, double, true, W>(mine, e0, dg, F, g.colidx, succ,
                                           reinterpret_cast<const double*>(b.psi),
                                           [&](int j, const Lanes<W>&, const double (&a)[2 * W]) {
                                             const int32_t vj = __shfl_sync(kFull, v, j);
-                                            double contrib = finish_f64<W>(b.psi, b.sigma, vj,
+                                            double contrib = finish_f64<SK, W>(b.psi, b.sigma, vj,
                                                                            my_bits(lshfl(F, j)), a);
                                             contrib = warp_sum_f64(contrib);
                                             if (ln == 0 && contrib != 0.0) bc[vj] += contrib;
@@ -1809,6 +1913,7 @@ __global__ void k_ms_init_seeds_ctl(MsBuffers b, long long nseeds, unsigned long
 
 int ms_init(cudaStream_t s, const DevGraph& g, const MsBuffers& b, int nlanes, int sigma_kind,
             unsigned long long sigma_limit, int32_t* dist, int64_t dist_ld) {
+  sigma_kind = fwd_kind(sigma_kind);
   const LaneSet act = lane_set(nlanes, b.words);
   if (b.words == 2) {
     const Lanes<2> a = lane_cast<2>(act);
@@ -1868,6 +1973,7 @@ void init_seeds_w(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const M
 int ms_init_seeds(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
                   const int32_t* seed_v, const uint64_t* seed_mask, int64_t nseeds, int sigma_kind,
                   unsigned long long sigma_limit, int32_t* dist, int64_t dist_ld) {
+  sigma_kind = fwd_kind(sigma_kind);
   cudaMemsetAsync(b.ctl, 0, sizeof(BatchCtl), s);
   if (b.words == 2)
     init_seeds_w<2>(c, s, g, b, seed_v, seed_mask, nseeds, sigma_kind, sigma_limit, nullptr, 0);
@@ -1993,7 +2099,16 @@ int backward_body_w(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const
   k_ms_back_clear<W><<<c.grid, c.block, 0, s>>>(b);
   // the segmented variant has no weighted finalisation
   const bool seg = hd.segmented && !b.lane_w;
-  if (sigma_kind == kSigmaF64) {
+  if (sigma_kind == kSigmaU64F64) {
+    if (seg)
+      k_ms_delta_seg<kSigmaU64F64, W><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
+    else
+      k_ms_delta<kSigmaU64F64, W><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
+    if (hd.n_out > 0) {
+      k_ms_hub_delta<kSigmaU64F64, W><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
+      ++launches;
+    }
+  } else if (sigma_kind == kSigmaF64) {
     if (seg)
       k_ms_delta_seg<kSigmaF64, W><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
     else
@@ -2020,6 +2135,7 @@ int backward_body_w(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const
 int ms_topdown(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
                const HubData& hd, const LaneSet& act, int sigma_kind, int32_t* dist,
                int64_t dist_ld) {
+  sigma_kind = fwd_kind(sigma_kind);
   if (b.words == 2)
     return b.lane_filter
                ? topdown_w<2, true>(c, s, g, b, hd, lane_cast<2>(act), sigma_kind, dist, dist_ld)
@@ -2032,6 +2148,7 @@ int ms_topdown(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBu
 int ms_bottomup(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
                 const HubData& hd, const LaneSet& act, int sigma_kind, int32_t* dist,
                 int64_t dist_ld) {
+  sigma_kind = fwd_kind(sigma_kind);
   if (b.words == 2)
     return b.lane_filter
                ? bottomup_w<2, true>(c, s, g, b, hd, lane_cast<2>(act), sigma_kind, dist, dist_ld)

@@ -28,12 +28,15 @@ __global__ void k_add_sources(double* bc, const int32_t* src, int64_t k, double 
     atomicAdd(bc + src[i], extra);
 }
 
-// Flags (bit 0) a decreasing rowptr step and (bit 1) a column index outside
-// [0, n); the host rejects the graph when any bit is set.
+// Flags (bit 0) a decreasing rowptr step, (bit 1) a column index outside
+// [0, n) and (bit 2) a rowptr that does not start at 0 or end at nnz; the
+// host rejects the graph when any bit is set.  With all three clear every row
+// range lies inside [0, nnz), so no kernel indexes colidx out of bounds.
 __global__ void k_validate_csr(const int64_t* rowptr, const int32_t* colidx, int64_t n, int64_t nnz,
                                int* bad) {
   int local = 0;
   const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  if (blockIdx.x == 0 && threadIdx.x == 0 && (rowptr[0] != 0 || rowptr[n] != nnz)) local |= 4;
   for (int64_t v = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; v < n; v += stride)
     if (rowptr[v + 1] < rowptr[v]) local |= 1;
   for (int64_t e = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; e < nnz; e += stride) {

@@ -1,0 +1,180 @@
+// xf64.cuh -- extended-precision arithmetic on the integer pipes for the
+// FP64 dependency sweep of Brandes' algorithm.
+//
+// The reference keeps the dependencies in Float64: coeff = (1 + delta[w]) /
+// sigma[w] and delta[v] += sigma[v] * coeff (src/centrality/betweenness.jl:
+// 96-99).  On this GPU an FP64 instruction costs about 68 FP32 instructions of
+// pipe time, and the dependency sweep adds one term per (DAG arc, source), so
+// an FP64-pipe implementation is bound by the FP64 unit.  The sweep instead
+// works on non-negative values in this format:
+//
+//   xf64{m, e}  =  m * 2^(e - 1085),   m in [2^62, 2^63)  or  m = 0 with e = 0.
+//
+// A finite positive double with biased exponent E and 53-bit significand M
+// converts exactly to {M << 10, E}: the format is an IEEE binary64 value with
+// 10 more significand bits and an integer exponent.  Every operation below
+// truncates at most one unit of its 63-bit result (relative error < 2^-62),
+// against the 2^-53 of one FP64 rounding; results go back to binary64 with
+// round-to-nearest-even.  Path counts are exact uint64 integers, and their
+// reciprocal is computed here by Newton iteration in 64-bit fixed point.
+//
+// All functions are __host__ __device__ so that the host tests check the same
+// code against exact rational arithmetic; only the three primitives
+// (high product, clamped right shift, leading zeros) differ by target.
+#pragma once
+
+#include <stdint.h>
+
+#ifndef __CUDACC__
+#define __host__
+#define __device__
+#define __forceinline__ inline
+#endif
+
+namespace lgbc {
+
+struct xf64 {
+  uint64_t m;
+  int32_t e;
+};
+
+constexpr int kXfBias = 1085;  // 1075 (binary64: value = M * 2^(E - 1075)) + 10 guard bits
+
+// ---- primitives ------------------------------------------------------------
+__host__ __device__ __forceinline__ uint64_t xf_mulhi(uint64_t a, uint64_t b) {
+#ifdef __CUDA_ARCH__
+  return __umul64hi(a, b);
+#else
+  return static_cast<uint64_t>((static_cast<unsigned __int128>(a) * b) >> 64);
+#endif
+}
+
+// x >> n for any n >= 0 (0 once n >= 64).
+__host__ __device__ __forceinline__ uint64_t xf_shr(uint64_t x, uint32_t n) {
+#ifdef __CUDA_ARCH__
+  uint64_t r;
+  asm("shr.b64 %0, %1, %2;" : "=l"(r) : "l"(x), "r"(n));  // PTX clamps n to 64
+  return r;
+#else
+  return n >= 64 ? 0 : x >> n;
+#endif
+}
+
+__host__ __device__ __forceinline__ int xf_clz(uint64_t x) {
+#ifdef __CUDA_ARCH__
+  return __clzll(static_cast<long long>(x));
+#else
+  return x ? __builtin_clzll(x) : 64;
+#endif
+}
+
+// ---- conversions -------------------------------------------------------------
+__host__ __device__ __forceinline__ xf64 xf_zero() { return xf64{0ull, 0}; }
+
+// A non-negative binary64 value given by its bits (zero or normal).
+__host__ __device__ __forceinline__ xf64 xf_from_bits(uint64_t b) {
+  const int E = static_cast<int>(b >> 52);
+  if (E == 0) return xf_zero();
+  return xf64{((b & 0x000FFFFFFFFFFFFFull) | 0x0010000000000000ull) << 10, E};
+}
+
+// Round to the nearest binary64 value (ties to even); the bits of the result.
+// Values stay inside the normal range here (2^-1022 <= x < 2^1024).
+__host__ __device__ __forceinline__ uint64_t xf_to_bits(xf64 a) {
+  if (a.m == 0) return 0ull;
+  const uint64_t M = a.m >> 10;
+  const uint32_t r = static_cast<uint32_t>(a.m & 1023u);
+  const uint64_t up = (r > 512u || (r == 512u && (M & 1u))) ? 1ull : 0ull;
+  // M carries the implicit bit 2^52, which adds one to the exponent field;
+  // a round-up to 2^53 carries once more, as it must.
+  return (static_cast<uint64_t>(a.e - 1) << 52) + M + up;
+}
+
+// ---- arithmetic on non-negative values ---------------------------------------
+// a + b.  Both sums of terms < 2^63 fit 64 bits; one shift renormalises.
+__host__ __device__ __forceinline__ xf64 xf_add(xf64 a, xf64 b) {
+  const int E = a.e > b.e ? a.e : b.e;
+  uint64_t m = xf_shr(a.m, static_cast<uint32_t>(E - a.e)) +
+               xf_shr(b.m, static_cast<uint32_t>(E - b.e));
+  const uint32_t c = static_cast<uint32_t>(m >> 63);
+  m >>= c;
+  return xf64{m, m ? E + static_cast<int>(c) : 0};
+}
+
+// a + x for a non-negative binary64 x given by its bits (zero or normal).
+__host__ __device__ __forceinline__ xf64 xf_add_bits(xf64 a, uint64_t xb) {
+  return xf_add(a, xf_from_bits(xb));
+}
+
+// (hi : lo) of a 64 x 64-bit product of normalised operands (hi >= 2^61),
+// normalised to m in [2^62, 2^63); e_hi is the exponent the result would
+// have with m = hi.
+__host__ __device__ __forceinline__ xf64 xf_norm_product(uint64_t hi, uint64_t lo, int e_hi) {
+  if (hi == 0 && lo == 0) return xf_zero();
+  // hi >= 2^61 for normalised operands; move the top bit to position 62
+  const int lz = xf_clz(hi) - 1;  // 0, 1 or 2 for normalised operands
+  uint64_t m;
+  if (lz >= 0)
+    m = lz == 0 ? hi : ((hi << lz) | (lo >> (64 - lz)));
+  else
+    m = hi >> 1;
+  return xf64{m, e_hi - lz};
+}
+
+// a * s for an integer s >= 1 (a path count).
+__host__ __device__ __forceinline__ xf64 xf_mul_u64(xf64 a, uint64_t s) {
+  if (a.m == 0 || s == 0) return xf_zero();
+  const int lz = xf_clz(s);
+  const uint64_t sn = s << lz;  // in [2^63, 2^64)
+  // a.m * sn = (hi 2^64 + lo); value = a.m sn 2^(a.e - kXfBias - lz)
+  return xf_norm_product(xf_mulhi(a.m, sn), a.m * sn, a.e + 64 - lz);
+}
+
+// a * b.
+__host__ __device__ __forceinline__ xf64 xf_mul(xf64 a, xf64 b) {
+  if (a.m == 0 || b.m == 0) return xf_zero();
+  const uint64_t bn = b.m << 1;  // in [2^63, 2^64); b = bn 2^(b.e - kXfBias - 1)
+  return xf_norm_product(xf_mulhi(a.m, bn), a.m * bn, a.e + b.e - kXfBias + 63);
+}
+
+// 1 / s for an integer s >= 1: R ~ 2^127 / sn by two Newton steps in 64-bit
+// fixed point from a 24-bit FP32 seed (relative error < 2^-61).
+__host__ __device__ __forceinline__ xf64 xf_recip_u64(uint64_t s) {
+  const int lz = xf_clz(s);
+  const uint64_t sn = s << lz;  // 1/s = 2^lz / sn
+  if (sn == 0x8000000000000000ull) return xf64{1ull << 62, lz + 960};  // a power of two: exact
+  // seed: x ~ 2^127 / sn from the FP32 reciprocal of its top 24 bits
+  const float t = static_cast<float>(static_cast<uint32_t>(sn >> 40));  // exact, in [2^23, 2^24)
+  uint32_t rb;  // bits of r ~ 1/t, in (2^-24, 2^-23]; Newton removes the seed's error
+#ifdef __CUDA_ARCH__
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(t));
+  rb = __float_as_uint(r);
+#else
+  const float r = 1.0f / t;
+  __builtin_memcpy(&rb, &r, 4);
+#endif
+  const int er = static_cast<int>((rb >> 23) & 0xFFu) - 127;              // -24 or -23
+  const uint64_t mr = static_cast<uint64_t>((rb & 0x7FFFFFu) | 0x800000u);
+  // x = r 2^87 = mr 2^(er - 23 + 87); er = -23 only when t = 2^23 (x = 2^64: clamp)
+  uint64_t x = er == -24 ? (mr << 40) : 0xFFFFFFFFFFFFFFFFull;
+#pragma unroll
+  for (int it = 0; it < 2; ++it) {
+    // err = 2^127 - sn x (two's complement over 128 bits), x += x err / 2^127
+    const uint64_t plo = sn * x;
+    const uint64_t phi = xf_mulhi(sn, x);
+    const uint64_t elo = 0ull - plo;
+    const uint64_t ehi = 0x8000000000000000ull - phi - (plo != 0 ? 1ull : 0ull);
+    // err >> 63 as a signed 64-bit value (|err| < 2^106 after the seed)
+    const int64_t e63 = static_cast<int64_t>((ehi << 1) | (elo >> 63));
+    const uint64_t mag = static_cast<uint64_t>(e63 < 0 ? -e63 : e63);
+    const uint64_t corr = xf_mulhi(x, mag);  // x |err| / 2^127 = (x |e63|) >> 64
+    x = e63 < 0 ? x - corr : x + corr;
+  }
+  // 1/s = x 2^(lz - 127); x in (2^63, 2^64) up to the last units
+  const int lx = xf_clz(x);  // 0 (or 1 if x fell just below 2^63)
+  const uint64_t xn = x << lx;
+  return xf64{xn >> 1, lz - 127 + 64 - lx + kXfBias - 63};
+}
+
+}  // namespace lgbc

@@ -59,7 +59,8 @@ class LgbcTuning(ctypes.Structure):
                 ("hub_degree", ctypes.c_int32), ("lanes", ctypes.c_int32),
                 ("dense_edges", ctypes.c_int32), ("segment_degree", ctypes.c_int32),
                 ("source_order", ctypes.c_int32), ("graph_loop", ctypes.c_int32),
-                ("stack_vertices", ctypes.c_int32), ("hub_order", ctypes.c_int32)]
+                ("stack_vertices", ctypes.c_int32), ("hub_order", ctypes.c_int32),
+                ("dependency_df32", ctypes.c_int32)]
 
 
 class LgbcTrainCfg(ctypes.Structure):
