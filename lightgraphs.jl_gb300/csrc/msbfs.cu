@@ -239,9 +239,40 @@ __device__ __forceinline__ df32 acc_done(df32 acc) { return fast_two_sum(acc.hi,
 
 template <class T, class A> __device__ __forceinline__ void acc_row(A& acc, T x);
 template <> __device__ __forceinline__ void acc_row(unsigned long long& acc, unsigned long long x) { acc += x; }
-// FP64 dependencies: psi rows hold binary64 bits, summed in the extended format.
-template <> __device__ __forceinline__ void acc_row(xf64& acc, unsigned long long x) {
-  acc = xf_add_bits(acc, x);
+// FP64 dependencies: psi rows hold binary64 bits, summed by the gather
+// accumulator (renormalised at the end of every 32-edge chunk).
+template <> __device__ __forceinline__ void acc_row(xg64& acc, unsigned long long x) {
+  xg_add_bits(acc, x);
+}
+// In a two-word batch, slot 0 (lanes 0-31) of the gather accumulators adds on
+// the FP64 pipe (binary64 running sums, its bits kept in xg64::m) while
+// slots 1-3 add on the integer pipes: the two units work in parallel and
+// neither carries all the adds.
+template <int W> __device__ __forceinline__ constexpr bool fp64_slot(int k) { return W == 2 && k == 0; }
+
+template <class T, class A, int W>
+__device__ __forceinline__ void acc_slot(A& acc, T x, int k) { acc_row<T, A>(acc, x); }
+template <>
+__device__ __forceinline__ void acc_slot<unsigned long long, xg64, 2>(xg64& acc, unsigned long long x,
+                                                                     int k) {
+  if (fp64_slot<2>(k))
+    acc.m = static_cast<unsigned long long>(__double_as_longlong(
+        __longlong_as_double(static_cast<long long>(acc.m)) + __longlong_as_double(static_cast<long long>(x))));
+  else
+    xg_add_bits(acc, x);
+}
+
+template <class A> __device__ __forceinline__ void acc_chunk_end(A&) {}
+template <> __device__ __forceinline__ void acc_chunk_end(xg64& a) { xg_norm(a); }
+template <int W, class A, int K> __device__ __forceinline__ void chunk_end(A (&a)[K]) {
+#pragma unroll
+  for (int k = 0; k < K; ++k)
+    if (!fp64_slot<W>(k)) acc_chunk_end(a[k]);
+}
+
+// The extended value of slot k of a normalised gather accumulator.
+template <int W> __device__ __forceinline__ xf64 gather_value(const xg64& a, int k) {
+  return fp64_slot<W>(k) ? xf_from_bits(a.m) : xg_to_xf(a);
 }
 template <> __device__ __forceinline__ void acc_row(double& acc, double x) { acc += x; }
 template <> __device__ __forceinline__ void acc_row(df32& acc, float2 x) { acc_add(acc, x.x, x.y); }
@@ -255,7 +286,7 @@ template <class A> __device__ __forceinline__ A zero_acc();
 template <> __device__ __forceinline__ unsigned long long zero_acc() { return 0ull; }
 template <> __device__ __forceinline__ double zero_acc() { return 0.0; }
 template <> __device__ __forceinline__ df32 zero_acc() { return df32{0.f, 0.f}; }
-template <> __device__ __forceinline__ xf64 zero_acc() { return xf_zero(); }
+template <> __device__ __forceinline__ xg64 zero_acc() { return xg_zero(); }
 
 template <class A, int K> __device__ __forceinline__ void zero_accs(A (&a)[K]) {
 #pragma unroll
@@ -315,17 +346,16 @@ __device__ __forceinline__ void gather_chunk(int32_t nb, const Lanes<W>& f, cons
         const int64_t off = static_cast<int64_t>(ok ? st.v[r + q] : 0) * RS;
         my[q] = my_bits(fj);
 #pragma unroll
-        for (int k = 0; k < 2 * W; ++k) {
-          x[q][k] = zero_row<T>();
+        for (int k = 0; k < 2 * W; ++k)  // x[q][k] is read below only under the same bit
           if (my[q] & (1u << k)) x[q][k] = r0[off + 32 * k];
-        }
       }
 #pragma unroll
       for (int q = 0; q < G; ++q)
 #pragma unroll
         for (int k = 0; k < 2 * W; ++k)
-          if (my[q] & (1u << k)) acc_row<T, A>(acc[k], x[q][k]);
+          if (my[q] & (1u << k)) acc_slot<T, A, W>(acc[k], x[q][k], k);
     }
+    chunk_end<W>(acc);
     __syncwarp();
     return;
   }
@@ -356,9 +386,10 @@ __device__ __forceinline__ void gather_chunk(int32_t nb, const Lanes<W>& f, cons
       }
 #pragma unroll
       for (int q = 0; q < 4; ++q)
-        if (ok[q]) acc_row<T, A>(acc[k], x[q]);
+        if (ok[q]) acc_slot<T, A, W>(acc[k], x[q], k);
     }
   }
+  chunk_end<W>(acc);
 }
 
 // Path-count gather over in-edges [e0, e1) of one vertex: for every
@@ -462,7 +493,11 @@ __device__ __forceinline__ void psi_range_x(const int32_t* __restrict__ ci, int6
                                             const Lanes<W>& F, const Lanes<W>* __restrict__ succ,
                                             const void* __restrict__ psi, int dense,
                                             xf64 (&acc)[2 * W]) {
-  psi_range<unsigned long long, xf64, W>(ci, e0, e1, F, succ, psi, dense, acc);
+  xg64 a[2 * W];
+  zero_accs(a);
+  psi_range<unsigned long long, xg64, W>(ci, e0, e1, F, succ, psi, dense, a);
+#pragma unroll
+  for (int k = 0; k < 2 * W; ++k) acc[k] = gather_value<W>(a[k], k);
 }
 
 __device__ __forceinline__ int64_t shfl_i64(int64_t x, int src) {
@@ -566,9 +601,10 @@ __device__ __forceinline__ void seg_gather(bool valid, int64_t e0, int deg, cons
         nm = lor(nm, fq[q]);
 #pragma unroll
         for (int k = 0; k < 2 * W; ++k)
-          if (my[q] & (1u << k)) acc_row<T, A>(acc[k], xr[q][k]);
+          if (my[q] & (1u << k)) acc_slot<T, A, W>(acc[k], xr[q][k], k);
       }
     }
+    chunk_end<W>(acc);
     __syncwarp();
   }
   if (cur >= 0) {
@@ -1284,7 +1320,6 @@ __global__ void __launch_bounds__(256, W == 1 ? 5 : 4) k_ms_delta(DevGraph g, Ms
       }
     } else if (SK == kSigmaU64F64) {
       xf64 acc[2 * W];
-      zero_accs(acc);
       psi_range_x<W>(g.colidx, e0, e1, F, succ, b.psi, hd.dense_edges, acc);
       const xf64 contrib = warp_sum_x(
           finish_x<W>(b.psi, b.sigma, v, mine, acc, b.lane_w ? weights_of<W>(b, v) : nullptr));
@@ -1327,7 +1362,6 @@ __global__ void __launch_bounds__(256, W == 1 ? 5 : 4) k_ms_hub_delta(DevGraph g
       for (int k = 0; k < 2 * W; ++k) part[k] = df_to_double(a[k]);
     } else if (SK == kSigmaU64F64) {
       xf64 a[2 * W];
-      zero_accs(a);
       psi_range_x<W>(g.colidx, I.lo, I.hi, F, succ, b.psi, hd.dense_edges, a);
 #pragma unroll
       for (int k = 0; k < 2 * W; ++k) part[k] = __longlong_as_double(static_cast<long long>(xf_to_bits(a[k])));
@@ -1529,12 +1563,19 @@ __global__ void __launch_bounds__(256, W == 1 ? 3 : 2) k_ms_delta_seg(DevGraph g
                                           if (ln == 0 && contrib.hi != 0.f) bc[vj] += df_to_double(contrib);
                                         });
     } else if (SK == kSigmaU64F64) {
-      seg_gather<unsigned long long, xf64, true, W>(
+      seg_gather<unsigned long long, xg64, true, W>(
           mine, e0, dg, F, g.colidx, succ, reinterpret_cast<const unsigned long long*>(b.psi),
-          [&](int j, const Lanes<W>&, const xf64 (&a)[2 * W]) {
+          [&](int j, const Lanes<W>&, const xg64 (&a)[2 * W]) {
             const int32_t vj = __shfl_sync(kFull, v, j);
+            xf64 d[2 * W];
+#pragma unroll
+            for (int k = 0; k < 2 * W; ++k) {
+              xg64 t = a[k];  // flushed mid-chunk: renormalise first
+              if (!fp64_slot<W>(k)) xg_norm(t);
+              d[k] = gather_value<W>(t, k);
+            }
             const xf64 contrib =
-                warp_sum_x(finish_x<W>(b.psi, b.sigma, vj, my_bits(lshfl(F, j)), a, nullptr));
+                warp_sum_x(finish_x<W>(b.psi, b.sigma, vj, my_bits(lshfl(F, j)), d, nullptr));
             if (ln == 0) bc_add_x(bc, vj, contrib);
           });
     } else {

@@ -177,4 +177,49 @@ __host__ __device__ __forceinline__ xf64 xf_recip_u64(uint64_t s) {
   return xf64{xn >> 1, lz - 127 + 64 - lx + kXfBias - 63};
 }
 
+// ---- gather accumulator ------------------------------------------------------
+// The dependency gathers add up to 32 terms (one 32-edge chunk) per lane
+// between two renormalisations, so their accumulator skips the per-add
+// renormalisation of xf_add:
+//
+//   xg{m, e}  =  m * 2^(e - 1080),   m in [2^57, 2^58) after xg_norm (or 0, e = 0),
+//
+// terms enter as (53-bit significand << 5) in [2^57, 2^58) and after k adds
+// m < (k + 1) 2^58 < 2^64 for k <= 32.  Each add truncates less than one unit
+// of the 58-bit scale (relative error < 2^-57, against binary64's 2^-53).
+struct xg64 {
+  uint64_t m;
+  int32_t e;
+};
+
+__host__ __device__ __forceinline__ xg64 xg_zero() { return xg64{0ull, 0}; }
+
+// x >> n for n in [0, 2046]: amounts of 64 and more act as 63, which is exact
+// for terms (< 2^58) and off by at most one unit for an accumulator.
+__host__ __device__ __forceinline__ uint64_t xg_shr(uint64_t x, uint32_t n) {
+  return x >> (n < 63u ? n : 63u);
+}
+
+// a += x for a positive normal binary64 x given by its bits (psi > 0 always).
+__host__ __device__ __forceinline__ void xg_add_bits(xg64& a, uint64_t xb) {
+  const uint32_t hi = static_cast<uint32_t>(xb >> 32);
+  const int ex = static_cast<int>(hi >> 20);
+  const uint64_t t = (static_cast<uint64_t>((hi & 0xFFFFFu) | 0x100000u) << 37) |
+                     (static_cast<uint64_t>(static_cast<uint32_t>(xb)) << 5);
+  const int E = a.e > ex ? a.e : ex;
+  a.m = xg_shr(a.m, static_cast<uint32_t>(E - a.e)) + xg_shr(t, static_cast<uint32_t>(E - ex));
+  a.e = E;
+}
+
+// Back to m in [2^57, 2^58) after at most 32 adds.
+__host__ __device__ __forceinline__ void xg_norm(xg64& a) {
+  const int top = 63 - xf_clz(a.m);  // 57..63 (or -1 for 0)
+  const int sh = top > 57 ? top - 57 : 0;
+  a.m >>= sh;
+  a.e += sh;
+}
+
+// The extended value of a normalised gather accumulator.
+__host__ __device__ __forceinline__ xf64 xg_to_xf(xg64 a) { return xf64{a.m << 5, a.e}; }
+
 }  // namespace lgbc

@@ -5,6 +5,7 @@
 //   A a_bits b_bits -> double a + double b
 //   X a_bits b_bits -> double a * double b
 //   S n b1 .. bn   -> sum of n doubles, accumulated term by term
+//   G n b1 .. bn   -> the same with the gather accumulator (xg64)
 // and prints, per line, the result as "m e bits" (xf64 and its binary64 rounding).
 #include <cstdio>
 #include <cstring>
@@ -32,6 +33,19 @@ int main() {
       unsigned long long a, b;
       std::scanf("%llu %llu", &a, &b);
       r = xf_mul(xf_from_bits(a), xf_from_bits(b));
+    } else if (op[0] == 'G') {
+      // G n b1 .. bn: the gather accumulator, renormalised every 32 terms
+      int n;
+      std::scanf("%d", &n);
+      xg64 g = xg_zero();
+      for (int i = 0; i < n; ++i) {
+        unsigned long long b;
+        std::scanf("%llu", &b);
+        xg_add_bits(g, b);
+        if (i % 32 == 31) xg_norm(g);
+      }
+      xg_norm(g);
+      r = xg_to_xf(g);
     } else if (op[0] == 'S') {
       int n;
       std::scanf("%d", &n);
