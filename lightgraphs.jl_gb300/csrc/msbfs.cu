@@ -708,13 +708,23 @@ __device__ __forceinline__ xf64 finish_x(void* psi, const void* sigma, int32_t v
   return contrib;
 }
 
+// Sum over the warp (zeros allowed): every value is aligned to the largest
+// exponent and the 63-bit significands are added exactly as four 16-bit
+// pieces by redux (each piece sum < 2^21); the total (< 2^68) keeps its top
+// 63 bits.  Relative error < 2^-56.
 __device__ __forceinline__ xf64 warp_sum_x(xf64 a) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    const xf64 b{__shfl_xor_sync(kFull, a.m, o), __shfl_xor_sync(kFull, a.e, o)};
-    a = xf_add(a, b);
-  }
-  return a;
+  const int E = static_cast<int>(__reduce_max_sync(kFull, static_cast<unsigned>(a.e)));
+  if (E == 0) return xf_zero();  // every value is zero (warp-uniform)
+  const uint64_t m = xf_shr(a.m, static_cast<uint32_t>(E - a.e));
+  const uint32_t lo = static_cast<uint32_t>(m), hi = static_cast<uint32_t>(m >> 32);
+  const uint64_t s0 = __reduce_add_sync(kFull, lo & 0xFFFFu);
+  const uint64_t s1 = __reduce_add_sync(kFull, lo >> 16);
+  const uint64_t s2 = __reduce_add_sync(kFull, hi & 0xFFFFu);
+  const uint64_t s3 = __reduce_add_sync(kFull, hi >> 16);
+  // total >> 5 = s3 2^43 + s2 2^27 + s1 2^11 + s0 2^-5 < 2^63
+  const uint64_t t = (s3 << 43) + (s2 << 27) + (s1 << 11) + (s0 >> 5);
+  const int lz = xf_clz(t) - 1;  // 0..5: the largest value alone is >= 2^57 after the shift
+  return xf64{t << lz, E + 5 - lz};
 }
 
 // bc[v] += x, rounded once (lane 0 of the warp that owns v at this level).

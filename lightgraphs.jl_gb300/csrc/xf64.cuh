@@ -137,35 +137,65 @@ __host__ __device__ __forceinline__ xf64 xf_mul(xf64 a, xf64 b) {
   return xf_norm_product(xf_mulhi(a.m, bn), a.m * bn, a.e + b.e - kXfBias + 63);
 }
 
-// 1 / s for an integer s >= 1: R ~ 2^127 / sn by two Newton steps in 64-bit
-// fixed point from a 24-bit FP32 seed (relative error < 2^-61).
+// 1 / s for an integer s >= 1: R ~ 2^127 / sn (sn = s normalised to
+// [2^63, 2^64)) from a double-float seed -- the FP32 reciprocal of sn's top
+// 24 bits refined by one FP32 Newton step against its top 48 bits (about 46
+// correct bits) -- and one Newton step in 64-bit fixed point (relative error
+// < 2^-61).
+__host__ __device__ __forceinline__ float xf_rcp_seed(float t) {
+#ifdef __CUDA_ARCH__
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(t));
+  return r;
+#else
+  return 1.0f / t;
+#endif
+}
+
+__host__ __device__ __forceinline__ float xf_fmaf(float a, float b, float c) {
+#ifdef __CUDA_ARCH__
+  return __fmaf_rn(a, b, c);
+#else
+  return __builtin_fmaf(a, b, c);
+#endif
+}
+
+__host__ __device__ __forceinline__ uint32_t xf_float_bits(float f) {
+#ifdef __CUDA_ARCH__
+  return __float_as_uint(f);
+#else
+  uint32_t u;
+  __builtin_memcpy(&u, &f, 4);
+  return u;
+#endif
+}
+
 __host__ __device__ __forceinline__ xf64 xf_recip_u64(uint64_t s) {
   const int lz = xf_clz(s);
   const uint64_t sn = s << lz;  // 1/s = 2^lz / sn
   if (sn == 0x8000000000000000ull) return xf64{1ull << 62, lz + 960};  // a power of two: exact
-  // seed: x ~ 2^127 / sn from the FP32 reciprocal of its top 24 bits
-  const float t = static_cast<float>(static_cast<uint32_t>(sn >> 40));  // exact, in [2^23, 2^24)
-  uint32_t rb;  // bits of r ~ 1/t, in (2^-24, 2^-23]; Newton removes the seed's error
-#ifdef __CUDA_ARCH__
-  float r;
-  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(t));
-  rb = __float_as_uint(r);
-#else
-  const float r = 1.0f / t;
-  __builtin_memcpy(&rb, &r, 4);
-#endif
-  const int er = static_cast<int>((rb >> 23) & 0xFFu) - 127;              // -24 or -23
+  // t = sn / 2^40 as a float pair: th in [2^23, 2^24) and tl in [0, 1), both exact
+  const float th = static_cast<float>(static_cast<uint32_t>(sn >> 40));
+  const float tl = static_cast<float>(static_cast<uint32_t>(sn >> 16) & 0xFFFFFFu) * 0x1p-24f;
+  const float r0 = xf_rcp_seed(th);                                  // in (2^-24, 2^-23]
+  const float e = xf_fmaf(-tl, r0, xf_fmaf(-th, r0, 1.0f));          // 1 - t r0
+  const float c = r0 * e;                                            // 1/t ~ r0 + c
+  // x ~ 2^127 / sn = 2^87 / t = (r0 + c) 2^87, r0 2^87 = mr 2^(er + 64) with er = -24, or
+  // er = -23 at r0 = 2^-23 where r0 2^87 = 2^64 wraps to 0 and the negative c
+  // brings x back below 2^64 (the sum is taken modulo 2^64; x itself fits)
+  const uint32_t rb = xf_float_bits(r0);
+  const int er = static_cast<int>((rb >> 23) & 0xFFu) - 127;
   const uint64_t mr = static_cast<uint64_t>((rb & 0x7FFFFFu) | 0x800000u);
-  // x = r 2^87 = mr 2^(er - 23 + 87); er = -23 only when t = 2^23 (x = 2^64: clamp)
-  uint64_t x = er == -24 ? (mr << 40) : 0xFFFFFFFFFFFFFFFFull;
-#pragma unroll
-  for (int it = 0; it < 2; ++it) {
+  const int64_t cx = static_cast<int64_t>(static_cast<int32_t>(c * 0x1p70f)) << 17;  // c 2^87
+  uint64_t x = (mr << (er + 64)) + static_cast<uint64_t>(cx);
+  if (x == 0) x = 0xFFFFFFFFFFFFFFFFull;  // t = 2^23 exactly (sn < 2^63 + 2^16): seed 2^64
+  {
     // err = 2^127 - sn x (two's complement over 128 bits), x += x err / 2^127
     const uint64_t plo = sn * x;
     const uint64_t phi = xf_mulhi(sn, x);
     const uint64_t elo = 0ull - plo;
     const uint64_t ehi = 0x8000000000000000ull - phi - (plo != 0 ? 1ull : 0ull);
-    // err >> 63 as a signed 64-bit value (|err| < 2^106 after the seed)
+    // err >> 63 as a signed 64-bit value (|err| < 2^84 after the seed)
     const int64_t e63 = static_cast<int64_t>((ehi << 1) | (elo >> 63));
     const uint64_t mag = static_cast<uint64_t>(e63 < 0 ? -e63 : e63);
     const uint64_t corr = xf_mulhi(x, mag);  // x |err| / 2^127 = (x |e63|) >> 64
@@ -194,11 +224,8 @@ struct xg64 {
 
 __host__ __device__ __forceinline__ xg64 xg_zero() { return xg64{0ull, 0}; }
 
-// x >> n for n in [0, 2046]: amounts of 64 and more act as 63, which is exact
-// for terms (< 2^58) and off by at most one unit for an accumulator.
-__host__ __device__ __forceinline__ uint64_t xg_shr(uint64_t x, uint32_t n) {
-  return x >> (n < 63u ? n : 63u);
-}
+// x >> n for n in [0, 2046] (0 once n >= 64).
+__host__ __device__ __forceinline__ uint64_t xg_shr(uint64_t x, uint32_t n) { return xf_shr(x, n); }
 
 // a += x for a positive normal binary64 x given by its bits (psi > 0 always).
 __host__ __device__ __forceinline__ void xg_add_bits(xg64& a, uint64_t xb) {

@@ -90,8 +90,8 @@ def test_reciprocal_of_path_counts(harness):
     for x, r in zip(s, res):
         exact_round += bool(check(r, Fraction(1, x)))
     # a reciprocal within 2^-60 of exact rounds correctly unless it sits that
-    # close to a rounding tie
-    assert exact_round >= len(s) - 2
+    # close to a rounding tie (about 2^-8 of the cases)
+    assert exact_round >= len(s) - len(s) // 100
 
 
 def test_product_with_path_counts(harness):
