@@ -85,6 +85,23 @@ int lgbc_gdistances(lgbc_graph *g, const int32_t *src, int64_t nsrc,
 int lgbc_gdistances_batch(lgbc_graph *g, const int32_t *src, int64_t nsrc,
                           int32_t *dist_out /* nsrc x n */);
 
+/* Path counts and distances of dijkstra_shortest_paths(g, s) with unit
+ * weights (src/shortestpaths/dijkstra.jl:59-141): DijkstraState.pathcounts
+ * (:10, summed at :102,118, reset to 1 at the source at :135) and .dists,
+ * for nsrc independent sources.  Row i (source src[i]) is
+ *   sigma_out[i * n + v]  the number of shortest paths from src[i] to v as a
+ *                         Float64: exact (the same bits as the reference's
+ *                         sums) below 2^53, the exact count rounded to
+ *                         nearest above; 1 at src[i]; 0 where src[i] does
+ *                         not reach v
+ *   dist_out[i * n + v]   hop distance, LGBC_UNREACHED where not reached
+ *                         (dist_out may be NULL).
+ * Counts are exact uint64 integers on the device; a batch whose counts could
+ * pass 2^64 is recomputed with FP64 counts.  Sources run as bit lanes of the
+ * multi-source BFS, 64 per batch. */
+int lgbc_path_counts(lgbc_graph *g, const int32_t *src, int64_t nsrc, double *sigma_out,
+                     int32_t *dist_out);
+
 /* Unscaled Brandes betweenness over the given sources:
  * the source loop of src/centrality/betweenness.jl:46-68 (and of
  * Parallel.betweenness_centrality, src/Parallel/centrality/betweenness.jl:9-72)
@@ -223,22 +240,31 @@ int lgbc_set_tuning(lgbc_graph *g, const lgbc_tuning *t);
 int lgbc_tune(lgbc_graph *g, const char *cache_path);
 
 /* gdistances for callers that cannot allocate device memory: no counterpart
- * in the reference.  Some callers cannot call cudaMalloc -- code that runs
- * while a CUDA graph is being captured on its stream, or hosts whose device
- * memory belongs to another allocator with a fixed budget -- so this entry
- * point allocates nothing.  Every input and output is a caller-owned DEVICE
- * pointer: the CSR (in_rowptr / in_colidx NULL for an undirected graph), the
- * nsrc sources, and dist (n int32, LGBC_UNREACHED where no source reaches).
- * Results equal lgbc_gdistances'.  The BFS queue, frontier bitmaps and control
- * block live in one static device array of about 17 MB that every GPU which
- * loads the library holds until exit, so n is limited to
- * LGBC_NOALLOC_MAX_VERTICES (larger graphs get LGBC_EINVAL).  The first call on
- * a device looks up that array's address (cudaGetSymbolAddress) and the
- * device's launch shape; make that first call before any stream capture.
- * `stream` is a cudaStream_t (NULL = default stream); the call returns when
- * dist is complete.  All calls share the one array: calls that overlap on the
- * GPU (from several host threads or streams at once) race and must not be
- * issued. */
+ * in the reference.  The handle-based entry points copy the CSR to the device
+ * and keep a BFS workspace, both from cudaMalloc.  Some callers cannot make
+ * that call: a host whose device memory belongs to another allocator with a
+ * fixed budget (a Julia CuArray pool, a serving process that reserves the
+ * GPU's memory when it starts), where a cudaMalloc outside that allocator can
+ * fail or take memory the budget counts on, and a loop that must not pay the
+ * device-wide synchronisation cudaFree implies.  This entry point allocates
+ * nothing.  Every input and output is a caller-owned DEVICE pointer: the CSR
+ * (in_rowptr / in_colidx NULL for an undirected graph), the nsrc sources, and
+ * dist (n int32, LGBC_UNREACHED where no source reaches).  Results equal
+ * lgbc_gdistances'.  The BFS queue, frontier bitmaps and control block live in
+ * one static device array of about 17 MB that every GPU which loads the
+ * library holds until the process exits, so n is limited to
+ * LGBC_NOALLOC_MAX_VERTICES (larger graphs get LGBC_EINVAL).  The CSR and the
+ * sources are checked on the device before any kernel indexes with them
+ * (rowptr running from 0 to nnz without decreasing, column ids and sources
+ * in [0, n)); a bad input gets LGBC_EINVAL.  The first call on a device looks
+ * up that array's address (cudaGetSymbolAddress) and the device's launch
+ * shape; make that first call before any stream capture.  `stream` is a
+ * cudaStream_t (NULL = default stream); the call synchronises that stream
+ * after the check and after every BFS level, and returns when dist is
+ * complete.  All calls share the one array, which keeps the last call's
+ * contents (each call clears what must start at zero): calls that overlap on
+ * the GPU (from several host threads or streams at once) race on it and must
+ * not be issued. */
 #define LGBC_NOALLOC_MAX_VERTICES (1 << 22)
 int lgbc_gdistances_noalloc(int64_t n, int64_t nnz, const int64_t *rowptr,
                             const int32_t *colidx, const int64_t *in_rowptr,

@@ -536,7 +536,7 @@ LoopKey loop_key(lgbc_graph* g, int backward, int sigma_kind, const LaneSet& act
 // stats (distance-only batches): per-lane distance statistics, accumulated.
 int run_ms_batch(lgbc_graph* g, const int32_t* lane_src, int nl, int sigma_kind, double* bc,
                  int32_t* dist, int64_t dist_ld, const Seeds& seeds, const double* lane_w,
-                 const LevelStats* stats, unsigned long long* stress) {
+                 const LevelStats* stats, unsigned long long* stress, const PathExport* pexp) {
   const DevGraph dg = g->dev();
   LGBC_TRY(ensure_hubs(g));
   const HubData hd = hub_data(g);
@@ -544,9 +544,11 @@ int run_ms_batch(lgbc_graph* g, const int32_t* lane_src, int nl, int sigma_kind,
   const int words = nl > kMaxLanes ? 2 : 1;
   if (nl < 1 || nl > kWideLanes)
     return fail(LGBC_EINVAL, "internal: a multi-source batch holds 1 to 128 lanes");
-  if (words > 1 && (dist || stats || stress || sigma_kind == kSigmaNone ||
+  if (words > 1 && (dist || stats || stress || pexp || sigma_kind == kSigmaNone ||
                     g->ms.sigma_words < words || !g->ms.claim))
     return fail(LGBC_EINVAL, "internal: a two-word batch is a Brandes batch");
+  if (pexp && (sigma_kind == kSigmaNone || seeds.v))
+    return fail(LGBC_EINVAL, "internal: a path-count export needs a plain batch with path counts");
   // two-word lane sets are read as single 16-byte accesses
   auto misaligned = [&](const void* p) {
     return words > 1 && (reinterpret_cast<uintptr_t>(p) & 15u) != 0;
@@ -607,6 +609,11 @@ int run_ms_batch(lgbc_graph* g, const int32_t* lane_src, int nl, int sigma_kind,
         g->launches += ms_cleanup_all(g->cfg, g->stream, b);
         return check_launch(g);
       }
+      if (pexp) {
+        g->launches += ms_export(g->cfg, g->stream, b, sigma_kind, pexp->sigma, pexp->dist, pexp->ld);
+        g->launches += ms_cleanup_all(g->cfg, g->stream, b);
+        return check_launch(g);
+      }
       const int maxl = c.maxlevel;
       LoopGraph* bg = nullptr;
       LGBC_TRY(get_loop(g, loop_key(g, 1, sigma_kind, act, nullptr, 0, bc, bw, hd), &bg));
@@ -664,6 +671,11 @@ int run_ms_batch(lgbc_graph* g, const int32_t* lane_src, int nl, int sigma_kind,
     }
     if (sigma_kind == kSigmaNone) {
       if (stats) g->launches += ms_level_stats(g->cfg, g->stream, b, *stats);
+      g->launches += ms_cleanup_all(g->cfg, g->stream, b);
+      return check_launch(g);
+    }
+    if (pexp) {
+      g->launches += ms_export(g->cfg, g->stream, b, sigma_kind, pexp->sigma, pexp->dist, pexp->ld);
       g->launches += ms_cleanup_all(g->cfg, g->stream, b);
       return check_launch(g);
     }

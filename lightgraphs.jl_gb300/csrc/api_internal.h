@@ -240,6 +240,13 @@ struct Seeds {
   int64_t lane_w_n = 0;
   int64_t lane_w_count = 0;
 };
+// Forward-sweep export of a one-word batch with path counts (lgbc_path_counts):
+// the batch stops after its forward sweep, with sigma / dist written per lane.
+struct PathExport {
+  double* sigma = nullptr;
+  int32_t* dist = nullptr;  // may be null
+  int64_t ld = 0;           // row length (n)
+};
 }  // namespace lgbc::api
 
 struct lgbc_graph {
@@ -310,11 +317,13 @@ MsBuffers ms_buffers(lgbc_graph* g, const int32_t* lane_src, const double* lane_
 // dependency sweep into bc.  Returns LGBC_OK, or 1 when the batch must be
 // replayed with FP64 path counts.  lane_w (sigma batches): per-lane weights of
 // the accumulation into bc; stats (distance-only batches): per-lane distance
-// statistics, accumulated; stress (distance-only batches): the stress sweep.
+// statistics, accumulated; stress (distance-only batches): the stress sweep;
+// pexp (one-word batches with path counts): export the forward sweep and
+// skip the dependency sweep.
 int run_ms_batch(lgbc_graph* g, const int32_t* lane_src, int nl, int sigma_kind, double* bc,
                  int32_t* dist, int64_t dist_ld, const Seeds& seeds = Seeds(),
                  const double* lane_w = nullptr, const LevelStats* stats = nullptr,
-                 unsigned long long* stress = nullptr);
+                 unsigned long long* stress = nullptr, const PathExport* pexp = nullptr);
 // The path-count / dependency kind of a Brandes batch on this handle: exact
 // uint64 path counts with FP64 dependencies (default) or, with the
 // dependency_df32 tuning field, double-float dependencies.

@@ -178,6 +178,60 @@ extern "C" int lgbc_stress(lgbc_graph* g, const int32_t* src, int64_t nsrc, int6
 }
 
 // ---------------------------------------------------------------------------
+// Path counts (DijkstraState.pathcounts / .dists with unit weights)
+// ---------------------------------------------------------------------------
+extern "C" int lgbc_path_counts(lgbc_graph* g, const int32_t* src, int64_t nsrc,
+                                double* sigma_out, int32_t* dist_out) {
+  LGBC_TRY(check_graph(g));
+  std::lock_guard<std::mutex> lock(g->mu);
+  LGBC_TRY(use_device(g));
+  LGBC_TRY(check_sources(g, src, nsrc));
+  if (nsrc > 0 && g->n > 0 && !sigma_out) return fail(LGBC_EINVAL, "null output");
+  reset_stats(g);
+  if (nsrc == 0 || g->n == 0) return LGBC_OK;
+  LGBC_TRY(ensure_ms(g, true));
+  LGBC_TRY(ensure_src(g, nsrc));
+  LGBC_CUDA(cudaMemcpyAsync(g->d_src, src, static_cast<size_t>(nsrc) * 4, cudaMemcpyHostToDevice,
+                            g->stream));
+  const int64_t n = g->n;
+  const int lanes = kMaxLanes;  // one-word batches
+  double* d_pc = nullptr;
+  int32_t* d_d = nullptr;
+  LGBC_TRY(dev_alloc(&d_pc, static_cast<size_t>(lanes) * static_cast<size_t>(n)));
+  std::unique_ptr<double, void (*)(double*)> g1(d_pc, [](double* q) { cudaFree(q); });
+  LGBC_TRY(dev_alloc(&d_d, static_cast<size_t>(lanes) * static_cast<size_t>(n)));
+  std::unique_ptr<int32_t, void (*)(int32_t*)> g2(d_d, [](int32_t* q) { cudaFree(q); });
+  for (int64_t s0 = 0; s0 < nsrc; s0 += lanes) {
+    const int nl = static_cast<int>(std::min<int64_t>(lanes, nsrc - s0));
+    const int64_t cells = static_cast<int64_t>(nl) * n;
+    PathExport px;
+    px.sigma = d_pc;
+    px.dist = d_d;
+    px.ld = n;
+    int rc = LGBC_OK;
+    for (int kind : {static_cast<int>(kSigmaU64), static_cast<int>(kSigmaF64)}) {
+      // unreached: pathcounts 0 and distance typemax, as dijkstra.jl:66-69 start them
+      g->launches += fill_f64(g->cfg, g->stream, d_pc, cells, 0.0);
+      g->launches += fill_i32(g->cfg, g->stream, d_d, cells, kUnreached);
+      rc = run_ms_batch(g, g->d_src + s0, nl, kind, nullptr, nullptr, 0, Seeds(), nullptr,
+                        nullptr, nullptr, &px);
+      if (rc != 1) break;  // 1: a count may pass 2^64, replay with FP64 counts
+      g->stats.wide_batches++;
+    }
+    if (rc != LGBC_OK) return rc < 0 ? rc : fail(LGBC_ECUDA, "internal: FP64 replay overflowed");
+    LGBC_CUDA(cudaMemcpyAsync(sigma_out + s0 * n, d_pc, static_cast<size_t>(cells) * 8,
+                              cudaMemcpyDeviceToHost, g->stream));
+    if (dist_out)
+      LGBC_CUDA(cudaMemcpyAsync(dist_out + s0 * n, d_d, static_cast<size_t>(cells) * 4,
+                                cudaMemcpyDeviceToHost, g->stream));
+    g->stats.batches++;
+  }
+  LGBC_CUDA(cudaStreamSynchronize(g->stream));
+  finish_stats(g);
+  return LGBC_OK;
+}
+
+// ---------------------------------------------------------------------------
 // BFS parents and reachability
 // ---------------------------------------------------------------------------
 extern "C" int lgbc_bfs_parents(lgbc_graph* g, int32_t s, int dir, int32_t* parents_out) {

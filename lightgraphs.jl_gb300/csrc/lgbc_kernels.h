@@ -167,6 +167,12 @@ struct LevelStats {
 int ms_level_stats(const LaunchCfg& c, cudaStream_t s, const MsBuffers& b, const LevelStats& st);
 // After a distance-only batch: clear visit / masks of every listed vertex.
 int ms_cleanup_all(const LaunchCfg& c, cudaStream_t s, const MsBuffers& b);
+// After the forward sweep of a one-word batch with path counts (uint64 or
+// FP64 kind): sigma_out[l * ld + v] = path count of lane l at v as binary64,
+// dist_out[l * ld + v] = its level (dist_out may be null), for every listed
+// (vertex, lane); unlisted entries are left as they are.
+int ms_export(const LaunchCfg& c, cudaStream_t s, const MsBuffers& b, int sigma_kind,
+              double* sigma_out, int32_t* dist_out, int64_t ld);
 // Zero visit and both mask buffers outright (after an aborted batch).
 int ms_reset_all(cudaStream_t s, const DevGraph& g, const MsBuffers& b);
 

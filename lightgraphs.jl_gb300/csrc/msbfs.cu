@@ -1804,6 +1804,45 @@ __global__ void k_ms_cleanup_all(MsBuffers b) {
   }
 }
 
+// Export of a one-word forward sweep with path counts (before the batch is
+// cleaned up): every listed (v, lanes) at level L gives, for each of its
+// lanes l, sigma_out[l * ld + v] = the path count as binary64 (exact below
+// 2^53; the uint64 count rounded to nearest above) and dist_out[l * ld + v] =
+// L.  Thread t of the warp that owns an entry writes lanes t and t + 32.
+// These are DijkstraState.pathcounts and .dists of
+// dijkstra_shortest_paths(g, s) with unit weights
+// (src/shortestpaths/dijkstra.jl:59-141); vertices a lane never lists keep
+// the caller's prefill (0 and LGBC_UNREACHED).
+template <int SK>
+__global__ void k_ms_export(MsBuffers b, double* sigma_out, int32_t* dist_out, int64_t ld) {
+  using T = typename Sig<SK>::T;
+  const BatchCtl* c = b.ctl;
+  const int maxl = c->maxlevel;
+  const unsigned long long total = b.lvl_off[maxl + 1];
+  const T* sigma = reinterpret_cast<const T*>(b.sigma);
+  const int ln = lane_id();
+  for (unsigned long long i = gwarp(); i < total; i += nwarps()) {
+    // the level of entry i: the largest L with lvl_off[L] <= i
+    int lo = 0, hi = maxl;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (b.lvl_off[mid] <= i) lo = mid;
+      else hi = mid - 1;
+    }
+    const int32_t v = b.qv[i];
+    const uint64_t F = b.qm[i];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const int l = 32 * k + ln;
+      if ((F >> l) & 1ull) {
+        const int64_t o = static_cast<int64_t>(l) * ld + v;
+        sigma_out[o] = sigma_f64(sigma[static_cast<int64_t>(v) * 64 + l]);
+        if (dist_out) dist_out[o] = lo;
+      }
+    }
+  }
+}
+
 // Distance statistics of every lane after a forward sweep: cnt[lane] +=
 // vertices the lane reached at levels >= 1, dsum[lane] += the sum of those
 // levels, dmax[lane] = max(dmax[lane], deepest level).  A warp loads 32 list
@@ -2285,6 +2324,15 @@ int ms_level_stats(const LaunchCfg& c, cudaStream_t s, const MsBuffers& b, const
 
 int ms_cleanup_all(const LaunchCfg& c, cudaStream_t s, const MsBuffers& b) {
   k_ms_cleanup_all<<<c.grid, c.block, 0, s>>>(b);
+  return 1;
+}
+
+int ms_export(const LaunchCfg& c, cudaStream_t s, const MsBuffers& b, int sigma_kind,
+              double* sigma_out, int32_t* dist_out, int64_t ld) {
+  if (sigma_kind == kSigmaF64)
+    k_ms_export<kSigmaF64><<<c.grid, c.block, 0, s>>>(b, sigma_out, dist_out, ld);
+  else
+    k_ms_export<kSigmaU64><<<c.grid, c.block, 0, s>>>(b, sigma_out, dist_out, ld);
   return 1;
 }
 

@@ -1,15 +1,19 @@
 // noalloc.cu -- gdistances for callers that cannot allocate device memory.
 //
 // lgbc_gdistances needs a graph handle, whose CSR and BFS workspace come from
-// cudaMalloc.  Some callers cannot allocate: code that runs while a CUDA graph
-// is being captured on its stream (an allocation there breaks the capture or
-// forces a synchronisation), and hosts whose device memory belongs to another
-// allocator with a fixed budget (a Julia CuArray pool, a serving runtime).
+// cudaMalloc.  Some callers cannot allocate: hosts whose device memory
+// belongs to another allocator with a fixed budget (a Julia CuArray pool, a
+// serving process that reserves the GPU's memory when it starts), where an
+// outside cudaMalloc can fail or take memory the budget counts on, and loops
+// that must not pay the device-wide synchronisation of cudaFree.
 // lgbc_gdistances_noalloc takes every input and output as caller-owned device
 // pointers and keeps its own scratch -- the frontier queue, the two frontier
-// bitmaps and the level control block -- in the file-scope device array
-// below, which every GPU that loads the library holds until the process exits.
-// Its size fixes the largest graph: LGBC_NOALLOC_MAX_VERTICES vertices.
+// bitmaps, the level control block and the input-check flag -- in the
+// file-scope device array below, which every GPU that loads the library holds
+// until the process exits.  Its size fixes the largest graph:
+// LGBC_NOALLOC_MAX_VERTICES vertices.  Each call clears what must start at
+// zero (the check flag here; bitmaps and control block in bfs_init), and
+// calls that overlap on the GPU race on the shared array.
 #include <cstdio>
 #include <mutex>
 
@@ -135,7 +139,10 @@ extern "C" int lgbc_gdistances_noalloc(int64_t n, int64_t nnz, const int64_t* ro
   int h_bad = 0;
   NA_CUDA(cudaMemcpyAsync(&h_bad, bad, sizeof(int), cudaMemcpyDeviceToHost, s));
   NA_CUDA(cudaStreamSynchronize(s));
-  if (h_bad) return err(LGBC_EINVAL, "invalid CSR or a source id outside [0, n)");
+  if (h_bad)
+    return err(LGBC_EINVAL,
+               "lgbc_gdistances_noalloc: invalid CSR (rowptr must run from 0 to nnz without "
+               "decreasing, column ids in [0, n)) or a source id outside [0, n)");
 
   // the same level loop as lgbc_gdistances (bfs.cu kernels), default tuning
   const double alpha = 14.0, beta = 24.0;

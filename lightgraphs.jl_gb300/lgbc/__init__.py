@@ -15,6 +15,8 @@ CUDA library ``liblgbc.so`` through its C ABI (include/lgbc.h):
 
     stress_centrality(g[, vs | k])                  src/centrality/stress.jl:33-49
     bfs_parents, bfs_tree, tree, has_path           src/traversals/bfs.jl:10-76,150-172
+    path_counts(g, sources) -- dijkstra_shortest_paths(g, s).pathcounts / .dists
+                                                    src/shortestpaths/dijkstra.jl:59-141
     core_number(g)                                  src/degeneracy.jl:38-80
     closeness_centrality, radiality_centrality      src/centrality/{closeness,radiality}.jl
     eccentricity, diameter, radius, periphery, center  src/distance.jl:73-170
@@ -37,7 +39,7 @@ from .distance import (center, closeness_centrality, diameter, eccentricity, per
 from .learned import (SourceProposal, betweenness_centrality_learned, core_number,
                       dependency_mass, features)
 from .traversals import (bfs_parents, bfs_tree, gdistances, gdistances_, has_path,
-                         multi_gdistances, tree)
+                         multi_gdistances, path_counts, tree)
 
 __all__ = [
     "Parallel", "ArgumentError", "BoundsError", "LGBCError", "MethodError",
@@ -47,5 +49,5 @@ __all__ = [
     "multi_gdistances", "learned", "SourceProposal", "betweenness_centrality_learned",
     "core_number", "dependency_mass", "features", "closeness_centrality", "radiality_centrality",
     "eccentricity", "diameter", "radius", "periphery", "center", "stress_centrality",
-    "bfs_parents", "bfs_tree", "tree", "has_path", "graph_from_edges",
+    "bfs_parents", "bfs_tree", "tree", "has_path", "graph_from_edges", "path_counts",
 ]

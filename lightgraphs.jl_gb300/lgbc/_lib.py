@@ -90,6 +90,7 @@ def _declare(lib) -> None:
         "lgbc_gdistances": ([p, p, i64, p], c_int),
         "lgbc_gdistances_batch": ([p, p, i64, p], c_int),
         "lgbc_betweenness": ([p, p, i64, c_int, p], c_int),
+        "lgbc_path_counts": ([p, p, i64, p, p], c_int),
         "lgbc_betweenness_dev": ([p, p, i64, c_int, p], c_int),
         "lgbc_graph_sync": ([p], c_int),
         "lgbc_timer_start": ([p], c_int),

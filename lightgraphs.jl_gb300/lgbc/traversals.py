@@ -5,6 +5,8 @@ Reference: src/traversals/bfs.jl (LightGraphs.jl v1.3.5)
   gdistances(g, source; sort_alg=QuickSort)                :141
   bfs_parents / bfs_tree / tree                            :10-19, :35-76
   has_path(g, u, v; exclude_vertices)                      :150-172
+and, from src/shortestpaths/dijkstra.jl:59-141 (unit weights),
+  dijkstra_shortest_paths(g, s).pathcounts / .dists        path_counts
 ``source`` is one vertex or a collection (a multi-source BFS: distance to the
 nearest source).  Unreachable vertices hold typemax(eltype(g)).  The
 ``sort_alg`` keyword only orders the reference's level queue and is accepted
@@ -118,3 +120,24 @@ def has_path(g, u: int, v: int, *, exclude_vertices=()) -> bool:
                                         _lib.ptr(ex) if len(ex) else None, len(ex),
                                         ctypes.byref(res)))
     return bool(res.value)
+
+
+def path_counts(g, sources):
+    """DijkstraState.pathcounts and .dists of dijkstra_shortest_paths(g, s)
+    with unit weights (src/shortestpaths/dijkstra.jl:59-141), one row per
+    entry of ``sources`` (1-based): (pathcounts float64 (len, nv),
+    dists eltype(g) (len, nv)).  pathcounts is 1 at the source and 0 where
+    the source does not reach; counts below 2^53 are exact, larger ones are
+    the exact count rounded to the nearest Float64.  dists holds
+    typemax(eltype(g)) where the source does not reach."""
+    src = _sources0(g, sources)
+    n = g.nv()
+    pc = np.zeros((len(src), n), np.float64)
+    dist = np.empty((len(src), n), np.int32)
+    if len(src) and n:
+        h = g.device_handle()
+        _lib.check(_lib.lib().lgbc_path_counts(h.handle, _lib.ptr(src), len(src), _lib.ptr(pc),
+                                               _lib.ptr(dist)))
+    else:
+        dist.fill(_lib.UNREACHED)
+    return pc, _to_eltype(dist, g.eltype)
