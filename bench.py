@@ -226,19 +226,45 @@ def workload(rank: int, args):
     return g, src, k_act, gen_s, name
 
 
-def many_graphs(rank: int, count: int):
+def many_graphs(rank: int, count: int, gen=None):
     """Config C3: `count` BA graphs, n uniform in [200, 20000] (seed 0), k = 3,
-    graph i seeded 1000 + i."""
-    from lgbc import generators as G
+    graph i seeded 1000 + i.  `gen` is the generator module (the library's by
+    default; the CPU arm passes the oracle's, built from the same source)."""
+    if gen is None:
+        from lgbc import generators as gen
     rng = np.random.default_rng(0 + rank)
     ns = rng.integers(200, 20001, count)
-    return [G.barabasi_albert(int(n), 3, seed=1000 + i) for i, n in enumerate(ns)]
+    return [gen.barabasi_albert(int(n), 3, seed=1000 + i) for i, n in enumerate(ns)]
+
+
+def reference_workload(args):
+    """The workload's graph and sources for the CPU arm: the same generator
+    source, seeds and `sample` draw as `workload`, built through the oracle's
+    copy of the generators so that this arm maps no library of the product."""
+    from oracle import oracle
+    from lgbc.centrality import sample  # pure Python (src/utils.jl:12-43)
+    if args.workload == "c1":
+        g = oracle.erdos_renyi_nm(10000, 50000, seed=1)
+        return g, np.arange(g.nv(), dtype=np.int32), "er10k_m50k_exact_bc"
+    if args.workload == "c4":
+        g = oracle.rmat(22, 16, seed=1, directed=True)
+        k = args.k or 16384
+        name = "rmat22_directed_sampled_bc_k"
+    else:
+        g = oracle.rmat(args.scale, 16, seed=1)
+        k = args.k or 4096
+        name = f"rmat{args.scale}_sampled_bc_k"
+    src1 = sample(range(1, g.nv() + 1), k, rng=np.random.default_rng(2))
+    src = (np.asarray(src1, np.int64) - 1).astype(np.int32)
+    return g, src, name + str(len(src))
 
 
 # ----------------------------------------------------------------------------- CPU arms
-def cpu_betweenness_sample(g, src: np.ndarray, nthreads: int, target_s: float, seed: int):
-    """Time the oracle's faithful mode (the reference's algorithm) on a bounded
-    sample of the workload's sources; returns (GTEPS, sample description)."""
+def cpu_betweenness_sample(g, src: np.ndarray, nthreads: int, target_s: float, seed: int,
+                           mode: str = "faithful"):
+    """Time the oracle (mode "faithful": the reference's heap Dijkstra with
+    predecessor lists; "fast": BFS Brandes, the same values) on a bounded
+    sample of the workload's sources; returns (GTEPS, seconds, sources)."""
     from oracle import oracle
     rp, ci = g.csr()
     kw = {}
@@ -251,14 +277,14 @@ def cpu_betweenness_sample(g, src: np.ndarray, nthreads: int, target_s: float, s
     # calibrate with one source per thread
     cal = rng.choice(act, size=min(len(act), nthreads), replace=False)
     t = time.perf_counter()
-    oracle.betweenness_raw(rp, ci, cal, mode="faithful", nthreads=nthreads, **kw)
+    oracle.betweenness_raw(rp, ci, cal, mode=mode, nthreads=nthreads, **kw)
     dt = max(time.perf_counter() - t, 1e-3)
     per_round = dt
     rounds = max(1, int(target_s / per_round))
     count = min(len(act), rounds * nthreads)
     samp = rng.choice(act, size=count, replace=False)
     t = time.perf_counter()
-    oracle.betweenness_raw(rp, ci, samp, mode="faithful", nthreads=nthreads, **kw)
+    oracle.betweenness_raw(rp, ci, samp, mode=mode, nthreads=nthreads, **kw)
     dt = time.perf_counter() - t
     m = g.ne()
     return count * m / dt / 1e9, dt, count
@@ -271,7 +297,7 @@ def run_reference(args, dist: Dist):
     nthreads = os.cpu_count() or 1
     if args.workload == "c3":
         return run_reference_many(args, nthreads)
-    g, src, k_act, _, wname = workload(0, args)
+    g, src, wname = reference_workload(args)
     rp, ci = g.csr()
     kw = {}
     if g.is_directed():
@@ -279,8 +305,8 @@ def run_reference(args, dist: Dist):
         kw = dict(directed=True, in_rowptr=irp, in_colidx=ici)
     deg = g.degrees()
     act = src[deg[src] > 0]
+    k_act = len(act)
     from oracle import oracle
-    oracle.build()
     m = g.ne()
     per_step = []
     count = None
@@ -446,6 +472,24 @@ def run_ours(args, dist: Dist):
     gd_t = ms.value / 1e3 / gd_reps
     gd_active = int(np.count_nonzero(np.diff(rp)[gsrc] > 0))
 
+    # ---- the double-float dependency variant (opt-in, narrower than FP64) ------------
+    df32 = None
+    if not tuning.get("dependency_df32", 0):
+        dg.set_tuning(dependency_df32=1)
+        try:
+            step_dev()
+            _lib.check(lib.lgbc_timer_start(h))
+            df_steps = max(1, min(args.steps, 3))
+            for _ in range(df_steps):
+                step_dev()
+            _lib.check(lib.lgbc_timer_stop(h, ctypes.byref(ms), None))
+        finally:
+            dg.set_tuning(dependency_df32=0)
+        df_t = ms.value / 1e3 / df_steps
+        df32 = {"value": te_step / df_t / 1e9, "unit": UNIT, "ms_per_step": df_t * 1e3,
+                "dtype": dep_dtype({"dependency_df32": 1}),
+                "note": "opt-in variant (tuning dependency_df32=1); not the headline"}
+
     # ---- roofline --------------------------------------------------------------------
     peak, peak_kind = peak_hbm()
     t_step = t_dev / args.steps
@@ -457,6 +501,7 @@ def run_ours(args, dist: Dist):
 
     # ---- CPU baseline (rank 0, N = 1 only) -------------------------------------------
     cpu = None
+    gd_cpu = None
     if dist.world == 1 and not args.no_cpu:
         nthreads = os.cpu_count() or 1
         cpu_v, cpu_t, cpu_n = cpu_betweenness_sample(g, src, nthreads, args.cpu_seconds, 7)
@@ -464,6 +509,20 @@ def run_ours(args, dist: Dist):
                "sample": f"{cpu_n} of the {k_act} active sources ({cpu_t:.1f} s), faithful "
                          "heap-Dijkstra restatement of src/shortestpaths/dijkstra.jl:59-141 + "
                          "_accumulate_basic!, one source per thread"}
+        fv, ft, fn = cpu_betweenness_sample(g, src, nthreads, args.cpu_seconds / 3, 8,
+                                            mode="fast")
+        cpu["fast_mode"] = {"value": fv, "unit": UNIT, "cores": nthreads, "kind": "port",
+                            "sample": f"{fn} of the {k_act} active sources ({ft:.1f} s), BFS "
+                                      "Brandes with the same values, one source per thread"}
+        from oracle import oracle
+        oracle.gdistances_many(rp, ci, gsrc[:nthreads], nthreads=nthreads)
+        t0 = time.perf_counter()
+        oracle.gdistances_many(rp, ci, gsrc, nthreads=nthreads)
+        gcpu_t = time.perf_counter() - t0
+        gd_cpu = {"ms": gcpu_t * 1e3, "gteps": gd_active * m / gcpu_t / 1e9, "cores": nthreads,
+                  "kind": "port",
+                  "sample": "the same 64 sources: the gdistances! restatement "
+                            "(src/traversals/bfs.jl:95-124), one source per thread"}
 
     if dist.rank == 0:
         line = {
@@ -495,7 +554,9 @@ def run_ours(args, dist: Dist):
             "kernel_stats_per_step": stats,
             "gdistances": {"sources": 64, "active": gd_active, "ms": gd_t * 1e3,
                            "gteps": gd_active * m / gd_t / 1e9,
-                           "algorithmic_gbs": gd_algorithmic_bytes(n, nnz, 64) / gd_t / 1e9},
+                           "algorithmic_gbs": gd_algorithmic_bytes(n, nnz, 64) / gd_t / 1e9,
+                           "cpu": gd_cpu},
+            "df32_variant": df32,
         }
         print(json.dumps(line), flush=True)
     lib.lgbc_device_free(bc_dev)
@@ -534,7 +595,7 @@ def run_ours_many(args, dist: Dist):
 def run_reference_many(args, nthreads: int):
     """C3 on the host cores: the faithful oracle on a bounded sample of graphs."""
     from oracle import oracle
-    graphs = many_graphs(0, args.graphs)
+    graphs = many_graphs(0, args.graphs, gen=oracle)
     rng = np.random.default_rng(5)
     per_step = []
     for it in range(args.warmup + args.steps):

@@ -66,9 +66,9 @@ end
 # ---------------------------------------------------------------- device graphs
 mutable struct DeviceGraph
     ptr::Ptr{Cvoid}
-    ne::Int
-    function DeviceGraph(ptr, ne)
-        d = new(ptr, ne)
+    fp::UInt64   # fingerprint of the adjacency lists the device copy was built from
+    function DeviceGraph(ptr, fp)
+        d = new(ptr, fp)
         finalizer(d) do x
             x.ptr != C_NULL && ccall(SYM[:lgbc_graph_destroy], Cint, (Ptr{Cvoid},), x.ptr)
             x.ptr = C_NULL
@@ -94,13 +94,31 @@ function flatten(adj::Vector{Vector{T}}) where {T<:Integer}
     return rowptr, colidx
 end
 
+"""A 64-bit fingerprint of every (vertex, neighbour) entry of `adj`: any
+add_edge! / rem_edge! sequence that leaves the lists different changes it
+(up to 64-bit collisions), including edits that keep ne(g) the same."""
+function fingerprint(adj::Vector{Vector{T}}) where {T<:Integer}
+    h = UInt64(length(adj))
+    @inbounds for v in eachindex(adj)
+        l = adj[v]
+        h = (h ⊻ UInt64(length(l))) * 0x100000001b3
+        for u in l
+            x = (UInt64(v) << 32) ⊻ UInt64(u)
+            x = (x ⊻ (x >> 33)) * 0xff51afd7ed558ccd
+            h = (h + (x ⊻ (x >> 29))) * 0x9e3779b97f4a7c15
+        end
+    end
+    return h
+end
+
 const CACHE = WeakKeyDict{AbstractGraph,DeviceGraph}()
 const CACHE_LOCK = ReentrantLock()
 
 function device_graph(g::Union{SimpleGraph,SimpleDiGraph})
     lock(CACHE_LOCK) do
+        fp = fingerprint(g.fadjlist)
         d = get(CACHE, g, nothing)
-        d !== nothing && d.ne == ne(g) && return d
+        d !== nothing && d.fp == fp && return d
         rowptr, colidx = flatten(g.fadjlist)
         dir = is_directed(g)
         in_rowptr, in_colidx = dir ? flatten(g.badjlist) : (Int64[], Int32[])
@@ -113,7 +131,7 @@ function device_graph(g::Union{SimpleGraph,SimpleDiGraph})
                         dir ? pointer(in_rowptr) : C_NULL, dir ? pointer(in_colidx) : C_NULL,
                         Cint(dir)))
         end
-        d = DeviceGraph(out[], ne(g))
+        d = DeviceGraph(out[], fp)
         CACHE[g] = d
         return d
     end

@@ -305,6 +305,18 @@ int orc_gdistances(int64_t n, const int64_t* rowptr, const int32_t* colidx,
   return 0;
 }
 
+// nsrc independent single-source gdistances (the loop above per source), one
+// source per host thread: dist[i * n + v] is the level of v from src[i].
+int orc_gdistances_many(int64_t n, const int64_t* rowptr, const int32_t* colidx,
+                        const int32_t* src, int64_t nsrc, int nthreads, int32_t* dist) {
+  for (int64_t i = 0; i < nsrc; ++i)
+    if (src[i] < 0 || src[i] >= n) return -1;
+  parallel_over(nsrc, nthreads, [&](int64_t i, int) {
+    orc_gdistances(n, rowptr, colidx, src + i, 1, dist + i * n);
+  });
+  return 0;
+}
+
 // dijkstra_shortest_paths(g, s; allpaths=true, trackvertices=true) with unit
 // weights (src/shortestpaths/dijkstra.jl:59-144).  Outputs: dists (INT64_MAX
 // = unreached), pathcounts, closest_vertices (n entries), predecessors as a

@@ -18,7 +18,14 @@ The oracle restates LightGraphs.jl v1.3.5 (paths relative to that project):
   * ``core_number``       -- src/degeneracy.jl:38-80
   * ``stress``            -- src/centrality/stress.jl:33-77
   * ``bfs_parents``, ``has_path`` -- src/traversals/bfs.jl:40-66, :150-172
+  * ``gdistances_many``   -- gdistances per source, one source per host thread
 Parity is pinned against the reference's golden vectors (tests/golden/).
+
+The shared object also carries the seeded graph generators of the workloads
+(``rmat``, ``erdos_renyi_nm``, ``barabasi_albert``): the library's own host
+source lightgraphs.jl_gb300/csrc/generators.cpp compiled in here as well, so
+that the CPU arm of bench.py builds the same graphs without mapping the CUDA
+library.
 """
 from __future__ import annotations
 
@@ -33,6 +40,9 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 _BUILD = os.path.join(_HERE, "_build")
 _SO = os.path.join(_BUILD, "liblgoracle.so")
 _SRC = os.path.join(_HERE, "lg_oracle.cpp")
+_ROOT = os.path.dirname(_HERE)
+_GEN = os.path.join(_ROOT, "lightgraphs.jl_gb300", "csrc", "generators.cpp")
+_INC = os.path.join(_ROOT, "include")
 _lock = threading.Lock()
 _lib = None
 
@@ -43,12 +53,13 @@ UNREACHED64 = np.iinfo(np.int64).max
 def build(force: bool = False) -> str:
     """Compile the oracle into ``oracle/_build/liblgoracle.so`` (g++, -O3)."""
     os.makedirs(_BUILD, exist_ok=True)
+    srcs = [_SRC, _GEN, os.path.join(_INC, "lgbc_gen.h")]
     if (not force and os.path.exists(_SO)
-            and os.path.getmtime(_SO) >= os.path.getmtime(_SRC)):
+            and os.path.getmtime(_SO) >= max(os.path.getmtime(p) for p in srcs)):
         return _SO
     tmp = _SO + f".tmp{os.getpid()}"
-    cmd = ["g++", "-O3", "-std=c++17", "-shared", "-fPIC", "-pthread",
-           _SRC, "-o", tmp]
+    cmd = ["g++", "-O3", "-std=c++17", "-shared", "-fPIC", "-pthread", "-I", _INC,
+           _SRC, _GEN, "-o", tmp]
     subprocess.run(cmd, check=True)
     os.replace(tmp, _SO)
     return _SO
@@ -65,6 +76,18 @@ def _load():
         p = ctypes.c_void_p
         lib.orc_gdistances.argtypes = [i64, p, p, p, i64, p]
         lib.orc_gdistances.restype = ctypes.c_int
+        lib.orc_gdistances_many.argtypes = [i64, p, p, p, i64, ctypes.c_int, p]
+        lib.orc_gdistances_many.restype = ctypes.c_int
+        P = ctypes.POINTER(_Csr)
+        lib.lgbc_gen_rmat.argtypes = [ctypes.c_int, ctypes.c_int, dbl, dbl, dbl,
+                                      ctypes.c_uint64, ctypes.c_int, P]
+        lib.lgbc_gen_rmat.restype = ctypes.c_int
+        lib.lgbc_gen_erdos_renyi.argtypes = [i64, i64, ctypes.c_uint64, ctypes.c_int, P]
+        lib.lgbc_gen_erdos_renyi.restype = ctypes.c_int
+        lib.lgbc_gen_barabasi_albert.argtypes = [i64, ctypes.c_int, ctypes.c_uint64, P]
+        lib.lgbc_gen_barabasi_albert.restype = ctypes.c_int
+        lib.lgbc_csr_free.argtypes = [P]
+        lib.lgbc_csr_free.restype = None
         lib.orc_dijkstra.argtypes = [i64, p, p, i32, p, p, p, p, p, i64]
         lib.orc_dijkstra.restype = i64
         lib.orc_betweenness.argtypes = [i64, p, p, p, p, ctypes.c_int, p, i64,
@@ -80,6 +103,81 @@ def _load():
         lib.orc_core_number.restype = ctypes.c_int
         _lib = lib
         return lib
+
+
+class _Csr(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int64), ("nnz", ctypes.c_int64), ("m", ctypes.c_int64),
+                ("directed", ctypes.c_int), ("rowptr", ctypes.POINTER(ctypes.c_int64)),
+                ("colidx", ctypes.POINTER(ctypes.c_int32)),
+                ("in_rowptr", ctypes.POINTER(ctypes.c_int64)),
+                ("in_colidx", ctypes.POINTER(ctypes.c_int32))]
+
+
+class CsrGraph:
+    """A generated graph as plain arrays: rowptr / colidx (out-lists), the
+    in-lists of a digraph, m (edges counted once, or arcs)."""
+
+    def __init__(self, c: _Csr):
+        n, nnz = int(c.n), int(c.nnz)
+        self.n, self.m, self.directed = n, int(c.m), bool(c.directed)
+        self.rowptr = np.ctypeslib.as_array(c.rowptr, shape=(n + 1,)).copy()
+        self.colidx = (np.ctypeslib.as_array(c.colidx, shape=(nnz,)).copy() if nnz
+                       else np.zeros(0, np.int32))
+        self.in_rowptr = self.in_colidx = None
+        if self.directed:
+            self.in_rowptr = np.ctypeslib.as_array(c.in_rowptr, shape=(n + 1,)).copy()
+            self.in_colidx = (np.ctypeslib.as_array(c.in_colidx, shape=(nnz,)).copy() if nnz
+                              else np.zeros(0, np.int32))
+
+    def nv(self):
+        return self.n
+
+    def ne(self):
+        return self.m
+
+    def is_directed(self):
+        return self.directed
+
+    def csr(self):
+        return self.rowptr, self.colidx
+
+    def in_csr(self):
+        return (self.in_rowptr, self.in_colidx) if self.directed else (self.rowptr, self.colidx)
+
+    def degrees(self):
+        d = np.diff(self.rowptr)
+        return d + np.diff(self.in_rowptr) if self.directed else d
+
+
+def _generated(rc, c):
+    lib = _load()
+    if rc != 0:
+        raise ValueError("generator parameters out of range")
+    g = CsrGraph(c)
+    lib.lgbc_csr_free(ctypes.byref(c))
+    return g
+
+
+def rmat(scale, edgefactor=16, a=0.57, b=0.19, c=0.19, *, seed=1, directed=False) -> CsrGraph:
+    """The library's R-MAT generator (same source, same seeds, same graph)."""
+    out = _Csr()
+    rc = _load().lgbc_gen_rmat(int(scale), int(edgefactor), float(a), float(b), float(c),
+                               int(seed) & (2**64 - 1), int(bool(directed)), ctypes.byref(out))
+    return _generated(rc, out)
+
+
+def erdos_renyi_nm(n, m, *, seed=1, directed=False) -> CsrGraph:
+    out = _Csr()
+    rc = _load().lgbc_gen_erdos_renyi(int(n), int(m), int(seed) & (2**64 - 1),
+                                      int(bool(directed)), ctypes.byref(out))
+    return _generated(rc, out)
+
+
+def barabasi_albert(n, k, *, seed=1) -> CsrGraph:
+    out = _Csr()
+    rc = _load().lgbc_gen_barabasi_albert(int(n), int(k), int(seed) & (2**64 - 1),
+                                          ctypes.byref(out))
+    return _generated(rc, out)
 
 
 def _ptr(a):
@@ -99,6 +197,21 @@ def gdistances(rowptr, colidx, sources) -> np.ndarray:
     src = np.ascontiguousarray(np.atleast_1d(np.asarray(sources, dtype=np.int32)))
     dist = np.empty(n, dtype=np.int32)
     rc = lib.orc_gdistances(n, _ptr(rowptr), _ptr(colidx), _ptr(src), len(src), _ptr(dist))
+    if rc != 0:
+        raise ValueError("oracle gdistances: bad source")
+    return dist
+
+
+def gdistances_many(rowptr, colidx, sources, nthreads=1) -> np.ndarray:
+    """One single-source gdistances per source, (len, n) int32, one source
+    per host thread."""
+    lib = _load()
+    rowptr, colidx = _csr(rowptr, colidx)
+    n = len(rowptr) - 1
+    src = np.ascontiguousarray(np.atleast_1d(np.asarray(sources, dtype=np.int32)))
+    dist = np.empty((len(src), n), dtype=np.int32)
+    rc = lib.orc_gdistances_many(n, _ptr(rowptr), _ptr(colidx), _ptr(src), len(src),
+                                 int(nthreads), _ptr(dist))
     if rc != 0:
         raise ValueError("oracle gdistances: bad source")
     return dist

@@ -3,7 +3,7 @@
 Run from the repository root in a checkout that has the LightGraphs.jl v1.3.5
 sources next to it:
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <path to the LightGraphs.jl v1.3.5 checkout>
 
 It copies, in plain text, the reference's golden graph and vectors:
   * test/testdata/graph-50-500.jgz     -> graph-50-500.lg   (gunzipped LG format)
@@ -108,4 +108,6 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path to the LightGraphs.jl checkout>")
+    main(sys.argv[1])
