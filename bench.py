@@ -226,6 +226,25 @@ def workload(rank: int, args):
     return g, src, k_act, gen_s, name
 
 
+def one_batch(g, src: np.ndarray, b: int, wname: str):
+    """Batch b (128 sources) of the workload as the library batches it: the
+    active sources ordered by their BFS distances to the 16 highest-degree
+    vertices (ties: smaller id), lexicographically, then by id -- the order
+    the source_order tuning gives.  A profiling case of one representative
+    batch of the full step."""
+    import lgbc
+    deg = g.degrees()
+    act = src[deg[src] > 0]
+    lm = np.lexsort((np.arange(g.nv()), -deg))[:16]
+    lm = lm[deg[lm] > 0]
+    d = lgbc.multi_gdistances(g, list(lm + 1)).astype(np.int64)[:, act]
+    order = np.lexsort((act,) + tuple(d[j] for j in reversed(range(len(lm)))))
+    sel = act[order][128 * b:128 * (b + 1)]
+    if len(sel) == 0:
+        raise SystemExit(f"--profile-batch {b}: the workload has {len(act)} active sources")
+    return sel.astype(np.int32), f"{wname}_batch{b}"
+
+
 def many_graphs(rank: int, count: int, gen=None):
     """Config C3: `count` BA graphs, n uniform in [200, 20000] (seed 0), k = 3,
     graph i seeded 1000 + i.  `gen` is the generator module (the library's by
@@ -359,6 +378,9 @@ def run_ours(args, dist: Dist):
     if args.workload == "c3":
         return run_ours_many(args, dist)
     g, src, k_act, gen_s, wname = workload(dist.rank, args)
+    if args.profile_batch is not None:
+        src, wname = one_batch(g, src, args.profile_batch, wname)
+        k_act = len(src)
     n, m = g.nv(), g.ne()
     rp, ci = g.csr()
     nnz = len(ci)
@@ -380,6 +402,28 @@ def run_ours(args, dist: Dist):
         tune_s = time.perf_counter() - t0
     tuning = {k: getattr(dg.tuning(), k) for k, _ in _lib.LgbcTuning._fields_}
     log(f"[rank {dist.rank}] tuning {tuning}" + (f" (autotuned in {tune_s:.2f} s)" if tune_s else ""))
+    if args.profile_gdistances:
+        # only the gdistances calls of the workload (for ncu launch lists):
+        # the 64-source batch, then single-source calls from 8 of its sources
+        rng = np.random.default_rng(3 + dist.rank)
+        gsrc = rng.choice(n, 64, replace=False).astype(np.int32)
+        out = np.empty((64, n), np.int32)
+        ms = ctypes.c_double()
+        _lib.check(lib.lgbc_timer_start(h))
+        for _ in range(max(1, args.steps)):
+            _lib.check(lib.lgbc_gdistances_batch(h, _lib.ptr(gsrc), 64, _lib.ptr(out)))
+        _lib.check(lib.lgbc_timer_stop(h, ctypes.byref(ms), None))
+        t_batch = ms.value / max(1, args.steps)
+        ss = [np.array([s_], np.int32) for s_ in gsrc[np.diff(rp)[gsrc] > 0][:8]]
+        _lib.check(lib.lgbc_timer_start(h))
+        for a in ss:
+            _lib.check(lib.lgbc_gdistances(h, _lib.ptr(a), 1, _lib.ptr(out[0])))
+        _lib.check(lib.lgbc_timer_stop(h, ctypes.byref(ms), None))
+        if dist.rank == 0:
+            print(json.dumps({"profile_gdistances": True, "batch64_ms": t_batch,
+                              "single_source_ms": ms.value / max(1, len(ss))}), flush=True)
+        return
+
     bc_dev = ctypes.c_void_p()
     _lib.check(lib.lgbc_device_alloc(ctypes.byref(bc_dev), 8 * n))
     srcp = _lib.ptr(src)
@@ -471,6 +515,17 @@ def run_ours(args, dist: Dist):
     _lib.check(lib.lgbc_timer_stop(h, ctypes.byref(ms), None))
     gd_t = ms.value / 1e3 / gd_reps
     gd_active = int(np.count_nonzero(np.diff(rp)[gsrc] > 0))
+    # single-source gdistances (the direction-optimising BFS of bfs.cu), 8 of
+    # the sources one call each; each call's time includes its n-entry read-back
+    one = np.empty(n, np.int32)
+    ss = [np.array([s_], np.int32) for s_ in gsrc[np.diff(rp)[gsrc] > 0][:8]]
+    for a in ss[:1]:
+        _lib.check(lib.lgbc_gdistances(h, _lib.ptr(a), 1, _lib.ptr(one)))
+    _lib.check(lib.lgbc_timer_start(h))
+    for a in ss:
+        _lib.check(lib.lgbc_gdistances(h, _lib.ptr(a), 1, _lib.ptr(one)))
+    _lib.check(lib.lgbc_timer_stop(h, ctypes.byref(ms), None))
+    ss_t = ms.value / 1e3 / max(1, len(ss))
 
     # ---- the double-float dependency variant (opt-in, narrower than FP64) ------------
     df32 = None
@@ -555,7 +610,14 @@ def run_ours(args, dist: Dist):
             "gdistances": {"sources": 64, "active": gd_active, "ms": gd_t * 1e3,
                            "gteps": gd_active * m / gd_t / 1e9,
                            "algorithmic_gbs": gd_algorithmic_bytes(n, nnz, 64) / gd_t / 1e9,
-                           "cpu": gd_cpu},
+                           "roofline_frac": gd_algorithmic_bytes(n, nnz, 64) / gd_t / 1e9 / peak,
+                           "cpu": gd_cpu,
+                           "single_source": {
+                               "sources": len(ss), "ms_per_call": ss_t * 1e3,
+                               "gteps": m / ss_t / 1e9,
+                               "algorithmic_gbs": gd_algorithmic_bytes(n, nnz, 1) / ss_t / 1e9,
+                               "note": "one lgbc_gdistances call per source, its 4n-byte "
+                                       "result read back inside the timed region"}},
             "df32_variant": df32,
         }
         print(json.dumps(line), flush=True)
@@ -765,6 +827,11 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--profile-only", action="store_true",
                     help="run only the device-resident steps (for ncu launch lists)")
+    ap.add_argument("--profile-gdistances", action="store_true",
+                    help="run only the workload's gdistances calls (for ncu launch lists)")
+    ap.add_argument("--profile-batch", type=int, default=None,
+                    help="run only batch B (128 sources, in the library's source order) of the "
+                         "workload: a one-batch case of the full step for profiling")
     args = ap.parse_args()
     dist = Dist()
     try:

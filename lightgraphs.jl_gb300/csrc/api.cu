@@ -115,6 +115,7 @@ int ensure_bfs(lgbc_graph* g) {
   const size_t n = static_cast<size_t>(g->n);
   const size_t words = (n + 31) / 32 + 4;
   LGBC_TRY(dev_alloc(&w.queue, n + 1));
+  LGBC_TRY(dev_alloc(&w.large, n + 1));
   LGBC_TRY(dev_alloc(&w.bm0, words));
   LGBC_TRY(dev_alloc(&w.bm1, words));
   LGBC_TRY(dev_alloc(&w.ctl, 1));
@@ -1222,7 +1223,7 @@ namespace lgbc::api {
 // caller has filled (kUnreached, and any other value on vertices the search
 // must treat as already visited).
 int run_bfs(lgbc_graph* g, const DevGraph& dg, int64_t nsrc) {
-  BfsBuffers b{g->bfs.queue, {g->bfs.bm0, g->bfs.bm1}, g->bfs.ctl};
+  BfsBuffers b{g->bfs.queue, {g->bfs.bm0, g->bfs.bm1}, g->bfs.ctl, g->bfs.large};
   g->launches += bfs_init(g->cfg, g->stream, dg, b, g->d_src, nsrc, g->d_dist);
   LGBC_TRY(check_launch(g));
   LGBC_TRY(read_ctl(g, b.ctl));

@@ -145,7 +145,9 @@ struct BfsWorkspace {
   uint32_t* bm0 = nullptr;
   uint32_t* bm1 = nullptr;
   BatchCtl* ctl = nullptr;
+  int32_t* large = nullptr;
   void release() {
+    dev_free(large);
     dev_free(queue);
     dev_free(bm0);
     dev_free(bm1);

@@ -6,8 +6,12 @@
 // INT32_MAX where nothing reaches it.  The per-level sort of the reference
 // (bfs.jl:121) only fixes visiting order and does not change any distance.
 //
-// Top-down levels expand the frontier queue over out-edges (one warp per
-// frontier vertex, atomicCAS on the distance claims a vertex once).
+// Top-down levels expand the frontier queue over out-edges with degree-binned
+// thread mapping: a warp takes 32 frontier vertices and streams their
+// concatenated out-lists 32 edges at a time, so a lane never idles on a short
+// list; a vertex with more than kBfsLarge out-edges (an R-MAT hub has 65K) is
+// deferred to a list whose edges the whole grid expands in a second kernel.
+// atomicCAS on the distance claims a vertex once.
 // Bottom-up levels give each unvisited vertex one thread that scans its
 // in-edges and stops at the first in-neighbour in the frontier bitmap; the
 // bitmap is staged in shared memory when it fits, and a warp owns 32
@@ -25,6 +29,10 @@ __device__ __forceinline__ long long gwarp() {
 }
 __device__ __forceinline__ long long nwarps() {
   return (static_cast<long long>(gridDim.x) * blockDim.x) >> 5;
+}
+
+__device__ __forceinline__ int64_t shfl_i64(int64_t x, int src) {
+  return static_cast<int64_t>(shfl_u64(static_cast<uint64_t>(x), src));
 }
 
 __device__ __forceinline__ uint32_t* bm_at(const BfsBuffers& b, int level) {
@@ -45,6 +53,7 @@ __global__ void k_bfs_ctl_reset(BatchCtl* c) {
   c->overflow_list = 0;
   c->overflow_sigma = 0;
   c->mode = 0;
+  c->large = 0;
 }
 
 // Level 0: claim each source once (duplicates in the source list are
@@ -77,14 +86,42 @@ __global__ void k_bfs_seed_done(BatchCtl* c) {
   }
 }
 
-// Zero the bitmap that the coming top-down level fills with atomicOr.
+// Zero the bitmap that the coming top-down level fills with atomicOr, and the
+// level's deferred-vertex count.
 __global__ void k_bfs_clear_next(BfsBuffers b, int64_t nwords) {
   uint32_t* nbm = bm_at(b, b.ctl->level + 1);
+  if (blockIdx.x == 0 && threadIdx.x == 0) b.ctl->large = 0;
   for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < nwords;
        i += static_cast<int64_t>(gridDim.x) * blockDim.x)
     nbm[i] = 0u;
 }
 
+// Claim w for level nl if no one has; returns whether this thread did.
+__device__ __forceinline__ bool bfs_claim(const DevGraph& g, uint32_t* nbm, int32_t* dist,
+                                          int32_t w, int32_t nl, unsigned long long& mf,
+                                          unsigned long long& mu) {
+  if (dist[w] != kUnreached || atomicCAS(dist + w, kUnreached, nl) != kUnreached) return false;
+  atomicOr(nbm + (w >> 5), 1u << (w & 31));
+  mf += static_cast<unsigned long long>(g.rowptr[w + 1] - g.rowptr[w]);
+  mu += static_cast<unsigned long long>(g.in_rowptr[w + 1] - g.in_rowptr[w]);
+  return true;
+}
+
+__device__ __forceinline__ void bfs_flush_counts(BatchCtl* c, unsigned long long mf,
+                                                 unsigned long long mu) {
+  mf = warp_sum_u64(mf);
+  mu = warp_sum_u64(mu);
+  if (lane_id() == 0) {
+    if (mf) atomicAdd(&c->mf, mf);
+    if (mu) atomicAdd(&c->mu_done, mu);
+  }
+}
+
+// Top-down level: lane j of a warp holds frontier entry base + j.  Vertices
+// with more than kBfsLarge out-edges go to b.large (when there is one); the
+// others' out-lists are walked as one concatenation, edge k of it by lane
+// k % 32 (the owning vertex found by a binary search over the warp's
+// inclusive degree scan).
 __global__ void __launch_bounds__(256) k_bfs_td(DevGraph g, BfsBuffers b, int32_t* dist) {
   BatchCtl* c = b.ctl;
   const unsigned long long lo = c->lo, hi = c->hi;
@@ -92,32 +129,77 @@ __global__ void __launch_bounds__(256) k_bfs_td(DevGraph g, BfsBuffers b, int32_
   uint32_t* nbm = bm_at(b, nl);
   const int ln = lane_id();
   unsigned long long mf = 0, mu = 0;
-  for (unsigned long long i = lo + gwarp(); i < hi; i += nwarps()) {
-    const int32_t v = b.queue[i];
+  for (unsigned long long base = lo + static_cast<unsigned long long>(gwarp()) * kWarp; base < hi;
+       base += static_cast<unsigned long long>(nwarps()) * kWarp) {
+    const unsigned long long i = base + ln;
+    int32_t v = 0;
+    int64_t e0 = 0, deg = 0;
+    if (i < hi) {
+      v = b.queue[i];
+      e0 = g.rowptr[v];
+      deg = g.rowptr[v + 1] - e0;
+    }
+    const bool defer = b.large != nullptr && deg > kBfsLarge;
+    const unsigned long long slot = warp_append(defer, &c->large);
+    if (defer) b.large[slot] = v;
+    const int d = defer ? 0 : static_cast<int>(deg);
+    int incl = d;
+#pragma unroll
+    for (int o = 1; o < kWarp; o <<= 1) {
+      const int y = __shfl_up_sync(kFull, incl, o);
+      if (ln >= o) incl += y;
+    }
+    const int total = __shfl_sync(kFull, incl, kWarp - 1);
+    const int off = incl - d;
+    for (int k0 = 0; k0 < total; k0 += kWarp) {
+      const int k = k0 + ln;
+      int j = 0;  // the lane whose list holds concatenated edge k: the first with incl > k
+#pragma unroll
+      for (int step = 16; step >= 1; step >>= 1) {
+        const int iv = __shfl_sync(kFull, incl, j + step - 1);
+        if (iv <= k) j += step;
+      }
+      const int64_t ej = shfl_i64(e0, j);
+      const int oj = __shfl_sync(kFull, off, j);
+      bool app = false;
+      int32_t w = 0;
+      if (k < total) {
+        w = g.colidx[ej + (k - oj)];
+        app = bfs_claim(g, nbm, dist, w, nl, mf, mu);
+      }
+      const unsigned long long q = warp_append(app, &c->tail);
+      if (app) b.queue[q] = w;
+    }
+  }
+  bfs_flush_counts(c, mf, mu);
+}
+
+// The deferred high-degree frontier vertices: for each in turn, the whole
+// grid walks its out-list (a warp takes 32 consecutive edges).
+__global__ void __launch_bounds__(256) k_bfs_td_large(DevGraph g, BfsBuffers b, int32_t* dist) {
+  BatchCtl* c = b.ctl;
+  const unsigned long long nlarge = c->large;
+  if (nlarge == 0) return;
+  const int32_t nl = c->level + 1;
+  uint32_t* nbm = bm_at(b, nl);
+  const int ln = lane_id();
+  unsigned long long mf = 0, mu = 0;
+  for (unsigned long long h = 0; h < nlarge; ++h) {
+    const int32_t v = b.large[h];
     const int64_t e0 = g.rowptr[v], e1 = g.rowptr[v + 1];
-    for (int64_t e = e0; e < e1; e += kWarp) {
+    for (int64_t e = e0 + gwarp() * kWarp; e < e1; e += nwarps() * kWarp) {
       const int64_t idx = e + ln;
       bool app = false;
       int32_t w = 0;
       if (idx < e1) {
         w = g.colidx[idx];
-        if (dist[w] == kUnreached && atomicCAS(dist + w, kUnreached, nl) == kUnreached) {
-          app = true;
-          atomicOr(nbm + (w >> 5), 1u << (w & 31));
-          mf += static_cast<unsigned long long>(g.rowptr[w + 1] - g.rowptr[w]);
-          mu += static_cast<unsigned long long>(g.in_rowptr[w + 1] - g.in_rowptr[w]);
-        }
+        app = bfs_claim(g, nbm, dist, w, nl, mf, mu);
       }
-      const unsigned long long slot = warp_append(app, &c->tail);
-      if (app) b.queue[slot] = w;
+      const unsigned long long q = warp_append(app, &c->tail);
+      if (app) b.queue[q] = w;
     }
   }
-  mf = warp_sum_u64(mf);
-  mu = warp_sum_u64(mu);
-  if (ln == 0) {
-    if (mf) atomicAdd(&c->mf, mf);
-    if (mu) atomicAdd(&c->mu_done, mu);
-  }
+  bfs_flush_counts(c, mf, mu);
 }
 
 template <bool STAGE>
@@ -255,7 +337,9 @@ int bfs_topdown(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const Bfs
   const int64_t nwords = (g.n + 31) >> 5;
   k_bfs_clear_next<<<c.grid, c.block, 0, s>>>(b, nwords);
   k_bfs_td<<<c.grid, c.block, 0, s>>>(g, b, dist);
-  return 2;
+  if (!b.large) return 2;
+  k_bfs_td_large<<<c.grid, c.block, 0, s>>>(g, b, dist);
+  return 3;
 }
 
 int bfs_bottomup(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const BfsBuffers& b,

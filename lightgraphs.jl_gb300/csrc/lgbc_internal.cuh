@@ -51,6 +51,7 @@ struct BatchCtl {
   // outside it discovers nothing at level L + 1, so bottom-up scans skip it
   unsigned long long front_union[kMaxWords];
   unsigned long long next_union[kMaxWords];  // lanes of Q_{L+1}, accumulated after its appends
+  unsigned long long large;     // single-source BFS: high-degree frontier vertices deferred this level
 };
 
 // ---------------------------------------------------------------------------

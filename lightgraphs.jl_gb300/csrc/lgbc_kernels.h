@@ -181,7 +181,10 @@ struct BfsBuffers {
   int32_t* queue;               // n: every level, concatenated
   uint32_t* bm[2];              // (n + 31) / 32 words each: frontier bitmaps
   BatchCtl* ctl;
+  int32_t* large = nullptr;     // n or null: frontier vertices with more than kBfsLarge
+                                // out-edges, expanded by the whole grid (null: by one warp)
 };
+constexpr int kBfsLarge = 1024;
 int bfs_init(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const BfsBuffers& b,
              const int32_t* src, int64_t nsrc, int32_t* dist);
 int bfs_topdown(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const BfsBuffers& b,
