@@ -161,7 +161,13 @@ struct LearnedWorkspace {
   int32_t* core = nullptr;
   uint8_t* flag = nullptr;
   int32_t* list = nullptr;
-  unsigned long long* counters = nullptr;  // [0] self-loop flag, [1] lowered, [2] list size
+  int32_t* large = nullptr;                // hubs deferred by a core pass
+  int32_t* log_v = nullptr;                // vertices lowered by a core pass
+  int32_t* log_old = nullptr;              //   and their values before it
+  int32_t* hub_v = nullptr;                // the same for the hubs
+  int32_t* hub_old = nullptr;
+  unsigned long long* counters = nullptr;  // [0] self-loop flag, [1] lowered this pass,
+                                           // [2] list size, [3] deferred hubs, [4] lowered hubs
   float4* feat = nullptr;
   float* y = nullptr;
   float* fscr = nullptr;
@@ -179,6 +185,11 @@ struct LearnedWorkspace {
     dev_free(core);
     dev_free(flag);
     dev_free(list);
+    dev_free(large);
+    dev_free(log_v);
+    dev_free(log_old);
+    dev_free(hub_v);
+    dev_free(hub_old);
     dev_free(counters);
     dev_free(feat);
     dev_free(y);

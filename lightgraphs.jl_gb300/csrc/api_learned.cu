@@ -18,7 +18,12 @@ int ensure_learned(lgbc_graph* g) {
   LGBC_TRY(dev_alloc(&w.core, n));
   LGBC_TRY(dev_alloc(&w.flag, n));
   LGBC_TRY(dev_alloc(&w.list, n));
-  LGBC_TRY(dev_alloc(&w.counters, 4));
+  LGBC_TRY(dev_alloc(&w.large, n));
+  LGBC_TRY(dev_alloc(&w.log_v, n));
+  LGBC_TRY(dev_alloc(&w.log_old, n));
+  LGBC_TRY(dev_alloc(&w.hub_v, n));
+  LGBC_TRY(dev_alloc(&w.hub_old, n));
+  LGBC_TRY(dev_alloc(&w.counters, 5));
   LGBC_TRY(dev_alloc(&w.feat, n));
   LGBC_TRY(dev_alloc(&w.y, n));
   LGBC_TRY(dev_alloc(&w.fscr, tiles + 1));
@@ -45,7 +50,7 @@ unsigned long long read_counter(lgbc_graph* g, int i, int* rc) {
 int compute_core(lgbc_graph* g, bool strict) {
   LearnedWorkspace& w = g->learned;
   const DevGraph dg = g->dev();
-  LGBC_CUDA(cudaMemsetAsync(w.counters, 0, 4 * 8, g->stream));
+  LGBC_CUDA(cudaMemsetAsync(w.counters, 0, 5 * 8, g->stream));
   g->launches += core_degree(g->cfg, g->stream, dg, w.core, reinterpret_cast<int*>(w.counters));
   LGBC_TRY(check_launch(g));
   int rc = LGBC_OK;
@@ -57,7 +62,9 @@ int compute_core(lgbc_graph* g, bool strict) {
   int64_t nlist = g->n;
   w.core_passes = 0;
   while (nlist > 0) {
-    g->launches += core_pass(g->cfg, g->stream, dg, list, nlist, w.core, w.flag, w.counters + 1);
+    const CorePassBuffers cb{w.counters + 1, w.counters + 4, w.counters + 3, w.log_v,
+                             w.log_old,      w.hub_v,        w.hub_old,      w.large};
+    g->launches += core_pass(g->cfg, g->stream, dg, list, nlist, w.core, w.flag, cb);
     LGBC_CUDA(cudaMemsetAsync(w.counters + 2, 0, 8, g->stream));
     g->launches += core_compact(g->cfg, g->stream, g->n, w.flag, w.list, w.counters + 2);
     LGBC_TRY(check_launch(g));

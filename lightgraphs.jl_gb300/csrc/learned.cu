@@ -59,64 +59,310 @@ __global__ void __launch_bounds__(256) k_core_degree(DevGraph g, int32_t* deg, i
   }
 }
 
-// Neighbour entries u != v of v with core[u] >= h (warp-wide count).
-__device__ __forceinline__ int count_at_least(const DevGraph& g, int32_t v, const int32_t* core,
-                                              int32_t h) {
+// ---- h-index passes ------------------------------------------------------------
+// One pass computes, for every vertex of the list (all vertices at first), the
+// h-index of its neighbours' values -- the largest h <= c (its own value) with
+// #{neighbour entries u != v : core[u] >= h} >= h -- and lowers core[v] to it.
+// Updates are in place; a value read while a neighbour is being lowered is at
+// least that neighbour's core number, so every stored value stays >= the core
+// number.  Each lowered vertex is logged with its old value; after the pass,
+// k_core_flag flags the neighbours u whose count at their own value the drop
+// can have changed: lo < core[u] <= c_old (a neighbour that did not count for
+// u before, or still counts, cannot change u's h-index).  Only flagged
+// vertices are searched again; a pass that lowers nothing is the fixed point,
+// the core numbers.
+struct CoreLog {
+  unsigned long long* count;  // lowered vertices this pass
+  int32_t* v;                 // n entries: the vertex
+  int32_t* old;               // n entries: its value before the pass
+};
+
+// A vertex with at most kCoreCached neighbour entries keeps their values
+// (capped at c) in registers, entry k * 32 + lane in slot k of that lane, so
+// the search reads memory once; larger lists go to k_core_pass_large.
+constexpr int kCoreSlots = 8;
+constexpr int kCoreCached = kCoreSlots * kWarp;
+// A vertex with at most kCoreThread entries is searched by one thread.
+constexpr int kCoreThread = 16;
+
+__device__ __forceinline__ int core_entries(const DevGraph& g, int32_t v) {
+  int64_t d = g.rowptr[v + 1] - g.rowptr[v];
+  if (is_digraph(g)) d += g.in_rowptr[v + 1] - g.in_rowptr[v];
+  return d > kCoreCached ? kCoreCached + 1 : static_cast<int>(d);
+}
+
+// Entry j of v's out-list followed by its in-list (a digraph counts every arc
+// at both ends); -1 past the end.
+__device__ __forceinline__ int32_t core_entry(const DevGraph& g, int32_t v, int64_t o0, int64_t n0,
+                                              int64_t j) {
+  if (j < n0) return g.colidx[o0 + j];
+  if (!is_digraph(g)) return -1;
+  const int64_t k = g.in_rowptr[v] + (j - n0);
+  return k < g.in_rowptr[v + 1] ? g.in_colidx[k] : -1;
+}
+
+// One thread: values counted down from min(c, entries).  Returns the new value.
+__device__ __forceinline__ int32_t core_search_thread(const DevGraph& g, int32_t v, int32_t c,
+                                                      int ent, const int32_t* core) {
+  const int64_t o0 = g.rowptr[v], n0 = g.rowptr[v + 1] - o0;
+  int32_t x[kCoreThread];
+#pragma unroll
+  for (int k = 0; k < kCoreThread; ++k) {
+    x[k] = -1;
+    if (k < ent) {
+      const int32_t u = core_entry(g, v, o0, n0, k);
+      if (u >= 0 && u != v) {
+        const int32_t cu = core[u];
+        x[k] = cu < c ? cu : c;
+      }
+    }
+  }
+  int h = c < ent ? c : ent;
+  for (; h > 0; --h) {
+    int cnt = 0;
+#pragma unroll
+    for (int k = 0; k < kCoreThread; ++k) cnt += x[k] >= h ? 1 : 0;
+    if (cnt >= h) break;
+  }
+  return h;
+}
+
+// One warp, values in registers: count(c), then a binary search in
+// [count(c), c - 1] with warp sums.  Returns the new value (c: unchanged).
+__device__ __forceinline__ int32_t core_search_warp(const DevGraph& g, int32_t v, int32_t c,
+                                                    const int32_t* core) {
+  const int ln = lane_id();
+  const int64_t o0 = g.rowptr[v], n0 = g.rowptr[v + 1] - o0;
+  int32_t x[kCoreSlots];
+#pragma unroll
+  for (int k = 0; k < kCoreSlots; ++k) {
+    x[k] = -1;
+    const int32_t u = core_entry(g, v, o0, n0, static_cast<int64_t>(k) * kWarp + ln);
+    if (u >= 0 && u != v) {
+      const int32_t cu = core[u];
+      x[k] = cu < c ? cu : c;
+    }
+  }
+  auto count = [&](int32_t h) {
+    int cnt = 0;
+#pragma unroll
+    for (int k = 0; k < kCoreSlots; ++k) cnt += x[k] >= h ? 1 : 0;
+    return static_cast<int>(__reduce_add_sync(kFull, static_cast<unsigned>(cnt)));
+  };
+  const int cnt = count(c);
+  if (cnt >= c) return c;
+  int lo = cnt, hi = c - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (count(mid) >= mid) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ void core_log(const CoreLog& lg, unsigned long long at, int32_t v,
+                                         int32_t old) {
+  lg.v[at] = v;
+  lg.old[at] = old;
+}
+
+// One pass: lane j of a warp takes list entry base + j.  Vertices with at
+// most kCoreThread entries are searched by their own lane; the others, one at
+// a time, by the whole warp, or deferred to `large` (more than kCoreCached
+// entries) for k_core_pass_large.
+__global__ void __launch_bounds__(256) k_core_pass(DevGraph g, const int32_t* list, long long nlist,
+                                                  int32_t* core, CoreLog lg, int32_t* large,
+                                                  unsigned long long* nlarge) {
+  const int ln = lane_id();
+  for (long long base = gwarp() * kWarp; base < nlist; base += nwarps() * kWarp) {
+    const long long i = base + ln;
+    int32_t v = 0, c = 0;
+    int ent = 0;
+    if (i < nlist) {
+      v = list ? list[i] : static_cast<int32_t>(i);
+      c = core[v];
+      if (c > 0) ent = core_entries(g, v);
+    }
+    int32_t h = c;
+    if (c > 0 && ent <= kCoreThread) h = core_search_thread(g, v, c, ent, core);
+    const bool lowered = h < c;
+    if (lowered) core[v] = h;
+    const unsigned long long at = warp_append(lowered, lg.count);
+    if (lowered) core_log(lg, at, v, c);
+    unsigned rest = __ballot_sync(kFull, c > 0 && ent > kCoreThread);
+    while (rest) {
+      const int j = __ffs(rest) - 1;
+      rest &= rest - 1u;
+      const int32_t vj = __shfl_sync(kFull, v, j);
+      const int32_t cj = __shfl_sync(kFull, c, j);
+      const int entj = __shfl_sync(kFull, ent, j);
+      if (entj > kCoreCached) {
+        if (ln == 0) large[atomicAdd(nlarge, 1ull)] = vj;
+        continue;
+      }
+      const int32_t hj = core_search_warp(g, vj, cj, core);
+      if (hj < cj && ln == 0) {
+        core[vj] = hj;
+        core_log(lg, atomicAdd(lg.count, 1ull), vj, cj);
+      }
+    }
+  }
+}
+
+// The vertices with more than kCoreCached neighbour entries (the hubs): one
+// block per vertex.  One pass over the list builds a histogram of the
+// neighbours' values capped at cap = min(c, kCoreHist) in shared memory, from
+// whose suffix sums S(h) = #{core[u] >= h} the largest h <= cap with
+// S(h) >= h is read directly; only an h-index above kCoreHist falls back to a
+// binary search with one list pass per probe.
+constexpr int kCoreHist = 1024;
+
+__device__ __forceinline__ int block_sum_int(int x, int* red) {
+  x = static_cast<int>(__reduce_add_sync(kFull, static_cast<unsigned>(x)));
+  __syncthreads();
+  if (lane_id() == 0) red[threadIdx.x >> 5] = x;
+  __syncthreads();
+  int t = 0;
+  for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) t += red[w];
+  return t;
+}
+
+__device__ __forceinline__ int block_count_at_least(const DevGraph& g, int32_t v, const int32_t* core,
+                                                    int32_t h, int* red) {
   int c = 0;
-  for (int64_t e = g.rowptr[v] + lane_id(); e < g.rowptr[v + 1]; e += kWarp) {
+  for (int64_t e = g.rowptr[v] + threadIdx.x; e < g.rowptr[v + 1]; e += blockDim.x) {
     const int32_t u = g.colidx[e];
     c += (u != v && core[u] >= h) ? 1 : 0;
   }
   if (is_digraph(g))
-    for (int64_t e = g.in_rowptr[v] + lane_id(); e < g.in_rowptr[v + 1]; e += kWarp) {
+    for (int64_t e = g.in_rowptr[v] + threadIdx.x; e < g.in_rowptr[v + 1]; e += blockDim.x) {
       const int32_t u = g.in_colidx[e];
       c += (u != v && core[u] >= h) ? 1 : 0;
     }
-  return __reduce_add_sync(kFull, c);
+  return block_sum_int(c, red);
 }
 
-// Flag the neighbours u != v of v whose value is above lo.
-__device__ __forceinline__ void flag_above(const DevGraph& g, int32_t v, const int32_t* core,
-                                           int32_t lo, uint8_t* flag) {
-  for (int64_t e = g.rowptr[v] + lane_id(); e < g.rowptr[v + 1]; e += kWarp) {
-    const int32_t u = g.colidx[e];
-    if (u != v && core[u] > lo) flag[u] = 1;
-  }
-  if (is_digraph(g))
-    for (int64_t e = g.in_rowptr[v] + lane_id(); e < g.in_rowptr[v + 1]; e += kWarp) {
-      const int32_t u = g.in_colidx[e];
-      if (u != v && core[u] > lo) flag[u] = 1;
-    }
-}
-
-// One h-index pass over the vertices of `list` (all vertices when list is
-// null).  A vertex whose value drops from c to h flags every neighbour whose
-// value is above h: only those can lose it from their own h-index count.
-// Updates are in place; a value read while a neighbour is being lowered is at
-// least the neighbour's core number, and the flag set by the neighbour brings
-// the vertex back in the next pass.
-__global__ void __launch_bounds__(256) k_core_pass(DevGraph g, const int32_t* list, long long nlist,
-                                                  int32_t* core, uint8_t* flag,
-                                                  unsigned long long* changed) {
-  const int ln = lane_id();
-  for (long long i = gwarp(); i < nlist; i += nwarps()) {
-    const int32_t v = list ? list[i] : static_cast<int32_t>(i);
+__global__ void __launch_bounds__(256) k_core_pass_large(DevGraph g, const int32_t* large,
+                                                        const unsigned long long* nlarge,
+                                                        int32_t* core, CoreLog lg) {
+  // lg: the hubs' own log (their neighbours are flagged by k_core_flag_large)
+  __shared__ int hist[kCoreHist + 1];
+  __shared__ int red[8];
+  __shared__ int s_h;
+  const unsigned long long nl = *nlarge;
+  const bool dir = is_digraph(g);
+  for (unsigned long long i = blockIdx.x; i < nl; i += gridDim.x) {
+    const int32_t v = large[i];
     const int32_t c = core[v];
-    if (c == 0) continue;
-    const int cnt = count_at_least(g, v, core, c);
-    if (cnt >= c) continue;
-    // h-index: the largest h with count(>= h) >= h.  count(>= cnt) >=
-    // count(>= c) = cnt, so h lies in [cnt, c - 1].
-    int lo = cnt, hi = c - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (count_at_least(g, v, core, mid) >= mid) lo = mid; else hi = mid - 1;
+    const int cap = c < kCoreHist ? c : kCoreHist;
+    for (int b = threadIdx.x; b <= cap; b += blockDim.x) hist[b] = 0;
+    __syncthreads();
+    // lanes with the same bin add their count with one atomic
+    auto bin_list = [&](const int32_t* ci, int64_t e0, int64_t e1) {
+      for (int64_t b0 = e0 + (threadIdx.x & ~(kWarp - 1)); b0 < e1; b0 += blockDim.x) {
+        const int64_t e = b0 + lane_id();
+        int bin = -1;
+        if (e < e1) {
+          const int32_t u = ci[e];
+          if (u != v) {
+            const int32_t cu = core[u];
+            bin = cu < cap ? cu : cap;
+          }
+        }
+        const unsigned peers = __match_any_sync(kFull, bin);
+        if (bin >= 0 && lane_id() == __ffs(peers) - 1) atomicAdd(&hist[bin], __popc(peers));
+      }
+    };
+    bin_list(g.colidx, g.rowptr[v], g.rowptr[v + 1]);
+    if (dir) bin_list(g.in_colidx, g.in_rowptr[v], g.in_rowptr[v + 1]);
+    __syncthreads();
+    if (threadIdx.x < kWarp) {
+      // lane j owns bins [j B, (j + 1) B) of [0, cap] (B = ceil((cap + 1) / 32))
+      const int ln = threadIdx.x;
+      const int B = (cap + kWarp) / kWarp;
+      const int b0 = ln * B, b1 = min(b0 + B, cap + 1);
+      int part = 0;
+      for (int b = b0; b < b1; ++b) part += hist[b];
+      int incl = part;  // suffix sum over lanes >= ln
+#pragma unroll
+      for (int o = 1; o < kWarp; o <<= 1) {
+        const int y = __shfl_down_sync(kFull, incl, o);
+        if (ln + o < kWarp) incl += y;
+      }
+      int S = incl - part;  // #{values >= b1}
+      int best = -1;
+      for (int b = b1 - 1; b >= b0 && best < 0; --b) {
+        S += hist[b];
+        if (S >= b) best = b;
+      }
+      best = static_cast<int>(__reduce_max_sync(kFull, static_cast<unsigned>(best + 1))) - 1;
+      if (ln == 0) s_h = best;
     }
-    if (ln == 0) {
-      core[v] = lo;
-      atomicAdd(changed, 1ull);
+    __syncthreads();
+    int h = s_h;  // the h-index over values capped at cap: exact when h < kCoreHist
+    if (h >= kCoreHist && c > kCoreHist) {
+      if (block_count_at_least(g, v, core, c, red) >= c) {
+        h = c;
+      } else {
+        int lo = kCoreHist, hi = c - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (block_count_at_least(g, v, core, mid, red) >= mid) lo = mid; else hi = mid - 1;
+        }
+        h = lo;
+      }
     }
-    flag_above(g, v, core, lo, flag);
+    if (h < c && threadIdx.x == 0) {
+      core[v] = h;
+      core_log(lg, atomicAdd(lg.count, 1ull), v, c);
+    }
+    __syncthreads();  // hist and s_h are reused by the next vertex
+  }
+}
+
+// After a pass: for each logged vertex v (value c_old -> lo), flag the
+// neighbours u with lo < core[u] <= c_old.  A warp per logged vertex (lists
+// of at most kCoreCached entries); k_core_flag_large gives each logged hub a
+// block.
+__global__ void __launch_bounds__(256) k_core_flag(DevGraph g, const int32_t* core, uint8_t* flag,
+                                                  CoreLog lg) {
+  const unsigned long long nlog = *lg.count;
+  const int ln = lane_id();
+  for (unsigned long long i = gwarp(); i < nlog; i += nwarps()) {
+    const int32_t v = lg.v[i];
+    const int32_t c_old = lg.old[i];
+    const int32_t lo = core[v];
+    for (int64_t e = g.rowptr[v] + ln; e < g.rowptr[v + 1]; e += kWarp) {
+      const int32_t u = g.colidx[e];
+      const int32_t cu = core[u];
+      if (u != v && cu > lo && cu <= c_old) flag[u] = 1;
+    }
+    if (is_digraph(g))
+      for (int64_t e = g.in_rowptr[v] + ln; e < g.in_rowptr[v + 1]; e += kWarp) {
+        const int32_t u = g.in_colidx[e];
+        const int32_t cu = core[u];
+        if (u != v && cu > lo && cu <= c_old) flag[u] = 1;
+      }
+  }
+}
+
+__global__ void __launch_bounds__(256) k_core_flag_large(DevGraph g, const int32_t* core,
+                                                        uint8_t* flag, CoreLog lg) {
+  const unsigned long long nlog = *lg.count;
+  for (unsigned long long i = blockIdx.x; i < nlog; i += gridDim.x) {
+    const int32_t v = lg.v[i];
+    const int32_t c_old = lg.old[i];
+    const int32_t lo = core[v];
+    for (int64_t e = g.rowptr[v] + threadIdx.x; e < g.rowptr[v + 1]; e += blockDim.x) {
+      const int32_t u = g.colidx[e];
+      const int32_t cu = core[u];
+      if (u != v && cu > lo && cu <= c_old) flag[u] = 1;
+    }
+    if (is_digraph(g))
+      for (int64_t e = g.in_rowptr[v] + threadIdx.x; e < g.in_rowptr[v + 1]; e += blockDim.x) {
+        const int32_t u = g.in_colidx[e];
+        const int32_t cu = core[u];
+        if (u != v && cu > lo && cu <= c_old) flag[u] = 1;
+      }
   }
 }
 
@@ -594,12 +840,20 @@ int core_degree(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, int32_t* 
 }
 
 int core_pass(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const int32_t* list,
-              int64_t nlist, int32_t* core, uint8_t* flag, unsigned long long* changed) {
+              int64_t nlist, int32_t* core, uint8_t* flag, const CorePassBuffers& b) {
   if (nlist <= 0) return 0;
-  const int64_t want = (nlist + 7) / 8;
+  const int64_t want = (nlist + 255) / 256;  // a warp takes 32 entries, a block 256
   const int grid = static_cast<int>(want < c.grid ? want : c.grid);
-  k_core_pass<<<grid, 256, 0, s>>>(g, list, nlist, core, flag, changed);
-  return 1;
+  const CoreLog lg{b.changed, b.log_v, b.log_old};
+  const CoreLog lh{b.changed_hubs, b.hub_v, b.hub_old};
+  cudaMemsetAsync(b.changed, 0, sizeof(unsigned long long), s);
+  cudaMemsetAsync(b.changed_hubs, 0, sizeof(unsigned long long), s);
+  cudaMemsetAsync(b.nlarge, 0, sizeof(unsigned long long), s);
+  k_core_pass<<<grid, 256, 0, s>>>(g, list, nlist, core, lg, b.large, b.nlarge);
+  k_core_pass_large<<<c.grid, 256, 0, s>>>(g, b.large, b.nlarge, core, lh);
+  k_core_flag<<<c.grid, 256, 0, s>>>(g, core, flag, lg);
+  k_core_flag_large<<<c.grid, 256, 0, s>>>(g, core, flag, lh);
+  return 4;
 }
 
 int core_compact(const LaunchCfg& c, cudaStream_t s, int64_t n, uint8_t* flag, int32_t* list,

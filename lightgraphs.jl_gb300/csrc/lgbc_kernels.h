@@ -236,10 +236,23 @@ int add_endpoints_many(const LaunchCfg& c, cudaStream_t s, double* bc, const int
 // ---- learned source proposal: learned.cu ----------------------------------
 // deg[v] = neighbours other than v; *loops |= 1 if v has a self-loop.
 int core_degree(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, int32_t* deg, int* loops);
-// One h-index pass over list[0, nlist) (all vertices when list is null);
-// lowered vertices flag their neighbours; *changed counts the lowered ones.
+// One h-index pass over list[0, nlist) (all vertices when list is null):
+// lowered vertices are logged (vertex, old value) -- those with more than 256
+// neighbour entries ("hubs", deferred to `large` and searched by a block each)
+// in the hub log -- and then their neighbours whose count can have changed
+// are flagged.  Every array holds n entries.
+struct CorePassBuffers {
+  unsigned long long* changed;       // lowered non-hub vertices this pass
+  unsigned long long* changed_hubs;  // lowered hubs this pass
+  unsigned long long* nlarge;        // hubs deferred this pass
+  int32_t* log_v;
+  int32_t* log_old;
+  int32_t* hub_v;
+  int32_t* hub_old;
+  int32_t* large;
+};
 int core_pass(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const int32_t* list,
-              int64_t nlist, int32_t* core, uint8_t* flag, unsigned long long* changed);
+              int64_t nlist, int32_t* core, uint8_t* flag, const CorePassBuffers& b);
 // list <- flagged vertices (flags cleared), *count += their number.
 int core_compact(const LaunchCfg& c, cudaStream_t s, int64_t n, uint8_t* flag, int32_t* list,
                  unsigned long long* count);

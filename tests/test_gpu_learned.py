@@ -289,3 +289,40 @@ def test_core_number_golden_decomposition(known):
     from conftest import golden_path
     g = lgbc.loadgraph(golden_path("graph-decomposition.lg"))
     assert lgbc.core_number(g).tolist() == known["core_number"]["expected"]
+
+
+def _complete(n):
+    iu = np.triu_indices(n, 1)
+    return lgbc.SimpleGraph.from_edge_arrays(n, iu[0], iu[1])
+
+
+@pytest.mark.parametrize("name", ["rmat16", "clique1100_with_tail", "hub_digraph"])
+def test_core_number_hubs(name):
+    # vertices with more than 256 neighbour entries take the block-per-vertex
+    # histogram pass; a core number above 1,024 (the 1,100-clique: 1,099)
+    # takes its binary-search fallback
+    if name == "rmat16":
+        g = gen.rmat(16, 16, seed=4)
+        kw = {}
+    elif name == "clique1100_with_tail":
+        k = _complete(1100)
+        rp, ci = k.csr()
+        src = np.repeat(np.arange(1100), np.diff(rp))
+        extra = np.arange(1100, 1400)
+        src = np.concatenate([src, extra, extra[1:]])
+        dst = np.concatenate([ci, extra % 1100, extra[:-1]])
+        g = lgbc.SimpleGraph.from_edge_arrays(1400, src, dst)
+        kw = {}
+    else:
+        rng = np.random.default_rng(9)
+        s = np.concatenate([np.zeros(2000, np.int64), rng.integers(1, 3000, 20000)])
+        d = np.concatenate([rng.integers(1, 3000, 2000), rng.integers(1, 3000, 20000)])
+        keep = s != d
+        g = lgbc.SimpleDiGraph.from_edge_arrays(3000, s[keep], d[keep])
+        irp, ici = g.in_csr()
+        kw = dict(directed=True, in_rowptr=irp, in_colidx=ici)
+    rp, ci = g.csr()
+    got = lgbc.core_number(g)
+    np.testing.assert_array_equal(got, oracle.core_number(rp, ci, **kw))
+    if name == "clique1100_with_tail":
+        assert got[:1100].min() == 1099
