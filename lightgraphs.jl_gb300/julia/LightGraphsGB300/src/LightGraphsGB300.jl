@@ -33,7 +33,8 @@ using LightGraphs: AbstractGraph, SimpleGraph, SimpleDiGraph, DefaultDistance, n
 using Libdl
 
 export betweenness_centrality, gdistances, gdistances!, stress_centrality, closeness_centrality,
-       radiality_centrality, eccentricity, bfs_parents, bfs_tree, has_path, core_number
+       radiality_centrality, eccentricity, bfs_parents, bfs_tree, has_path, core_number,
+       path_counts
 
 const LGBC_OK = Cint(0)
 const LGBC_EINVAL = Cint(-1)
@@ -235,6 +236,33 @@ function stress_centrality(g::Union{SimpleGraph,SimpleDiGraph}, vs=vertices(g))
 end
 stress_centrality(g::Union{SimpleGraph,SimpleDiGraph}, k::Integer) =
     stress_centrality(g, LightGraphs.sample(vertices(g), k))
+
+# ---------------------------------------------------------------- path counts
+"""
+    path_counts(g, sources) -> (pathcounts, dists)
+
+`dijkstra_shortest_paths(g, s).pathcounts` and `.dists` with unit weights
+(src/shortestpaths/dijkstra.jl:59-141) for every `s` in `sources`, as
+`nv(g) x length(sources)` matrices (column `i` for `sources[i]`): counts as
+Float64 (exact below 2^53), `typemax(T)` distances where `s` does not reach.
+"""
+function path_counts(g::Union{SimpleGraph{T},SimpleDiGraph{T}}, sources) where {T}
+    src = sources0(g, sources)
+    pc = zeros(Float64, nv(g), length(src))
+    lv = Matrix{Int32}(undef, nv(g), length(src))
+    if nv(g) > 0 && !isempty(src)
+        d = device_graph(g)
+        GC.@preserve src pc lv begin
+            check(ccall(SYM[:lgbc_path_counts], Cint,
+                        (Ptr{Cvoid}, Ptr{Int32}, Int64, Ptr{Float64}, Ptr{Int32}),
+                        d.ptr, src, length(src), pc, lv))
+        end
+    else
+        fill!(lv, typemax(Int32))
+    end
+    dists = T[l == typemax(Int32) ? typemax(T) : T(l) for l in lv]
+    return pc, dists
+end
 
 # ---------------------------------------------------------------- distance reductions
 """(reachable count incl. the source, distance sum, largest distance) per source."""
