@@ -46,7 +46,7 @@ function __init__()
     LIB[] = Libdl.dlopen(path)
     for s in (:lgbc_graph_create, :lgbc_graph_destroy, :lgbc_gdistances, :lgbc_betweenness,
               :lgbc_last_error, :lgbc_stress, :lgbc_distance_stats, :lgbc_bfs_parents,
-              :lgbc_has_path, :lgbc_core_number, :lgbc_tune)
+              :lgbc_has_path, :lgbc_core_number, :lgbc_tune, :lgbc_path_counts)
         SYM[s] = Libdl.dlsym(LIB[], s)
     end
 end
