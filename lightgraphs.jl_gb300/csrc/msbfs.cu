@@ -31,6 +31,7 @@
 // cut into kHubChunk-edge items processed by the whole grid (k_ms_hub_*).
 // Stress, distance and level-statistics batches are one-word.
 #include <algorithm>
+#include <type_traits>
 
 #include "lgbc_kernels.h"
 #include "xf64.cuh"
@@ -240,39 +241,46 @@ __device__ __forceinline__ df32 acc_done(df32 acc) { return fast_two_sum(acc.hi,
 template <class T, class A> __device__ __forceinline__ void acc_row(A& acc, T x);
 template <> __device__ __forceinline__ void acc_row(unsigned long long& acc, unsigned long long x) { acc += x; }
 // FP64 dependencies: psi rows hold binary64 bits, summed by the gather
-// accumulator (renormalised at the end of every 32-edge chunk).
-template <> __device__ __forceinline__ void acc_row(xg64& acc, unsigned long long x) {
-  xg_add_bits(acc, x);
-}
-// In a two-word batch, slot 0 (lanes 0-31) of the gather accumulators adds on
-// the FP64 pipe (binary64 running sums, its bits kept in xg64::m) while
-// slots 1-3 add on the integer pipes: the two units work in parallel and
-// neither carries all the adds.
-template <int W> __device__ __forceinline__ constexpr bool fp64_slot(int k) { return W == 2 && k == 0; }
+// accumulator (renormalised at the end of every 32-edge chunk).  In a
+// two-word batch the first NF slots (lanes 0 .. 32 NF - 1) add on the FP64
+// pipe instead (binary64 running sums, their bits kept in m) while the other
+// slots add on the integer pipes: the two units work in parallel and neither
+// carries all the adds.  NF is a property of the accumulator type, chosen per
+// kernel from its measured FP64-pipe load.
+template <int NF> struct XgAcc : xg64 {};
+
+template <class A, int W> struct Fp64Slots {
+  static constexpr int value = 0;
+};
+template <int NF, int W> struct Fp64Slots<XgAcc<NF>, W> {
+  static constexpr int value = W == 2 ? NF : 0;
+};
 
 template <class T, class A, int W>
-__device__ __forceinline__ void acc_slot(A& acc, T x, int k) { acc_row<T, A>(acc, x); }
-template <>
-__device__ __forceinline__ void acc_slot<unsigned long long, xg64, 2>(xg64& acc, unsigned long long x,
-                                                                     int k) {
-  if (fp64_slot<2>(k))
-    acc.m = static_cast<unsigned long long>(__double_as_longlong(
-        __longlong_as_double(static_cast<long long>(acc.m)) + __longlong_as_double(static_cast<long long>(x))));
-  else
-    xg_add_bits(acc, x);
+__device__ __forceinline__ void acc_slot(A& acc, T x, int k) {
+  if constexpr (std::is_same<A, XgAcc<1>>::value || std::is_same<A, XgAcc<2>>::value) {
+    if (k < Fp64Slots<A, W>::value)
+      acc.m = static_cast<unsigned long long>(__double_as_longlong(
+          __longlong_as_double(static_cast<long long>(acc.m)) +
+          __longlong_as_double(static_cast<long long>(x))));
+    else
+      xg_add_bits(acc, x);
+  } else {
+    acc_row<T, A>(acc, x);
+  }
 }
 
 template <class A> __device__ __forceinline__ void acc_chunk_end(A&) {}
-template <> __device__ __forceinline__ void acc_chunk_end(xg64& a) { xg_norm(a); }
+template <int NF> __device__ __forceinline__ void acc_chunk_end(XgAcc<NF>& a) { xg_norm(a); }
 template <int W, class A, int K> __device__ __forceinline__ void chunk_end(A (&a)[K]) {
 #pragma unroll
   for (int k = 0; k < K; ++k)
-    if (!fp64_slot<W>(k)) acc_chunk_end(a[k]);
+    if (k >= Fp64Slots<A, W>::value) acc_chunk_end(a[k]);
 }
 
 // The extended value of slot k of a normalised gather accumulator.
-template <int W> __device__ __forceinline__ xf64 gather_value(const xg64& a, int k) {
-  return fp64_slot<W>(k) ? xf_from_bits(a.m) : xg_to_xf(a);
+template <int W, class A> __device__ __forceinline__ xf64 gather_value(const A& a, int k) {
+  return k < Fp64Slots<A, W>::value ? xf_from_bits(a.m) : xg_to_xf(a);
 }
 template <> __device__ __forceinline__ void acc_row(double& acc, double x) { acc += x; }
 template <> __device__ __forceinline__ void acc_row(df32& acc, float2 x) { acc_add(acc, x.x, x.y); }
@@ -286,7 +294,8 @@ template <class A> __device__ __forceinline__ A zero_acc();
 template <> __device__ __forceinline__ unsigned long long zero_acc() { return 0ull; }
 template <> __device__ __forceinline__ double zero_acc() { return 0.0; }
 template <> __device__ __forceinline__ df32 zero_acc() { return df32{0.f, 0.f}; }
-template <> __device__ __forceinline__ xg64 zero_acc() { return xg_zero(); }
+template <> __device__ __forceinline__ XgAcc<1> zero_acc() { return XgAcc<1>{}; }
+template <> __device__ __forceinline__ XgAcc<2> zero_acc() { return XgAcc<2>{}; }
 
 template <class A, int K> __device__ __forceinline__ void zero_accs(A (&a)[K]) {
 #pragma unroll
@@ -488,14 +497,14 @@ __device__ __forceinline__ void psi_range_f64(const int32_t* __restrict__ ci, in
   psi_range<double, double, W>(ci, e0, e1, F, succ, psi, dense, acc);
 }
 
-template <int W>
+template <int W, int NF = 1>
 __device__ __forceinline__ void psi_range_x(const int32_t* __restrict__ ci, int64_t e0, int64_t e1,
                                             const Lanes<W>& F, const Lanes<W>* __restrict__ succ,
                                             const void* __restrict__ psi, int dense,
                                             xf64 (&acc)[2 * W]) {
-  xg64 a[2 * W];
+  XgAcc<NF> a[2 * W];
   zero_accs(a);
-  psi_range<unsigned long long, xg64, W>(ci, e0, e1, F, succ, psi, dense, a);
+  psi_range<unsigned long long, XgAcc<NF>, W>(ci, e0, e1, F, succ, psi, dense, a);
 #pragma unroll
   for (int k = 0; k < 2 * W; ++k) acc[k] = gather_value<W>(a[k], k);
 }
@@ -1573,15 +1582,15 @@ __global__ void __launch_bounds__(256, W == 1 ? 3 : 2) k_ms_delta_seg(DevGraph g
                                           if (ln == 0 && contrib.hi != 0.f) bc[vj] += df_to_double(contrib);
                                         });
     } else if (SK == kSigmaU64F64) {
-      seg_gather<unsigned long long, xg64, true, W>(
+      seg_gather<unsigned long long, XgAcc<1>, true, W>(
           mine, e0, dg, F, g.colidx, succ, reinterpret_cast<const unsigned long long*>(b.psi),
-          [&](int j, const Lanes<W>&, const xg64 (&a)[2 * W]) {
+          [&](int j, const Lanes<W>&, const XgAcc<1> (&a)[2 * W]) {
             const int32_t vj = __shfl_sync(kFull, v, j);
             xf64 d[2 * W];
 #pragma unroll
             for (int k = 0; k < 2 * W; ++k) {
-              xg64 t = a[k];  // flushed mid-chunk: renormalise first
-              if (!fp64_slot<W>(k)) xg_norm(t);
+              XgAcc<1> t = a[k];  // flushed mid-chunk: renormalise first
+              if (k >= Fp64Slots<XgAcc<1>, W>::value) xg_norm(t);
               d[k] = gather_value<W>(t, k);
             }
             const xf64 contrib =
