@@ -714,6 +714,21 @@ def run_c5_kernels(args):
     m.close()
 
 
+CEILING_ARMS = ("mass", "sqrt_mass", "uniform_active")
+
+
+def ceiling_arms(compare, g, exact_bc, ks, args, recs):
+    """Adds the fixed-proposal arms built from exact per-source masses (what a
+    perfect predictor of the network's target could reach) to ``recs``."""
+    methods = ("learned", "learned_systematic")
+    if not args.c5_ceiling:
+        return recs, methods, None
+    props, mass_ms = compare.ceiling_proposals(g)
+    for name in CEILING_ARMS:
+        recs = recs + compare.run_fixed(g, exact_bc, props[name], ks, name, seeds=args.c5_seeds)
+    return recs, methods + CEILING_ARMS, mass_ms
+
+
 def run_c5(args, dist: Dist):
     """Config C5: train the proposal on 128 R-MAT scale-14 + 128 BA graphs,
     then compare uniform and learned sampling against exact BC on (a) the
@@ -742,8 +757,9 @@ def run_c5(args, dist: Dist):
     st = g.device_handle().stats()
     log(f"exact BC on rmat{args.scale}: {ex_ms / 1e3:.1f} s, {st['active_sources']} active sources")
     recs, build_ms = compare.run_estimators(g, ex, prop, ks_u, ks_l, seeds=args.c5_seeds)
-    evals[f"rmat{args.scale}"] = dict(n=g.nv(), m=g.ne(), exact_ms=ex_ms,
-                                      **compare.summarise(recs, build_ms, kt))
+    recs, methods, mass_ms = ceiling_arms(compare, g, ex, ks_l, args, recs)
+    evals[f"rmat{args.scale}"] = dict(n=g.nv(), m=g.ne(), exact_ms=ex_ms, mass_ms=mass_ms,
+                                      **compare.summarise(recs, build_ms, kt, methods))
     log(json.dumps(evals[f"rmat{args.scale}"]["equal_error"]))
     g.device_handle().close()
     del g
@@ -777,11 +793,26 @@ def run_c5(args, dist: Dist):
         del big
         ex, ex_ms = compare.exact(sub)
         recs, build_ms = compare.run_estimators(sub, ex, prop, ks_u, ks_l, seeds=args.c5_seeds)
+        recs, methods, mass_ms = ceiling_arms(compare, sub, ex, ks_l, args, recs)
         evals[f"rmat{args.c5_ball_scale}_ball{args.c5_ball}"] = dict(
-            n=sub.nv(), m=sub.ne(), center=center, exact_ms=ex_ms, whole_graph=whole,
-            **compare.summarise(recs, build_ms, kt))
+            n=sub.nv(), m=sub.ne(), center=center, exact_ms=ex_ms, mass_ms=mass_ms,
+            whole_graph=whole, **compare.summarise(recs, build_ms, kt, methods))
         log(json.dumps(evals[f"rmat{args.c5_ball_scale}_ball{args.c5_ball}"]["equal_error"]))
     out["evaluations"] = evals
+    # time ratio at equal L1 per graph and budget, learned (with build) and the ceiling arms
+    ceiling = {}
+    for name, e in evals.items():
+        per_k = {}
+        for r in e["equal_error"]:
+            row = {"learned": r["time_ratio_with_build"]}
+            for m in CEILING_ARMS:
+                for x in e.get("equal_error_" + m, []):
+                    if x["k_uniform"] == r["k_uniform"]:
+                        row[m] = x["time_ratio"]
+            per_k[str(r["k_uniform"])] = row
+        ceiling[name] = per_k
+    out["ceiling"] = ceiling
+    log(json.dumps(out["ceiling"]))
     main_eval = evals[f"rmat{args.scale}"]
     head = next(r for r in main_eval["equal_error"] if r["k_uniform"] == 4096)
     head_sys = next(r for r in main_eval["equal_error_systematic"] if r["k_uniform"] == 4096)
@@ -789,6 +820,7 @@ def run_c5(args, dist: Dist):
         "metric": "GPU time of learned sampling at uniform sampling's L1 error, relative to uniform",
         "value": head["time_ratio_with_build"], "unit": "ratio", "n_gpus": 1,
         "steps": sum(len(e["uniform"]) + len(e["learned"]) + len(e["learned_systematic"])
+                     + sum(len(e.get(m, [])) for m in CEILING_ARMS)
                      for e in evals.values()) * args.c5_seeds,
         "warmup": 0, "ms_per_step": None, "higher_is_better": False, "scaling": "none",
         "vs_baseline": None, "dtype": "u64 path counts, f64 weighted dependencies; MLP bf16/f32",
@@ -820,6 +852,8 @@ def main():
     ap.add_argument("--c5-seeds", type=int, default=8)
     ap.add_argument("--c5-ball-scale", type=int, default=24, help="c5: 0 skips the ball graph")
     ap.add_argument("--c5-ball", type=int, default=100000)
+    ap.add_argument("--c5-ceiling", type=int, default=1,
+                    help="c5: 1 adds the proposals built from exact masses (0 skips them)")
     ap.add_argument("--c5-kernels", action="store_true",
                     help="c5: only run the proposal's kernels once on R-MAT --scale (profiling)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0,

@@ -504,7 +504,7 @@ __global__ void __launch_bounds__(256) k_mlp_residual(const float4* __restrict__
   }
 }
 
-// Block-wide sum of one float per thread (blockDim.x == kGradRows).
+// Block-wide sum of one float per thread (blockDim.x a multiple of 32).
 __device__ __forceinline__ float block_sum(float v, float* red) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
   __syncthreads();
@@ -515,107 +515,137 @@ __device__ __forceinline__ float block_sum(float v, float* red) {
   return s;
 }
 
+// Mean residual and loss of the batch, once per step (one block, fixed order):
+// center = sum(e) / B, loss = sum((e - center)^2) / B.
+__global__ void __launch_bounds__(1024) k_mlp_center(const float* __restrict__ e, int B,
+                                                     float* __restrict__ center,
+                                                     float* __restrict__ loss) {
+  __shared__ float red[32];
+  const int t = threadIdx.x;
+  float s = 0.f;
+  for (int r = t; r < B; r += blockDim.x) s += e[r];
+  const float mean = block_sum(s, red) / static_cast<float>(B);
+  float q = 0.f;
+  for (int r = t; r < B; r += blockDim.x) {
+    const float d = e[r] - mean;
+    q += d * d;
+  }
+  q = block_sum(q, red);
+  if (t == 0) {
+    *center = mean;
+    *loss = q / static_cast<float>(B);
+  }
+}
+
 // Gradient of the per-batch centred squared error
 //   loss = (1 / B) sum_r (e_r - mean(e))^2,   dloss / dyhat_r = 2 (e_r - mean(e)) / B
 // (the softmax proposal is shift-invariant, so only relative log-masses
-// within one graph matter).  Block b handles rows [b * kGradRows, ...) and
-// writes its partial gradient to part[b][kMlpParams]; block 0 also writes the
-// loss.  Activations of the block's rows are staged in shared memory and the
-// weight gradients reduced over rows there.
+// within one graph matter).  Block b handles rows [b * kGradRows, ...) with
+// two threads per row and writes its partial gradient to part[b][kMlpParams]
+// (the batch mean comes from k_mlp_center).  Activations of the block's rows are staged
+// in shared memory and the weight gradients reduced over rows there.
+// dloss / da2[r][j] is not staged: it is g_r W3[j] where relu(a2[r][j]) > 0,
+// else 0, recomputed from the staged relu(a2) and g.  A 64-row block holds
+// 68 KB of shared memory; at two blocks per SM every thread keeps its 64-wide
+// h1 and dh1 rows in registers without spilling (three blocks spill ~400 B).
 constexpr int kStride = kH + 1;  // padded row stride (no bank conflicts)
 
-__global__ void __launch_bounds__(kGradRows) k_mlp_grad(const float4* __restrict__ x,
-                                                       long long r0, int B,
-                                                       const float* __restrict__ e,
-                                                       const __nv_bfloat16* __restrict__ P,
-                                                       MlpNorm nm, float* __restrict__ part,
-                                                       float* __restrict__ loss) {
+// Hidden unit of step q (0..31) for half h of a row's pair of threads:
+// 16-unit runs alternate between the halves, so the 32 lanes of a warp
+// (16 rows x 2 halves) write 32 distinct banks of a kStride-padded row.
+__device__ __forceinline__ int pair_unit(int h, int q) { return ((q >> 4) << 5) | (h << 4) | (q & 15); }
+
+__global__ void __launch_bounds__(kGradThreads, 2) k_mlp_grad(const float4* __restrict__ x,
+                                                             long long r0, int B,
+                                                             const float* __restrict__ e,
+                                                             const float* __restrict__ center,
+                                                             const __nv_bfloat16* __restrict__ P,
+                                                             MlpNorm nm, float* __restrict__ part) {
   extern __shared__ __align__(16) float sm[];
   float* w = sm;                                  // kMlpParamsPadded
   float* s_h1 = w + kMlpParamsPadded;             // [rows][kStride]
   float* s_h2 = s_h1 + kGradRows * kStride;       // relu(a2)
-  float* s_d2 = s_h2 + kGradRows * kStride;       // dloss / da2
-  float* s_d1 = s_d2 + kGradRows * kStride;       // dloss / da1
+  float* s_d1 = s_h2 + kGradRows * kStride;       // dloss / da1
   float* s_x = s_d1 + kGradRows * kStride;        // [rows][4] standardised inputs
   float* s_g = s_x + kGradRows * 4;               // dloss / dyhat
-  float* red = s_g + kGradRows;                   // 32
   load_weights(P, w);
   const int t = threadIdx.x;
+  const float mean = *center;
 
-  // mean residual over the whole batch (every block, same order)
-  float s = 0.f;
-  for (int r = t; r < B; r += blockDim.x) s += e[r];
-  const float mean = block_sum(s, red) / static_cast<float>(B);
-
-  const int r = blockIdx.x * kGradRows + t;
+  const int rl = t >> 1, half = t & 1;
+  const int r = blockIdx.x * kGradRows + rl;
   const bool live = r < B;
   float gr = 0.f;
   if (live) gr = 2.f * (e[r] - mean) / static_cast<float>(B);
-  if (blockIdx.x == 0) {
-    float q = 0.f;
-    for (int i = t; i < B; i += blockDim.x) {
-      const float d = e[i] - mean;
-      q += d * d;
-    }
-    q = block_sum(q, red);
-    if (t == 0) *loss = q / static_cast<float>(B);
-  }
-  s_g[t] = gr;
+  if (half == 0) s_g[rl] = gr;
   {
     float xs[4] = {0.f, 0.f, 0.f, 0.f};
     float h1[kH], dh1[kH];
     if (live) standardise(x[r0 + r], nm, xs);
     layer1(w, xs, h1);
 #pragma unroll
-    for (int i = 0; i < kH; ++i) {
-      dh1[i] = 0.f;
-      s_h1[t * kStride + i] = h1[i];
-    }
+    for (int i = 0; i < kH; ++i) dh1[i] = 0.f;
+    // register indices stay compile-time: select between the halves' units
 #pragma unroll
-    for (int f = 0; f < 4; ++f) s_x[t * 4 + f] = xs[f];
+    for (int q = 0; q < kH / 2; ++q)
+      s_h1[rl * kStride + pair_unit(half, q)] = half ? h1[pair_unit(1, q)] : h1[pair_unit(0, q)];
+    s_x[rl * 4 + 2 * half] = half ? xs[2] : xs[0];
+    s_x[rl * 4 + 2 * half + 1] = half ? xs[3] : xs[1];
+    // this thread's 32 units of layer 2; the pair's dh1 halves are summed below
 #pragma unroll 2
-    for (int j = 0; j < kH; ++j) {
+    for (int q = 0; q < kH / 2; ++q) {
+      const int j = pair_unit(half, q);
       const float a = layer2_unit(w, h1, j);
       const float d2 = a > 0.f ? gr * w[kMlpW3 + j] : 0.f;
-      s_h2[t * kStride + j] = fmaxf(a, 0.f);
-      s_d2[t * kStride + j] = d2;
+      s_h2[rl * kStride + j] = fmaxf(a, 0.f);
       const float4* row = reinterpret_cast<const float4*>(w + kMlpW2 + kH * j);
 #pragma unroll
       for (int i = 0; i < kH / 4; ++i) {
-        const float4 q = row[i];
-        dh1[4 * i + 0] = fmaf(q.x, d2, dh1[4 * i + 0]);
-        dh1[4 * i + 1] = fmaf(q.y, d2, dh1[4 * i + 1]);
-        dh1[4 * i + 2] = fmaf(q.z, d2, dh1[4 * i + 2]);
-        dh1[4 * i + 3] = fmaf(q.w, d2, dh1[4 * i + 3]);
+        const float4 v = row[i];
+        dh1[4 * i + 0] = fmaf(v.x, d2, dh1[4 * i + 0]);
+        dh1[4 * i + 1] = fmaf(v.y, d2, dh1[4 * i + 1]);
+        dh1[4 * i + 2] = fmaf(v.z, d2, dh1[4 * i + 2]);
+        dh1[4 * i + 3] = fmaf(v.w, d2, dh1[4 * i + 3]);
       }
     }
+    // the pair's two partial sums (a + b == b + a, so both threads agree)
 #pragma unroll
-    for (int i = 0; i < kH; ++i) s_d1[t * kStride + i] = h1[i] > 0.f ? dh1[i] : 0.f;
+    for (int i = 0; i < kH; ++i) dh1[i] += __shfl_xor_sync(kFull, dh1[i], 1);
+#pragma unroll
+    for (int q = 0; q < kH / 2; ++q) {
+      const int i0 = pair_unit(0, q), i1 = pair_unit(1, q);
+      const float hv = half ? h1[i1] : h1[i0], dv = half ? dh1[i1] : dh1[i0];
+      s_d1[rl * kStride + pair_unit(half, q)] = hv > 0.f ? dv : 0.f;
+    }
   }
   __syncthreads();
 
   const int rows_here = min(kGradRows, B - static_cast<int>(blockIdx.x) * kGradRows);
   float* out = part + static_cast<int64_t>(blockIdx.x) * kMlpParams;
-  // dW2[j][i] = sum_r d2[r][j] h1[r][i]: thread t owns j = t / 2 and 32 i's
+  // dW2[j][i] = sum_r d2[r][j] h1[r][i]: thread t owns j = t / 2 and the 32
+  // i's of parity t & 1 (the two halves read neighbouring banks)
   {
-    const int j = t >> 1, i0 = (t & 1) * 32;
+    const int j = t >> 1, ip = t & 1;
+    const float w3 = w[kMlpW3 + j];
     float acc[32];
 #pragma unroll
     for (int q = 0; q < 32; ++q) acc[q] = 0.f;
     for (int rr = 0; rr < rows_here; ++rr) {
-      const float d = s_d2[rr * kStride + j];
-      const float* h = s_h1 + rr * kStride + i0;
+      const float d = s_h2[rr * kStride + j] > 0.f ? s_g[rr] * w3 : 0.f;
+      const float* h = s_h1 + rr * kStride + ip;
 #pragma unroll
-      for (int q = 0; q < 32; ++q) acc[q] = fmaf(d, h[q], acc[q]);
+      for (int q = 0; q < 32; ++q) acc[q] = fmaf(d, h[2 * q], acc[q]);
     }
 #pragma unroll
-    for (int q = 0; q < 32; ++q) out[kMlpW2 + kH * j + i0 + q] = acc[q];
+    for (int q = 0; q < 32; ++q) out[kMlpW2 + kH * j + 2 * q + ip] = acc[q];
   }
   if (t < kH) {  // dW3[j], db2[j]
+    const float w3 = w[kMlpW3 + t];
     float a3 = 0.f, a2 = 0.f;
     for (int rr = 0; rr < rows_here; ++rr) {
-      a3 = fmaf(s_g[rr], s_h2[rr * kStride + t], a3);
-      a2 += s_d2[rr * kStride + t];
+      const float h2 = s_h2[rr * kStride + t];
+      a3 = fmaf(s_g[rr], h2, a3);
+      a2 += h2 > 0.f ? s_g[rr] * w3 : 0.f;
     }
     out[kMlpW3 + t] = a3;
     out[kMlpB2 + t] = a2;
@@ -878,7 +908,7 @@ int mlp_forward(const LaunchCfg& c, cudaStream_t s, const float4* x, int64_t row
 }
 
 size_t mlp_grad_smem() {
-  return sizeof(float) * (kMlpParamsPadded + 4 * kGradRows * kStride + kGradRows * 4 + kGradRows + 32);
+  return sizeof(float) * (kMlpParamsPadded + 3 * kGradRows * kStride + kGradRows * 4 + kGradRows);
 }
 
 int mlp_configure() {
@@ -888,14 +918,15 @@ int mlp_configure() {
 }
 
 int mlp_train_step(cudaStream_t s, const float4* x, const float* target, int64_t r0, int B,
-                   const __nv_bfloat16* P, const MlpNorm& nm, float* e, float* part, float* loss,
-                   float* grad, float* master, __nv_bfloat16* Pw, float* m1, float* m2,
-                   const AdamStep& st) {
+                   const __nv_bfloat16* P, const MlpNorm& nm, float* e, float* center,
+                   float* part, float* loss, float* grad, float* master, __nv_bfloat16* Pw,
+                   float* m1, float* m2, const AdamStep& st) {
   const int nb = (B + kGradRows - 1) / kGradRows;
   k_mlp_residual<<<(B + 255) / 256, 256, 0, s>>>(x, target, r0, B, P, nm, e);
-  k_mlp_grad<<<nb, kGradRows, mlp_grad_smem(), s>>>(x, r0, B, e, P, nm, part, loss);
+  k_mlp_center<<<1, 1024, 0, s>>>(e, B, center, loss);
+  k_mlp_grad<<<nb, kGradThreads, mlp_grad_smem(), s>>>(x, r0, B, e, center, P, nm, part);
   k_mlp_reduce_adam<<<(kMlpParams + 255) / 256, 256, 0, s>>>(part, nb, grad, master, Pw, m1, m2, st);
-  return 3;
+  return 4;
 }
 
 int mlp_to_bf16(cudaStream_t s, const float* master, __nv_bfloat16* P) {

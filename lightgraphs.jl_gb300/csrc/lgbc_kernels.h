@@ -269,7 +269,8 @@ constexpr int kMlpW3 = kMlpB2 + kMlpHidden;
 constexpr int kMlpB3 = kMlpW3 + kMlpHidden;
 constexpr int kMlpParams = kMlpB3 + 1;                  // 4545
 constexpr int kMlpParamsPadded = (kMlpParams + 3) & ~3;
-constexpr int kGradRows = 2 * kMlpHidden;               // rows (threads) per gradient block
+constexpr int kGradRows = kMlpHidden;                   // rows per gradient block
+constexpr int kGradThreads = 2 * kMlpHidden;            // two threads per row
 static_assert(kMlpParams == 4545, "parameter count");
 
 struct MlpNorm {
@@ -284,13 +285,13 @@ int mlp_forward(const LaunchCfg& c, cudaStream_t s, const float4* x, int64_t row
                 const __nv_bfloat16* P, const MlpNorm& nm, float* y);
 // Opt the gradient kernel into its dynamic shared memory (once per device).
 int mlp_configure();
-// One step on rows [r0, r0 + B): residuals e, block partials part, the loss,
-// the reduced gradient (grad may be null) and, when master is not null, an
-// Adam update of master / Pw / m1 / m2.
+// One step on rows [r0, r0 + B): residuals e, their mean (center, one
+// float), block partials part, the loss, the reduced gradient (grad may be
+// null) and, when master is not null, an Adam update of master / Pw / m1 / m2.
 int mlp_train_step(cudaStream_t s, const float4* x, const float* target, int64_t r0, int B,
-                   const __nv_bfloat16* P, const MlpNorm& nm, float* e, float* part, float* loss,
-                   float* grad, float* master, __nv_bfloat16* Pw, float* m1, float* m2,
-                   const AdamStep& st);
+                   const __nv_bfloat16* P, const MlpNorm& nm, float* e, float* center,
+                   float* part, float* loss, float* grad, float* master, __nv_bfloat16* Pw,
+                   float* m1, float* m2, const AdamStep& st);
 int mlp_to_bf16(cudaStream_t s, const float* master, __nv_bfloat16* P);
 // Weights and standardisation of an MLP handle (mlp.cu), for graph calls.
 struct MlpView {

@@ -253,16 +253,17 @@ int lgbc_mlp_grad(lgbc_mlp* m, const float* x, const float* target, int64_t rows
   const int nb = (B + kGradRows - 1) / kGradRows;
   Scratch sc;
   float4* dx;
-  float *dt, *de, *dpart, *dloss, *dgrad;
+  float *dt, *de, *dcenter, *dpart, *dloss, *dgrad;
   MLP_TRY(sc.get(&dx, static_cast<size_t>(B)));
   MLP_TRY(sc.get(&dt, static_cast<size_t>(B)));
   MLP_TRY(sc.get(&de, static_cast<size_t>(B)));
+  MLP_TRY(sc.get(&dcenter, 1));
   MLP_TRY(sc.get(&dpart, static_cast<size_t>(nb) * kMlpParams));
   MLP_TRY(sc.get(&dloss, 1));
   MLP_TRY(sc.get(&dgrad, kMlpParams));
   MLP_CUDA(cudaMemcpyAsync(dx, x, sizeof(float4) * B, cudaMemcpyHostToDevice, m->stream));
   MLP_CUDA(cudaMemcpyAsync(dt, target, sizeof(float) * B, cudaMemcpyHostToDevice, m->stream));
-  mlp_train_step(m->stream, dx, dt, 0, B, m->P, norm_of(m), de, dpart, dloss, dgrad, nullptr,
+  mlp_train_step(m->stream, dx, dt, 0, B, m->P, norm_of(m), de, dcenter, dpart, dloss, dgrad, nullptr,
                  nullptr, nullptr, nullptr, AdamStep{});
   MLP_CUDA(cudaGetLastError());
   MLP_CUDA(cudaMemcpyAsync(grad, dgrad, sizeof(float) * kMlpParams, cudaMemcpyDeviceToHost,
@@ -294,10 +295,11 @@ int lgbc_mlp_train(lgbc_mlp* m, const float* x, const float* target, int64_t row
   const int nb = (Bmax + kGradRows - 1) / kGradRows;
   Scratch sc;
   float4* dx;
-  float *dt, *de, *dpart, *dloss;
+  float *dt, *de, *dcenter, *dpart, *dloss;
   MLP_TRY(sc.get(&dx, static_cast<size_t>(rows)));
   MLP_TRY(sc.get(&dt, static_cast<size_t>(rows)));
   MLP_TRY(sc.get(&de, static_cast<size_t>(Bmax)));
+  MLP_TRY(sc.get(&dcenter, 1));
   MLP_TRY(sc.get(&dpart, static_cast<size_t>(nb) * kMlpParams));
   MLP_TRY(sc.get(&dloss, static_cast<size_t>(cfg->steps > 0 ? cfg->steps : 1)));
   MLP_CUDA(cudaMemcpyAsync(dx, x, sizeof(float4) * rows, cudaMemcpyHostToDevice, m->stream));
@@ -326,7 +328,8 @@ int lgbc_mlp_train(lgbc_mlp* m, const float* x, const float* target, int64_t row
     st.eps = cfg->eps;
     st.bc1 = static_cast<float>(1.0 - std::pow(static_cast<double>(cfg->beta1), static_cast<double>(m->t)));
     st.bc2 = static_cast<float>(1.0 - std::pow(static_cast<double>(cfg->beta2), static_cast<double>(m->t)));
-    mlp_train_step(m->stream, dx, dt, r0, B, m->P, nm, de, dpart, dloss + step, nullptr, m->master,
+    mlp_train_step(m->stream, dx, dt, r0, B, m->P, nm, de, dcenter, dpart, dloss + step, nullptr,
+                   m->master,
                    m->P, m->m1, m->m2, st);
   }
   MLP_CUDA(cudaGetLastError());

@@ -10,6 +10,11 @@ rank error together with GPU time (CUDA events on the graph's stream).
 * learned -- ``betweenness_centrality_learned``: k i.i.d. sources from the
   proposal, weights 1/(k p), rescaled with k = n.
 
+* ceiling arms -- i.i.d. draws from proposals built from exact per-source
+  information that a predictor can at best reproduce: p proportional to the
+  exact dependency mass (a perfect prediction of the network's target), to
+  its square root, and uniform over the non-isolated sources.
+
 "Equal error" compares, for every uniform budget k_u, the learned budget k_l
 at which the learned estimator's mean L1 error equals uniform's at k_u
 (log-log interpolation between measured budgets); both estimators' GPU time is
@@ -25,10 +30,10 @@ import numpy as np
 
 from . import _lib
 from . import generators as gen
-from .centrality import betweenness_centrality, sample
+from .centrality import _rescale_, betweenness_centrality, sample
 from .graphs import SimpleGraph
-from .learned import (SourceProposal, betweenness_centrality_learned, l1_error,
-                      top_rank_error)
+from .learned import (SourceProposal, betweenness_centrality_learned, betweenness_raw_weighted,
+                      dependency_mass, l1_error, top_rank_error)
 from .traversals import gdistances
 
 
@@ -136,6 +141,38 @@ def run_estimators(g, exact_bc, proposal: SourceProposal, ks_uniform, ks_learned
     return recs, build_ms
 
 
+def ceiling_proposals(g):
+    """Proposals from exact per-source information: ``mass`` (p proportional
+    to sum_v delta_s(v)), ``sqrt_mass`` and ``uniform_active`` (uniform over
+    vertices with an edge), plus the GPU milliseconds of the exact masses."""
+    with _Timer(g) as t:
+        mass = dependency_mass(g)
+    out = {}
+    for name, w in (("mass", mass), ("sqrt_mass", np.sqrt(mass)),
+                    ("uniform_active", (g.degrees() > 0).astype(np.float64))):
+        out[name] = w / w.sum()
+    return out, t.ms
+
+
+def run_fixed(g, exact_bc, p, ks, method: str, seeds=8, seed0=100):
+    """Records for k i.i.d. draws from the fixed proposal p (drawn on the
+    host) with weights 1/(k p), through the weighted Brandes call; GPU time
+    covers that call only."""
+    n = g.nv()
+    recs = []
+    for k in ks:
+        for s in range(seeds):
+            rng = np.random.default_rng(seed0 + s)
+            src = rng.choice(n, size=int(k), p=p).astype(np.int32)
+            w = 1.0 / (int(k) * p[src])
+            with _Timer(g) as t:
+                b = betweenness_raw_weighted(g, src, w)
+            _rescale_(b, n, True, g.is_directed(), n)
+            recs.append(dict(method=method, k=int(k), seed=s, l1=l1_error(b, exact_bc),
+                             top1=top_rank_error(b, exact_bc), gpu_ms=t.ms))
+    return recs
+
+
 def _means(recs, method):
     ks = sorted({r["k"] for r in recs if r["method"] == method})
     out = []
@@ -169,12 +206,15 @@ def _interp_lin(xs, ys, x):
         float(ys[0] + (ys[-1] - ys[0]) * (x - xs[0]) / (xs[-1] - xs[0]))
 
 
-def summarise(recs, build_ms: float, k_targets):
-    """Mean errors per budget and, per learned scheme, the equal-error
-    GPU-time comparison against uniform sampling."""
+def summarise(recs, build_ms: float, k_targets,
+              methods=("learned", "learned_systematic")):
+    """Mean errors per budget and, per method, the equal-error GPU-time
+    comparison against uniform sampling (``equal_error`` for "learned",
+    ``equal_error_<method>`` for the others; ``build_ms`` is added to the
+    learned methods only)."""
     uni = _means(recs, "uniform")
     out = dict(uniform=uni, build_ms=build_ms)
-    for method in ("learned", "learned_systematic"):
+    for method in methods:
         lrn = _means(recs, method)
         if not lrn:
             continue
@@ -184,11 +224,13 @@ def summarise(recs, build_ms: float, k_targets):
             u = next(r for r in uni if r["k"] == ku)
             kl = _interp_loglog(lk, [r["l1"] for r in lrn], u["l1"])
             tl = _interp_lin(lk, [r["gpu_ms"] for r in lrn], kl)
+            bm = build_ms if method.startswith("learned") else 0.0
             table.append(dict(k_uniform=ku, l1_uniform=u["l1"], top1_uniform=u["top1"],
                               ms_uniform=u["gpu_ms"], k_learned_equal_l1=kl, ms_learned=tl,
-                              ms_learned_with_build=tl + build_ms,
+                              ms_learned_with_build=tl + bm,
                               time_ratio=tl / u["gpu_ms"],
-                              time_ratio_with_build=(tl + build_ms) / u["gpu_ms"]))
+                              time_ratio_with_build=(tl + bm) / u["gpu_ms"]))
         out[method] = lrn
-        out["equal_error" if method == "learned" else "equal_error_systematic"] = table
+        key = {"learned": "equal_error", "learned_systematic": "equal_error_systematic"}
+        out[key.get(method, "equal_error_" + method)] = table
     return out

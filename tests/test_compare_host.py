@@ -48,3 +48,19 @@ def test_means_per_budget():
     assert row["k"] == 8 and row["l1"] == pytest.approx(1.5)
     assert row["l1_sd"] == pytest.approx(np.std([0, 1, 2, 3]))
     assert row["gpu_ms"] == pytest.approx(2.5)  # median
+
+
+def test_summarise_ceiling_arms_carry_no_build():
+    # a fixed proposal built from exact masses: half the sources at equal
+    # error, same cost per source -> ratio 0.5 with and without the build
+    ks = [256, 512, 1024, 2048, 4096, 8192, 16384]
+    recs = _records("uniform", [1024, 4096, 16384], 1.0, 0.04)
+    recs += _records("learned", ks, 0.8, 0.05)
+    recs += _records("mass", ks, math.sqrt(0.5), 0.04)
+    out = compare.summarise(recs, build_ms=10.0, k_targets=[1024, 4096, 16384],
+                            methods=("learned", "mass"))
+    for row in out["equal_error_mass"]:
+        assert row["k_learned_equal_l1"] == pytest.approx(0.5 * row["k_uniform"])
+        assert row["time_ratio"] == pytest.approx(0.5)
+        assert row["time_ratio_with_build"] == pytest.approx(0.5)
+    assert out["equal_error"][0]["time_ratio_with_build"] > 0.8

@@ -159,7 +159,7 @@ def test_mlp_forward_matches_fp64():
     m.close()
 
 
-@pytest.mark.parametrize("rows", [1000, 4096])
+@pytest.mark.parametrize("rows", [65, 1000, 4096])
 def test_mlp_gradient_matches_fp64(rows):
     m = SourceProposal(seed=11)
     rng = np.random.default_rng(rows)
