@@ -168,10 +168,10 @@ int lgbc_graph_stats(const lgbc_graph *g, lgbc_stats *out);
  *                 cut into 256-edge work items spread over the whole GPU
  *                 instead of being expanded by one warp (default 256).
  *   lanes         sources per multi-source batch of the betweenness entry
- *                 points, stacked unions included (1..128, default 128; above
- *                 64 a batch keeps two 64-bit lane words per vertex); unions
- *                 of many graphs use the default.  Stress and distance
- *                 batches use at most 64.
+ *                 points, stacked unions included (1..256, default 128; above
+ *                 64 a batch keeps two 64-bit lane words per vertex, above 128
+ *                 four); unions of many graphs use the default.  Stress and
+ *                 distance batches use at most 64.
  *   dense_edges   a 32-edge chunk with more than this many edges that carry
  *                 lanes is gathered thread-per-lane (bit-transposed) instead
  *                 of edge by edge (32 = always edge by edge).

@@ -541,21 +541,21 @@ int run_ms_batch(lgbc_graph* g, const int32_t* lane_src, int nl, int sigma_kind,
   const DevGraph dg = g->dev();
   LGBC_TRY(ensure_hubs(g));
   const HubData hd = hub_data(g);
-  // more than 64 lanes: a two-word batch (Brandes batches only)
-  const int words = nl > kMaxLanes ? 2 : 1;
+  // more than 64 lanes: a two- or four-word batch (Brandes batches only)
+  const int words = lane_words(nl);
   if (nl < 1 || nl > kWideLanes)
-    return fail(LGBC_EINVAL, "internal: a multi-source batch holds 1 to 128 lanes");
+    return fail(LGBC_EINVAL, "internal: a multi-source batch holds 1 to 256 lanes");
   if (words > 1 && (dist || stats || stress || pexp || sigma_kind == kSigmaNone ||
                     g->ms.sigma_words < words || !g->ms.claim))
-    return fail(LGBC_EINVAL, "internal: a two-word batch is a Brandes batch");
+    return fail(LGBC_EINVAL, "internal: a multi-word batch is a Brandes batch");
   if (pexp && (sigma_kind == kSigmaNone || seeds.v))
     return fail(LGBC_EINVAL, "internal: a path-count export needs a plain batch with path counts");
-  // two-word lane sets are read as single 16-byte accesses
+  // a W-word lane set is read as one aligned 8 W-byte access
   auto misaligned = [&](const void* p) {
-    return words > 1 && (reinterpret_cast<uintptr_t>(p) & 15u) != 0;
+    return words > 1 && (reinterpret_cast<uintptr_t>(p) & (8u * words - 1u)) != 0;
   };
   if (misaligned(seeds.mask) || misaligned(seeds.seg_mark))
-    return fail(LGBC_EINVAL, "internal: seed lane sets must start on a 16-byte boundary");
+    return fail(LGBC_EINVAL, "internal: seed lane sets must be aligned to their size");
   const LaneSet act = lane_set(nl, words);
   for (;;) {
     MsBuffers b = ms_buffers(g, lane_src, lane_w);
@@ -709,7 +709,7 @@ int run_betweenness(lgbc_graph* g, int64_t k_act, int endpoints, double* bc_dev,
     return check_launch(g);
   }
   const int lanes = std::max(1, std::min<int>(kWideLanes, g->tune.lanes));
-  if (k_act > 0) LGBC_TRY(ensure_ms(g, true, lanes > kMaxLanes ? 2 : 1));
+  if (k_act > 0) LGBC_TRY(ensure_ms(g, true, lane_words(lanes)));
   for (int64_t s0 = 0; s0 < k_act; s0 += lanes) {
     const int nl = static_cast<int>(std::min<int64_t>(lanes, k_act - s0));
     const double* lw = d_w ? d_w + s0 : nullptr;
@@ -845,7 +845,7 @@ int create_replicated(lgbc_graph* g, int64_t copies, lgbc_graph** out) {
 int run_stacked(lgbc_graph* g, int64_t copies, double* bc_dev, const std::vector<double>* w) {
   const int64_t n = g->n;
   const int L = std::max(1, std::min<int>(kWideLanes, g->tune.lanes));
-  const int W = L > kMaxLanes ? 2 : 1;  // lane words per vertex of the union batches
+  const int W = lane_words(L);  // lane words per vertex of the union batches
   const int64_t row = 64 * W;            // weights per copy row
   if (!g->stack || g->stack_copies != copies) {
     if (g->stack) lgbc_graph_destroy(g->stack);
@@ -902,13 +902,13 @@ int run_stacked(lgbc_graph* g, int64_t copies, double* bc_dev, const std::vector
     bstart[static_cast<size_t>(u + 1)] = static_cast<int64_t>(sv.size());
   }
   // one device buffer: weight rows | voff | marks | seed masks | seed vertices,
-  // each part starting on a 16-byte boundary (two-word lane sets are read as
-  // one 16-byte access)
-  auto up16 = [](size_t x) { return (x + 15) & ~static_cast<size_t>(15); };
-  const size_t o_voff = up16(wrows.size() * 8);
-  const size_t o_marks = up16(o_voff + voff.size() * 8);
-  const size_t o_sm = up16(o_marks + marks.size() * 8);
-  const size_t o_sv = up16(o_sm + sm.size() * 8);
+  // each part starting on a 32-byte boundary (a W-word lane set is read as
+  // one aligned 8 W-byte access)
+  auto up32 = [](size_t x) { return (x + 31) & ~static_cast<size_t>(31); };
+  const size_t o_voff = up32(wrows.size() * 8);
+  const size_t o_marks = up32(o_voff + voff.size() * 8);
+  const size_t o_sm = up32(o_marks + marks.size() * 8);
+  const size_t o_sv = up32(o_sm + sm.size() * 8);
   const size_t bytes = o_sv + sv.size() * 4 + 16;
   unsigned char* buf = nullptr;
   LGBC_TRY(dev_alloc(&buf, bytes));

@@ -126,7 +126,7 @@ int many_group(const std::vector<ManyGraph>& grp, int endpoints, double* bc_raw_
   }
   // L lanes per batch (the handle's default batch width), W lane words
   const int L = std::max(1, std::min<int>(kWideLanes, g->tune.lanes));
-  const int W = L > kMaxLanes ? 2 : 1;
+  const int W = lane_words(L);
   if (g->tune.source_order == 1 && maxa > L)
     LGBC_TRY(order_many(g, grp, voff, act));
   // batch b, lane l holds the (L b + l)-th ordered source of every graph;

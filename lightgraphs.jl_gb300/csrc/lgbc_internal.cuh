@@ -8,8 +8,11 @@ namespace lgbc {
 
 constexpr int kWarp = 32;
 constexpr int kMaxLanes = 64;            // sources per one-word multi-source batch
-constexpr int kMaxWords = 2;             // 64-bit lane words per vertex in a wide batch
-constexpr int kWideLanes = 64 * kMaxWords;  // sources per wide (two-word) batch
+constexpr int kMaxWords = 4;             // 64-bit lane words per vertex in a wide batch
+constexpr int kWideLanes = 64 * kMaxWords;  // sources per widest (four-word) batch
+
+// Lane words of a batch of nl lanes: 1, 2 or 4 (three-word batches round up).
+constexpr int lane_words(int nl) { return nl > 2 * kMaxLanes ? 4 : (nl > kMaxLanes ? 2 : 1); }
 constexpr int32_t kUnreached = INT32_MAX;
 constexpr unsigned kFull = 0xffffffffu;
 

@@ -253,7 +253,7 @@ template <class A, int W> struct Fp64Slots {
   static constexpr int value = 0;
 };
 template <int NF, int W> struct Fp64Slots<XgAcc<NF>, W> {
-  static constexpr int value = W == 2 ? NF : 0;
+  static constexpr int value = W == 1 ? 0 : NF * (W / 2);  // NF of every four slots
 };
 
 template <class T, class A, int W>
@@ -951,7 +951,7 @@ __global__ void __launch_bounds__(256) k_ms_hub_discover(DevGraph g, MsBuffers b
 // set, mark it visited and pull its path counts from its predecessors
 // (hubs: k_ms_hub_pull).
 template <int SK, bool DIST, int W>
-__global__ void __launch_bounds__(256, 4) k_ms_td_settle(DevGraph g, MsBuffers b, HubData hd,
+__global__ void __launch_bounds__(256, W == 4 ? 3 : 4) k_ms_td_settle(DevGraph g, MsBuffers b, HubData hd,
                                                       Lanes<W> act, int32_t* dist, int64_t ld) {
   using T = typename Sig<SK>::T;
   BatchCtl* c = b.ctl;
@@ -1000,7 +1000,7 @@ __global__ void __launch_bounds__(256, 4) k_ms_td_settle(DevGraph g, MsBuffers b
 // to k_ms_hub_pull.
 // ---------------------------------------------------------------------------
 template <int SK, bool DIST, int W, bool LF>
-__global__ void __launch_bounds__(256, 4) k_ms_bu(DevGraph g, MsBuffers b, HubData hd, Lanes<W> act,
+__global__ void __launch_bounds__(256, W == 4 ? 3 : 4) k_ms_bu(DevGraph g, MsBuffers b, HubData hd, Lanes<W> act,
                                                int32_t* dist, int64_t ld) {
   using T = typename Sig<SK>::T;
   BatchCtl* c = b.ctl;
@@ -1080,7 +1080,7 @@ __global__ void __launch_bounds__(256, 4) k_ms_bu(DevGraph g, MsBuffers b, HubDa
 // lanes).  Partial sums go to the hub's slot; its last item stores sigma and,
 // bottom-up, appends the hub to the next level.
 template <int SK, bool DIST, bool BU, int W, bool LF>
-__global__ void __launch_bounds__(256, 4) k_ms_hub_pull(DevGraph g, MsBuffers b, HubData hd,
+__global__ void __launch_bounds__(256, W == 4 ? 3 : 4) k_ms_hub_pull(DevGraph g, MsBuffers b, HubData hd,
                                                      Lanes<W> act, int32_t* dist, int64_t ld) {
   using T = typename Sig<SK>::T;
   BatchCtl* c = b.ctl;
@@ -1304,7 +1304,7 @@ __global__ void k_ms_back_clear(MsBuffers b) {
 // Writes F_L into mb[L & 1] for every v (hubs included) before
 // k_ms_hub_delta finishes the hubs.
 template <int SK, int W>
-__global__ void __launch_bounds__(256, W == 1 ? 5 : 4) k_ms_delta(DevGraph g, MsBuffers b, HubData hd, double* bc) {
+__global__ void __launch_bounds__(256, W == 1 ? 5 : (W == 2 ? 4 : 3)) k_ms_delta(DevGraph g, MsBuffers b, HubData hd, double* bc) {
   BatchCtl* c = b.ctl;
   const int L = c->level;
   const unsigned long long lo = b.lvl_off[L], hi = b.lvl_off[L + 1];
@@ -1358,7 +1358,7 @@ __global__ void __launch_bounds__(256, W == 1 ? 5 : 4) k_ms_delta(DevGraph g, Ms
 // Hub dependencies at level L over out-edge items; partial psi sums are
 // combined in FP64 atomics, the hub's last item finalises delta / psi / bc.
 template <int SK, int W>
-__global__ void __launch_bounds__(256, W == 1 ? 5 : 4) k_ms_hub_delta(DevGraph g, MsBuffers b,
+__global__ void __launch_bounds__(256, W == 1 ? 5 : (W == 2 ? 4 : 3)) k_ms_hub_delta(DevGraph g, MsBuffers b,
                                                                      HubData hd, double* bc) {
   BatchCtl* c = b.ctl;
   const int L = c->level;
@@ -2008,25 +2008,35 @@ __global__ void k_ms_init_seeds_ctl(MsBuffers b, long long nseeds, unsigned long
   b.lvl_off[1] = static_cast<unsigned long long>(nseeds);
 }
 
+// A multi-word batch (Brandes batches only: no distance rows).
+template <int W>
+void init_wide(cudaStream_t s, const DevGraph& g, const MsBuffers& b, int nlanes, const Lanes<W>& a,
+               int sigma_kind, unsigned long long sigma_limit) {
+  switch (sigma_kind) {
+    case kSigmaU64:
+      k_ms_init<kSigmaU64, W><<<1, kWideLanes, 0, s>>>(g, b, nlanes, a, b.cap, sigma_limit, nullptr, 0);
+      break;
+    case kSigmaF64:
+      k_ms_init<kSigmaF64, W><<<1, kWideLanes, 0, s>>>(g, b, nlanes, a, b.cap, ~0ull, nullptr, 0);
+      break;
+    default:
+      k_ms_init<kSigmaNone, W><<<1, kWideLanes, 0, s>>>(g, b, nlanes, a, b.cap, ~0ull, nullptr, 0);
+      break;
+  }
+}
+
 }  // namespace
 
 int ms_init(cudaStream_t s, const DevGraph& g, const MsBuffers& b, int nlanes, int sigma_kind,
             unsigned long long sigma_limit, int32_t* dist, int64_t dist_ld) {
   sigma_kind = fwd_kind(sigma_kind);
   const LaneSet act = lane_set(nlanes, b.words);
+  if (b.words == 4) {
+    init_wide<4>(s, g, b, nlanes, lane_cast<4>(act), sigma_kind, sigma_limit);
+    return 1;
+  }
   if (b.words == 2) {
-    const Lanes<2> a = lane_cast<2>(act);
-    switch (sigma_kind) {
-      case kSigmaU64:
-        k_ms_init<kSigmaU64, 2><<<1, kWideLanes, 0, s>>>(g, b, nlanes, a, b.cap, sigma_limit, nullptr, 0);
-        break;
-      case kSigmaF64:
-        k_ms_init<kSigmaF64, 2><<<1, kWideLanes, 0, s>>>(g, b, nlanes, a, b.cap, ~0ull, nullptr, 0);
-        break;
-      default:
-        k_ms_init<kSigmaNone, 2><<<1, kWideLanes, 0, s>>>(g, b, nlanes, a, b.cap, ~0ull, nullptr, 0);
-        break;
-    }
+    init_wide<2>(s, g, b, nlanes, lane_cast<2>(act), sigma_kind, sigma_limit);
     return 1;
   }
   const Lanes<1> a = lane_cast<1>(act);
@@ -2074,7 +2084,9 @@ int ms_init_seeds(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const M
                   unsigned long long sigma_limit, int32_t* dist, int64_t dist_ld) {
   sigma_kind = fwd_kind(sigma_kind);
   cudaMemsetAsync(b.ctl, 0, sizeof(BatchCtl), s);
-  if (b.words == 2)
+  if (b.words == 4)
+    init_seeds_w<4>(c, s, g, b, seed_v, seed_mask, nseeds, sigma_kind, sigma_limit, nullptr, 0);
+  else if (b.words == 2)
     init_seeds_w<2>(c, s, g, b, seed_v, seed_mask, nseeds, sigma_kind, sigma_limit, nullptr, 0);
   else
     init_seeds_w<1>(c, s, g, b, seed_v, seed_mask, nseeds, sigma_kind, sigma_limit, dist, dist_ld);
@@ -2083,7 +2095,9 @@ int ms_init_seeds(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const M
 
 int ms_premark(const LaunchCfg& c, cudaStream_t s, const MsBuffers& b, const int64_t* seg_off,
                const uint64_t* seg_mark, int64_t nseg) {
-  if (b.words == 2)
+  if (b.words == 4)
+    k_ms_premark<4><<<c.grid, c.block, 0, s>>>(b.visit, seg_off, seg_mark, nseg);
+  else if (b.words == 2)
     k_ms_premark<2><<<c.grid, c.block, 0, s>>>(b.visit, seg_off, seg_mark, nseg);
   else
     k_ms_premark<1><<<c.grid, c.block, 0, s>>>(b.visit, seg_off, seg_mark, nseg);
@@ -2091,6 +2105,9 @@ int ms_premark(const LaunchCfg& c, cudaStream_t s, const MsBuffers& b, const int
 }
 
 namespace {
+
+// The segmented low-degree kernels exist for one- and two-word batches.
+template <int W> constexpr bool has_seg() { return W < 4; }
 
 template <int W, bool LF>
 int topdown_w(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
@@ -2113,9 +2130,9 @@ int topdown_w(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuf
       k_ms_td_settle<kSigmaNone, false, W><<<c.grid, c.block, 0, s>>>(g, b, hd, act, nullptr, 0);
     }
   } else if (sigma_kind == kSigmaU64) {
-    if (hd.segmented)
-      k_ms_td_settle_seg<kSigmaU64, W><<<c.grid, c.block, 0, s>>>(g, b, hd, act);
-    else
+    if (has_seg<W>() && hd.segmented) {
+      if constexpr (has_seg<W>()) k_ms_td_settle_seg<kSigmaU64, W><<<c.grid, c.block, 0, s>>>(g, b, hd, act);
+    } else
       k_ms_td_settle<kSigmaU64, false, W><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
     if (hd.n_in > 0) {
       k_ms_hub_pull<kSigmaU64, false, false, W, false><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist,
@@ -2123,9 +2140,9 @@ int topdown_w(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuf
       ++launches;
     }
   } else {
-    if (hd.segmented)
-      k_ms_td_settle_seg<kSigmaF64, W><<<c.grid, c.block, 0, s>>>(g, b, hd, act);
-    else
+    if (has_seg<W>() && hd.segmented) {
+      if constexpr (has_seg<W>()) k_ms_td_settle_seg<kSigmaF64, W><<<c.grid, c.block, 0, s>>>(g, b, hd, act);
+    } else
       k_ms_td_settle<kSigmaF64, false, W><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
     if (hd.n_in > 0) {
       k_ms_hub_pull<kSigmaF64, false, false, W, false><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist,
@@ -2167,9 +2184,9 @@ int bottomup_w(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBu
       }
     }
   } else if (sigma_kind == kSigmaU64) {
-    if (hd.segmented)
-      k_ms_bu_seg<kSigmaU64, W, LF><<<c.grid, c.block, 0, s>>>(g, b, hd, act);
-    else
+    if (has_seg<W>() && hd.segmented) {
+      if constexpr (has_seg<W>()) k_ms_bu_seg<kSigmaU64, W, LF><<<c.grid, c.block, 0, s>>>(g, b, hd, act);
+    } else
       k_ms_bu<kSigmaU64, false, W, LF><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
     if (hd.n_in > 0) {
       k_ms_hub_pull<kSigmaU64, false, true, W, LF><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist,
@@ -2177,9 +2194,9 @@ int bottomup_w(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBu
       ++launches;
     }
   } else {
-    if (hd.segmented)
-      k_ms_bu_seg<kSigmaF64, W, LF><<<c.grid, c.block, 0, s>>>(g, b, hd, act);
-    else
+    if (has_seg<W>() && hd.segmented) {
+      if constexpr (has_seg<W>()) k_ms_bu_seg<kSigmaF64, W, LF><<<c.grid, c.block, 0, s>>>(g, b, hd, act);
+    } else
       k_ms_bu<kSigmaF64, false, W, LF><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist, dist_ld);
     if (hd.n_in > 0) {
       k_ms_hub_pull<kSigmaF64, false, true, W, LF><<<c.grid, c.block, 0, s>>>(g, b, hd, act, dist,
@@ -2197,29 +2214,29 @@ int backward_body_w(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const
   int launches = 2;
   k_ms_back_clear<W><<<c.grid, c.block, 0, s>>>(b);
   // the segmented variant has no weighted finalisation
-  const bool seg = hd.segmented && !b.lane_w;
+  const bool seg = has_seg<W>() && hd.segmented && !b.lane_w;
   if (sigma_kind == kSigmaU64F64) {
-    if (seg)
-      k_ms_delta_seg<kSigmaU64F64, W><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
-    else
+    if (seg) {
+      if constexpr (has_seg<W>()) k_ms_delta_seg<kSigmaU64F64, W><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
+    } else
       k_ms_delta<kSigmaU64F64, W><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
     if (hd.n_out > 0) {
       k_ms_hub_delta<kSigmaU64F64, W><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
       ++launches;
     }
   } else if (sigma_kind == kSigmaF64) {
-    if (seg)
-      k_ms_delta_seg<kSigmaF64, W><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
-    else
+    if (seg) {
+      if constexpr (has_seg<W>()) k_ms_delta_seg<kSigmaF64, W><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
+    } else
       k_ms_delta<kSigmaF64, W><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
     if (hd.n_out > 0) {
       k_ms_hub_delta<kSigmaF64, W><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
       ++launches;
     }
   } else {
-    if (seg)
-      k_ms_delta_seg<kSigmaU64, W><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
-    else
+    if (seg) {
+      if constexpr (has_seg<W>()) k_ms_delta_seg<kSigmaU64, W><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
+    } else
       k_ms_delta<kSigmaU64, W><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
     if (hd.n_out > 0) {
       k_ms_hub_delta<kSigmaU64, W><<<c.grid, c.block, 0, s>>>(g, b, hd, bc);
@@ -2235,6 +2252,10 @@ int ms_topdown(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBu
                const HubData& hd, const LaneSet& act, int sigma_kind, int32_t* dist,
                int64_t dist_ld) {
   sigma_kind = fwd_kind(sigma_kind);
+  if (b.words == 4)
+    return b.lane_filter
+               ? topdown_w<4, true>(c, s, g, b, hd, lane_cast<4>(act), sigma_kind, dist, dist_ld)
+               : topdown_w<4, false>(c, s, g, b, hd, lane_cast<4>(act), sigma_kind, dist, dist_ld);
   if (b.words == 2)
     return b.lane_filter
                ? topdown_w<2, true>(c, s, g, b, hd, lane_cast<2>(act), sigma_kind, dist, dist_ld)
@@ -2248,6 +2269,10 @@ int ms_bottomup(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsB
                 const HubData& hd, const LaneSet& act, int sigma_kind, int32_t* dist,
                 int64_t dist_ld) {
   sigma_kind = fwd_kind(sigma_kind);
+  if (b.words == 4)
+    return b.lane_filter
+               ? bottomup_w<4, true>(c, s, g, b, hd, lane_cast<4>(act), sigma_kind, dist, dist_ld)
+               : bottomup_w<4, false>(c, s, g, b, hd, lane_cast<4>(act), sigma_kind, dist, dist_ld);
   if (b.words == 2)
     return b.lane_filter
                ? bottomup_w<2, true>(c, s, g, b, hd, lane_cast<2>(act), sigma_kind, dist, dist_ld)
@@ -2276,6 +2301,7 @@ int ms_backward_level(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, con
 
 int ms_backward_body(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, const MsBuffers& b,
                      const HubData& hd, int sigma_kind, double* bc) {
+  if (b.words == 4) return backward_body_w<4>(c, s, g, b, hd, sigma_kind, bc);
   if (b.words == 2) return backward_body_w<2>(c, s, g, b, hd, sigma_kind, bc);
   return backward_body_w<1>(c, s, g, b, hd, sigma_kind, bc);
 }
@@ -2319,7 +2345,9 @@ int st_backward_level(const LaunchCfg& c, cudaStream_t s, const DevGraph& g, con
 }
 
 int ms_cleanup(const LaunchCfg& c, cudaStream_t s, const MsBuffers& b) {
-  if (b.words == 2)
+  if (b.words == 4)
+    k_ms_cleanup<4><<<c.grid, c.block, 0, s>>>(b);
+  else if (b.words == 2)
     k_ms_cleanup<2><<<c.grid, c.block, 0, s>>>(b);
   else
     k_ms_cleanup<1><<<c.grid, c.block, 0, s>>>(b);

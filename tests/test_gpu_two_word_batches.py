@@ -122,7 +122,7 @@ def test_tuning_limits():
     h.set_tuning(lanes=128)
     assert h.tuning().lanes == 128
     with pytest.raises(Exception):
-        h.set_tuning(lanes=129)
+        h.set_tuning(lanes=0)
     assert h.tuning().lanes == 128
 
 
