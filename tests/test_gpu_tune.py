@@ -65,7 +65,7 @@ def test_tuning_validation():
     g = gen.rmat(8, 4, seed=2)
     h = g.device_handle()
     for bad in (dict(source_order=2), dict(graph_loop=-1), dict(stack_vertices=-5),
-                dict(lanes=0), dict(lanes=129), dict(alpha=0.0), dict(hub_degree=0)):
+                dict(lanes=0), dict(lanes=257), dict(alpha=0.0), dict(hub_degree=0)):
         with pytest.raises(lgbc.ArgumentError):
             h.set_tuning(**bad)
     h.set_tuning(lanes=7, source_order=0, graph_loop=0, stack_vertices=0)
