@@ -1,5 +1,7 @@
 // api_many.cu -- lgbc_betweenness_many: exact betweenness of many graphs as
 // disjoint unions of similar-size graphs.
+#include <atomic>
+
 #include "api_internal.h"
 
 using namespace lgbc;
@@ -219,6 +221,59 @@ int many_group(const std::vector<ManyGraph>& grp, int endpoints, double* bc_raw_
   return LGBC_OK;
 }
 
+// Runs the groups kManyInFlight at a time: each group has its own union
+// handle and stream, so while one group's batches run on the GPU the next
+// group's host work (union CSR, handle set-up, source ordering, seeds) goes
+// on in another host thread.  Groups write disjoint ranges of bc_raw_out.
+// The first failure stops the remaining groups; its code and message are
+// returned in the calling thread.
+int run_groups(const std::vector<std::vector<ManyGraph>>& groups, int endpoints,
+               double* bc_raw_out) {
+  constexpr size_t kManyInFlight = 2;
+  int dev = 0;
+  LGBC_CUDA(cudaGetDevice(&dev));
+  std::atomic<size_t> next{0};
+  std::mutex mu;
+  int first_rc = LGBC_OK;
+  std::string first_msg;
+  auto record = [&](int rc, const std::string& msg) {
+    std::lock_guard<std::mutex> lock(mu);
+    if (first_rc == LGBC_OK) {
+      first_rc = rc;
+      first_msg = msg;
+    }
+  };
+  auto stopped = [&]() {
+    std::lock_guard<std::mutex> lock(mu);
+    return first_rc != LGBC_OK;
+  };
+  auto worker = [&]() {
+    const cudaError_t e = cudaSetDevice(dev);
+    if (e != cudaSuccess) {
+      record(LGBC_ECUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+      return;
+    }
+    for (size_t i = next.fetch_add(1); i < groups.size() && !stopped(); i = next.fetch_add(1)) {
+      int rc;
+      try {
+        rc = many_group(groups[i], endpoints, bc_raw_out);
+      } catch (const std::bad_alloc&) {
+        rc = fail(LGBC_ENOMEM, "host allocation failed");
+      }
+      if (rc != LGBC_OK) {
+        record(rc, g_last_error);
+        return;
+      }
+    }
+  };
+  std::vector<std::thread> extra;
+  for (size_t t = 1; t < std::min(kManyInFlight, groups.size()); ++t) extra.emplace_back(worker);
+  worker();
+  for (auto& t : extra) t.join();
+  if (first_rc != LGBC_OK) return fail(first_rc, first_msg);
+  return LGBC_OK;
+}
+
 }  // namespace lgbc::api
 
 extern "C" int lgbc_betweenness_many(int64_t ngraphs, const int64_t* n, const int64_t* rowptr_off,
@@ -245,18 +300,16 @@ extern "C" int lgbc_betweenness_many(int64_t ngraphs, const int64_t* n, const in
   std::stable_sort(order.begin(), order.end(),
                    [&](size_t a, size_t b) { return gs[a].n > gs[b].n; });
   const int64_t kGroupVertices = int64_t(1) << 21;
-  std::vector<ManyGraph> grp;
+  std::vector<std::vector<ManyGraph>> groups(1);
   int64_t gv = 0;
   for (size_t oi = 0; oi < order.size(); ++oi) {
     const ManyGraph& m = gs[order[oi]];
-    if (!grp.empty() && gv + m.n > kGroupVertices) {
-      LGBC_TRY(many_group(grp, endpoints, bc_raw_out));
-      grp.clear();
+    if (!groups.back().empty() && gv + m.n > kGroupVertices) {
+      groups.emplace_back();
       gv = 0;
     }
-    grp.push_back(m);
+    groups.back().push_back(m);
     gv += m.n;
   }
-  if (!grp.empty()) LGBC_TRY(many_group(grp, endpoints, bc_raw_out));
-  return LGBC_OK;
+  return run_groups(groups, endpoints, bc_raw_out);
 }

@@ -152,3 +152,27 @@ def test_many_graphs_two_words():
     outs = lgbc.betweenness_centrality_many(gs, normalize=False)
     for g, z in zip(gs, outs):
         assert_bc_close(z, oracle_bc(g, normalize=False))
+
+
+@pytest.mark.parametrize("endpoints", [False, True])
+def test_many_graphs_two_groups_in_flight(endpoints):
+    # a 2,097,000-vertex graph (a 600-vertex BA component, the rest isolated)
+    # fills one union group alone, so the small graphs form a second group,
+    # run at the same time from a second host thread
+    small = G.barabasi_albert(600, 3, seed=77)
+    rp, ci = small.csr()
+    n_big = 2_097_000
+    big = lgbc.SimpleGraph.from_csr(np.concatenate([rp, np.full(n_big - small.nv(), rp[-1])]), ci)
+    gs = [G.barabasi_albert(int(n), 3, seed=90 + i) for i, n in enumerate([500, 140, 800])]
+    outs = lgbc.betweenness_centrality_many([big] + gs, normalize=False, endpoints=endpoints)
+    # with endpoints, each source of degree > 0 (isolated ones are skipped)
+    # adds n - 1 to itself and 1 to every other vertex, reached or not
+    # (_accumulate_endpoints! walks all n vertices): after the undirected
+    # halving, + (n_big - 600) / 2 on the component and 600 / 2 on each
+    # isolated vertex
+    extra = (n_big - small.nv()) / 2 if endpoints else 0.0
+    assert_bc_close(outs[0][:small.nv()],
+                    oracle_bc(small, normalize=False, endpoints=endpoints) + extra)
+    assert np.all(outs[0][small.nv():] == (small.nv() / 2 if endpoints else 0.0))
+    for g, z in zip(gs, outs[1:]):
+        assert_bc_close(z, oracle_bc(g, normalize=False, endpoints=endpoints))
