@@ -224,12 +224,14 @@ int many_group(const std::vector<ManyGraph>& grp, int endpoints, double* bc_raw_
 // Runs the groups kManyInFlight at a time: each group has its own union
 // handle and stream, so while one group's batches run on the GPU the next
 // group's host work (union CSR, handle set-up, source ordering, seeds) goes
-// on in another host thread.  Groups write disjoint ranges of bc_raw_out.
+// on in another host thread, and the groups' latency-bound kernels overlap
+// on the GPU (1,024 BA graphs on GB300: 12.08 s one at a time, 9.65 s two,
+// 8.79 s three).  Groups write disjoint ranges of bc_raw_out.
 // The first failure stops the remaining groups; its code and message are
 // returned in the calling thread.
 int run_groups(const std::vector<std::vector<ManyGraph>>& groups, int endpoints,
                double* bc_raw_out) {
-  constexpr size_t kManyInFlight = 2;
+  constexpr size_t kManyInFlight = 3;
   int dev = 0;
   LGBC_CUDA(cudaGetDevice(&dev));
   std::atomic<size_t> next{0};
