@@ -21,8 +21,8 @@ features: log(1 + degree), log(1 + core number) (core_number,
 src/degeneracy.jl:38-80), the mean log(1 + degree) of the neighbours and
 log(1 + the neighbours' degree sum).  Training targets are exact masses from
 the GPU's multi-source BFS.  Uniform sampling (``betweenness_centrality(g,
-k)``) and the exact call stay available as the fallback and the judge of the
-estimator's error.
+k)``) and the exact call stay available as the fallback and as the yardstick
+of the estimator's error.
 """
 from __future__ import annotations
 
