@@ -261,6 +261,8 @@ int run_groups(const std::vector<std::vector<ManyGraph>>& groups, int endpoints,
         rc = many_group(groups[i], endpoints, bc_raw_out);
       } catch (const std::bad_alloc&) {
         rc = fail(LGBC_ENOMEM, "host allocation failed");
+      } catch (const std::exception& ex) {  // never let one leave a worker thread
+        rc = fail(LGBC_EINVAL, std::string("many-graph union: ") + ex.what());
       }
       if (rc != LGBC_OK) {
         record(rc, g_last_error);
