@@ -724,9 +724,10 @@ def ceiling_arms(compare, g, exact_bc, ks, args, recs):
     if not args.c5_ceiling:
         return recs, methods, None
     props, mass_ms = compare.ceiling_proposals(g)
-    for name in CEILING_ARMS:
+    arms = tuple(name for name in CEILING_ARMS if name in props)
+    for name in arms:
         recs = recs + compare.run_fixed(g, exact_bc, props[name], ks, name, seeds=args.c5_seeds)
-    return recs, methods + CEILING_ARMS, mass_ms
+    return recs, methods + arms, mass_ms
 
 
 def run_c5(args, dist: Dist):

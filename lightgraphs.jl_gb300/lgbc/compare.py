@@ -150,7 +150,8 @@ def ceiling_proposals(g):
     out = {}
     for name, w in (("mass", mass), ("sqrt_mass", np.sqrt(mass)),
                     ("uniform_active", (g.degrees() > 0).astype(np.float64))):
-        out[name] = w / w.sum()
+        if w.sum() > 0:  # a graph without paths of length 2 has no mass to sample by
+            out[name] = w / w.sum()
     return out, t.ms
 
 
